@@ -1,0 +1,282 @@
+#!/usr/bin/env python
+"""Plain-MC photon-transport throughput (photons/ms) of the GB300 engine.
+
+One step = one complete simulation of the workload's photon budget.  By default the workload is
+the heterogeneous cube with reflection, 50 time gates and four detectors at 1e8 photons.
+
+  value   device-resident: inputs uploaded once into a session, CUDA-event time of the transport
+          launches only (L2 flushed before every timed step)
+  e2e     the public call a user makes, mcx_gb300.run(cfg) -> mcx_run_simulation, with host
+          buffers: Config preparation, volume upload, transport, normalisation, field and
+          detected-photon copy back, all inside the timed region
+  --impl reference   the reference arm (see `reference_arm`)
+
+Multi-GPU (torchrun, one rank per GPU): every rank simulates its own photon range of the same
+size (weak scaling, no collective in the data path); rank 0 prints.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "photons/ms (plain MC)"
+WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000}
+
+# Instructions issued per transport step (warp-level, ncu smsp__inst_executed.sum divided by the
+# kernel's own step counter / 32 lanes) from the committed ncu captures under profiles/.
+# None until a capture exists for the workload.
+ISSUE_PER_STEP = {"workload0": None, "workload1": None, "workload2": None}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (getattr(self, "out", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        d["_source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0, "_source": "fallback"}
+
+
+def make_cfg(name: str, nphoton: int, seed: int):
+    from mcx_gb300 import problems
+
+    return problems.WORKLOADS[name](nphoton, seed=seed)
+
+
+def cpu_baseline(name: str, sample: int) -> dict:
+    """The CPU oracle (a C++/OpenMP restatement of MCX's loop; MCX itself has no CPU path) on a
+    bounded sample of the same workload, on every host core."""
+    import mcx_gb300
+    from oracle import oracle
+
+    pc = mcx_gb300.prepare(make_cfg(name, sample, 4242))
+    cores = os.cpu_count() or 1
+    r = oracle.run(pc, nphoton=sample, seed=4242, threads=cores)
+    sec = r["stat"]["seconds"]
+    return {"value": sample / (sec * 1e3), "unit": "photons/ms", "cores": cores, "kind": "port",
+            "sample": f"{sample} photons of {name} ({sec:.2f} s)"}
+
+
+def reference_arm(args, world, rank) -> None:
+    """The reference arm: MCX's transport exists only as CUDA (src/mcx_core.cu has no CPU path),
+    so the arm times the oracle -- the CPU restatement of that path -- on all host cores, on a
+    bounded sample per step."""
+    if rank != 0:
+        return
+    name = args.workload
+    sample = args.cpu_sample or {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}[name]
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(name, max(1000, sample // 10))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(name, sample))
+    wall = time.perf_counter() - t0
+    v = sample * args.steps / (wall * 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "photons/ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "photons_per_step": sample, "note": "CPU restatement of the CUDA-only path"},
+        "cpu_baseline": {"value": v, "unit": "photons/ms", "cores": vals[0]["cores"], "kind": "port",
+                         "sample": f"{sample} photons of {name} per step"},
+        "e2e": {"value": v, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="workload1", choices=sorted(WORKLOAD_PHOTONS))
+    ap.add_argument("--photons", type=float, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import mcx_gb300
+    from mcx_gb300 import Session
+
+    name = args.workload
+    nphoton = int(args.photons) if args.photons else WORKLOAD_PHOTONS[name]
+    seed = 20251203
+    cfg = make_cfg(name, nphoton, seed)
+    pc = mcx_gb300.prepare(cfg)
+    sess = Session(pc, device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    base = rank * nphoton * (args.warmup + args.steps + 1)
+    for i in range(args.warmup):
+        sess.run(base + i * nphoton, nphoton, seed)
+    sess.reset()
+    kernel_ms = []
+    barrier()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            kernel_ms.append(sess.run(base + (args.warmup + i) * nphoton, nphoton, seed))
+        barrier()
+        wall_ms = (time.perf_counter() - t0) * 1e3
+    _, _, ndet, st = sess.read(with_field=False)
+    sess.close()
+    dev_ms = sum(kernel_ms)
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    value = nphoton * args.steps * world / dev_ms
+
+    # end to end through the public API with host buffers
+    e2e_ms = []
+    h2d = d2h = 0
+    for i in range(1 + args.steps):
+        c = make_cfg(name, nphoton, seed + 1 + i)
+        barrier()
+        t0 = time.perf_counter()
+        r = mcx_gb300.run(c)
+        barrier()
+        if i:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        nvox = int(np.prod(c["vol"].shape))
+        h2d = nvox * 4 + np.asarray(c["prop"]).nbytes + (np.asarray(c["detpos"]).nbytes if "detpos" in c else 0)
+        d2h = r["flux"].nbytes + (r["detp"].nbytes if "detp" in r else 0)
+    e2e_tot = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_tot], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_tot = float(t.item())
+    e2e = nphoton * args.steps * world / e2e_tot
+
+    pk = peaks()
+    steps_per_photon = st.n_steps / max(1, st.n_photon)
+    dep_per_photon = st.n_deposit / max(1, st.n_photon)
+    props = torch.cuda.get_device_properties(local)
+    f_clk = (clk.summary()["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)) * 1e6
+    ips = ISSUE_PER_STEP.get(name)
+    roof = {"bound": "fp32-issue", "unit": "photons/ms", "achieved": value / world, "peak": None, "frac": None,
+            "traffic": None, "steps_per_photon": steps_per_photon, "deposits_per_photon": dep_per_photon,
+            "issue_per_step": ips, "sm_clock_hz": f_clk, "peak_source": pk.get("_source")}
+    if ips:
+        p_issue = props.multi_processor_count * 4 * f_clk / (ips * steps_per_photon) / 1e3
+        roof.update(peak=p_issue, frac=(value / world) / p_issue)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "photons_per_step": nphoton, "volume": list(cfg["vol"].shape),
+                   "gates": pc.ngates, "parallelism": f"replicas{world}", "l2": "flushed before each timed step",
+                   "grid": st.grid, "block": st.block, "chunk": st.chunk},
+        "e2e": {"value": e2e, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": e2e_tot / args.steps},
+        "wall_ms_per_step": wall_ms / args.steps,
+        "gpu_launches": args.steps,
+        "detected_per_step": ndet / max(1, args.steps),
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        sample = args.cpu_sample or {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}[name]
+        line["cpu_baseline"] = cpu_baseline(name, sample)
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,102 @@
+/*
+ * mcx_gb300.h -- C-ABI of libmcx_gb300.so beyond the two MCX entry points.
+ *
+ * The drop-in boundary itself is mcx_run_simulation / mcx_list_gpu (include/mcx_abi.h),
+ * replacing src/mcx_core.h:200-201 of MCX.  The functions below are what a front-end that
+ * does not link MCX's own mcx_utils.c needs around them (Config defaults and preparation,
+ * error retrieval), plus a device-resident session interface used for benchmarking and by
+ * the batched scheduler.  All take plain pointers and sizes.
+ */
+#ifndef MCX_GB300_H
+#define MCX_GB300_H
+
+#include <stdint.h>
+#include "mcx_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Config preparation (host only; no GPU needed) -------------------------------------- */
+
+/* Default values of every Config field.
+ * Replaces mcx_initcfg, src/mcx_utils.c:248-378 (the parentid default is mpPython). */
+void mcxg_initcfg(Config* cfg);
+
+/* Prepare a filled Config for mcx_run_simulation: origin shift of source and detectors,
+ * time-gate checks, source-direction normalisation, boundary flags, unitinmm scaling,
+ * mus==0 media, launch voxel in srcparam2.z/.w, detector masking.  Returns 0 or a negative
+ * MCX error id (message via mcxg_last_error).
+ * Replaces mcx_validatecfg + mcx_preprocess, src/mcx_utils.c:3748-3857 and 1525-1820, for the
+ * label-media pencil-source subset the engine runs. */
+int  mcxg_validatecfg(Config* cfg);
+
+/* Set bit 31 of every voxel that a detector sphere covers on an interface.
+ * Replaces mcx_maskdet, src/mcx_utils.c:4214-4340 (label media). */
+void mcxg_maskdet(Config* cfg);
+
+/* ---- Errors ------------------------------------------------------------------------------ */
+
+/* When no front-end provides mcx_error() (src/mcx_utils.c:1314), the engine records its
+ * error here instead of exiting; mcx_run_simulation then returns normally. */
+const char* mcxg_last_error(void);
+int         mcxg_last_error_id(void);
+void        mcxg_clear_error(void);
+void        mcxg_set_error(int id, const char* msg);
+
+/* ---- Run statistics ---------------------------------------------------------------------- */
+
+/* Everything the last mcx_run_simulation on this thread measured, beyond what Config holds:
+ * FP64 energy tallies for the balance launched = absorbed + escaped + detected, the GPU's
+ * own step / scatter / deposit counters, kernel time from CUDA events, launch shape. */
+typedef struct mcxg_stats {
+    double e_launch;          /* total launched packet weight */
+    double e_escape;          /* residual weight of photons that left undetected or timed out */
+    double e_detect;          /* residual weight of detected photons */
+    double e_absdep;          /* absorbed weight recorded in the field */
+    double e_absother;        /* absorbed weight outside the recorded time window */
+    uint64_t n_steps, n_scatter, n_deposit, n_launch, n_photon, n_detected;
+    uint64_t n_tile_deposit;  /* deposits absorbed by the per-CTA shared-memory tile */
+    double kernel_ms;         /* transport kernels, CUDA events */
+    double total_ms;          /* whole mcx_run_simulation call, host clock */
+    int grid, block, chunk, launches;
+    uint32_t error_flags;     /* device-side error word (0 = clean) */
+} mcxg_stats;
+
+int mcxg_get_stats(mcxg_stats* out);
+
+/* ---- RNG test kernel --------------------------------------------------------------------- */
+
+/* Run the xorshift128+ generator on the GPU from four 32-bit seed words and copy n floats
+ * to host memory.  Replaces the -D R kernel mcx_test_rng, src/mcx_core.cu:1731-1742. */
+int mcxg_rng_test(const uint32_t seeds[4], float* out, int n);
+
+/* n floats of the per-photon stream of photon `pid` under `seed`, generated on the GPU. */
+int mcxg_photon_stream(uint64_t seed, uint64_t pid, float* out, int n);
+
+/* ---- Device-resident sessions ------------------------------------------------------------ */
+
+/* A prepared simulation held on one device: labels, properties, detectors and output
+ * buffers are uploaded once; runs then launch only the transport kernel.  Used by the
+ * benchmark (inputs resident in HBM) and by the batched scheduler. */
+typedef struct mcxg_session mcxg_session;
+
+mcxg_session* mcxg_session_create(const Config* cfg, int device);
+/* Clear the fluence, detected-photon and tally buffers. */
+int  mcxg_session_reset(mcxg_session* s);
+/* Simulate photons [photon_offset, photon_offset + nphoton) with RNG seed `seed` into the
+ * session's buffers (accumulating); kernel time in *kernel_ms when non-NULL. */
+int  mcxg_session_run(mcxg_session* s, uint64_t photon_offset, uint64_t nphoton, uint64_t seed, float* kernel_ms);
+/* Copy out the raw accumulated field (maxgate x Nvox floats, shadow copies merged) and
+ * up to max_records detected records; returns the number of detected photons seen. */
+int64_t mcxg_session_read(mcxg_session* s, float* field, float* detp, uint64_t max_records, mcxg_stats* stats);
+void mcxg_session_destroy(mcxg_session* s);
+
+/* Launch-shape override used by the autotuner (0 = engine default). */
+void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCX_GB300_H */

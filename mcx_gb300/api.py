@@ -1,0 +1,247 @@
+"""pmcx-style Python interface of the GB300 engine.
+
+``run(cfg)`` takes the same dictionary ``pmcx.run`` takes (src/pmcx.cpp:400-1065 parse_config,
+1066-1357 pmcx_interface) and returns the same outputs: ``flux`` as an F-ordered
+``[Nx, Ny, Nz, Nt]`` float32 array, ``detp`` as an F-ordered ``[reclen, ndetected]`` array and
+``stat`` with runtime / nphoton / energytot / energyabs / normalizer / unitinmm / workload.
+Internally it fills an MCX ``Config`` through ctypes, prepares it with ``mcxg_validatecfg`` and
+calls the drop-in entry points ``mcx_list_gpu`` and ``mcx_run_simulation`` of libmcx_gb300.so,
+exactly as pmcx drives MCX's own core.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Any
+
+import numpy as np
+
+from . import abi
+from ._lib import lib, libc
+
+_OUTPUT_TYPES = {"x": 0, "flux": 0, "f": 1, "fluence": 1, "e": 2, "energy": 2}
+_SRC_TYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
+              "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid", "ring"]
+_SAVEDET_CHARS = "dspmxvwi"      # detid, nscat, ppath, momentum, exit pos, exit dir, w0, iquv (src/mcx_utils.c)
+
+_SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "printnum", "maxvoidstep",
+                "maxjumpdebug", "gscatter", "srcnum", "srcid", "replaydet", "gpuid", "voidtime", "debuglevel"]
+_SCALARS_FLOAT = ["tstart", "tstep", "tend", "sradius", "minenergy", "unitinmm", "omega"]
+_SCALARS_CHAR = ["isreflect", "isref3", "isrefint", "isnormalized", "issrcfrom0", "autopilot", "issaveref",
+                 "issaveexit", "ismomentum", "isspecular", "issave2pt", "issavedet", "isgpuinfo", "isrowmajor",
+                 "issaveseed", "faststep"]
+
+
+class MCXError(RuntimeError):
+    """An error reported by the engine (the MCX error id is in ``.id``)."""
+
+    def __init__(self, id_: int, msg: str):
+        super().__init__(f"MCX error {id_}: {msg}")
+        self.id = id_
+
+
+def _check(rc: int | None = None) -> None:
+    eid = lib.mcxg_last_error_id()
+    if eid:
+        raise MCXError(eid, lib.mcxg_last_error().decode(errors="replace"))
+    if rc:
+        raise MCXError(rc, "engine call failed")
+
+
+def _set_vec(dst, vals, n) -> None:
+    vals = list(np.asarray(vals, dtype=np.float64).ravel())
+    for i, name in enumerate("xyzw"[:n]):
+        if i < len(vals):
+            setattr(dst, name, vals[i])
+
+
+class PreparedConfig:
+    """A filled and validated ``Config`` plus the numpy buffers it points into."""
+
+    def __init__(self, cfg: dict[str, Any], verbose: bool = False):
+        self.c = abi.Config()
+        lib.mcxg_initcfg(C.byref(self.c))
+        self.keep: list[Any] = []
+        c = self.c
+        c.flog = C.c_void_p.in_dll(libc, "stderr").value if verbose else None
+        for k in _SCALARS_INT:
+            if k in cfg:
+                setattr(c, k, int(float(cfg[k])))
+        for k in _SCALARS_FLOAT:
+            if k in cfg:
+                setattr(c, k, float(cfg[k]))
+        for k in _SCALARS_CHAR:
+            if k in cfg:
+                setattr(c, k, bytes([int(cfg[k]) & 0xFF]))
+        if "seed" in cfg:
+            seed = cfg["seed"]
+            if isinstance(seed, np.ndarray) or isinstance(seed, (list, tuple)):
+                raise MCXError(-6, "photon replay is not supported by the GB300 engine")
+            c.seed = int(seed)
+        if "session" in cfg:
+            c.session = str(cfg["session"]).encode()[: abi.SESSION_LEN - 1]
+        if "srctype" in cfg:
+            st = cfg["srctype"]
+            c.srctype = bytes([_SRC_TYPES.index(st.lower()) if isinstance(st, str) else int(st)])
+        if "outputtype" in cfg:
+            ot = cfg["outputtype"]
+            c.outputtype = bytes([_OUTPUT_TYPES[ot.lower()] if isinstance(ot, str) else int(ot)])
+        if "savedetflag" in cfg:
+            f = cfg["savedetflag"]
+            if isinstance(f, str):
+                f = sum(1 << _SAVEDET_CHARS.index(ch) for ch in f.lower() if ch in _SAVEDET_CHARS)
+            c.savedetflag = int(f)
+        if "bc" in cfg:
+            c.bc = str(cfg["bc"]).encode()[:12]
+        for key, n in (("srcpos", 4), ("srcdir", 4), ("srcparam1", 4), ("srcparam2", 4), ("srciquv", 4)):
+            if key in cfg:
+                _set_vec(getattr(c, key), cfg[key], n)
+        if "steps" in cfg:
+            _set_vec(c.steps, cfg["steps"], 3)
+
+        if "vol" not in cfg or "prop" not in cfg:
+            raise MCXError(-4, "the 'vol' and 'prop' fields are required")
+        vol = np.asarray(cfg["vol"])
+        if vol.ndim != 3:
+            raise MCXError(-4, "the 'vol' field must be a 3-D label array")
+        if vol.dtype.kind == "f":
+            raise MCXError(-6, "only label-based media are supported by the GB300 engine")
+        vol32 = np.asfortranarray(vol.astype(np.uint32, copy=False)).ravel(order="F").copy()
+        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in vol.shape)
+        c.mediabyte = {1: 1, 2: 2, 4: 4, 8: 4}[vol.dtype.itemsize]
+        self.vol = vol32
+        c.vol = vol32.ctypes.data
+
+        prop = np.ascontiguousarray(np.asarray(cfg["prop"], dtype=np.float32).reshape(-1, 4))
+        self.prop = prop
+        c.prop = prop.ctypes.data
+        c.medianum = prop.shape[0]
+
+        if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
+            dp = np.asarray(cfg["detpos"], dtype=np.float32)
+            dp = dp.reshape(-1, dp.shape[-1]) if dp.ndim > 1 else dp.reshape(1, -1)
+            if dp.shape[1] == 3:
+                dp = np.hstack([dp, np.full((dp.shape[0], 1), float(cfg.get("detradius", 1.0)), np.float32)])
+            self.detpos = np.ascontiguousarray(dp[:, :4])
+            c.detpos = self.detpos.ctypes.data
+            c.detnum = self.detpos.shape[0]
+        else:
+            self.detpos = None
+            c.detnum = 0
+        if "issavedet" not in cfg and c.detnum == 0:
+            c.issavedet = b"\x00"
+
+        lib.mcxg_clear_error()
+        rc = lib.mcxg_validatecfg(C.byref(c))
+        _check(rc)
+
+    @property
+    def dims(self) -> tuple[int, int, int]:
+        return int(self.c.dim.x), int(self.c.dim.y), int(self.c.dim.z)
+
+    @property
+    def ngates(self) -> int:
+        return max(1, int((self.c.tend - self.c.tstart) / self.c.tstep + 0.5))
+
+    @property
+    def reclen(self) -> int:
+        return int(self.c.his.colcount)
+
+
+def prepare(cfg: dict[str, Any], verbose: bool = False) -> PreparedConfig:
+    """Fill and validate a Config (no GPU needed); the oracle consumes the same object."""
+    return PreparedConfig(cfg, verbose=verbose)
+
+
+def gpuinfo() -> list[dict[str, Any]]:
+    """Device list as ``pmcx.gpuinfo()`` reports it (src/pmcx.cpp:1404)."""
+    c = abi.Config()
+    lib.mcxg_initcfg(C.byref(c))
+    c.flog = None
+    c.isgpuinfo = bytes([3])
+    info = C.POINTER(abi.GPUInfo)()
+    lib.mcxg_clear_error()
+    n = lib.mcx_list_gpu(C.byref(c), C.byref(info))
+    _check()
+    out = []
+    if info:
+        count = info[0].devcount if n else 0
+        for i in range(count):
+            g = info[i]
+            out.append({f[0]: (getattr(g, f[0]).decode() if f[0] == "name" else getattr(g, f[0]))
+                        for f in abi.GPUInfo._fields_ if not f[0].startswith("_pad")})
+        libc.free(info)
+    return out
+
+
+def run(cfg: dict[str, Any], verbose: bool = False, fp64_field: bool = False) -> dict[str, Any]:
+    """Run one simulation on the GPU; same inputs and outputs as ``pmcx.run``.
+
+    ``fp64_field`` accumulates the fluence in FP64 on the device (the reference-accuracy twin of
+    the FP32 production path, used to state its accumulation error)."""
+    pc = prepare(cfg, verbose=verbose)
+    return run_prepared(pc, fp64_field=fp64_field)
+
+
+def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]:
+    c = pc.c
+    nx, ny, nz = pc.dims
+    info = C.POINTER(abi.GPUInfo)()
+    lib.mcxg_clear_error()
+    nact = lib.mcx_list_gpu(C.byref(c), C.byref(info))
+    _check()
+    if nact == 0:
+        if info:
+            libc.free(info)
+        raise MCXError(-1, "no active GPU device found")
+    maxgate = pc.ngates if c.maxgate == 0 else min(int(c.maxgate), pc.ngates)
+    flux = None
+    if c.issave2pt != b"\x00":
+        flux = np.zeros(nx * ny * nz * maxgate, dtype=np.float32)
+        c.exportfield = flux.ctypes.data
+    try:
+        (lib.mcxg_run_simulation_fp64 if fp64_field else lib.mcx_run_simulation)(C.byref(c), info)
+        _check()
+    finally:
+        libc.free(info)
+        det_ptr = c.exportdetected
+        ndet = int(c.detectedcount)
+        detp = None
+        if det_ptr:
+            reclen = pc.reclen
+            if ndet and reclen:
+                buf = (C.c_float * (reclen * ndet)).from_address(det_ptr)
+                detp = np.frombuffer(buf, dtype=np.float32).copy().reshape((reclen, ndet), order="F")
+            libc.free(C.c_void_p(det_ptr))
+            c.exportdetected = None
+    st = abi.Stats()
+    lib.mcxg_get_stats(C.byref(st))
+    out: dict[str, Any] = {}
+    if flux is not None:
+        out["flux"] = flux.reshape((nx, ny, nz, maxgate), order="F")
+        c.exportfield = None
+    if c.issavedet != b"\x00" and detp is not None:
+        out["detp"] = detp
+    out["stat"] = {
+        "runtime": int(c.runtime),
+        "nphoton": int(c.nphoton) * (int(c.respin) if c.respin > 1 else 1),
+        "energytot": float(c.energytot),
+        "energyabs": float(c.energyabs),
+        "normalizer": float(c.normalizer),
+        "unitinmm": float(c.unitinmm),
+        "workload": [1.0],
+        "detected": int(c.his.detected),
+        # beyond pmcx: FP64 tallies and the GPU's own counters
+        "e_launch": st.e_launch, "e_escape": st.e_escape, "e_detect": st.e_detect,
+        "e_absdep": st.e_absdep, "e_absother": st.e_absother,
+        "n_steps": st.n_steps, "n_scatter": st.n_scatter, "n_deposit": st.n_deposit,
+        "n_launch": st.n_launch, "n_photon": st.n_photon, "n_detected": st.n_detected,
+        "n_tile_deposit": st.n_tile_deposit, "kernel_ms": st.kernel_ms, "total_ms": st.total_ms,
+        "grid": st.grid, "block": st.block, "chunk": st.chunk, "launches": st.launches,
+        "error_flags": st.error_flags,
+    }
+    return out
+
+
+def version() -> str:
+    return "mcx-gb300 0.1 (MCX v2025.10 compatible)"

@@ -1,0 +1,834 @@
+// engine.cu -- host driver of the GB300 engine and the C-ABI entry points.
+//
+// mcx_run_simulation / mcx_list_gpu replace MCX's src/mcx_core.cu:2621-2726 and 2740-4110 with
+// the same contract towards the front-ends (Config in, fluence / detected photons / energies /
+// runtime out, errors through mcx_error) but a different inside: one persistent transport
+// launch per (time-gate group x respin) on a private stream, all outputs merged and normalised
+// on the device before a single copy back, FP64 energy tallies, stream-ordered allocations
+// that are reused across calls.
+//
+// Config fields read: nphoton, seed, srcpos, srcdir, srcparam2 (launch voxel/label), tstart,
+// tstep, tend, steps, dim, medianum, prop, detnum, detpos, maxdetphoton, maxgate, respin,
+// vol, isreflect, isnormalized, issavedet, issave2pt, isspecular, outputtype, minenergy,
+// unitinmm, flog, maxvoidstep, voidtime, savedetflag, deviceid, parentid, gscatter, bc.
+// Config fields written: exportfield (+=), exportdetected (realloc), detectedcount, runtime,
+// energytot, energyabs, energyesc, normalizer, his.{normalizer,detected,respin,colcount,...},
+// deviceid (compacted by mcx_list_gpu).
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mcx_abi.h"
+#include "../../include/mcx_gb300.h"
+#include "mcxg_common.h"
+#include "transport.cuh"
+
+// Provided by an MCX front-end (src/mcx_utils.c) when one is linked; absent otherwise.
+extern "C" void mcx_error(const int id, const char* msg, const char* file, const int linenum) __attribute__((weak));
+extern "C" void mcx_savedata(float* dat, size_t len, Config* cfg) __attribute__((weak));
+extern "C" void mcx_savedetphoton(float* ppath, void* seeds, int count, int seedbyte, Config* cfg) __attribute__((weak));
+extern "C" int omp_get_thread_num(void) __attribute__((weak));
+
+namespace mcxg {
+
+namespace {
+thread_local int t_err_id = 0;
+thread_local std::string t_err_msg;
+thread_local mcxg_stats t_stats;
+
+struct LaunchOverride {
+    int block = 0, blocks_per_sm = 0, chunk = 0, tile = -1;
+} g_override;
+std::mutex g_override_mu;
+}  // namespace
+
+[[noreturn]] void raise(int id, const std::string& msg, const char* file, int line) { throw Error{id, msg, file, line}; }
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) MCXG_RAISE(-(int)e_, cudaGetErrorString(e_));            \
+    } while (0)
+
+namespace {
+
+// Route an engine error to the front-end's mcx_error (which exits or throws, as MCX does) or,
+// without a front-end, record it for mcxg_last_error().
+void report(const Error& e) {
+    t_err_id = e.id ? e.id : -1;
+    t_err_msg = e.msg;
+    if (mcx_error) mcx_error(t_err_id, e.msg.c_str(), e.file, e.line);
+}
+
+// A device allocation released at scope exit, stream-ordered so the pool reuses it.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t s = nullptr;
+    void alloc(size_t n, cudaStream_t stream) {
+        release();
+        s = stream;
+        bytes = n;
+        if (n) CK(cudaMallocAsync(&p, n, stream));
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        bytes = 0;
+    }
+    ~DevBuf() { release(); }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+
+// Void skipping of a pencil source launched outside the volume or in a 0 voxel
+// (src/mcx_core.cu:866-956).  The path is deterministic, so the host traces it once and every
+// photon starts from the result.  Returns the entry voxel or -1.
+int host_skipvoid(const Config* cfg, float4& p, float3& v, float& t, int fd[3]) {
+    const float mx = (float)cfg->dim.x, my = (float)cfg->dim.y, mz = (float)cfg->dim.z;
+    const float minaccum = kR_C0 * cfg->unitinmm;
+    const float rv[3] = {1.f / v.x, 1.f / v.y, 1.f / v.z};
+    auto inside = [&](const int f[3]) {
+        return (unsigned short)f[0] < mx && (unsigned short)f[1] < my && (unsigned short)f[2] < mz;
+    };
+    auto index = [&](const int f[3]) { return (long)f[2] * cfg->dim.x * cfg->dim.y + (long)f[1] * cfg->dim.x + f[0]; };
+    int f[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
+    int count = 1;
+    while (true) {
+        if (inside(f) && (cfg->vol[index(f)] & kMED_MASK)) {
+            p.x -= v.x; p.y -= v.y; p.z -= v.z;
+            f[0] = (int)std::floor(p.x); f[1] = (int)std::floor(p.y); f[2] = (int)std::floor(p.z);
+            t -= minaccum;
+            count = 0;
+            int axis = -1;
+            while (!inside(f) || !(cfg->vol[index(f)] & kMED_MASK)) {
+                const float h0 = std::fabs((f[0] + (v.x > 0.f) - p.x) * rv[0]);
+                const float h1 = std::fabs((f[1] + (v.y > 0.f) - p.y) * rv[1]);
+                const float h2 = std::fabs((f[2] + (v.z > 0.f) - p.z) * rv[2]);
+                const float d = std::fmin(std::fmin(h0, h1), h2);
+                axis = (d == h0) ? 0 : ((d == h1) ? 1 : 2);
+                t += minaccum * d;
+                p.x += d * v.x; p.y += d * v.y; p.z += d * v.z;
+                if (axis == 0) f[0] += (v.x > 0.f ? 1 : -1);
+                if (axis == 1) f[1] += (v.y > 0.f ? 1 : -1);
+                if (axis == 2) f[2] += (v.z > 0.f ? 1 : -1);
+                if (count++ > 3) break;
+            }
+            if (!inside(f)) return -1;
+            t = cfg->voidtime ? t : 0.f;
+            const long id = index(f);
+            const Medium& np = cfg->prop[cfg->vol[id] & kMED_MASK];
+            if (cfg->isspecular && axis >= 0 && np.n != cfg->prop[0].n) {
+                // specular loss at the entry face (reflectcoeff, src/mcx_core.cu:552-570) and refraction
+                const float n1 = cfg->prop[0].n, n2 = np.n;
+                const float vv[3] = {v.x, v.y, v.z};
+                const float Icos = std::fabs(vv[axis]);
+                const float a = n1 * n1, b = n2 * n2;
+                float c = 1.f - a / b * (1.f - Icos * Icos);
+                float R = 1.f;
+                if (c > 0.f) {
+                    float Re = a * Icos * Icos + b * c;
+                    c = std::sqrt(c);
+                    const float Im = 2.f * n1 * n2 * Icos * c;
+                    R = (Re - Im) / (Re + Im);
+                    Re = b * Icos * Icos + a * c * c;
+                    R = (R + (Re - Im) / (Re + Im)) * 0.5f;
+                }
+                p.w *= 1.f - R;
+                if (p.w > kEPS) {
+                    float w3[3] = {v.x * n1 / n2, v.y * n1 / n2, v.z * n1 / n2};
+                    const int a1 = (axis + 1) % 3, a2 = (axis + 2) % 3;
+                    const float s = w3[a1] * w3[a1] + w3[a2] * w3[a2];
+                    w3[axis] = (s < 1.f) ? std::sqrt(1.f - s) * (float)((w3[axis] > 0.f) - (w3[axis] < 0.f)) : 0.f;
+                    const float r = 1.f / std::sqrt(w3[0] * w3[0] + w3[1] * w3[1] + w3[2] * w3[2]);
+                    v = f3(w3[0] * r, w3[1] * r, w3[2] * r);
+                }
+            }
+            fd[0] = f[0]; fd[1] = f[1]; fd[2] = f[2];
+            return (int)id;
+        }
+        if ((p.x < 0.f && v.x <= 0.f) || (p.x >= mx && v.x >= 0.f) || (p.y < 0.f && v.y <= 0.f) ||
+            (p.y >= my && v.y >= 0.f) || (p.z < 0.f && v.z <= 0.f) || (p.z >= mz && v.z >= 0.f))
+            return -1;
+        p.x += v.x; p.y += v.y; p.z += v.z;
+        f[0] = (int)std::floor(p.x); f[1] = (int)std::floor(p.y); f[2] = (int)std::floor(p.z);
+        t += minaccum;
+        if (count++ > cfg->maxvoidstep) return -1;
+    }
+}
+
+// Byte-label volume of the host uint32 volume (bit 31 -> bit 7).  Done on the device when the
+// session uploads; this host twin serves the void-skipping trace only.
+uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Session: one prepared simulation on one device.
+// ---------------------------------------------------------------------------------------------
+struct Session {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    KParams kp{};
+    bool reflect = false, savedet = false, use64 = false;
+    int block = 256, grid = 0, sms = 0;
+    size_t smem = 0;
+    size_t nvox = 0, fieldlen = 0;
+    int totalgates = 1;
+    DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos;
+    double kernel_ms = 0.0;
+    int launches = 0;
+
+    ~Session() {
+        labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
+        detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
+        if (stream) cudaStreamSynchronize(stream);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void create(const Config* cfg, int dev, bool fp64_field) {
+        device = dev;
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&ev0));
+        CK(cudaEventCreate(&ev1));
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;   // keep freed blocks for the next run instead of returning them
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, device));
+        sms = prop.multiProcessorCount;
+
+        if (cfg->medianum < 1 || cfg->medianum > (unsigned)kMaxMedia)
+            MCXG_RAISE(-6, "the GB300 engine supports 1 to 128 media labels");
+        if (!cfg->vol) MCXG_RAISE(-4, "the 'vol' field in the input structure can not be empty");
+        if (cfg->dim.x >= 32768 || cfg->dim.y >= 32768 || cfg->dim.z >= 32768)
+            MCXG_RAISE(-6, "volume dimensions must be below 32768");
+        nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        use64 = fp64_field;
+
+        // gates held on the device at once (src/mcx_core.cu:2898-2902, 2944-2956)
+        totalgates = (int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5f);
+        if (totalgates < 1) totalgates = 1;
+        int maxgate = (cfg->maxgate > 0) ? std::min<int>((int)cfg->maxgate, totalgates) : totalgates;
+        size_t freeb = 0, totalb = 0;
+        cudaMemGetInfo(&freeb, &totalb);
+        const size_t per_gate = nvox * (use64 ? sizeof(double) : 2 * sizeof(float)) + nvox * sizeof(float);
+        const size_t budget = freeb > (size_t)(1u << 30) ? freeb - (size_t)(1u << 30) : freeb / 2;
+        if ((size_t)maxgate * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / per_gate));
+        fieldlen = nvox * (size_t)maxgate;
+
+        // labels: upload the uint32 volume, pack to one byte per voxel on the device
+        {
+            DevBuf vol32;
+            vol32.alloc(nvox * sizeof(uint32_t), stream);
+            CK(cudaMemcpyAsync(vol32.p, cfg->vol, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+            labels.alloc(nvox, stream);
+            err.alloc(sizeof(unsigned), stream);
+            CK(cudaMemsetAsync(err.p, 0, sizeof(unsigned), stream));
+            CK(launch_labels_from_vol(vol32.as<uint32_t>(), labels.as<uint8_t>(), nvox, cfg->medianum, err.as<unsigned>(), stream));
+            unsigned e = 0;
+            CK(cudaMemcpyAsync(&e, err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            if (e & kErrBadLabel) MCXG_RAISE(-4, "input media optical properties are less than the labels in the volume");
+        }
+
+        KParams& k = kp;
+        std::memset(&k, 0, sizeof(k));
+        k.nx = (int)cfg->dim.x; k.ny = (int)cfg->dim.y; k.nz = (int)cfg->dim.z;
+        k.dimxy = cfg->dim.x * cfg->dim.y;
+        k.nvox = (unsigned)nvox;
+        k.medianum = (int)cfg->medianum;
+        for (unsigned i = 0; i < cfg->medianum; i++)
+            k.prop[i] = make_float4(cfg->prop[i].mua, cfg->prop[i].mus, cfg->prop[i].g, cfg->prop[i].n);
+        k.oneoverc0 = kR_C0 * cfg->unitinmm;
+        k.Rtstep = 1.f / cfg->tstep;
+        k.maxgate = maxgate;
+        k.doreflect = cfg->isreflect ? 1 : 0;
+        k.save2pt = cfg->issave2pt ? 1 : 0;
+        k.outputtype = cfg->outputtype;
+        if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
+            MCXG_RAISE(-6, "the GB300 engine supports flux, fluence and energy outputs");
+        k.minenergy = cfg->minenergy;
+        k.gscatter = (float)cfg->gscatter;
+        k.maxvoidstep = (float)cfg->maxvoidstep;
+        std::memcpy(k.bc, cfg->bc, 12);
+        reflect = cfg->isreflect != 0;
+        for (int i = 0; i < 6; i++)
+            if (cfg->bc[i] == BC_REFLECT || cfg->bc[i] == BC_MIRROR) reflect = true;
+
+        // detectors and record layout (src/mcx_core.cu:2840-2847)
+        savedet = cfg->issavedet && (cfg->detnum > 0 || std::any_of(cfg->bc + 6, cfg->bc + 12, [](char c) { return c != 0; }));
+        const unsigned f = cfg->savedetflag;
+        k.savedetflag = f;
+        k.nmedia_det = (int)cfg->medianum - 1;
+        k.partialdata = (cfg->medianum - 1) * (((f >> 1) & 1u) + ((f >> 2) & 1u) + ((f >> 3) & 1u));
+        k.reclen = k.partialdata + (f & 1u) + 3u * (((f >> 4) & 1u) + ((f >> 5) & 1u)) + ((f >> 6) & 1u);
+        k.maxdet = cfg->maxdetphoton;
+        k.ndet = (int)cfg->detnum;
+        if (cfg->detnum) {
+            detpos.alloc(sizeof(float4) * cfg->detnum, stream);
+            CK(cudaMemcpyAsync(detpos.p, cfg->detpos, sizeof(float4) * cfg->detnum, cudaMemcpyHostToDevice, stream));
+            k.detpos = detpos.as<float4>();
+        }
+
+        // launch state of the pencil beam, void skipping folded in (src/mcx_core.cu:1236-1243, 1652-1672)
+        float4 p = cfg->srcpos;
+        float3 v = f3(cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z);
+        float t = 0.f;
+        uint32_t sidx, smed;
+        std::memcpy(&sidx, &cfg->srcparam2.z, 4);
+        std::memcpy(&smed, &cfg->srcparam2.w, 4);
+        int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
+        k.src_ok = 1;
+        if ((smed & kMED_MASK) == 0) {
+            const int id = host_skipvoid(cfg, p, v, t, fd);
+            if (id < 0) {
+                k.src_ok = 0;
+            } else {
+                sidx = (uint32_t)id;
+                smed = host_label(cfg, id);
+            }
+        }
+        if (std::fabs(p.w) <= cfg->minenergy) k.src_ok = 0;
+        k.src_p = p;
+        k.src_v = make_float4(v.x, v.y, v.z, 0.f);
+        k.src_t = t;
+        k.src_idx = sidx;
+        k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
+        if (k.src_ok) {
+            k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
+        }
+        k.step_cap = 20000000u;   // a photon longer than this is a fault: flagged and stopped
+
+        // output and scratch buffers
+        field.alloc(fieldlen * sizeof(float), stream);
+        outbuf.alloc(fieldlen * sizeof(float), stream);
+        if (use64) field64.alloc(fieldlen * sizeof(double), stream);
+        else shadow.alloc(fieldlen * sizeof(float), stream);
+        if (savedet) {
+            detp.alloc((size_t)k.maxdet * k.reclen * sizeof(float), stream);
+            detcount.alloc(sizeof(unsigned), stream);
+        }
+        energy.alloc(sizeof(double) * kNumEnergy, stream);
+        counters.alloc(sizeof(unsigned long long) * kNumCounters, stream);
+        work.alloc(sizeof(unsigned long long), stream);
+        k.labels = labels.as<uint8_t>();
+        k.field = field.as<float>();
+        k.shadow = shadow.as<float>();
+        k.field64 = field64.as<double>();
+        k.detp = detp.as<float>();
+        k.detcount = detcount.as<unsigned>();
+        k.energy = energy.as<double>();
+        k.counters = counters.as<unsigned long long>();
+        k.errflag = err.as<unsigned>();
+        k.work = work.as<unsigned long long>();
+        reset();
+
+        configure_launch(cfg);
+    }
+
+    // Block size, CTAs per SM and refill chunk; the deposit tile placed over the source.
+    void configure_launch(const Config* cfg) {
+        LaunchOverride o;
+        {
+            std::lock_guard<std::mutex> g(g_override_mu);
+            o = g_override;
+        }
+        block = o.block > 0 ? o.block : 256;
+        choose_tile(cfg, o.tile);
+        smem = transport_smem_bytes(kp, block, savedet);
+        int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        if (bps <= 0) {
+            kp.tile_on = 0;
+            smem = transport_smem_bytes(kp, block, savedet);
+            bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        }
+        if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
+        if (o.blocks_per_sm > 0) bps = std::min(bps, o.blocks_per_sm);
+        grid = bps * sms;
+        kp.chunk = o.chunk > 0 ? o.chunk : 64;
+    }
+
+    // Deposit tile: a box of voxels x gates around the point where photons enter the medium,
+    // extending along the launch direction, sized to a shared-memory budget.
+    void choose_tile(const Config* cfg, int tile_kb) {
+        KParams& k = kp;
+        k.tile_on = 0;
+        if (!k.save2pt || !k.src_ok) return;
+        const int kb = (tile_kb >= 0) ? tile_kb : 16;
+        if (kb <= 0) return;
+        const int elems = kb * 1024 / (int)sizeof(float);
+        int tg = std::min(k.maxgate, 4);
+        int edge = 1;
+        while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+        while (edge < 6 && tg > 1) {
+            tg--;
+            edge = 1;
+            while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+        }
+        edge = std::min(edge, std::max(k.nx, std::max(k.ny, k.nz)));
+        const int tnx = std::min(edge, k.nx), tny = std::min(edge, k.ny), tnz = std::min(edge, k.nz);
+        const float c[3] = {k.src_p.x + 0.5f * edge * k.src_v.x, k.src_p.y + 0.5f * edge * k.src_v.y,
+                            k.src_p.z + 0.5f * edge * k.src_v.z};
+        auto place = [](float center, int n, int dim) { return std::max(0, std::min(dim - n, (int)std::floor(center - 0.5f * n))); };
+        k.tnx = tnx; k.tny = tny; k.tnz = tnz;
+        k.tx0 = place(c[0], tnx, k.nx);
+        k.ty0 = place(c[1], tny, k.ny);
+        k.tz0 = place(c[2], tnz, k.nz);
+        k.tg0 = 0;
+        k.tng = tg;
+        k.tile_on = 1;
+        (void)cfg;
+    }
+
+    void reset() {
+        CK(cudaMemsetAsync(field.p, 0, field.bytes, stream));
+        if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, stream));
+        if (field64.p) CK(cudaMemsetAsync(field64.p, 0, field64.bytes, stream));
+        if (detcount.p) CK(cudaMemsetAsync(detcount.p, 0, detcount.bytes, stream));
+        CK(cudaMemsetAsync(energy.p, 0, energy.bytes, stream));
+        CK(cudaMemsetAsync(counters.p, 0, counters.bytes, stream));
+        CK(cudaMemsetAsync(err.p, 0, err.bytes, stream));
+        kernel_ms = 0.0;
+        launches = 0;
+    }
+
+    void set_window(float twin0, float twin1) {
+        kp.twin0 = twin0;
+        kp.twin1 = twin1;
+    }
+
+    // One persistent transport launch over photons [offset, offset + n).
+    float run(uint64_t offset, uint64_t n, uint64_t seed) {
+        CK(cudaSetDevice(device));
+        kp.photon_offset = offset;
+        kp.nphoton = n;
+        kp.seed = seed;
+        CK(cudaMemsetAsync(work.p, 0, sizeof(unsigned long long), stream));
+        CK(cudaEventRecord(ev0, stream));
+        CK(launch_transport(kp, reflect, savedet, grid, block, smem, stream));
+        CK(cudaEventRecord(ev1, stream));
+        CK(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        kernel_ms += ms;
+        launches++;
+        return ms;
+    }
+
+    // Merge shadow copies, optionally scale, and copy the field out.
+    void read_field(float* host, float scale, int positive_only) {
+        CK(launch_merge_field(outbuf.as<float>(), field.as<float>(), shadow.as<float>(), field64.as<double>(), fieldlen, scale,
+                              positive_only, stream));
+        CK(cudaMemcpyAsync(host, outbuf.p, fieldlen * sizeof(float), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+    }
+
+    unsigned detected() {
+        if (!detcount.p) return 0;
+        unsigned d = 0;
+        CK(cudaMemcpyAsync(&d, detcount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        return d;
+    }
+
+    void read_stats(mcxg_stats* st) {
+        double e[kNumEnergy];
+        unsigned long long c[kNumCounters];
+        unsigned ef = 0;
+        CK(cudaMemcpyAsync(e, energy.p, sizeof(e), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(c, counters.p, sizeof(c), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(&ef, err.p, sizeof(ef), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        st->e_launch = e[kELaunch]; st->e_escape = e[kEEscape]; st->e_detect = e[kEDetect];
+        st->e_absdep = e[kEAbsDep]; st->e_absother = e[kEAbsOther];
+        st->n_steps = c[kCntSteps]; st->n_scatter = c[kCntScatter]; st->n_deposit = c[kCntDeposit];
+        st->n_launch = c[kCntLaunch]; st->n_photon = c[kCntPhoton]; st->n_detected = c[kCntDetected];
+        st->n_tile_deposit = c[kCntTileDeposit];
+        st->kernel_ms = kernel_ms;
+        st->grid = grid; st->block = block; st->chunk = kp.chunk; st->launches = launches;
+        st->error_flags = ef;
+    }
+};
+
+}  // namespace mcxg
+
+using namespace mcxg;
+
+// ---------------------------------------------------------------------------------------------
+// Error plumbing
+// ---------------------------------------------------------------------------------------------
+extern "C" const char* mcxg_last_error(void) { return t_err_msg.c_str(); }
+extern "C" int mcxg_last_error_id(void) { return t_err_id; }
+extern "C" void mcxg_clear_error(void) { t_err_id = 0; t_err_msg.clear(); }
+extern "C" void mcxg_set_error(int id, const char* msg) { t_err_id = id; t_err_msg = msg ? msg : ""; }
+extern "C" int mcxg_get_stats(mcxg_stats* out) {
+    if (!out) return -1;
+    *out = t_stats;
+    return 0;
+}
+extern "C" void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile) {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    g_override.block = block;
+    g_override.blocks_per_sm = blocks_per_sm;
+    g_override.chunk = chunk;
+    g_override.tile = tile;
+}
+
+// ---------------------------------------------------------------------------------------------
+// mcx_list_gpu (src/mcx_core.cu:2621-2726)
+// ---------------------------------------------------------------------------------------------
+extern "C" int mcx_list_gpu(Config* cfg, GPUInfo** info) {
+    try {
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess) {
+            if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                MCXG_RAISE(-(int)e, "A CUDA-capable GPU is not found or configured");
+            MCXG_RAISE(-(int)e, cudaGetErrorString(e));
+        }
+        if (count == 0) {
+            if (cfg->flog) fprintf(cfg->flog, "ERROR: No CUDA-capable GPU device found\n");
+            return 0;
+        }
+        *info = (GPUInfo*)calloc((size_t)count, sizeof(GPUInfo));
+        if (cfg->gpuid && cfg->gpuid > count) {
+            if (cfg->flog) fprintf(cfg->flog, "ERROR: Specified GPU ID is out of range\n");
+            free(*info);
+            *info = nullptr;
+            return 0;
+        }
+        int active = 0;
+        for (int dev = 0; dev < count; dev++) {
+            cudaDeviceProp dp;
+            CK(cudaGetDeviceProperties(&dp, dev));
+            if (cfg->isgpuinfo == 3) {
+                active++;
+            } else if (cfg->deviceid[dev] == '1') {
+                cfg->deviceid[dev] = '\0';
+                cfg->deviceid[active] = (char)(dev + 1);
+                active++;
+            }
+            GPUInfo& g = (*info)[dev];
+            strncpy(g.name, dp.name, MCXG_SESSION_LEN - 1);
+            g.id = dev + 1;
+            g.devcount = count;
+            g.major = dp.major;
+            g.minor = dp.minor;
+            g.globalmem = dp.totalGlobalMem;
+            g.constmem = dp.totalConstMem;
+            g.sharedmem = dp.sharedMemPerBlock;
+            g.regcount = dp.regsPerBlock;
+            int clk = 0;
+            cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, dev);
+            g.clock = clk;
+            g.sm = dp.multiProcessorCount;
+            g.core = dp.multiProcessorCount * 128;
+            g.maxmpthread = dp.maxThreadsPerMultiProcessor;
+            g.maxgate = cfg->maxgate;
+            // this engine's persistent launch: 256-thread CTAs filling every SM
+            g.autoblock = 256;
+            g.autothread = g.autoblock * (dp.maxThreadsPerMultiProcessor / g.autoblock) * g.sm;
+            if (cfg->isgpuinfo) {
+                FILE* o = stdout;
+                fprintf(o, "=============================   GPU Information  ================================\n");
+                fprintf(o, "Device %d of %d:\t\t%s\n", g.id, g.devcount, g.name);
+                fprintf(o, "Compute Capability:\t%u.%u\n", g.major, g.minor);
+                fprintf(o, "Global Memory:\t\t%.0f B\nConstant Memory:\t%.0f B\nShared Memory:\t\t%.0f B\nRegisters:\t\t%u\nClock Speed:\t\t%.2f GHz\n",
+                        (double)g.globalmem, (double)g.constmem, (double)g.sharedmem, (unsigned)g.regcount, g.clock * 1e-6f);
+                fprintf(o, "Number of SMs:\t\t%u\nNumber of Cores:\t%u\n", g.sm, g.core);
+                fprintf(o, "Auto-thread:\t\t%d\nAuto-block:\t\t%d\n", g.autothread, g.autoblock);
+            }
+        }
+        if (cfg->isgpuinfo == 2 && cfg->parentid == mpStandalone) exit(0);
+        if (active < MCXG_MAX_DEVICE) cfg->deviceid[active] = '\0';
+        return active;
+    } catch (const Error& e) {
+        report(e);
+        return 0;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// mcx_run_simulation (src/mcx_core.cu:2740-4110)
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
+    const auto t_start = std::chrono::steady_clock::now();
+    const int threadid = omp_get_thread_num ? omp_get_thread_num() : 0;
+    if (threadid >= MCXG_MAX_DEVICE || cfg->deviceid[threadid] == '\0') return;
+    if (threadid > 0) {
+        // one device per call: replicas on further devices are left to the caller
+        if (cfg->flog) fprintf(cfg->flog, "WARNING: the GB300 engine runs on one device per call; thread %d idle\n", threadid);
+        return;
+    }
+    const int gpuid = cfg->deviceid[threadid] - 1;
+    if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
+    (void)gpu;
+    if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "photon replay is not supported by the GB300 engine");
+    if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
+    if (cfg->srctype != 0) MCXG_RAISE(-6, "the GB300 engine supports the pencil source only");
+    if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media are supported by the GB300 engine");
+    if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
+
+    std::memset(&t_stats, 0, sizeof(t_stats));
+    Session S;
+    S.create(cfg, gpuid, fp64_field);
+    const KParams& k = S.kp;
+    const size_t dimxyz = S.nvox;
+    const int maxgate = k.maxgate;
+    const unsigned hostdetreclen = k.reclen;
+
+    if (cfg->exportfield == nullptr && cfg->issave2pt)
+        cfg->exportfield = (float*)calloc(dimxyz * (size_t)maxgate, sizeof(float));
+    if (cfg->exportdetected == nullptr)
+        cfg->exportdetected = (float*)malloc((size_t)hostdetreclen * std::max(1u, cfg->maxdetphoton) * sizeof(float));
+    cfg->detectedcount = 0;
+    cfg->his.detected = 0;
+    cfg->his.respin = cfg->respin;
+    cfg->his.colcount = hostdetreclen;
+    cfg->energytot = 0.0;
+    cfg->energyabs = 0.0;
+    cfg->energyesc = 0.0;
+    cfg->runtime = 0;
+
+    if (S.totalgates > maxgate && cfg->isnormalized) {
+        if (cfg->flog)
+            fprintf(cfg->flog, "WARNING: GPU memory can not hold all time gates, disabling normalization to allow multiple runs\n");
+        cfg->isnormalized = 0;
+    }
+    const int reps = std::abs(cfg->respin);
+    const uint64_t nper = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps;
+    const uint64_t seed = (uint64_t)(uint32_t)cfg->seed;
+    if (cfg->flog && cfg->printnum >= 0)
+        fprintf(cfg->flog, "GPU=%d (%s) np=%.0f grid=%d block=%d chunk=%d maxgate=%d repetition=%d\n", gpuid + 1,
+                gpu ? gpu[gpuid].name : "", (double)cfg->nphoton, S.grid, S.block, k.chunk, maxgate, reps);
+
+    std::vector<float> host_field(cfg->issave2pt ? S.fieldlen : 0);
+    std::vector<float> host_det;
+    mcxg_stats total{};
+    uint64_t run_index = 0;
+    for (int gate0 = 0; gate0 < S.totalgates; gate0 += maxgate) {
+        const float twin0 = cfg->tstart + cfg->tstep * gate0;
+        S.set_window(twin0, twin0 + cfg->tstep * maxgate);
+        S.reset();
+        for (int it = 0; it < reps; it++) {
+            if (S.savedet) CK(cudaMemsetAsync(S.detcount.p, 0, sizeof(unsigned), S.stream));
+            S.run(run_index * nper, nper, seed);
+            run_index++;
+            if (S.savedet) {
+                const unsigned det = S.detected();
+                cfg->his.detected += det;
+                const unsigned keep = std::min(det, cfg->maxdetphoton);
+                if (det > cfg->maxdetphoton && cfg->flog)
+                    fprintf(cfg->flog, "WARNING: the detected photon number is more than what your have specified (%u > %u), please use the -H option to specify a greater number\n",
+                            det, cfg->maxdetphoton);
+                if (keep && cfg->exportdetected) {
+                    cfg->exportdetected = (float*)realloc(cfg->exportdetected,
+                                                          (cfg->detectedcount + keep) * (size_t)hostdetreclen * sizeof(float));
+                    CK(cudaMemcpyAsync(cfg->exportdetected + cfg->detectedcount * hostdetreclen, S.detp.p,
+                                       (size_t)keep * hostdetreclen * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+                    CK(cudaStreamSynchronize(S.stream));
+                    cfg->detectedcount += keep;
+                }
+            }
+        }
+        mcxg_stats st{};
+        S.read_stats(&st);
+        if (st.error_flags & kErrStepCap)
+            MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
+        total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
+        total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
+        total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;
+        total.n_launch += st.n_launch; total.n_photon += st.n_photon; total.n_detected += st.n_detected;
+        total.n_tile_deposit += st.n_tile_deposit;
+        total.grid = st.grid; total.block = st.block; total.chunk = st.chunk; total.launches += st.launches;
+        total.error_flags |= st.error_flags;
+        cfg->energytot += st.e_launch;
+        cfg->energyesc += st.e_escape + st.e_detect;
+
+        if (cfg->issave2pt) {
+            // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
+            float scale = 1.f;
+            if (cfg->isnormalized && st.e_launch > 0.0) {
+                const double Vvox = (double)cfg->steps.x * cfg->steps.y * cfg->steps.z;
+                if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+                    double s = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
+                    if (cfg->outputtype == otFluence) s *= cfg->tstep;
+                    scale = (float)s;
+                } else {
+                    scale = (float)(1.0 / cfg->energytot);
+                }
+                cfg->normalizer = scale;
+                cfg->his.normalizer = scale;
+            }
+            S.read_field(host_field.data(), scale, cfg->isnormalized == 2);
+            float* out = cfg->exportfield;
+            for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
+        }
+    }
+    cfg->runtime = (unsigned)std::ceil(S.kernel_ms);
+    cfg->energyabs = cfg->energytot - cfg->energyesc;
+    total.kernel_ms = S.kernel_ms;
+    total.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    t_stats = total;
+
+    if (cfg->flog && cfg->printnum >= 0) {
+        if (S.savedet) fprintf(cfg->flog, "detected %u photons, total: %lu\n", cfg->his.detected, (unsigned long)cfg->detectedcount);
+        fprintf(cfg->flog, "kernel complete:  \t%.3f ms\n", S.kernel_ms);
+        fprintf(cfg->flog, "simulated %.0f photons (%.0f) with %d threads (repeat x%d)\nMCX simulation speed: %.2f photon/ms\n",
+                (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1), (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1),
+                S.grid * S.block, reps, (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1) / std::max(1e-3, S.kernel_ms));
+        fprintf(cfg->flog, "total simulated energy: %.2f\tabsorbed: %5.5f%%\n(loss due to initial specular reflection is excluded in the total)\n",
+                cfg->energytot, cfg->energytot > 0 ? (cfg->energytot - cfg->energyesc) / cfg->energytot * 100.0 : 0.0);
+        fflush(cfg->flog);
+    }
+    // file output in the standalone CLI (src/mcx_core.cu:3932-3978) when its writers are linked
+    if (cfg->parentid == mpStandalone) {
+        if (cfg->issave2pt && mcx_savedata) mcx_savedata(cfg->exportfield, S.fieldlen, cfg);
+        if (cfg->issavedet && cfg->exportdetected && mcx_savedetphoton) {
+            cfg->his.unitinmm = cfg->unitinmm;
+            cfg->his.savedphoton = (unsigned)cfg->detectedcount;
+            cfg->his.totalphoton = (unsigned)cfg->nphoton;
+            cfg->his.detected = (unsigned)cfg->detectedcount;
+            mcx_savedetphoton(cfg->exportdetected, cfg->seeddata, (int)cfg->detectedcount, 0, cfg);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" void mcx_run_simulation(Config* cfg, GPUInfo* gpu) {
+    mcxg_clear_error();
+    try {
+        run_simulation(cfg, gpu, false);
+    } catch (const Error& e) {
+        report(e);
+    }
+}
+
+// Same run with the field accumulated in FP64 on the device: the reference-accuracy twin used
+// to state the FP32 accumulation error of the production path.
+extern "C" void mcxg_run_simulation_fp64(Config* cfg, GPUInfo* gpu) {
+    mcxg_clear_error();
+    try {
+        run_simulation(cfg, gpu, true);
+    } catch (const Error& e) {
+        report(e);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// RNG test kernels
+// ---------------------------------------------------------------------------------------------
+extern "C" int mcxg_rng_test(const uint32_t seeds[4], float* out, int n) {
+    mcxg_clear_error();
+    try {
+        uint32_t* ds = nullptr;
+        float* dout = nullptr;
+        CK(cudaMalloc(&ds, 16));
+        CK(cudaMalloc(&dout, sizeof(float) * (size_t)std::max(n, 1)));
+        CK(cudaMemcpy(ds, seeds, 16, cudaMemcpyHostToDevice));
+        CK(launch_rng_test(ds, dout, n, 0));
+        CK(cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost));
+        cudaFree(ds);
+        cudaFree(dout);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}
+
+extern "C" int mcxg_photon_stream(uint64_t seed, uint64_t pid, float* out, int n) {
+    mcxg_clear_error();
+    try {
+        float* dout = nullptr;
+        CK(cudaMalloc(&dout, sizeof(float) * (size_t)std::max(n, 1)));
+        CK(launch_photon_stream(seed, pid, dout, n, 0));
+        CK(cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost));
+        cudaFree(dout);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Sessions
+// ---------------------------------------------------------------------------------------------
+struct mcxg_session {
+    Session s;
+};
+
+extern "C" mcxg_session* mcxg_session_create(const Config* cfg, int device) {
+    mcxg_clear_error();
+    mcxg_session* h = new mcxg_session();
+    try {
+        h->s.create(cfg, device, false);
+        h->s.set_window(cfg->tstart, cfg->tstart + cfg->tstep * h->s.kp.maxgate);
+        return h;
+    } catch (const Error& e) {
+        delete h;
+        report(e);
+        return nullptr;
+    }
+}
+
+extern "C" int mcxg_session_reset(mcxg_session* h) {
+    try {
+        h->s.reset();
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}
+
+extern "C" int mcxg_session_run(mcxg_session* h, uint64_t photon_offset, uint64_t nphoton, uint64_t seed, float* kernel_ms) {
+    try {
+        const float ms = h->s.run(photon_offset, nphoton, seed);
+        if (kernel_ms) *kernel_ms = ms;
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}
+
+extern "C" int64_t mcxg_session_read(mcxg_session* h, float* field, float* detp, uint64_t max_records, mcxg_stats* stats) {
+    try {
+        Session& s = h->s;
+        if (field) s.read_field(field, 1.f, 0);
+        const unsigned det = s.detected();
+        if (detp && s.detp.p && det) {
+            const uint64_t n = std::min<uint64_t>(std::min<uint64_t>(det, s.kp.maxdet), max_records);
+            CK(cudaMemcpyAsync(detp, s.detp.p, n * s.kp.reclen * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
+            CK(cudaStreamSynchronize(s.stream));
+        }
+        if (stats) s.read_stats(stats);
+        return (int64_t)det;
+    } catch (const Error& e) {
+        report(e);
+        return (int64_t)t_err_id;
+    }
+}
+
+extern "C" void mcxg_session_destroy(mcxg_session* h) { delete h; }

@@ -1,0 +1,601 @@
+// transport.cu -- the GB300 photon-transport kernel (sm_103a).
+//
+// Algorithm: MCX's voxel Monte Carlo (src/mcx_core.cu:1767-2528, pencil source, label media),
+// one photon per thread, re-organised for Blackwell:
+//   * persistent CTAs (grid = SMs x resident CTAs) whose warps refill dead lanes from a
+//     warp-private pool of photon indices, topped up with one global atomic per `chunk`
+//     photons -- no lane waits for a slow photon of another lane to finish a static quota;
+//   * every photon owns an xorshift128+ state in registers, seeded from (seed, photon index)
+//     so results do not depend on grid shape or scheduling;
+//   * labels are one byte per voxel (bit 7 = detector mask) read through the read-only
+//     path; the (mua, mus, g, n) table and derived constants live in shared memory because
+//     lanes index them with divergent labels;
+//   * fluence deposits inside a per-CTA voxel x gate box (sized and placed by the host over
+//     the densest deposit region) go to a shared-memory tile and reach L2 once per CTA; the
+//     rest are fire-and-forget FP32 reductions;
+//   * FP64 is used only for the energy tallies.
+// Semantics that must match the reference step for step are annotated with its file:line.
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "transport.cuh"
+
+namespace mcxg {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// xorshift128+ step, float from the low 32 bits (src/mcx_rand_xorshift128p.cu:56-72).
+__device__ __forceinline__ float rng_next(unsigned long long& a, unsigned long long& b) {
+    unsigned long long s1 = a;
+    const unsigned long long s0 = b;
+    a = s0;
+    s1 ^= s1 << 23;
+    b = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+    const unsigned lo = (unsigned)(b + s0);
+    return __uint_as_float(0x3F800000u | (lo >> 9)) - 1.0f;
+}
+
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long& x) {
+    unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Per-photon stream: identical to oracle/mcx_oracle.cpp seed_photon().
+__device__ __forceinline__ void seed_photon(unsigned long long seed, unsigned long long pid,
+                                            unsigned long long& a, unsigned long long& b) {
+    unsigned long long x = seed * 0xD1B54A32D192ED03ull + pid;
+    a = splitmix64(x);
+    b = splitmix64(x);
+    if ((a | b) == 0ull) b = 1ull;
+}
+
+// src/mcx_core.cu:470-478: move a coordinate one ulp towards `dir` after an offset that keeps
+// it positive.
+__device__ __forceinline__ float nextafter_mcx(float a, int dir, float offset) {
+    unsigned i = __float_as_uint(a + offset);
+    i += (unsigned)dir ^ (i & 0x80000000u);
+    return __uint_as_float(i) - offset;
+}
+
+// src/mcx_core.cu:1011-1031
+__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float st, float ct, float sp, float cp) {
+    float nx, ny, nz;
+    if (vz > -1.f + kEPS && vz < 1.f - kEPS) {
+        const float t0 = 1.f - vz * vz;
+        const float t1 = st * rsqrtf(t0);
+        nx = t1 * (vx * vz * cp - vy * sp) + vx * ct;
+        ny = t1 * (vy * vz * cp + vx * sp) + vy * ct;
+        nz = -t1 * t0 * cp + vz * ct;
+    } else {
+        nx = st * cp;
+        ny = st * sp;
+        nz = (vz > 0.f) ? ct : -ct;
+    }
+    const float r = rsqrtf(nx * nx + ny * ny + nz * nz);
+    vx = nx * r; vy = ny * r; vz = nz * r;
+}
+
+// src/mcx_core.cu:523-537: refraction applied to the axis normal to the face, renormalised.
+__device__ __forceinline__ void transmit(float& vx, float& vy, float& vz, float n1, float n2, int axis) {
+    const float r = __fdividef(n1, n2);
+    vx *= r; vy *= r; vz *= r;
+    if (axis == 0) {
+        const float s = vy * vy + vz * vz;
+        vx = (s < 1.f) ? sqrtf(1.f - s) * (float)((vx > 0.f) - (vx < 0.f)) : 0.f;
+    } else if (axis == 1) {
+        const float s = vx * vx + vz * vz;
+        vy = (s < 1.f) ? sqrtf(1.f - s) * (float)((vy > 0.f) - (vy < 0.f)) : 0.f;
+    } else {
+        const float s = vx * vx + vy * vy;
+        vz = (s < 1.f) ? sqrtf(1.f - s) * (float)((vz > 0.f) - (vz < 0.f)) : 0.f;
+    }
+    const float k = rsqrtf(vx * vx + vy * vy + vz * vz);
+    vx *= k; vy *= k; vz *= k;
+}
+
+// src/mcx_core.cu:258-270
+__device__ int find_detector(const KParams& P, float px, float py, float pz) {
+    for (int i = 0; i < P.ndet; i++) {
+        const float4 d = P.detpos[i];
+        if ((d.x - px) * (d.x - px) + (d.y - py) * (d.y - py) + (d.z - pz) * (d.z - pz) < d.w * d.w)
+            return (d.w < 0.f) ? 0 : i + 1;
+    }
+    return 0;
+}
+
+struct Smem {
+    float4* prop;       // medianum x (mua, mus, g, n)
+    float4* aux;        // medianum x (unused, unused, n/c0, unused)
+    double* tally;      // kNumEnergy x blockDim
+    float* ppath;       // partialdata x blockDim (detector runs)
+    float* tile;        // deposit tile
+};
+
+template <bool SAVEDET>
+__device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
+    Smem s;
+    s.prop = reinterpret_cast<float4*>(raw);
+    s.aux = s.prop + P.medianum;
+    s.tally = reinterpret_cast<double*>(s.aux + P.medianum);
+    s.ppath = reinterpret_cast<float*>(s.tally + kNumEnergy * blockDim.x);
+    s.tile = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
+    return s;
+}
+
+template <bool REFLECT, bool SAVEDET>
+__global__ void __launch_bounds__(256) transport_kernel(const __grid_constant__ KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Smem S = carve<SAVEDET>(P, smem_raw);
+    const int tid = threadIdx.x;
+    const int B = blockDim.x;
+    const unsigned lane = tid & 31u;
+
+    for (int i = tid; i < P.medianum; i += B) {
+        const float4 pr = P.prop[i];
+        S.prop[i] = pr;
+        S.aux[i] = make_float4(0.f, 0.f, pr.w * P.oneoverc0, 0.f);
+    }
+    for (int k = 0; k < kNumEnergy; k++) S.tally[k * B + tid] = 0.0;
+    const int tile_elems = P.tile_on ? P.tnx * P.tny * P.tnz * P.tng : 0;
+    for (int i = tid; i < tile_elems; i += B) S.tile[i] = 0.f;
+    __syncthreads();
+
+    const float n0 = P.prop[0].w;
+    const unsigned nx = (unsigned)P.nx, ny = (unsigned)P.ny, nz = (unsigned)P.nz;
+
+    // warp photon pool [pool_next, pool_end), identical in every lane
+    unsigned long long pool_next = 0ull, pool_end = 0ull;
+    bool drained = (P.src_ok == 0);
+    bool alive = false;
+
+    // photon state
+    float px = 0.f, py = 0.f, pz = 0.f, w = 0.f;
+    float vx = 0.f, vy = 0.f, vz = 1.f, rvx = 0.f, rvy = 0.f, rvz = 0.f;
+    float pscat = 0.f, t = 0.f, pathlen = 0.f, w0 = 0.f, wlaunch = 0.f;
+    float eabs = 0.f, eoth = 0.f;       // absorbed weight recorded / not recorded in the field
+    int fx = 0, fy = 0, fz = 0, nscat = -1;
+    // det: detector bit of the current voxel.  carry: the reference's `isdet` as it stands at the
+    // end of a step -- the new voxel's bit (or the boundary code outside), which after a
+    // reflection still describes the voxel bounced off; it feeds the next step's mediaidold.
+    unsigned idx = 0u, det = 0u, carry = 0u, psteps = 0u;
+    int med = 0;
+    float4 pr = make_float4(0.f, 0.f, 0.f, 1.f);
+    unsigned long long r0 = 0ull, r1 = 0ull;
+    unsigned c_step = 0u, c_scat = 0u, c_dep = 0u, c_tile = 0u, c_launch = 0u, c_photon = 0u, c_det = 0u;
+
+    while (true) {
+        // ---- refill lanes that have no photon (warp-uniform control flow) -------------------
+        const unsigned need = __ballot_sync(kFull, !alive);
+        if (need != 0u && !drained) {
+            const unsigned n = __popc(need);
+            const unsigned rank = __popc(need & ((1u << lane) - 1u));
+            const unsigned long long avail = pool_end - pool_next;
+            unsigned long long mine = pool_next + rank;
+            if (avail < n) {
+                unsigned long long base = 0ull;
+                if (lane == 0) base = atomicAdd(P.work, (unsigned long long)P.chunk);
+                base = __shfl_sync(kFull, base, 0);
+                if (rank >= avail) mine = base + (rank - avail);
+                pool_next = base + (n - avail);
+                pool_end = base + (unsigned long long)P.chunk;
+                if (base >= P.nphoton) drained = true;
+            } else {
+                pool_next += n;
+            }
+            if (!alive && mine < P.nphoton) {
+                // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
+                // skipping and specular loss of skipvoid() are folded into src_* by the host)
+                seed_photon(P.seed, P.photon_offset + mine, r0, r1);
+                px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
+                vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
+                rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                t = P.src_t;
+                idx = P.src_idx;
+                med = (int)(P.src_label & kLabelMask);
+                det = (P.src_label & kLabelDet) ? kDET_MASK : 0u;
+                carry = det;
+                fx = P.src_fx; fy = P.src_fy; fz = P.src_fz;
+                pscat = 0.f; pathlen = 0.f; nscat = -1;
+                w0 = w; wlaunch = w; eabs = 0.f; eoth = 0.f; psteps = 0u;
+                pr = S.prop[med];
+                if (SAVEDET)
+                    for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
+                alive = true;
+                c_launch++;
+            }
+        }
+        if (!__any_sync(kFull, alive)) break;
+        if (!alive) continue;
+
+        // ---- one step (src/mcx_core.cu:1888-2514) --------------------------------------------
+        c_step++;
+        unsigned detflag = 0u;
+        bool kill = false;
+
+        if (pscat <= 0.f) {
+            pscat = -__logf(rng_next(r0, r1) + kEPS);                 // src/mcx_rand_xorshift128p.cu:122
+            if (nscat >= 0) {                                           // not the launch flight
+                float sphi, cphi;
+                __sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);   // src/mcx_core.cu:1930-1933
+                const float g = ((float)nscat > P.gscatter) ? 0.f : pr.z;
+                float ct;
+                if (fabsf(g) > kEPS) {                                  // Henyey-Greenstein, 1946-1959
+                    float tmp = __fdividef(1.f - g * g, 1.f - g + 2.f * g * rng_next(r0, r1));
+                    tmp *= tmp;
+                    ct = __fdividef(1.f + g * g - tmp, 2.f * g);
+                    ct = fmaxf(-1.f, fminf(1.f, ct));
+                } else {
+                    ct = 2.f * rng_next(r0, r1) - 1.f;                  // isotropic, 1961-1963
+                }
+                const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+                if (SAVEDET && med > 0) {                               // 1970-1993
+                    const unsigned M = (unsigned)P.nmedia_det;
+                    const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
+                    if (fS) S.ppath[(unsigned)(med - 1) * B + tid] += 1.f;
+                    if ((P.savedetflag >> 3) & 1u) S.ppath[(M * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
+                }
+                rotate(vx, vy, vz, st, ct, sphi, cphi);
+                nscat++;
+                rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                c_scat++;
+            } else {
+                nscat = 0;
+            }
+        }
+
+        const float n1 = pr.w;
+        pr = S.prop[med];
+
+        // distance to the nearest voxel face (hitgrid, src/mcx_core.cu:493-507)
+        const float hx = fabsf(((float)fx + (vx > 0.f ? 1.f : 0.f) - px) * rvx);
+        const float hy = fabsf(((float)fy + (vy > 0.f ? 1.f : 0.f) - py) * rvy);
+        const float hz = fabsf(((float)fz + (vz > 0.f ? 1.f : 0.f) - pz) * rvz);
+        const float dist = fminf(fminf(hx, hy), hz);
+        const int axis = (dist == hx) ? 0 : ((dist == hy) ? 1 : 2);
+
+        // src/mcx_core.cu:2101-2109
+        const float musp = ((float)nscat + 1.f > P.gscatter) ? pr.y * (1.f - pr.z) : pr.y;
+        const float sdist = dist * musp;
+        const bool stay = !(sdist < pscat);                 // flight ends inside this voxel
+        const float slen = stay ? pscat : sdist;
+        const float len = stay ? __fdividef(pscat, musp) : dist;
+
+        px = fmaf(len, vx, px);
+        py = fmaf(len, vy, py);
+        pz = fmaf(len, vz, pz);
+        const int ox = fx, oy = fy, oz = fz;
+        if (!stay) {
+            if (axis == 0) fx += (vx > 0.f) ? 1 : -1;
+            else if (axis == 1) fy += (vy > 0.f) ? 1 : -1;
+            else fz += (vz > 0.f) ? 1 : -1;
+        }
+        w *= __expf(-pr.x * len);                                       // 2140
+        pscat -= slen;
+        t = fmaf(len, S.aux[med].z, t);                                 // t += len*n/c0
+        pathlen += len;
+        if (SAVEDET && med > 0 && ((P.savedetflag >> 2) & 1u)) {
+            const unsigned fS = (P.savedetflag >> 1) & 1u;
+            S.ppath[((unsigned)P.nmedia_det * fS + (unsigned)(med - 1)) * B + tid] += len;
+        }
+        if (++psteps >= P.step_cap) {
+            atomicOr(P.errflag, kErrStepCap);
+            kill = true;
+        }
+
+        const unsigned detold = carry;   // mediaidold's detector bit (src/mcx_core.cu:2167)
+        const int medold = med;
+        bool inside = true;
+        int bcf = BC_UNKNOWN;
+        unsigned idxold = idx;
+
+        if (stay) {
+            carry = det;
+        } else {
+            inside = (unsigned)fx < nx && (unsigned)fy < ny && (unsigned)fz < nz;
+            if (inside) {                                               // 2181-2185
+                idx = (unsigned)fz * P.dimxy + (unsigned)fy * nx + (unsigned)fx;
+                const unsigned lab = __ldg(P.labels + idx);
+                med = (int)(lab & kLabelMask);
+                det = (lab & kLabelDet) ? kDET_MASK : 0u;
+            } else {                                                    // 2173-2178
+                med = 0;
+                idx = (fx < 0 || fy < 0 || fz < 0) ? kOUT_MIN : kOUT_MAX;
+                bcf = P.bc[(idx == kOUT_MAX) * 3 + axis];
+                det = (unsigned)bcf;
+            }
+            carry = det;
+
+            // deposit into the voxel just left, time bin taken at exit (2191-2292)
+            bool rec = false;
+            if (P.save2pt && t >= P.twin0 && t < P.twin1) {
+                const int tshift = min(P.maxgate - 1, (int)floorf((t - P.twin0) * P.Rtstep));
+                float weight;
+                if (P.outputtype == 2) weight = w0 - w;
+                else weight = (pr.x < kEPS) ? (w0 * pathlen) : __fdividef(w0 - w, pr.x);
+                if (weight != 0.f) {
+                    rec = true;
+                    c_dep++;
+                    const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
+                    if (P.tile_on && (unsigned)(ox - P.tx0) < (unsigned)P.tnx && (unsigned)(oy - P.ty0) < (unsigned)P.tny &&
+                        (unsigned)(oz - P.tz0) < (unsigned)P.tnz && (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
+                        const int ti = (((tshift - P.tg0) * P.tnz + (oz - P.tz0)) * P.tny + (oy - P.ty0)) * P.tnx + (ox - P.tx0);
+                        atomicAdd(S.tile + ti, weight);
+                        c_tile++;
+                    } else if (P.field64) {
+                        atomicAdd(P.field64 + addr, (double)weight);
+                    } else {
+                        atomicAdd(P.field + addr, weight);
+                    }
+                }
+            }
+            if (rec) eabs += w0 - w; else eoth += w0 - w;
+            w0 = w;
+            pathlen = 0.f;
+
+            // leaving into a 0 voxel or the outside without reflection (2307-2354)
+            if (med == 0 && ((!REFLECT || n1 == n0) || (bcf == BC_UNKNOWN && !P.doreflect) || bcf == BC_ABSORB ||
+                             bcf == BC_CYCLIC) && bcf != BC_MIRROR)
+                kill = true;
+        }
+        if (t > P.twin1) kill = true;
+
+        if (kill && !inside && bcf == BC_CYCLIC) {                      // 2311-2335
+            const float span = (axis == 0) ? (float)P.nx : ((axis == 1) ? (float)P.ny : (float)P.nz);
+            const float shift = (idx == kOUT_MIN) ? span : -span;
+            if (axis == 0) { px = nextafter_mcx(roundf(px + shift), (vx > 0.f) - (vx < 0.f), P.maxvoidstep); fx = (int)floorf(px); }
+            else if (axis == 1) { py = nextafter_mcx(roundf(py + shift), (vy > 0.f) - (vy < 0.f), P.maxvoidstep); fy = (int)floorf(py); }
+            else { pz = nextafter_mcx(roundf(pz + shift), (vz > 0.f) - (vz < 0.f), P.maxvoidstep); fz = (int)floorf(pz); }
+            if ((unsigned)fx < nx && (unsigned)fy < ny && (unsigned)fz < nz) {
+                idx = (unsigned)fz * P.dimxy + (unsigned)fy * nx + (unsigned)fx;
+                const unsigned lab = __ldg(P.labels + idx);
+                med = (int)(lab & kLabelMask);
+                det = (lab & kLabelDet) ? kDET_MASK : 0u;
+                carry = det;
+                continue;
+            }
+        }
+        if (kill) {
+            detflag = (!inside && P.bc[((idx == kOUT_MAX) ? 9 : 6) + axis]) ? kOUT_MIN : (detold & kDET_MASK);
+        } else {
+            // Russian roulette (2357-2378); off when minenergy is 0
+            if (P.minenergy > 0.f && fabsf(w) < P.minenergy) {
+                if (rng_next(r0, r1) * 10.f <= 1.f) {
+                    w *= 10.f;
+                } else {
+                    kill = true;
+                    detflag = detold & kDET_MASK;
+                }
+            }
+            // Fresnel reflection / refraction on crossing (2381-2503)
+            if (REFLECT && !kill && !stay) {
+                const float4 prn = S.prop[med];
+                pr = prn;
+                if (((med && P.doreflect) ||
+                     (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
+                    (bcf == BC_MIRROR || n1 != prn.w)) {
+                    float Rtotal = 1.f;
+                    const float a2 = n1 * n1, b2 = prn.w * prn.w;
+                    const float va = (axis == 0) ? vx : ((axis == 1) ? vy : vz);
+                    const float cphi = fabsf(va);
+                    const float sphi = 1.f - cphi * cphi;
+                    const float c2 = 1.f - __fdividef(a2, b2) * sphi;
+                    if (c2 > 0.f && bcf != BC_MIRROR) {
+                        float ctheta = a2 * cphi * cphi + b2 * c2;
+                        const float stheta = 2.f * n1 * prn.w * cphi * sqrtf(c2);
+                        Rtotal = __fdividef(ctheta - stheta, ctheta + stheta);
+                        ctheta = b2 * cphi * cphi + a2 * c2;
+                        Rtotal = (Rtotal + __fdividef(ctheta - stheta, ctheta + stheta)) * 0.5f;
+                    }
+                    if (Rtotal < 1.f && !(med == 0 && bcf == BC_MIRROR) && rng_next(r0, r1) > Rtotal) {
+                        transmit(vx, vy, vz, n1, prn.w, axis);
+                        if (med == 0) {
+                            kill = true;
+                            detflag = (!inside && P.bc[((idx == kOUT_MAX) ? 9 : 6) + axis]) ? kOUT_MIN : (detold & kDET_MASK);
+                        } else {
+                            rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                        }
+                    } else {
+                        // mirror the direction and nudge the position back into the voxel left
+                        if (axis == 0) {
+                            vx = -vx;
+                            px = nextafter_mcx(rintf(px), (vx > 0.f) - (vx < 0.f), P.maxvoidstep);
+                            fx = (int)floorf(px);
+                        } else if (axis == 1) {
+                            vy = -vy;
+                            py = nextafter_mcx(rintf(py), (vy > 0.f) - (vy < 0.f), P.maxvoidstep);
+                            fy = (int)floorf(py);
+                        } else {
+                            vz = -vz;
+                            pz = nextafter_mcx(rintf(pz), (vz > 0.f) - (vz < 0.f), P.maxvoidstep);
+                            fz = (int)floorf(pz);
+                        }
+                        rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                        idx = idxold;
+                        const unsigned lab = __ldg(P.labels + idx);
+                        med = (int)(lab & kLabelMask);
+                        det = (lab & kLabelDet) ? kDET_MASK : 0u;   // carry keeps the bounced-off value
+                        pr = S.prop[med];
+                    }
+                } else {
+                    pr = S.prop[medold];
+                }
+            }
+        }
+
+        if (kill) {
+            // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
+            bool detected = false;
+            if (SAVEDET && (detflag & kDET_MASK) && med == 0) {
+                const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
+                if (detid) {
+                    detected = true;
+                    c_det++;
+                    const unsigned slot = atomicAdd(P.detcount, 1u);
+                    if (slot < P.maxdet) {
+                        float* rec = P.detp + (size_t)slot * P.reclen;
+                        unsigned k = 0;
+                        if (P.savedetflag & 0x1u) rec[k++] = (float)detid;
+                        for (unsigned i = 0; i < P.partialdata; i++) rec[k++] = S.ppath[i * B + tid];
+                        if (P.savedetflag & 0x10u) { rec[k++] = px; rec[k++] = py; rec[k++] = pz; }
+                        if (P.savedetflag & 0x20u) { rec[k++] = vx; rec[k++] = vy; rec[k++] = vz; }
+                        if (P.savedetflag & 0x40u) rec[k++] = wlaunch;
+                    }
+                }
+            }
+            S.tally[kELaunch * B + tid] += (double)wlaunch;
+            S.tally[(detected ? kEDetect : kEEscape) * B + tid] += (double)w;
+            S.tally[kEAbsDep * B + tid] += (double)eabs;
+            S.tally[kEAbsOther * B + tid] += (double)eoth + ((double)w0 - (double)w);
+            c_photon++;
+            alive = false;
+        }
+    }
+
+    // ---- flush: tile, tallies, counters ------------------------------------------------------
+    __syncthreads();
+    for (int i = tid; i < tile_elems; i += B) {
+        const float v = S.tile[i];
+        if (v == 0.f) continue;
+        int r = i;
+        const int x = r % P.tnx; r /= P.tnx;
+        const int y = r % P.tny; r /= P.tny;
+        const int z = r % P.tnz; r /= P.tnz;
+        const int g = r;
+        const size_t addr = (size_t)((z + P.tz0) * (int)P.dimxy + (y + P.ty0) * P.nx + (x + P.tx0)) +
+                            (size_t)(g + P.tg0) * P.nvox;
+        if (P.field64) {
+            atomicAdd(P.field64 + addr, (double)v);
+        } else {
+            // two-copy accumulation (src/mcx_core.cu:2246-2253): once the primary copy grows past
+            // kMaxAccum, move what was there into the shadow copy so the primary stays small
+            const float old = atomicAdd(P.field + addr, v);
+            if (fabsf(old) > kMaxAccum) {
+                atomicAdd(P.field + addr, -old);
+                atomicAdd(P.shadow + addr, old);
+            }
+        }
+    }
+    for (int k = 0; k < kNumEnergy; k++) {
+        double v = S.tally[k * B + tid];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+        if (lane == 0 && v != 0.0) atomicAdd(P.energy + k, v);
+    }
+    unsigned cnt[7] = {c_step, c_scat, c_dep, c_launch, c_photon, c_det, c_tile};
+    const int cidx[7] = {kCntSteps, kCntScatter, kCntDeposit, kCntLaunch, kCntPhoton, kCntDetected, kCntTileDeposit};
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        unsigned long long v = cnt[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+        if (lane == 0 && v) atomicAdd(P.counters + cidx[k], v);
+    }
+}
+
+// The -D R test kernel: one thread fills `out` from four seed words
+// (src/mcx_core.cu:1731-1742, seeding src/mcx_rand_xorshift128p.cu:79-82).
+__global__ void rng_test_kernel(const uint32_t* seeds, float* out, int n) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    unsigned long long a = ((unsigned long long)seeds[0] << 32) | seeds[1];
+    unsigned long long b = ((unsigned long long)seeds[2] << 32) | seeds[3];
+    for (int i = 0; i < n; i++) out[i] = rng_next(a, b);
+}
+
+__global__ void photon_stream_kernel(unsigned long long seed, unsigned long long pid, float* out, int n) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    unsigned long long a, b;
+    seed_photon(seed, pid, a, b);
+    for (int i = 0; i < n; i++) out[i] = rng_next(a, b);
+}
+
+// uint32 MCX voxels (bit 31 detector mask) -> one byte per voxel.
+__global__ void labels_kernel(const uint32_t* __restrict__ vol, uint8_t* __restrict__ labels, size_t n,
+                              unsigned int medianum, unsigned int* err) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t v = vol[i];
+        const uint32_t lab = v & kMED_MASK;
+        if (lab >= medianum || lab > kLabelMask) atomicOr(err, kErrBadLabel);
+        labels[i] = (uint8_t)((lab & kLabelMask) | ((v & kDET_MASK) ? kLabelDet : 0u));
+    }
+}
+
+// field = (field + shadow or field64) * scale, in place (src/mcx_core.cu:3687-3696 shadow merge,
+// mcx_normalize src/mcx_utils.c:1227-1237 scaling; option 2 leaves negative values alone).
+__global__ void merge_kernel(float* __restrict__ out, const float* __restrict__ field, const float* __restrict__ shadow,
+                             const double* __restrict__ f64, size_t n, float scale, int positive_only) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float v = f64 ? (float)f64[i] : field[i] + (shadow ? shadow[i] : 0.f);
+        if (!(positive_only && v < 0.f)) v *= scale;
+        out[i] = v;
+    }
+}
+
+}  // namespace
+
+size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
+    size_t b = 2 * sizeof(float4) * (size_t)p.medianum;
+    b += sizeof(double) * kNumEnergy * (size_t)block;
+    if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
+    if (p.tile_on) b += sizeof(float) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
+    return b;
+}
+
+template <bool R, bool D>
+static const void* kernel_ptr() { return (const void*)transport_kernel<R, D>; }
+
+static const void* pick(bool reflect, bool savedet) {
+    if (reflect) return savedet ? kernel_ptr<true, true>() : kernel_ptr<true, false>();
+    return savedet ? kernel_ptr<false, true>() : kernel_ptr<false, false>();
+}
+
+int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_bytes) {
+    const void* k = pick(reflect, savedet);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem_bytes) != cudaSuccess) return 0;
+    return n;
+}
+
+cudaError_t launch_transport(const KParams& p, bool reflect, bool savedet, int grid, int block, size_t smem_bytes,
+                             cudaStream_t stream) {
+    const void* k = pick(reflect, savedet);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (e != cudaSuccess) return e;
+    if (reflect) {
+        if (savedet) transport_kernel<true, true><<<grid, block, smem_bytes, stream>>>(p);
+        else transport_kernel<true, false><<<grid, block, smem_bytes, stream>>>(p);
+    } else {
+        if (savedet) transport_kernel<false, true><<<grid, block, smem_bytes, stream>>>(p);
+        else transport_kernel<false, false><<<grid, block, smem_bytes, stream>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rng_test(const uint32_t* d_seeds, float* d_out, int n, cudaStream_t stream) {
+    rng_test_kernel<<<1, 32, 0, stream>>>(d_seeds, d_out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_photon_stream(unsigned long long seed, unsigned long long pid, float* d_out, int n, cudaStream_t stream) {
+    photon_stream_kernel<<<1, 32, 0, stream>>>(seed, pid, d_out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_labels_from_vol(const uint32_t* d_vol, uint8_t* d_labels, size_t n, unsigned int medianum,
+                                   unsigned int* d_err, cudaStream_t stream) {
+    const int block = 256;
+    const size_t g = (n + block - 1) / block;
+    labels_kernel<<<(unsigned)(g < 4096 ? (g ? g : 1) : 4096), block, 0, stream>>>(d_vol, d_labels, n, medianum, d_err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_field(float* out, const float* field, const float* shadow, const double* field64, size_t n,
+                               float scale, int positive_only, cudaStream_t stream) {
+    const int block = 256;
+    const size_t g = (n + block - 1) / block;
+    merge_kernel<<<(unsigned)(g < 4096 ? (g ? g : 1) : 4096), block, 0, stream>>>(out, field, shadow, field64, n, scale, positive_only);
+    return cudaGetLastError();
+}
+
+}  // namespace mcxg

@@ -1,0 +1,102 @@
+// transport.cuh -- parameters of the GB300 photon-transport kernel and its launch helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "mcxg_common.h"
+
+namespace mcxg {
+
+// Indices into the device counter array.
+enum Counter : int {
+    kCntSteps = 0, kCntScatter, kCntDeposit, kCntLaunch, kCntPhoton, kCntDetected, kCntTileDeposit, kCntWork, kNumCounters
+};
+// Indices into the device FP64 energy array.
+enum Energy : int { kELaunch = 0, kEEscape, kEDetect, kEAbsDep, kEAbsOther, kNumEnergy };
+// Bits of the device error word.
+enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow = 4u };
+
+// Everything one transport launch needs.  Passed as a __grid_constant__ kernel parameter, so
+// uniform reads come from the constant bank; the per-medium table is copied to shared memory
+// at kernel start because lanes index it with divergent labels.
+struct KParams {
+    // --- buffers (device pointers)
+    const uint8_t* labels;          // Nvox bytes: bit 7 detector mask, bits 0-6 medium label
+    float* field;                   // maxgate x Nvox raw flux accumulator
+    float* shadow;                  // maxgate x Nvox spill copy (values moved out past kMaxAccum)
+    double* field64;                // FP64 accumulator (reference-accuracy runs only), else null
+    float* detp;                    // maxdet x reclen detected-photon records
+    unsigned int* detcount;         // detected photons seen (may exceed maxdet)
+    double* energy;                 // kNumEnergy FP64 tallies
+    unsigned long long* counters;   // kNumCounters
+    unsigned int* errflag;          // device error word
+    const float4* detpos;           // ndet x {x, y, z, r}
+
+    // --- geometry
+    int nx, ny, nz;
+    unsigned int dimxy, nvox;
+
+    // --- launch state every photon starts from (pencil beam, after void skipping)
+    float4 src_p;                   // x, y, z, initial weight
+    float4 src_v;                   // unit direction
+    float src_t;                    // time already spent in the void
+    unsigned int src_idx;           // launch voxel
+    unsigned int src_label;         // its label byte (detector bit included)
+    int src_fx, src_fy, src_fz;     // integer voxel coordinates of the launch voxel
+    int src_ok;                     // 0: photons cannot enter the volume (all launches fail)
+
+    // --- time gates
+    float twin0, twin1, Rtstep, oneoverc0;
+    int maxgate;
+
+    // --- media (mua, mus, g, n) per label, already scaled to grid units
+    int medianum;
+    float4 prop[kMaxMedia];
+
+    // --- physics switches
+    int doreflect;                  // cfg->isreflect
+    int save2pt;                    // record the field
+    int outputtype;                 // 0 flux, 1 fluence, 2 energy
+    float minenergy;                // Russian roulette threshold (0 = off)
+    float gscatter;                 // scattering events after which mus' replaces mus
+    float maxvoidstep;              // offset used by the nextafter nudge
+    unsigned char bc[12];           // boundary condition codes per face, then detector flags
+
+    // --- detectors
+    int ndet;
+    unsigned int maxdet, reclen, partialdata, savedetflag;
+    int nmedia_det;                 // medianum - 1: rows of the per-medium record blocks
+
+    // --- work
+    unsigned long long nphoton;     // photons in this launch
+    unsigned long long photon_offset;  // global index of the first one (RNG stream id)
+    unsigned long long seed;
+    unsigned long long* work;       // photon counter the persistent warps draw chunks from
+    int chunk;                      // photons per warp refill
+    unsigned int step_cap;          // safety cap on steps per photon (error flag when hit)
+
+    // --- per-CTA shared-memory deposit tile (voxel box x gate range)
+    int tile_on;
+    int tx0, ty0, tz0, tnx, tny, tnz, tg0, tng;
+};
+
+// Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
+constexpr float kMaxAccum = 1000.f;
+
+// Host-side launch of the transport kernel variant matching the flags.  smem_bytes is the
+// dynamic shared memory per CTA; returns the CUDA error of the launch.
+cudaError_t launch_transport(const KParams& p, bool reflect, bool savedet, int grid, int block,
+                             size_t smem_bytes, cudaStream_t stream);
+// Shared memory the kernel needs for a given block size and parameter set.
+size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
+// Occupancy-derived CTAs per SM for the chosen variant.
+int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_bytes);
+
+cudaError_t launch_rng_test(const uint32_t* d_seeds, float* d_out, int n, cudaStream_t stream);
+cudaError_t launch_photon_stream(unsigned long long seed, unsigned long long pid, float* d_out, int n, cudaStream_t stream);
+cudaError_t launch_labels_from_vol(const uint32_t* d_vol, uint8_t* d_labels, size_t n, unsigned int medianum,
+                                   unsigned int* d_err, cudaStream_t stream);
+cudaError_t launch_merge_field(float* out, const float* field, const float* shadow, const double* field64, size_t n,
+                               float scale, int normalize_positive_only, cudaStream_t stream);
+
+}  // namespace mcxg

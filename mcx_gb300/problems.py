@@ -1,0 +1,136 @@
+"""Input decks: MCX's built-in cube benchmarks and the engine's three plain-MC workloads.
+
+``cube60`` / ``cube60b`` restate the built-in benchmarks of src/mcx_bench.c:47-152 (the decks the
+reference's regression tests and speed contest run).  ``workload0..2`` are the homogeneous,
+heterogeneous-with-detectors and large layered workloads the engine is benchmarked on; they are
+synthetic and fully determined by their seed.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+CUBE60_SEED = 1648335518      # RNGSeed of the cube60 decks, src/mcx_bench.c:50
+CUBE60_DETECTORS = [[29.0, 19.0, 0.0, 1.0], [29.0, 39.0, 0.0, 1.0], [19.0, 29.0, 0.0, 1.0], [39.0, 29.0, 0.0, 1.0]]
+
+
+def _cube60(nphoton: float, mismatch: bool, n_medium2: float) -> dict:
+    return {
+        "nphoton": int(nphoton),
+        "seed": CUBE60_SEED,
+        "vol": np.ones((60, 60, 60), dtype=np.uint8),
+        "prop": np.array([[0.0, 0.0, 1.0, 1.0], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.90, n_medium2]], np.float32),
+        "tstart": 0.0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [29.0, 29.0, 0.0], "srcdir": [0.0, 0.0, 1.0],
+        "detpos": np.array(CUBE60_DETECTORS, np.float32),
+        "issrcfrom0": 1,
+        "isreflect": 1 if mismatch else 0,
+        "issavedet": 1,
+    }
+
+
+def cube60(nphoton: float = 1e6) -> dict:
+    """Homogeneous 60^3 cube, no reflection (src/mcx_bench.c:47-101)."""
+    return _cube60(nphoton, False, 1.37)
+
+
+def cube60b(nphoton: float = 1e6) -> dict:
+    """The same cube with Fresnel reflection at the outer boundary (src/mcx_bench.c:104-152)."""
+    return _cube60(nphoton, True, 1.0)
+
+
+def sphere60b(nphoton: float = 1e6) -> dict:
+    """cube60 plus a label-2 sphere (R=15 at (30,30,30), medium 2 = (0.002, 5.0, 0.9, 1.0)) with
+    reflection on: the second deck of MCX's speed benchmark (mcxlab/examples/mcx_gpu_benchmarks.m:47-87)."""
+    cfg = _cube60(nphoton, True, 1.0)
+    cfg["seed"] = 29012392
+    sphere_labels((60, 60, 60), (30.0, 30.0, 30.0), 15.0, 2, cfg["vol"])
+    return cfg
+
+
+def sphere_labels(dim: tuple[int, int, int], center, radius: float, tag: int, vol: np.ndarray) -> np.ndarray:
+    """Rasterise a sphere: voxel centres (i + 0.5) within `radius` of `center` get `tag`
+    (the rule of MCX's shape rasteriser, src/mcx_shapes.c:237-289)."""
+    ii = np.arange(dim[0], dtype=np.float32)[:, None, None] + 0.5 - center[0]
+    jj = np.arange(dim[1], dtype=np.float32)[None, :, None] + 0.5 - center[1]
+    kk = np.arange(dim[2], dtype=np.float32)[None, None, :] + 0.5 - center[2]
+    mask = ii * ii + jj * jj + kk * kk <= np.float32(radius) * np.float32(radius)
+    vol[mask] = tag
+    return vol
+
+
+def workload0(nphoton: float = 1e6, seed: int = CUBE60_SEED) -> dict:
+    """Plain MC, homogeneous 60^3 cube: medium 1 (mua 0.005, mus 1.0, g 0.01, n 1.37) in a
+    background (0, 0, 1, 1); pencil at voxel (29,29,0) along +z; one 0-5 ns gate; no
+    reflection; float32 flux."""
+    return {
+        "nphoton": int(nphoton), "seed": seed,
+        "vol": np.ones((60, 60, 60), dtype=np.uint8),
+        "prop": np.array([[0.0, 0.0, 1.0, 1.0], [0.005, 1.0, 0.01, 1.37]], np.float32),
+        "tstart": 0.0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [29.0, 29.0, 0.0], "srcdir": [0.0, 0.0, 1.0],
+        "issrcfrom0": 1, "isreflect": 0, "issavedet": 0,
+    }
+
+
+def workload1(nphoton: float = 1e8, seed: int = CUBE60_SEED) -> dict:
+    """Plain MC, heterogeneous: the cube plus a label-2 sphere of radius 15 voxels centred at
+    (30,30,30) (mua 0.002, mus 5.0, g 0.9, n 1.37); Fresnel reflection against n=1 outside;
+    50 gates of 0.1 ns; four disk detectors of radius 1 on z=0 at 5/10/15/20 mm from the
+    source, saving detector id, per-medium scattering counts and partial path lengths."""
+    vol = np.ones((60, 60, 60), dtype=np.uint8)
+    sphere_labels((60, 60, 60), (30.0, 30.0, 30.0), 15.0, 2, vol)
+    det = np.array([[29.0 + d, 29.0, 0.0, 1.0] for d in (5, 10, 15, 20)], np.float32)
+    return {
+        "nphoton": int(nphoton), "seed": seed, "vol": vol,
+        "prop": np.array([[0.0, 0.0, 1.0, 1.0], [0.005, 1.0, 0.01, 1.37], [0.002, 5.0, 0.9, 1.37]], np.float32),
+        "tstart": 0.0, "tend": 5e-9, "tstep": 1e-10,
+        "srcpos": [29.0, 29.0, 0.0], "srcdir": [0.0, 0.0, 1.0],
+        "detpos": det, "issrcfrom0": 1, "isreflect": 1, "issavedet": 1, "savedetflag": "dsp",
+        "maxdetphoton": 2000000,
+    }
+
+
+LAYERED_PROPS = np.array([
+    [0.0, 0.0, 1.0, 1.0],
+    [0.019, 7.8, 0.89, 1.37],
+    [0.016, 16.0, 0.90, 1.37],
+    [0.004, 0.01, 0.90, 1.37],
+    [0.020, 9.0, 0.89, 1.37],
+    [0.080, 40.9, 0.84, 1.37],
+], np.float32)
+
+
+def layered_volume(n: int = 256, seed: int = 20251203) -> np.ndarray:
+    """Five nested axis-aligned ellipsoid shells centred near the middle of an n^3 grid, label 1
+    outermost to 5 innermost; semi-axes drawn from `seed`, each shell 72-88% of the previous."""
+    rng = np.random.default_rng(seed)
+    vol = np.zeros((n, n, n), dtype=np.uint8)
+    c = np.array([n / 2.0, n / 2.0, n / 2.0]) + rng.uniform(-2.0, 2.0, 3)
+    axes = np.array([0.46 * n, 0.44 * n, 0.42 * n]) * rng.uniform(0.95, 1.0, 3)
+    x = np.arange(n, dtype=np.float32) + 0.5
+    dx2 = (x - c[0]) ** 2
+    dy2 = (x - c[1]) ** 2
+    dz2 = (x - c[2]) ** 2
+    for label in range(1, 6):
+        a = axes.astype(np.float32)
+        inside = (dx2[:, None, None] / a[0] ** 2 + dy2[None, :, None] / a[1] ** 2 + dz2[None, None, :] / a[2] ** 2) <= 1.0
+        vol[inside] = label
+        axes = axes * rng.uniform(0.72, 0.88, 3)
+    return vol
+
+
+def workload2(nphoton: float = 1e9, seed: int = CUBE60_SEED, n: int = 256) -> dict:
+    """Plain MC, large layered volume: 256^3 nested ellipsoid shells (props above, n=1.37),
+    pencil beam launched from outside along +z through the volume centre line, normal to the
+    outer surface; one 0-5 ns gate; Fresnel reflection against n=1; float32 flux (64 MB)."""
+    vol = layered_volume(n)
+    return {
+        "nphoton": int(nphoton), "seed": seed, "vol": vol, "prop": LAYERED_PROPS.copy(),
+        "tstart": 0.0, "tend": 5e-9, "tstep": 5e-9,
+        "srcpos": [n / 2.0, n / 2.0, 0.0], "srcdir": [0.0, 0.0, 1.0],
+        "issrcfrom0": 1, "isreflect": 1, "issavedet": 0,
+    }
+
+
+WORKLOADS = {"workload0": workload0, "workload1": workload1, "workload2": workload2}

@@ -1,0 +1,623 @@
+// mcx_oracle.cpp -- CPU restatement of MCX's voxel photon-transport loop.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle and the CPU baseline of the
+// GB300 engine; the engine never calls it.  Only tests/, the smoke check in
+// __graft_entry__.py and the cpu_baseline leg of bench.py load it, and only as a checker.
+//
+// What it restates (MCX v2025.10, file:line within the reference project):
+//   xorshift128+ generator ............ src/mcx_rand_xorshift128p.cu:56-82, 109-138
+//   RNG test kernel (-D R) ............ src/mcx_core.cu:1731-1742
+//   mcx_nextafterf .................... src/mcx_core.cu:470-478
+//   hitgrid ........................... src/mcx_core.cu:493-507
+//   transmit .......................... src/mcx_core.cu:523-537
+//   reflectcoeff ...................... src/mcx_core.cu:552-570
+//   skipvoid (label media) ............ src/mcx_core.cu:866-956
+//   rotatevector ...................... src/mcx_core.cu:1011-1031
+//   launchnewphoton (pencil branch) ... src/mcx_core.cu:1089-1243, 1646-1717
+//   savedetphoton / finddetector ...... src/mcx_core.cu:258-270, 365-417
+//   mcx_main_loop<1,r,1,0,0> .......... src/mcx_core.cu:1767-2528
+// The control flow follows the reference step for step, in plain FP32 with libm's
+// logf/expf/sincosf/acosf/sinf standing in for the CUDA fast-math intrinsics the reference
+// is compiled with.  Differences that are deliberate:
+//   * RNG seeding: every photon gets its own xorshift128+ state derived from (seed, photon
+//     index) by the splitmix64 mixer, exactly as the GB300 engine seeds it.  The reference
+//     seeds one state per GPU thread from glibc rand(); streams therefore differ, statistics
+//     do not.  The generator itself is pinned bit-for-bit by tests/golden (the -D R vector).
+//   * Tallies are FP64 (field, energies) so the oracle carries no FP32 accumulation error;
+//     it also counts steps, scatters, deposits and per-voxel deposit hits, the algorithmic
+//     quantities the roofline is built from.
+// Parity is pinned against the reference's own golden numbers (absorbed fraction of cube60 /
+// cube60b, detected-photon count of cube60b, the RNG vector) and against the semi-infinite
+// CW diffusion solution; see tests/test_oracle_golden.py.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cfloat>
+#include <chrono>
+#include <vector>
+#include <atomic>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "mcx_oracle.h"
+
+namespace {
+
+constexpr float kEPS = FLT_EPSILON;
+constexpr uint32_t kDET_MASK = 0x80000000u;
+constexpr uint32_t kMED_MASK = 0x7FFFFFFFu;
+constexpr uint32_t kOUT_MIN = 0xFFFFFFFFu;   // left the volume through x/y/z = 0 side
+constexpr uint32_t kOUT_MAX = 0x7FFFFFFFu;   // left through the far side
+constexpr float kTWO_PI = 6.28318530717959f;
+constexpr float kR_C0 = 3.335640951981520e-12f;  // s/mm
+enum { BC_UNKNOWN = 0, BC_REFLECT = 1, BC_ABSORB = 2, BC_MIRROR = 3, BC_CYCLIC = 4 };
+
+// ---------------------------------------------------------------- xorshift128+ ----------
+struct Rng {
+    uint64_t s[2];
+    // src/mcx_rand_xorshift128p.cu:56-72: one step; the float is built from the low 32 bits
+    float next() {
+        uint64_t s1 = s[0];
+        const uint64_t s0 = s[1];
+        s[0] = s0;
+        s1 ^= s1 << 23;
+        s[1] = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+        uint32_t lo = (uint32_t)(s[1] + s0);
+        uint32_t bits = 0x3F800000u | (lo >> 9);
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f - 1.0f;
+    }
+};
+
+inline uint64_t splitmix64(uint64_t& x) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Per-photon seeding shared with the GB300 engine (mcx_gb300/csrc/rng.cuh).
+inline void seed_photon(Rng& r, uint64_t seed, uint64_t photon) {
+    uint64_t x = seed * 0xD1B54A32D192ED03ull + photon;
+    r.s[0] = splitmix64(x);
+    r.s[1] = splitmix64(x);
+    if ((r.s[0] | r.s[1]) == 0) r.s[1] = 1;
+}
+
+struct Prop { float mua, mus, g, n; };
+
+struct Ctx {
+    const OracleProblem* P;
+    uint32_t nx, ny, nz, dimxy, dimxyz;
+    float maxx, maxy, maxz;
+    float oneoverc0, minaccumtime, Rtstep, twin0, twin1;
+    uint32_t maxgate, medianum, detnum;
+    uint32_t partialdata, reclen;
+    int isreflect;                 // template flag of the reference (isreflect or any r/m face)
+    const Prop* prop;
+};
+
+// src/mcx_core.cu:470-478
+inline float nextafter_mcx(float a, int dir, float maxvoidstep) {
+    float f = a + maxvoidstep;
+    uint32_t i;
+    std::memcpy(&i, &f, 4);
+    i += (uint32_t)dir ^ (i & 0x80000000u);
+    std::memcpy(&f, &i, 4);
+    return f - maxvoidstep;
+}
+
+// src/mcx_core.cu:493-507
+inline float hitgrid(const float p[3], const float v[3], const float rv[3], short fd[4]) {
+    float h0 = std::fabs((fd[0] + (v[0] > 0.f) - p[0]) * rv[0]);
+    float h1 = std::fabs((fd[1] + (v[1] > 0.f) - p[1]) * rv[1]);
+    float h2 = std::fabs((fd[2] + (v[2] > 0.f) - p[2]) * rv[2]);
+    float d = std::fmin(std::fmin(h0, h1), h2);
+    fd[3] = (d == h0 ? 0 : (d == h1 ? 1 : 2));
+    return d;
+}
+
+// src/mcx_core.cu:523-537
+inline void transmit(float v[3], float n1, float n2, int axis) {
+    float t = n1 / n2;
+    v[0] *= t; v[1] *= t; v[2] *= t;
+    int a1 = (axis + 1) % 3, a2 = (axis + 2) % 3;
+    float s = v[a1] * v[a1] + v[a2] * v[a2];
+    v[axis] = (s < 1.f) ? std::sqrt(1.f - s) * (float)((v[axis] > 0.f) - (v[axis] < 0.f)) : 0.f;
+    float r = 1.f / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] *= r; v[1] *= r; v[2] *= r;
+}
+
+// src/mcx_core.cu:552-570
+inline float reflectcoeff(const float v[3], float n1, float n2, int axis) {
+    float Icos = std::fabs(v[axis]);
+    float a = n1 * n1, b = n2 * n2;
+    float c = 1.f - a / b * (1.f - Icos * Icos);
+    if (c > 0.f) {
+        float Re = a * Icos * Icos + b * c;
+        c = std::sqrt(c);
+        float Im = 2.f * n1 * n2 * Icos * c;
+        float R = (Re - Im) / (Re + Im);
+        Re = b * Icos * Icos + a * c * c;
+        return (R + (Re - Im) / (Re + Im)) * 0.5f;
+    }
+    return 1.f;
+}
+
+// src/mcx_core.cu:1011-1031
+inline void rotatevector(float v[3], float st, float ct, float sp, float cp) {
+    if (v[2] > -1.f + kEPS && v[2] < 1.f - kEPS) {
+        float t0 = 1.f - v[2] * v[2];
+        float t1 = st / std::sqrt(t0);
+        float nx = t1 * (v[0] * v[2] * cp - v[1] * sp) + v[0] * ct;
+        float ny = t1 * (v[1] * v[2] * cp + v[0] * sp) + v[1] * ct;
+        float nz = -t1 * t0 * cp + v[2] * ct;
+        v[0] = nx; v[1] = ny; v[2] = nz;
+    } else {
+        float nz = (v[2] > 0.f) ? ct : -ct;
+        v[0] = st * cp; v[1] = st * sp; v[2] = nz;
+    }
+    float r = 1.f / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] *= r; v[1] *= r; v[2] *= r;
+}
+
+inline bool inside(const Ctx& C, const short fd[4]) {
+    return (unsigned short)fd[0] < C.maxx && (unsigned short)fd[1] < C.maxy && (unsigned short)fd[2] < C.maxz;
+}
+
+inline uint32_t vidx(const Ctx& C, const short fd[4]) {
+    return (uint32_t)(fd[2] * (int)C.dimxy + fd[1] * (int)C.nx + fd[0]);
+}
+
+struct Tally {
+    double e_launch = 0, e_escape = 0, e_detect = 0, e_absdep = 0, e_absother = 0;
+    uint64_t steps = 0, scatters = 0, deposits = 0, launches = 0, detected = 0, photons = 0;
+};
+
+struct Photon {
+    float p[3], w;
+    float v[3], nscat;
+    float pscat, t, pathlen;
+    float w0, wlaunch;
+    float rv[3];
+    short fd[4];
+    uint32_t idx1d, mediaid;
+    int isdet;
+    Prop prop;
+    float ppath[3 * 128];          // nscat(M) | ppath(M) | mom(M), per medium label 1..M
+};
+
+// src/mcx_core.cu:866-956 (label media, no SVMC).  Returns the entry voxel or -1.
+int skipvoid(const Ctx& C, Photon& ph) {
+    const OracleProblem* P = C.P;
+    int count = 1;
+    short fd[4] = {0, 0, 0, -1};
+    fd[0] = (short)std::floor(ph.p[0]);
+    fd[1] = (short)std::floor(ph.p[1]);
+    fd[2] = (short)std::floor(ph.p[2]);
+    while (true) {
+        if (inside(C, fd)) {
+            uint32_t id = vidx(C, fd);
+            if (P->vol[id] & kMED_MASK) {
+                ph.p[0] -= ph.v[0]; ph.p[1] -= ph.v[1]; ph.p[2] -= ph.v[2];
+                fd[0] = (short)std::floor(ph.p[0]);
+                fd[1] = (short)std::floor(ph.p[1]);
+                fd[2] = (short)std::floor(ph.p[2]);
+                ph.t -= C.minaccumtime;
+                id = vidx(C, fd);
+                count = 0;
+                while (!inside(C, fd) || !(P->vol[id] & kMED_MASK)) {
+                    float d = hitgrid(ph.p, ph.v, ph.rv, fd);
+                    ph.t += C.minaccumtime * d;
+                    ph.p[0] += d * ph.v[0]; ph.p[1] += d * ph.v[1]; ph.p[2] += d * ph.v[2];
+                    if (fd[3] == 0) fd[0] += (ph.v[0] > 0.f ? 1 : -1);
+                    if (fd[3] == 1) fd[1] += (ph.v[1] > 0.f ? 1 : -1);
+                    if (fd[3] == 2) fd[2] += (ph.v[2] > 0.f ? 1 : -1);
+                    id = vidx(C, fd);
+                    if (count++ > 3) break;
+                }
+                ph.t = P->voidtime ? ph.t : 0.f;
+                const Prop& np = C.prop[P->vol[id] & kMED_MASK];
+                if (P->isspecular && np.n != C.prop[0].n) {
+                    ph.w *= 1.f - reflectcoeff(ph.v, C.prop[0].n, np.n, fd[3]);
+                    if (ph.w > kEPS) transmit(ph.v, C.prop[0].n, np.n, fd[3]);
+                }
+                return (int)id;
+            }
+        }
+        if ((ph.p[0] < 0.f && ph.v[0] <= 0.f) || (ph.p[0] >= C.maxx && ph.v[0] >= 0.f) ||
+            (ph.p[1] < 0.f && ph.v[1] <= 0.f) || (ph.p[1] >= C.maxy && ph.v[1] >= 0.f) ||
+            (ph.p[2] < 0.f && ph.v[2] <= 0.f) || (ph.p[2] >= C.maxz && ph.v[2] >= 0.f))
+            return -1;
+        ph.p[0] += ph.v[0]; ph.p[1] += ph.v[1]; ph.p[2] += ph.v[2];
+        fd[0] = (short)std::floor(ph.p[0]);
+        fd[1] = (short)std::floor(ph.p[1]);
+        fd[2] = (short)std::floor(ph.p[2]);
+        ph.t += C.minaccumtime;
+        if (count++ > P->maxvoidstep) return -1;
+    }
+}
+
+// src/mcx_core.cu:258-270
+uint32_t finddetector(const Ctx& C, const float p[3]) {
+    for (uint32_t i = 0; i < C.detnum; i++) {
+        const float* d = C.P->detpos + 4 * i;
+        if ((d[0] - p[0]) * (d[0] - p[0]) + (d[1] - p[1]) * (d[1] - p[1]) + (d[2] - p[2]) * (d[2] - p[2]) < d[3] * d[3])
+            return (d[3] < 0.f) ? 0 : i + 1;
+    }
+    return 0;
+}
+
+// src/mcx_core.cu:365-417 (savedetflag fields D,S,P,M,X,V,W; no seeds, no Stokes)
+void savedetphoton(const Ctx& C, OracleResult* R, std::atomic<uint64_t>& slot, const Photon& ph, uint32_t isdet, Tally& T) {
+    int detid = (isdet == kOUT_MIN) ? -1 : (int)finddetector(C, ph.p);
+    if (!detid) return;
+    T.detected++;
+    uint64_t base = slot.fetch_add(1);
+    if (base >= C.P->maxdetphoton || !R->detp) return;
+    float* rec = R->detp + base * C.reclen;
+    uint32_t k = 0, flag = C.P->savedetflag;
+    if (flag & 0x1) rec[k++] = (float)detid;
+    for (uint32_t i = 0; i < C.partialdata; i++) rec[k++] = ph.ppath[i];
+    if (flag & 0x10) { rec[k++] = ph.p[0]; rec[k++] = ph.p[1]; rec[k++] = ph.p[2]; }
+    if (flag & 0x20) { rec[k++] = ph.v[0]; rec[k++] = ph.v[1]; rec[k++] = ph.v[2]; }
+    if (flag & 0x40) rec[k++] = ph.wlaunch;
+}
+
+struct Runner {
+    Ctx C;
+    OracleResult* R;
+    std::atomic<uint64_t>* detslot;
+
+    void deposit(uint32_t idx, int tshift, double val) {
+        double* f = R->field + (size_t)idx + (size_t)tshift * C.dimxyz;
+#pragma omp atomic
+        *f += val;
+        if (R->hits) {
+            uint64_t* h = R->hits + (size_t)idx + (size_t)tshift * C.dimxyz;
+#pragma omp atomic
+            *h += 1;
+        }
+    }
+
+    // Terminate the current photon (energy and detection bookkeeping, src/mcx_core.cu:1113-1182).
+    void terminate(Photon& ph, uint32_t isdet, Tally& T) {
+        const OracleProblem* P = C.P;
+        bool det = false;
+        if (P->savedet && (isdet & kDET_MASK) == kDET_MASK && ph.mediaid == 0) {
+            uint64_t before = T.detected;
+            savedetphoton(C, R, *detslot, ph, isdet, T);
+            det = T.detected != before;
+        }
+        if (det) T.e_detect += ph.w; else T.e_escape += ph.w;
+        // absorption since the last recorded deposit is not in the field
+        T.e_absother += (double)ph.w0 - (double)ph.w;
+    }
+
+    // Launch a pencil-beam photon (src/mcx_core.cu:1236-1243, 1646-1717).  Returns false on failure.
+    bool launch(Photon& ph, Tally& T) {
+        const OracleProblem* P = C.P;
+        float attempts = 1.f;
+        do {
+            ph.p[0] = P->srcpos[0]; ph.p[1] = P->srcpos[1]; ph.p[2] = P->srcpos[2]; ph.w = P->srcpos[3];
+            ph.v[0] = P->srcdir[0]; ph.v[1] = P->srcdir[1]; ph.v[2] = P->srcdir[2];
+            ph.pscat = 0.f; ph.t = 0.f; ph.pathlen = C.minaccumtime;
+            ph.idx1d = P->src_idx;
+            ph.mediaid = P->src_med;
+            ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
+            if ((ph.mediaid & kMED_MASK) == 0) {
+                int id = skipvoid(C, ph);
+                if (id >= 0) {
+                    ph.idx1d = (uint32_t)id;
+                    ph.mediaid = P->vol[ph.idx1d];
+                }
+            }
+            ph.fd[0] = (short)std::floor(ph.p[0]);
+            ph.fd[1] = (short)std::floor(ph.p[1]);
+            ph.fd[2] = (short)std::floor(ph.p[2]);
+            attempts += 1.f;
+            if (attempts > (float)P->maxvoidstep) return false;
+        } while ((ph.mediaid & kMED_MASK) == 0 || std::fabs(ph.w) <= P->minenergy);
+        ph.prop = C.prop[ph.mediaid & kMED_MASK];
+        T.e_launch += ph.w;
+        T.launches++;
+        ph.w0 = ph.w;
+        ph.wlaunch = ph.w;
+        ph.nscat = kEPS;
+        ph.pathlen = 0.f;
+        ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
+        ph.isdet = (int)(ph.mediaid & kDET_MASK);
+        ph.mediaid &= kMED_MASK;
+        if (P->savedet) std::memset(ph.ppath, 0, sizeof(float) * C.partialdata);
+        return true;
+    }
+
+    // One photon from launch to termination (src/mcx_core.cu:1888-2514).
+    void run_photon(uint64_t pid, Tally& T) {
+        const OracleProblem* P = C.P;
+        Photon ph;
+        Rng rng;
+        seed_photon(rng, P->seed, pid);
+        std::memset(&ph, 0, sizeof(ph));
+        ph.fd[3] = -1;
+        if (!launch(ph, T)) return;
+        const uint32_t flag = P->savedetflag;
+        const int save_nscat = P->savedet && (flag & 0x2);
+        const int save_ppath = P->savedet && (flag & 0x4);
+        const int save_mom = P->savedet && (flag & 0x8);
+        const uint32_t M = C.medianum - 1;
+        const float n0 = C.prop[0].n;
+        const double maxsteps = 1e9;
+
+        for (double guard = 0; guard < maxsteps; guard += 1) {
+            T.steps++;
+            if (ph.pscat <= 0.f) {
+                ph.pscat = -std::log(rng.next() + kEPS);
+                if (ph.nscat != kEPS) {
+                    float cphi = 1.f, sphi = 0.f, stheta, ctheta, tmp0;
+                    tmp0 = kTWO_PI * rng.next();
+                    sphi = std::sin(tmp0); cphi = std::cos(tmp0);
+                    tmp0 = (ph.nscat > (float)P->gscatter) ? 0.f : ph.prop.g;
+                    if (std::fabs(tmp0) > kEPS) {
+                        const float g = ph.prop.g;
+                        tmp0 = (1.f - g * g) / (1.f - g + 2.f * g * rng.next());
+                        tmp0 *= tmp0;
+                        tmp0 = (1.f + g * g - tmp0) / (2.f * g);
+                        tmp0 = std::fmax(-1.f, std::fmin(1.f, tmp0));
+                        float theta = std::acos(tmp0);
+                        stheta = std::sin(theta);
+                        ctheta = tmp0;
+                    } else {
+                        float theta = std::acos(2.f * rng.next() - 1.f);
+                        stheta = std::sin(theta); ctheta = std::cos(theta);
+                    }
+                    if (save_nscat) ph.ppath[ph.mediaid - 1] += 1.f;
+                    if (save_mom) ph.ppath[M * (save_nscat + save_ppath) + ph.mediaid - 1] += 1.f - ctheta;
+                    rotatevector(ph.v, stheta, ctheta, sphi, cphi);
+                    ph.nscat += 1.f;
+                    ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
+                    T.scatters++;
+                }
+                ph.nscat = (float)(int)ph.nscat;
+            }
+
+            float n1 = ph.prop.n;
+            ph.prop = C.prop[ph.mediaid];
+
+            float len = hitgrid(ph.p, ph.v, ph.rv, ph.fd);
+            float musp = ph.prop.mus * ((ph.nscat + 1.f > (float)P->gscatter) ? (1.f - ph.prop.g) : 1.f);
+            float slen = len * musp;
+            slen = std::fmin(slen, ph.pscat);
+            len = (ph.prop.mus == 0.f) ? len : (slen / musp);
+
+            ph.p[0] += len * ph.v[0]; ph.p[1] += len * ph.v[1]; ph.p[2] += len * ph.v[2];
+            const bool stay = (slen == ph.pscat);
+            if (ph.fd[3] == 0) ph.fd[0] += stay ? 0 : (ph.v[0] > 0.f ? 1 : -1);
+            if (ph.fd[3] == 1) ph.fd[1] += stay ? 0 : (ph.v[1] > 0.f ? 1 : -1);
+            if (ph.fd[3] == 2) ph.fd[2] += stay ? 0 : (ph.v[2] > 0.f ? 1 : -1);
+
+            ph.w *= std::exp(-ph.prop.mua * len);
+            ph.pscat -= slen;
+            ph.t += len * ph.prop.n * C.oneoverc0;
+            ph.pathlen += len;
+            if (save_ppath) ph.ppath[M * save_nscat + ph.mediaid - 1] += len;
+
+            uint32_t mediaidold = ph.mediaid | ((uint32_t)ph.isdet & kDET_MASK);
+            uint32_t idx1dold = ph.idx1d;
+            ph.idx1d = vidx(C, ph.fd);
+            uint32_t isdet;
+            if (!inside(C, ph.fd)) {
+                ph.mediaid = 0;
+                ph.idx1d = (ph.fd[0] < 0 || ph.fd[1] < 0 || ph.fd[2] < 0) ? kOUT_MIN : kOUT_MAX;
+                isdet = (uint8_t)P->bc[(ph.idx1d == kOUT_MAX) * 3 + ph.fd[3]];
+            } else {
+                uint32_t m = P->vol[ph.idx1d];
+                isdet = m & kDET_MASK;
+                ph.mediaid = m & kMED_MASK;
+            }
+            ph.isdet = (int)isdet;
+
+            if (ph.idx1d != idx1dold && mediaidold) {
+                bool rec = false;
+                if (P->save2pt && ph.t >= C.twin0 && ph.t < C.twin1) {
+                    int tshift = (int)std::floor((ph.t - C.twin0) * C.Rtstep);
+                    if (tshift > (int)C.maxgate - 1) tshift = (int)C.maxgate - 1;
+                    float weight = 0.f;
+                    if (P->outputtype == 2) weight = ph.w0 - ph.w;                     // energy
+                    else if (P->outputtype == 0 || P->outputtype == 1)                 // flux / fluence
+                        weight = (ph.prop.mua < kEPS) ? (ph.w0 * ph.pathlen) : (ph.w0 - ph.w) / ph.prop.mua;
+                    else if (P->outputtype == 7) weight = ph.w0 * ph.pathlen;          // L
+                    if (std::fabs(weight) > 0.f) {
+                        deposit(idx1dold, tshift, (double)weight);
+                        T.deposits++;
+                        rec = true;
+                    }
+                }
+                if (rec) T.e_absdep += (double)ph.w0 - (double)ph.w;
+                else T.e_absother += (double)ph.w0 - (double)ph.w;
+                ph.w0 = ph.w;
+                ph.pathlen = 0.f;
+            } else {
+                ph.mediaid = mediaidold & kMED_MASK;   // same voxel: the label is unchanged
+            }
+            const uint32_t med = ph.mediaid;
+            const int bcf = (int)(isdet & 0xF);
+
+            // termination: exit to a 0 voxel without reflection, or beyond the time window
+            if ((med == 0 && ((!C.isreflect || (C.isreflect && n1 == n0)) ||
+                              ((bcf == BC_UNKNOWN && !P->isreflect) || bcf == BC_ABSORB || bcf == BC_CYCLIC)) && bcf != BC_MIRROR) ||
+                ph.t > C.twin1) {
+                if (isdet == BC_CYCLIC) {
+                    float* pp = ph.p;
+                    const float mx[3] = {C.maxx, C.maxy, C.maxz};
+                    int a = ph.fd[3];
+                    pp[a] = nextafter_mcx(std::round(pp[a] + ((ph.idx1d == kOUT_MIN) ? mx[a] : -mx[a])),
+                                          (ph.v[a] > 0.f) - (ph.v[a] < 0.f), (float)P->maxvoidstep);
+                    ph.fd[a] = (short)std::floor(pp[a]);
+                    if (inside(C, ph.fd)) {
+                        ph.idx1d = vidx(C, ph.fd);
+                        uint32_t m = P->vol[ph.idx1d];
+                        ph.isdet = (int)(m & kDET_MASK);
+                        ph.mediaid = m & kMED_MASK;
+                        continue;
+                    }
+                }
+                uint32_t detflag = (((ph.idx1d == kOUT_MAX && P->bc[9 + ph.fd[3]]) || (ph.idx1d == kOUT_MIN && P->bc[6 + ph.fd[3]]))
+                                    ? kOUT_MIN : (mediaidold & kDET_MASK));
+                ph.mediaid = med;
+                terminate(ph, detflag, T);
+                T.photons++;
+                return;
+            }
+
+            // Russian roulette (src/mcx_core.cu:2357-2378)
+            if (std::fabs(ph.w) < P->minenergy) {
+                if (rng.next() * 10.f <= 1.f) {
+                    ph.w *= 10.f;
+                } else {
+                    ph.mediaid = med;
+                    terminate(ph, mediaidold & kDET_MASK, T);
+                    T.photons++;
+                    return;
+                }
+            }
+
+            if (C.isreflect) {
+                ph.prop = C.prop[med];
+                if (((med && P->isreflect) ||
+                     (med == 0 && ((bcf == BC_UNKNOWN && P->isreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
+                    (bcf == BC_MIRROR || n1 != ph.prop.n)) {
+                    float Rtotal = 1.f;
+                    float tmp0 = n1 * n1, tmp1 = ph.prop.n * ph.prop.n;
+                    int a = ph.fd[3];
+                    float cphi = std::fabs(ph.v[a]);
+                    float sphi = 1.f - cphi * cphi;
+                    float c2 = 1.f - tmp0 / tmp1 * sphi;
+                    if (c2 > 0.f && bcf != BC_MIRROR) {
+                        float ctheta = tmp0 * cphi * cphi + tmp1 * c2;
+                        float stheta = 2.f * n1 * ph.prop.n * cphi * std::sqrt(c2);
+                        Rtotal = (ctheta - stheta) / (ctheta + stheta);
+                        ctheta = tmp1 * cphi * cphi + tmp0 * c2;
+                        Rtotal = (Rtotal + (ctheta - stheta) / (ctheta + stheta)) * 0.5f;
+                    }
+                    if (Rtotal < 1.f && !(med == 0 && bcf == BC_MIRROR) && rng.next() > Rtotal) {
+                        transmit(ph.v, n1, ph.prop.n, a);
+                        if (med == 0) {
+                            uint32_t detflag = (((ph.idx1d == kOUT_MAX && P->bc[9 + a]) || (ph.idx1d == kOUT_MIN && P->bc[6 + a]))
+                                                ? kOUT_MIN : (mediaidold & kDET_MASK));
+                            ph.mediaid = 0;
+                            terminate(ph, detflag, T);
+                            T.photons++;
+                            return;
+                        }
+                        ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
+                    } else {
+                        ph.v[a] = -ph.v[a];
+                        ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
+                        ph.p[a] = nextafter_mcx(std::nearbyint(ph.p[a]), (ph.v[a] > 0.f) - (ph.v[a] < 0.f), (float)P->maxvoidstep);
+                        ph.fd[a] = (short)std::floor(ph.p[a]);
+                        ph.idx1d = idx1dold;
+                        ph.mediaid = P->vol[ph.idx1d] & kMED_MASK;
+                        ph.prop = C.prop[ph.mediaid];
+                    }
+                } else {
+                    ph.prop = C.prop[mediaidold & kMED_MASK];
+                }
+            }
+        }
+        // unreachable for physical inputs; counted as escaped so the balance still closes
+        terminate(ph, 0, T);
+        T.photons++;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int oracle_version(void) { return 1; }
+
+// src/mcx_core.cu:1731-1742 with the host seeding of src/mcx_core.cu:3062-3066: the
+// generator is seeded with four 32-bit words and emits n uniform floats.
+void oracle_rng_kat(const uint32_t seeds[4], float* out, int n) {
+    Rng r;
+    r.s[0] = ((uint64_t)seeds[0] << 32) | seeds[1];
+    r.s[1] = ((uint64_t)seeds[2] << 32) | seeds[3];
+    for (int i = 0; i < n; i++) out[i] = r.next();
+}
+
+// Per-photon seeded stream, identical to the GB300 engine's: n floats of photon `pid`.
+void oracle_photon_stream(uint64_t seed, uint64_t pid, float* out, int n) {
+    Rng r;
+    seed_photon(r, seed, pid);
+    for (int i = 0; i < n; i++) out[i] = r.next();
+}
+
+int oracle_run(const OracleProblem* P, OracleResult* R) {
+    if (!P || !R || !P->vol || !P->prop || P->medianum < 1 || P->medianum > 128) return -1;
+    if (!R->field && P->save2pt) return -2;
+    Ctx C;
+    C.P = P;
+    C.nx = P->dim[0]; C.ny = P->dim[1]; C.nz = P->dim[2];
+    C.dimxy = C.nx * C.ny; C.dimxyz = C.dimxy * C.nz;
+    C.maxx = (float)C.nx; C.maxy = (float)C.ny; C.maxz = (float)C.nz;
+    C.oneoverc0 = kR_C0 * P->unitinmm;
+    C.minaccumtime = kR_C0 * P->unitinmm;
+    C.Rtstep = 1.f / P->tstep;
+    C.twin0 = P->twin0;
+    C.twin1 = P->twin1;
+    C.maxgate = P->maxgate;
+    C.medianum = P->medianum;
+    C.detnum = P->detnum;
+    uint32_t flag = P->savedetflag;
+    C.partialdata = (P->medianum - 1) * (((flag >> 1) & 1) + ((flag >> 2) & 1) + ((flag >> 3) & 1));
+    C.reclen = C.partialdata + (flag & 1) + 3 * (((flag >> 4) & 1) + ((flag >> 5) & 1)) + ((flag >> 6) & 1);
+    C.isreflect = P->isreflect;
+    for (int i = 0; i < 6; i++)
+        if (P->bc[i] == BC_REFLECT || P->bc[i] == BC_MIRROR) C.isreflect = 1;
+    std::vector<Prop> props(P->medianum);
+    for (uint32_t i = 0; i < P->medianum; i++) props[i] = {P->prop[4 * i], P->prop[4 * i + 1], P->prop[4 * i + 2], P->prop[4 * i + 3]};
+    C.prop = props.data();
+
+    std::atomic<uint64_t> slot(0);
+    Runner run;
+    run.C = C;
+    run.R = R;
+    run.detslot = &slot;
+
+    int nthreads = P->nthreads > 0 ? P->nthreads : 1;
+    std::vector<Tally> tallies(nthreads);
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t N = (int64_t)P->nphoton;
+#pragma omp parallel num_threads(nthreads)
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        Tally& T = tallies[tid];
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t i = 0; i < N; i++) run.run_photon(P->photon_offset + (uint64_t)i, T);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    Tally S;
+    for (auto& T : tallies) {
+        S.e_launch += T.e_launch; S.e_escape += T.e_escape; S.e_detect += T.e_detect;
+        S.e_absdep += T.e_absdep; S.e_absother += T.e_absother;
+        S.steps += T.steps; S.scatters += T.scatters; S.deposits += T.deposits;
+        S.launches += T.launches; S.detected += T.detected; S.photons += T.photons;
+    }
+    R->e_launch = S.e_launch; R->e_escape = S.e_escape; R->e_detect = S.e_detect;
+    R->e_absdep = S.e_absdep; R->e_absother = S.e_absother;
+    R->n_steps = S.steps; R->n_scatter = S.scatters; R->n_deposit = S.deposits;
+    R->n_launch = S.launches; R->n_detected = S.detected; R->n_photon = S.photons;
+    R->n_saved = slot.load() < P->maxdetphoton ? slot.load() : P->maxdetphoton;
+    R->reclen = C.reclen;
+    R->seconds = std::chrono::duration<double>(t1 - t0).count();
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+/* mcx_oracle.h -- C interface of the CPU oracle (test infrastructure only; see mcx_oracle.cpp). */
+#ifndef MCX_ORACLE_H
+#define MCX_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One preprocessed simulation: the same inputs the engine receives through Config after
+ * mcx_preprocess/mcx_maskdet (positions in grid units, mua/mus already scaled by unitinmm,
+ * bit 31 of vol = detector mask, src_idx/src_med = the launch voxel and its label). */
+typedef struct OracleProblem {
+    const uint32_t* vol;
+    uint32_t dim[3];
+    const float* prop;        /* medianum x {mua, mus, g, n} */
+    uint32_t medianum;
+    const float* detpos;      /* detnum x {x, y, z, r} */
+    uint32_t detnum;
+    float srcpos[4];          /* w = launch weight */
+    float srcdir[4];
+    uint32_t src_idx, src_med;
+    float twin0, twin1, tstep;
+    uint32_t maxgate;
+    float unitinmm;
+    int isreflect, isspecular, voidtime, maxvoidstep, save2pt, outputtype;
+    float minenergy;
+    uint32_t gscatter;
+    char bc[12];
+    int savedet;
+    uint32_t savedetflag, maxdetphoton;
+    uint64_t nphoton, photon_offset, seed;
+    int nthreads;
+} OracleProblem;
+
+/* Outputs: raw (unnormalised) field in FP64, optional per-voxel deposit counts, detected
+ * records, energy tallies and the algorithmic counters the roofline uses. */
+typedef struct OracleResult {
+    double* field;            /* maxgate x Nvox, accumulated (+=) */
+    uint64_t* hits;           /* optional, same shape */
+    float* detp;              /* optional, maxdetphoton x reclen */
+    double e_launch, e_escape, e_detect, e_absdep, e_absother;
+    uint64_t n_steps, n_scatter, n_deposit, n_launch, n_detected, n_photon, n_saved;
+    uint32_t reclen;
+    double seconds;
+} OracleResult;
+
+int  oracle_version(void);
+int  oracle_run(const OracleProblem* problem, OracleResult* result);
+void oracle_rng_kat(const uint32_t seeds[4], float* out, int n);
+void oracle_photon_stream(uint64_t seed, uint64_t pid, float* out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

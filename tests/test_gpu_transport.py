@@ -1,0 +1,254 @@
+"""Parity of the GB300 transport kernel with the CPU oracle and the reference goldens.
+
+Every test here runs the engine through its C-ABI (mcx_run_simulation via mcx_gb300.run, or the
+session / RNG entry points) on cuda:0.  Tolerances:
+  * integer work (RNG streams, photon counts, launch-shape independence of detected records):
+    bit-exact;
+  * per-voxel fluence: 16 independent seeds per side, per-voxel means within 3 standard errors
+    (tests/stats.py) in voxels with more than 1e3 oracle deposits;
+  * energy balance launched = absorbed + escaped + detected: 1e-5 relative (FP64 tallies);
+  * FP32 field accumulation against the FP64-accumulated twin: 1e-4 relative on the total,
+    2e-3 per voxel in voxels with more than 1e3 deposits.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mcx_gb300 import problems
+
+from .stats import assert_parity
+from .test_oracle_golden import diffusion_ratio, glibc_seed_words
+
+pytestmark = pytest.mark.gpu
+
+SEEDS = [1000 + 17 * i for i in range(16)]
+
+
+@pytest.fixture(scope="module")
+def lib(engine):
+    from mcx_gb300._lib import lib as L
+
+    return L
+
+
+def balance(s):
+    return abs(s["e_launch"] - (s["e_absdep"] + s["e_absother"] + s["e_escape"] + s["e_detect"])) / s["e_launch"]
+
+
+# ----------------------------------------------------------------------------- RNG -------------
+def test_rng_kat_gpu_bit_exact(lib, goldens):
+    seeds = (C.c_uint32 * 4)(*glibc_seed_words())
+    out = (C.c_float * 8)()
+    assert lib.mcxg_rng_test(seeds, out, 8) == 0, lib.mcxg_last_error()
+    got = np.frombuffer(out, np.float32).reshape(2, 2, 2, order="F")
+    expect = np.array(goldens["rng_kat"]["values_rowmajor"], np.float32).reshape(2, 2, 2)
+    assert np.array_equal(got, expect)
+
+
+@pytest.mark.parametrize("pid", [0, 1, 12345, 2**40 + 7])
+def test_photon_stream_matches_oracle(lib, oracle, pid):
+    out = (C.c_float * 256)()
+    assert lib.mcxg_photon_stream(987654321, pid, out, 256) == 0
+    assert np.array_equal(np.frombuffer(out, np.float32), oracle.photon_stream(987654321, pid, 256))
+
+
+# ----------------------------------------------------------------------------- goldens ---------
+@pytest.mark.parametrize("deck,idx", [("cube60", 0), ("cube60b", 1)])
+def test_absorbed_fraction_golden(engine, goldens, deck, idx):
+    g = goldens["absorbed_fraction"][idx]
+    r = engine.run(getattr(problems, deck)(1e6))
+    s = r["stat"]
+    frac = s["energyabs"] / s["energytot"]
+    assert g["lo"] <= frac < g["hi"], (frac, g["source"])
+    assert abs(s["energytot"] - 1e6) <= 10
+    assert s["n_photon"] == 1_000_000 and s["error_flags"] == 0
+    assert balance(s) < 1e-5
+
+
+def test_absorbed_fraction_golden_1e8(engine, goldens):
+    for g, deck in ((goldens["absorbed_fraction"][2], problems.cube60), (goldens["absorbed_fraction"][3], problems.sphere60b)):
+        r = engine.run(deck(g["nphoton"]))
+        s = r["stat"]
+        frac = s["energyabs"] / s["energytot"]
+        assert abs(frac - g["value"]) <= g["tol"], (frac, g["source"])
+        assert abs(s["energytot"] - g["nphoton"]) <= 10
+        assert balance(s) < 1e-5
+
+
+def test_detected_golden(engine, goldens):
+    g = goldens["detected"]
+    r = engine.run(problems.cube60b(g["nphoton"]))
+    assert g["lo"] <= r["stat"]["detected"] <= g["hi"]
+    assert r["detp"].shape == (3, r["stat"]["detected"])
+    assert set(np.unique(r["detp"][0]).astype(int)) <= {1, 2, 3, 4}
+
+
+def test_boundary_conditions_golden(engine, goldens):
+    g = goldens["boundary_detected"]
+    cfg = problems.cube60(g["nphoton"])
+    cfg["bc"] = g["bc"]
+    r = engine.run(cfg)
+    assert g["lo"] <= r["stat"]["detected"] <= g["hi"]
+    assert np.all(r["detp"][0] == -1)
+    g = goldens["cyclic"]
+    cfg = problems.cube60(g["nphoton"])
+    cfg.update(bc=g["bc"], issavedet=0)
+    s = engine.run(cfg)["stat"]
+    assert g["lo"] <= s["energyabs"] / s["energytot"] <= g["hi"]
+    g = goldens["reflect_bc"]
+    cfg = problems.cube60(g["nphoton"])
+    cfg.update(bc=g["bc"], isreflect=g["isreflect"])
+    s = engine.run(cfg)["stat"]
+    assert g["lo"] <= s["energyabs"] / s["energytot"] < g["hi"]
+
+
+# ----------------------------------------------------------------------------- parity ----------
+def _stack_gpu(engine, cfg_fn, n, seeds):
+    out = []
+    for sd in seeds:
+        r = engine.run(cfg_fn(n, seed=sd))
+        assert r["stat"]["error_flags"] == 0
+        out.append(r["flux"])
+    return np.stack(out)
+
+
+def _stack_oracle(engine, oracle, cfg_fn, n, seeds):
+    out, hits = [], None
+    pc = engine.prepare(cfg_fn(n))
+    for sd in seeds:
+        r = oracle.run(pc, seed=sd, hits=True)
+        out.append(r["flux"])
+        hits = r["hits"] if hits is None else hits + r["hits"]
+    return np.stack(out), hits
+
+
+@pytest.mark.parametrize("name,n", [("workload0", 100000), ("workload1", 50000)])
+def test_voxel_parity_16_seeds(engine, oracle, name, n):
+    fn = getattr(problems, name)
+    gpu = _stack_gpu(engine, fn, n, SEEDS)
+    cpu, hits = _stack_oracle(engine, oracle, fn, n, [s + 500000 for s in SEEDS])
+    rep = assert_parity(gpu, cpu, hits > 1000)
+    print(name, rep)
+
+
+def _small_layered(n, seed=0):
+    cfg = problems.workload2(n, seed=seed, n=64)
+    return cfg
+
+
+def test_voxel_parity_layered_skipvoid(engine, oracle):
+    gpu = _stack_gpu(engine, _small_layered, 20000, SEEDS)
+    cpu, hits = _stack_oracle(engine, oracle, _small_layered, 20000, [s + 500000 for s in SEEDS])
+    rep = assert_parity(gpu, cpu, hits > 1000)
+    print("layered64", rep)
+
+
+def test_step_and_deposit_counts_match_oracle(engine, oracle):
+    """Mean steps, scatters and deposits per photon are algorithmic quantities: the GPU's own
+    counters must agree with the oracle's within 4 standard errors of the photon mean."""
+    for fn, n in ((problems.workload0, 200000), (problems.workload1, 100000)):
+        g = engine.run(fn(n, seed=11))["stat"]
+        o = oracle.run(engine.prepare(fn(n)), seed=12)["stat"]
+        for key in ("n_steps", "n_scatter", "n_deposit"):
+            mg, mo = g[key] / g["n_photon"], o[key] / o["n_photon"]
+            # per-photon counts have a coefficient of variation below 1.5
+            assert abs(mg - mo) <= 4 * 1.5 * mo / np.sqrt(n), (fn.__name__, key, mg, mo)
+
+
+def test_detected_photons_parity(engine, oracle):
+    n = 1_000_000
+    g = engine.run(problems.workload1(n, seed=3))
+    o = oracle.run(engine.prepare(problems.workload1(n)), seed=4)
+    dg, do = g["detp"], o["detp"]
+    assert dg.shape[0] == do.shape[0] == 1 + 2 + 2      # detid, nscat(2), ppath(2)
+    for det in (1, 2, 3, 4):
+        ng, no = int((dg[0] == det).sum()), int((do[0] == det).sum())
+        assert abs(ng - no) <= 3 * np.sqrt(ng + no + 1), (det, ng, no)
+        if min(ng, no) > 50:
+            for row in range(1, 5):
+                a, b = dg[row][dg[0] == det], do[row][do[0] == det]
+                se = np.sqrt(a.var(ddof=1) / a.size + b.var(ddof=1) / b.size)
+                assert abs(a.mean() - b.mean()) <= 4 * se + 1e-6, (det, row, a.mean(), b.mean())
+
+
+def test_energy_balance_and_fp32_accumulation(engine):
+    cfg = problems.workload0(10_000_000, seed=77)
+    r32 = engine.run(cfg)
+    r64 = engine.run(cfg, fp64_field=True)
+    s = r32["stat"]
+    assert balance(s) < 1e-5 and balance(r64["stat"]) < 1e-5
+    # identical photon histories: the only difference is how the field was accumulated
+    assert r32["stat"]["n_steps"] == r64["stat"]["n_steps"]
+    f32, f64 = r32["flux"].astype(np.float64), r64["flux"].astype(np.float64)
+    tot_err = abs(f32.sum() - f64.sum()) / f64.sum()
+    assert tot_err < 1e-4, tot_err
+    hot = f64 > np.quantile(f64, 0.9)
+    rel = np.abs(f32[hot] - f64[hot]) / f64[hot]
+    assert rel.max() < 2e-3, rel.max()
+    # sum of flux*mua*Vvox/normaliser recovers the absorbed weight recorded by the kernel
+    raw = f32[..., 0] / s["normalizer"]
+    assert abs(raw.sum() * 0.005 - s["e_absdep"]) / s["e_absdep"] < 1e-4
+
+
+def test_diffusion_agreement_gpu(engine):
+    r = engine.run(problems.workload0(10_000_000, seed=5))
+    ratios = diffusion_ratio(r["flux"], 5e-9)
+    assert np.all(np.abs(ratios - 1.0) < 0.05), ratios
+
+
+# ----------------------------------------------------------------------------- engine ----------
+def test_launch_shape_independence(engine, lib):
+    """Photons are seeded by index, so block size and refill chunk change nothing but the FP32
+    summation order: detected records are bitwise identical, counters identical."""
+    cfg = problems.workload1(300000, seed=9)
+    try:
+        lib.mcxg_set_launch(128, 0, 8, -1)
+        a = engine.run(cfg)
+        lib.mcxg_set_launch(256, 2, 64, 0)
+        b = engine.run(cfg)
+    finally:
+        lib.mcxg_set_launch(0, 0, 0, -1)
+    for key in ("n_steps", "n_scatter", "n_deposit", "n_launch", "n_photon", "n_detected"):
+        assert a["stat"][key] == b["stat"][key], key
+    da = a["detp"][:, np.lexsort(a["detp"][::-1])]
+    db = b["detp"][:, np.lexsort(b["detp"][::-1])]
+    assert np.array_equal(da, db)
+    assert np.allclose(a["flux"], b["flux"], rtol=1e-4, atol=1e-9 * a["flux"].max())
+    assert abs(a["stat"]["e_absdep"] - b["stat"]["e_absdep"]) / a["stat"]["e_absdep"] < 1e-9
+
+
+def test_session_matches_run(engine):
+    cfg = problems.workload0(200000, seed=21)
+    r = engine.run(cfg)
+    pc = engine.prepare(problems.workload0(200000, seed=21))
+    with engine.Session(pc) as s:
+        s.run(0, 200000, 21)
+        field, _, _, st = s.read()
+    raw = r["flux"] / r["stat"]["normalizer"]
+    assert st.n_steps == r["stat"]["n_steps"]
+    assert np.allclose(field, raw, rtol=1e-4, atol=1e-6 * raw.max())
+
+
+def test_respin_accumulates(engine):
+    cfg = problems.workload0(100000, seed=31)
+    cfg["respin"] = 3
+    r = engine.run(cfg)
+    assert r["stat"]["n_photon"] == 300000 and r["stat"]["launches"] == 3
+    assert abs(r["stat"]["energytot"] - 300000) <= 10
+
+
+def test_errors_are_reported_not_faulted(engine):
+    cfg = problems.workload0(1000)
+    cfg["vol"] = cfg["vol"] * 3                      # label 3 with only 2 property rows
+    with pytest.raises(engine.MCXError):
+        engine.run(cfg)
+    cfg = problems.workload0(1000)
+    cfg["srctype"] = "planar"
+    with pytest.raises(engine.MCXError):
+        engine.run(cfg)
+    # the context is still usable
+    assert engine.run(problems.workload0(1000))["stat"]["n_photon"] == 1000
