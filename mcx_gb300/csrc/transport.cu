@@ -175,12 +175,14 @@ __global__ void __launch_bounds__(256) transport_kernel(const __grid_constant__ 
             const unsigned long long avail = pool_end - pool_next;
             unsigned long long mine = pool_next + rank;
             if (avail < n) {
+                // reserve at least what the dead lanes need, normally a whole chunk
+                const unsigned long long take = max((unsigned long long)P.chunk, (unsigned long long)(n - avail));
                 unsigned long long base = 0ull;
-                if (lane == 0) base = atomicAdd(P.work, (unsigned long long)P.chunk);
+                if (lane == 0) base = atomicAdd(P.work, take);
                 base = __shfl_sync(kFull, base, 0);
                 if (rank >= avail) mine = base + (rank - avail);
                 pool_next = base + (n - avail);
-                pool_end = base + (unsigned long long)P.chunk;
+                pool_end = base + take;
                 if (base >= P.nphoton) drained = true;
             } else {
                 pool_next += n;

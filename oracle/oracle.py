@@ -51,8 +51,12 @@ def load() -> C.CDLL:
     global _lib
     if _lib is None:
         if not LIB_PATH.exists():
-            from mcx_gb300.build import build_oracle  # the recipe lives with the engine's
-            build_oracle()
+            import importlib.util
+
+            spec = importlib.util.spec_from_file_location("mcx_gb300_build", HERE.parent / "mcx_gb300" / "build.py")
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_oracle()   # the recipe lives with the engine's
         _lib = C.CDLL(str(LIB_PATH))
         _lib.oracle_run.argtypes = [C.POINTER(OracleProblem), C.POINTER(OracleResult)]
         _lib.oracle_run.restype = C.c_int

@@ -20,9 +20,9 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def built():
     """Build the engine and the oracle once per session (fast no-op when up to date)."""
-    from mcx_gb300.build import build_all
+    import __graft_entry__
 
-    build_all()
+    __graft_entry__.build()
     return True
 
 
