@@ -95,6 +95,30 @@ void mcxg_session_destroy(mcxg_session* s);
 /* Launch-shape override used by the autotuner (0 = engine default). */
 void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile);
 
+/* ---- Allocation-free transport ----------------------------------------------------------- */
+
+/* No counterpart in MCX: an addition for callers that may not call cudaMalloc while they run,
+ * such as an application that owns all device memory through its own pool, or a latency-bound
+ * loop that cannot afford cudaMalloc's implicit device synchronisation.
+ *
+ * One transport launch over photons [photon_offset, photon_offset + nphoton) of the prepared
+ * Config `cfg` (mcxg_validatecfg or MCX's mcx_validatecfg), time-gate group `gate_group`, on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) of the current device.  The caller
+ * owns every buffer: d_labels (Nvox bytes, bit 7 = detector mask, bits 0-6 = medium label),
+ * d_field and d_spill (maxgate x Nvox floats each, zeroed by the caller before the first call;
+ * the fluence is their sum, unnormalised), d_detp (maxdetphoton x reclen floats; may be NULL when
+ * no detectors are saved).  Nothing is allocated: the photon counter, counters, FP64 energy
+ * tallies, error word and detector table live in a static device array of
+ * mcxg_noalloc_scratch_bytes() bytes that every GPU using the library keeps until the process
+ * exits.  Limits: at most 256 detectors.  The first call on a device looks up that array's device
+ * address, so make it before any stream capture.  Calls share the array and clear it on entry:
+ * calls that overlap on the GPU race and must be serialised.  When `stats` is non-NULL the call
+ * waits for the stream and reports energies, counters and the error word there.  Returns 0 or a
+ * negative MCX error id (message via mcxg_last_error). */
+int mcxg_run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, float* d_spill, float* d_detp,
+                     uint64_t photon_offset, uint64_t nphoton, int gate_group, void* stream, mcxg_stats* stats);
+size_t mcxg_noalloc_scratch_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,9 +65,15 @@ lib.mcxg_session_destroy.restype = None
 lib.mcxg_set_launch.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
 lib.mcxg_set_launch.restype = None
 
+lib.mcxg_run_noalloc.argtypes = [_CFG, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64,
+                                 C.c_int, C.c_void_p, C.POINTER(abi.Stats)]
+lib.mcxg_run_noalloc.restype = C.c_int
+lib.mcxg_noalloc_scratch_bytes.argtypes = []
+lib.mcxg_noalloc_scratch_bytes.restype = C.c_size_t
+
 EXPORTED = [
     "mcx_run_simulation", "mcx_list_gpu", "mcxg_run_simulation_fp64", "mcxg_initcfg", "mcxg_validatecfg",
     "mcxg_maskdet", "mcxg_last_error", "mcxg_last_error_id", "mcxg_clear_error", "mcxg_set_error", "mcxg_get_stats",
     "mcxg_rng_test", "mcxg_photon_stream", "mcxg_session_create", "mcxg_session_reset", "mcxg_session_run",
-    "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch",
+    "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
 ]

@@ -90,6 +90,8 @@ struct DevBuf {
 
 float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 
+}  // namespace
+
 // Void skipping of a pencil source launched outside the volume or in a 0 voxel
 // (src/mcx_core.cu:866-956).  The path is deterministic, so the host traces it once and every
 // photon starts from the result.  Returns the entry voxel or -1.
@@ -165,6 +167,8 @@ int host_skipvoid(const Config* cfg, float4& p, float3& v, float& t, int fd[3]) 
         if (count++ > cfg->maxvoidstep) return -1;
     }
 }
+
+namespace {
 
 // Byte-label volume of the host uint32 volume (bit 31 -> bit 7).  Done on the device when the
 // session uploads; this host twin serves the void-skipping trace only.

@@ -1,0 +1,245 @@
+// noalloc.cu -- a transport entry point that allocates no device memory.
+//
+// Who needs it: callers that are not allowed to call cudaMalloc once they are running -- a host
+// application that owns every byte of device memory through its own pool and hands the engine
+// only buffers it carved out itself, or a latency-critical loop where cudaMalloc's implicit
+// device synchronisation is unacceptable.  Such a caller allocates the labels, the two field
+// accumulators and the detected-photon buffer up front and passes them in; the few bytes of
+// bookkeeping the kernel needs besides those (photon counter, step/deposit counters, FP64
+// energy tallies, error word, detected-photon counter, detector table) live in the static
+// device array below instead of being allocated per call.
+//
+// The array is a file-scope `__device__` object: every process that loads libmcx_gb300.so keeps
+// kScratchBytes of it on each GPU it uses until it exits.  All calls share it and it keeps the
+// last call's contents, so each call clears what has to start at zero; two calls that overlap
+// on the GPU (different streams, or different host threads on one device) race on it and must
+// be serialised by the caller.
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/mcx_abi.h"
+#include "../../include/mcx_gb300.h"
+#include "mcxg_common.h"
+#include "transport.cuh"
+
+namespace mcxg {
+namespace {
+
+// Layout of the static scratch: counters, tallies, words, then the detector table.
+constexpr size_t kOffWork = 0;                                               // 1 x u64
+constexpr size_t kOffCounters = 64;                                          // kNumCounters x u64
+constexpr size_t kOffEnergy = kOffCounters + 8 * kNumCounters;               // kNumEnergy x f64
+constexpr size_t kOffErr = kOffEnergy + 8 * kNumEnergy;                      // u32
+constexpr size_t kOffDetCount = kOffErr + 4;                                 // u32
+constexpr size_t kOffDetPos = 256;                                           // kMaxDetectors x float4
+constexpr size_t kScratchBytes = kOffDetPos + sizeof(float4) * kMaxDetectors;
+static_assert(kOffDetCount + 4 <= kOffDetPos, "scratch layout overlaps");
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (looked up once per device).
+unsigned char* scratch_for(int device) {
+    if (device < 0 || device >= kMaxDevices) MCXG_RAISE(-6, "device index out of range for the allocation-free entry point");
+    std::lock_guard<std::mutex> g(g_mu);
+    if (!g_scratch_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) MCXG_RAISE(-(int)e, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        g_scratch_ptr[device] = p;
+    }
+    return static_cast<unsigned char*>(g_scratch_ptr[device]);
+}
+
+// Kernel parameters of a prepared Config (the same values Session::create derives in
+// engine.cu), without touching device memory.
+void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
+    std::memset(&k, 0, sizeof(k));
+    const size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+    int totalgates = (int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5f);
+    if (totalgates < 1) totalgates = 1;
+    k.nx = (int)cfg->dim.x; k.ny = (int)cfg->dim.y; k.nz = (int)cfg->dim.z;
+    k.dimxy = cfg->dim.x * cfg->dim.y;
+    k.nvox = (unsigned)nvox;
+    k.medianum = (int)cfg->medianum;
+    for (unsigned i = 0; i < cfg->medianum; i++)
+        k.prop[i] = make_float4(cfg->prop[i].mua, cfg->prop[i].mus, cfg->prop[i].g, cfg->prop[i].n);
+    k.oneoverc0 = kR_C0 * cfg->unitinmm;
+    k.Rtstep = 1.f / cfg->tstep;
+    k.maxgate = (cfg->maxgate > 0) ? std::min<int>((int)cfg->maxgate, totalgates) : totalgates;
+    k.doreflect = cfg->isreflect ? 1 : 0;
+    k.save2pt = cfg->issave2pt ? 1 : 0;
+    k.outputtype = cfg->outputtype;
+    if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
+        MCXG_RAISE(-6, "the GB300 engine supports flux, fluence and energy outputs");
+    k.minenergy = cfg->minenergy;
+    k.gscatter = (float)cfg->gscatter;
+    k.maxvoidstep = (float)cfg->maxvoidstep;
+    std::memcpy(k.bc, cfg->bc, 12);
+    reflect = cfg->isreflect != 0;
+    for (int i = 0; i < 6; i++)
+        if (cfg->bc[i] == BC_REFLECT || cfg->bc[i] == BC_MIRROR) reflect = true;
+    bool bcdet = false;
+    for (int i = 6; i < 12; i++) bcdet = bcdet || cfg->bc[i] != 0;
+    savedet = cfg->issavedet && (cfg->detnum > 0 || bcdet);
+    const unsigned f = cfg->savedetflag;
+    k.savedetflag = f;
+    k.nmedia_det = (int)cfg->medianum - 1;
+    k.partialdata = (cfg->medianum - 1) * (((f >> 1) & 1u) + ((f >> 2) & 1u) + ((f >> 3) & 1u));
+    k.reclen = k.partialdata + (f & 1u) + 3u * (((f >> 4) & 1u) + ((f >> 5) & 1u)) + ((f >> 6) & 1u);
+    k.maxdet = cfg->maxdetphoton;
+    k.ndet = (int)cfg->detnum;
+
+    float4 p = cfg->srcpos;
+    float3 v = make_float3(cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z);
+    float t = 0.f;
+    uint32_t sidx, smed;
+    std::memcpy(&sidx, &cfg->srcparam2.z, 4);
+    std::memcpy(&smed, &cfg->srcparam2.w, 4);
+    int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
+    k.src_ok = 1;
+    if ((smed & kMED_MASK) == 0) {
+        const int id = host_skipvoid(cfg, p, v, t, fd);
+        if (id < 0) {
+            k.src_ok = 0;
+        } else {
+            sidx = (uint32_t)id;
+            smed = cfg->vol[id];
+        }
+    }
+    if (std::fabs(p.w) <= cfg->minenergy) k.src_ok = 0;
+    k.src_p = p;
+    k.src_v = make_float4(v.x, v.y, v.z, 0.f);
+    k.src_t = t;
+    k.src_idx = sidx;
+    k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
+    if (k.src_ok) {
+        k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
+    }
+    k.step_cap = 20000000u;
+    k.chunk = 64;
+
+    // shared-memory deposit tile over the entry point, as the session places it: 16 KB, up to
+    // four gates, a cube extending along the launch direction
+    k.tile_on = 0;
+    if (k.save2pt && k.src_ok) {
+        const int elems = 16 * 1024 / (int)sizeof(float);
+        int tg = std::min(k.maxgate, 4), edge = 1;
+        while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+        while (edge < 6 && tg > 1) {
+            tg--;
+            edge = 1;
+            while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+        }
+        edge = std::min(edge, std::max(k.nx, std::max(k.ny, k.nz)));
+        k.tnx = std::min(edge, k.nx); k.tny = std::min(edge, k.ny); k.tnz = std::min(edge, k.nz);
+        auto place = [](float c, int n, int dim) { return std::max(0, std::min(dim - n, (int)std::floor(c - 0.5f * n))); };
+        k.tx0 = place(k.src_p.x + 0.5f * edge * k.src_v.x, k.tnx, k.nx);
+        k.ty0 = place(k.src_p.y + 0.5f * edge * k.src_v.y, k.tny, k.ny);
+        k.tz0 = place(k.src_p.z + 0.5f * edge * k.src_v.z, k.tnz, k.nz);
+        k.tg0 = 0;
+        k.tng = tg;
+        k.tile_on = 1;
+    }
+}
+
+#define NCK(call)                                                                \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) MCXG_RAISE(-(int)e_, cudaGetErrorString(e_));    \
+    } while (0)
+
+void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, float* d_spill, float* d_detp,
+                 uint64_t photon_offset, uint64_t nphoton, int gate_group, cudaStream_t stream, mcxg_stats* stats) {
+    if (!cfg || !d_labels || !d_field || !d_spill) MCXG_RAISE(-4, "labels, field and spill buffers are required");
+    if (cfg->srctype != 0) MCXG_RAISE(-6, "the GB300 engine supports the pencil source only");
+    if (cfg->medianum < 1 || cfg->medianum > (unsigned)kMaxMedia) MCXG_RAISE(-6, "the GB300 engine supports 1 to 128 media labels");
+    if (cfg->detnum > (unsigned)kMaxDetectors)
+        MCXG_RAISE(-6, "the allocation-free entry point holds at most 256 detectors in its static scratch");
+    if (cfg->dim.x >= 32768 || cfg->dim.y >= 32768 || cfg->dim.z >= 32768) MCXG_RAISE(-6, "volume dimensions must be below 32768");
+    int device = 0;
+    NCK(cudaGetDevice(&device));
+    unsigned char* s = scratch_for(device);
+
+    KParams k;
+    bool reflect = false, savedet = false;
+    fill_kparams(cfg, k, reflect, savedet);
+    if (savedet && !d_detp) MCXG_RAISE(-4, "a detected-photon buffer is required when detectors are saved");
+    const float twin0 = cfg->tstart + cfg->tstep * (float)k.maxgate * (float)gate_group;
+    k.twin0 = twin0;
+    k.twin1 = twin0 + cfg->tstep * (float)k.maxgate;
+    k.labels = d_labels;
+    k.field = d_field;
+    k.shadow = d_spill;
+    k.field64 = nullptr;
+    k.detp = savedet ? d_detp : nullptr;
+    k.work = reinterpret_cast<unsigned long long*>(s + kOffWork);
+    k.counters = reinterpret_cast<unsigned long long*>(s + kOffCounters);
+    k.energy = reinterpret_cast<double*>(s + kOffEnergy);
+    k.errflag = reinterpret_cast<unsigned*>(s + kOffErr);
+    k.detcount = reinterpret_cast<unsigned*>(s + kOffDetCount);
+    k.detpos = reinterpret_cast<const float4*>(s + kOffDetPos);
+    k.photon_offset = photon_offset;
+    k.nphoton = nphoton;
+    k.seed = (uint64_t)(uint32_t)cfg->seed;
+
+    // the array keeps the previous call's values: clear every accumulator, then the detectors
+    NCK(cudaMemsetAsync(s, 0, kOffDetPos, stream));
+    if (cfg->detnum)
+        NCK(cudaMemcpyAsync(s + kOffDetPos, cfg->detpos, sizeof(float4) * cfg->detnum, cudaMemcpyHostToDevice, stream));
+
+    const int block = 256;
+    const size_t smem = transport_smem_bytes(k, block, savedet);
+    const int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+    if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
+    int sms = 0;
+    NCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NCK(launch_transport(k, reflect, savedet, bps * sms, block, smem, stream));
+
+    if (stats) {
+        double e[kNumEnergy];
+        unsigned long long c[kNumCounters];
+        unsigned words[2];
+        NCK(cudaMemcpyAsync(e, s + kOffEnergy, sizeof(e), cudaMemcpyDeviceToHost, stream));
+        NCK(cudaMemcpyAsync(c, s + kOffCounters, sizeof(c), cudaMemcpyDeviceToHost, stream));
+        NCK(cudaMemcpyAsync(words, s + kOffErr, sizeof(words), cudaMemcpyDeviceToHost, stream));
+        NCK(cudaStreamSynchronize(stream));
+        std::memset(stats, 0, sizeof(*stats));
+        stats->e_launch = e[kELaunch]; stats->e_escape = e[kEEscape]; stats->e_detect = e[kEDetect];
+        stats->e_absdep = e[kEAbsDep]; stats->e_absother = e[kEAbsOther];
+        stats->n_steps = c[kCntSteps]; stats->n_scatter = c[kCntScatter]; stats->n_deposit = c[kCntDeposit];
+        stats->n_launch = c[kCntLaunch]; stats->n_photon = c[kCntPhoton]; stats->n_detected = words[1];
+        stats->n_tile_deposit = c[kCntTileDeposit];
+        stats->grid = bps * sms; stats->block = block; stats->chunk = k.chunk; stats->launches = 1;
+        stats->error_flags = words[0];
+    }
+}
+
+}  // namespace
+}  // namespace mcxg
+
+using namespace mcxg;
+
+// Allocation-free transport launch: see include/mcx_gb300.h for the contract.
+extern "C" int mcxg_run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, float* d_spill, float* d_detp,
+                                uint64_t photon_offset, uint64_t nphoton, int gate_group, void* stream, mcxg_stats* stats) {
+    mcxg_clear_error();
+    try {
+        run_noalloc(cfg, d_labels, d_field, d_spill, d_detp, photon_offset, nphoton, gate_group,
+                    static_cast<cudaStream_t>(stream), stats);
+        return 0;
+    } catch (const Error& e) {
+        mcxg_set_error(e.id ? e.id : -1, e.msg.c_str());
+        return e.id ? e.id : -1;
+    }
+}
+
+extern "C" size_t mcxg_noalloc_scratch_bytes(void) { return kScratchBytes; }

@@ -92,6 +92,10 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
 // Occupancy-derived CTAs per SM for the chosen variant.
 int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_bytes);
 
+// Void skipping of a pencil source launched outside the volume or in a 0 voxel, traced once on
+// the host (engine.cu).  Returns the entry voxel or -1.
+int host_skipvoid(const struct MCXConfig* cfg, float4& p, float3& v, float& t, int fd[3]);
+
 cudaError_t launch_rng_test(const uint32_t* d_seeds, float* d_out, int n, cudaStream_t stream);
 cudaError_t launch_photon_stream(unsigned long long seed, unsigned long long pid, float* d_out, int n, cudaStream_t stream);
 cudaError_t launch_labels_from_vol(const uint32_t* d_vol, uint8_t* d_labels, size_t n, unsigned int medianum,
