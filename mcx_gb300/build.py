@@ -23,7 +23,7 @@ ORACLE_LIB = ORACLE_DIR / "_build" / "libmcx_oracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr"] + ARCH
+              "--expt-relaxed-constexpr", "--use_fast_math"] + ARCH
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["transport.cu", "engine.cu", "noalloc.cu"]

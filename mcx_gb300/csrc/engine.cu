@@ -353,7 +353,9 @@ struct Session {
             std::lock_guard<std::mutex> g(g_override_mu);
             o = g_override;
         }
-        block = o.block > 0 ? o.block : 256;
+        block = o.block > 0 ? std::min(o.block, 256) : 256;
+        // a CTA-per-SM cap of 1-3 selects the larger register budget
+        set_transport_variant((o.blocks_per_sm > 0 && o.blocks_per_sm <= 3) ? 3 : 4);
         choose_tile(cfg, o.tile);
         smem = transport_smem_bytes(kp, block, savedet);
         int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
@@ -462,7 +464,7 @@ struct Session {
         st->e_launch = e[kELaunch]; st->e_escape = e[kEEscape]; st->e_detect = e[kEDetect];
         st->e_absdep = e[kEAbsDep]; st->e_absother = e[kEAbsOther];
         st->n_steps = c[kCntSteps]; st->n_scatter = c[kCntScatter]; st->n_deposit = c[kCntDeposit];
-        st->n_launch = c[kCntLaunch]; st->n_photon = c[kCntPhoton]; st->n_detected = c[kCntDetected];
+        st->n_launch = c[kCntLaunch]; st->n_photon = c[kCntPhoton]; st->n_detected = detected();
         st->n_tile_deposit = c[kCntTileDeposit];
         st->kernel_ms = kernel_ms;
         st->grid = grid; st->block = block; st->chunk = kp.chunk; st->launches = launches;

@@ -78,6 +78,15 @@ struct KParams {
     // --- per-CTA shared-memory deposit tile (voxel box x gate range)
     int tile_on;
     int tx0, ty0, tz0, tnx, tny, tnz, tg0, tng;
+
+    // --- derived at launch by launch_transport() from the fields above (constant-bank operands)
+    float d_inv_c0;                 // 1 / oneoverc0: time is carried in grid-length units
+    float d_tw0, d_tw1;             // time window in grid-length units
+    float d_bin_a, d_bin_b;         // gate index = floor(t * d_bin_a - d_bin_b)
+    float d_fnx, d_fny, d_fnz;      // dimensions as floats
+    float d_tx0, d_ty0, d_tz0, d_tx1, d_ty1, d_tz1;   // tile box as floats
+    float d_n0;                     // refractive index of medium 0
+    int d_gscat;                    // gscatter as an integer threshold
 };
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
@@ -87,6 +96,10 @@ constexpr float kMaxAccum = 1000.f;
 // dynamic shared memory per CTA; returns the CUDA error of the launch.
 cudaError_t launch_transport(const KParams& p, bool reflect, bool savedet, int grid, int block,
                              size_t smem_bytes, cudaStream_t stream);
+// Register-budget variant of the transport kernel: 4 (64 registers, 4 CTAs of 256 per SM) or
+// 3 (up to 85 registers).
+void set_transport_variant(int minb);
+int transport_variant();
 // Shared memory the kernel needs for a given block size and parameter set.
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
 // Occupancy-derived CTAs per SM for the chosen variant.
