@@ -35,6 +35,7 @@
 #include <cstring>
 #include <cfloat>
 #include <chrono>
+#include <cstdlib>
 #include <vector>
 #include <atomic>
 #ifdef _OPENMP
@@ -335,12 +336,17 @@ struct Runner {
         return true;
     }
 
-    // One photon from launch to termination (src/mcx_core.cu:1888-2514).
+    // One photon with its own per-photon stream.
     void run_photon(uint64_t pid, Tally& T) {
+        Rng rng;
+        seed_photon(rng, C.P->seed, pid);
+        run_photon_with(rng, T);
+    }
+
+    // One photon from launch to termination (src/mcx_core.cu:1888-2514), drawing from `rng`.
+    void run_photon_with(Rng& rng, Tally& T) {
         const OracleProblem* P = C.P;
         Photon ph;
-        Rng rng;
-        seed_photon(rng, P->seed, pid);
         std::memset(&ph, 0, sizeof(ph));
         ph.fd[3] = -1;
         if (!launch(ph, T)) return;
@@ -590,6 +596,18 @@ int oracle_run(const OracleProblem* P, OracleResult* R) {
 
     int nthreads = P->nthreads > 0 ? P->nthreads : 1;
     std::vector<Tally> tallies(nthreads);
+    // MCX's seeds: srand(seed) then four (rand()<<16)|(rand()<<1)|(rand()>>14) words per stream
+    // (src/mcx_core.cu:3247-3251, 3381-3387), drawn in stream order
+    std::vector<uint32_t> words;
+    if (P->seed_mode == 1) {
+        if (P->mcx_threads == 0) return -3;
+        words.resize((size_t)P->mcx_threads * 4);
+        srand((unsigned)P->seed);
+        for (auto& wd : words) {
+            const unsigned a = (unsigned)rand(), b = (unsigned)rand(), c = (unsigned)rand();
+            wd = (a << 16) | (b << 1) | (c >> 14);
+        }
+    }
     auto t0 = std::chrono::steady_clock::now();
     const int64_t N = (int64_t)P->nphoton;
 #pragma omp parallel num_threads(nthreads)
@@ -599,8 +617,22 @@ int oracle_run(const OracleProblem* P, OracleResult* R) {
         tid = omp_get_thread_num();
 #endif
         Tally& T = tallies[tid];
+        if (P->seed_mode == 1) {
+            // MCX's static partition: stream i runs threadphoton (+1 for i < oddphotons) photons
+            const int64_t nthr = (int64_t)words.size() / 4;
+            const int64_t per = N / nthr, odd = N - per * nthr;
+#pragma omp for schedule(dynamic, 64)
+            for (int64_t i = 0; i < nthr; i++) {
+                Rng rng;
+                rng.s[0] = ((uint64_t)words[4 * i] << 32) | words[4 * i + 1];
+                rng.s[1] = ((uint64_t)words[4 * i + 2] << 32) | words[4 * i + 3];
+                const int64_t n = per + (i < odd ? 1 : 0);
+                for (int64_t k = 0; k < n; k++) run.run_photon_with(rng, T);
+            }
+        } else {
 #pragma omp for schedule(dynamic, 256)
-        for (int64_t i = 0; i < N; i++) run.run_photon(P->photon_offset + (uint64_t)i, T);
+            for (int64_t i = 0; i < N; i++) run.run_photon(P->photon_offset + (uint64_t)i, T);
+        }
     }
     auto t1 = std::chrono::steady_clock::now();
     Tally S;

@@ -32,6 +32,12 @@ typedef struct OracleProblem {
     uint32_t savedetflag, maxdetphoton;
     uint64_t nphoton, photon_offset, seed;
     int nthreads;
+    /* seed_mode 0: one xorshift128+ state per photon from (seed, photon index).
+     * seed_mode 1: MCX's own scheme (src/mcx_core.cu:3014-3016, 3247-3251, 3381-3387): `mcx_threads`
+     * streams seeded with glibc rand() words after srand(seed); stream i simulates
+     * nphoton/mcx_threads photons (+1 for the first nphoton%mcx_threads streams) in sequence. */
+    int seed_mode;
+    uint32_t mcx_threads;
 } OracleProblem;
 
 /* Outputs: raw (unnormalised) field in FP64, optional per-voxel deposit counts, detected

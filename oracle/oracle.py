@@ -30,7 +30,8 @@ class OracleProblem(C.Structure):
         ("isspecular", C.c_int), ("voidtime", C.c_int), ("maxvoidstep", C.c_int), ("save2pt", C.c_int),
         ("outputtype", C.c_int), ("minenergy", C.c_float), ("gscatter", C.c_uint32), ("bc", C.c_uint8 * 12),
         ("savedet", C.c_int), ("savedetflag", C.c_uint32), ("maxdetphoton", C.c_uint32), ("nphoton", C.c_uint64),
-        ("photon_offset", C.c_uint64), ("seed", C.c_uint64), ("nthreads", C.c_int),
+        ("photon_offset", C.c_uint64), ("seed", C.c_uint64), ("nthreads", C.c_int), ("seed_mode", C.c_int),
+        ("mcx_threads", C.c_uint32),
     ]
 
 
@@ -81,9 +82,10 @@ def photon_stream(seed: int, pid: int, n: int) -> np.ndarray:
 
 
 def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: int = 0, threads: int | None = None,
-        hits: bool = False, gate_group: int = 0) -> dict[str, Any]:
+        hits: bool = False, gate_group: int = 0, mcx_threads: int = 0) -> dict[str, Any]:
     """Run the oracle on a prepared Config (``mcx_gb300.prepare``).  Normalisation follows
-    src/mcx_core.cu:3823-3925 in FP64."""
+    src/mcx_core.cu:3823-3925 in FP64.  ``mcx_threads`` > 0 seeds the RNG the way MCX does for
+    that many GPU threads (glibc rand() words after srand(seed), photons split statically)."""
     c = pc.c
     nx, ny, nz = pc.dims
     nvox = nx * ny * nz
@@ -123,6 +125,8 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
     P.photon_offset = photon_offset
     P.seed = int(c.seed if seed is None else seed) & 0xFFFFFFFF
     P.nthreads = threads or os.cpu_count() or 1
+    P.seed_mode = 1 if mcx_threads else 0
+    P.mcx_threads = int(mcx_threads)
 
     field = np.zeros(nvox * maxgate, dtype=np.float64)
     hit = np.zeros(nvox * maxgate, dtype=np.uint64) if hits else None

@@ -1,0 +1,199 @@
+"""Recipe and driver for the reference MCX CUDA build (the speed bar and a statistical oracle).
+
+MCX's transport exists only as CUDA (src/mcx_core.cu); on a GB300 the reference itself is that
+file compiled for sm_103a with the shipped configuration (xorshift128+, `-DUSE_ATOMIC
+-DSAVE_DETECTORS -use_fast_math`, src/Makefile's `fermi` target).  This module
+
+  stage()  copies the reference's src/ tree from a reference checkout into baseline/_ref/src
+           (git-ignored: an install of the reference, never part of this repository's history);
+  build()  compiles baseline/_ref/src into baseline/_ref/bin/mcx with nvcc and gcc directly
+           (the reference's own makefiles are not run);
+  run()    writes an MCX JSON input for a workload dict of mcx_gb300.problems, runs the binary
+           and returns its own speed report, energies, the flux (.mc2) and detected photons
+           (.mch).
+
+Test and benchmark infrastructure only: the engine never calls it.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import re
+import shutil
+import struct
+import subprocess
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+from typing import Any
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+REF = ROOT / "baseline" / "_ref"
+SRC = REF / "src"
+BIN = REF / "bin" / "mcx"
+
+C_FILES = ["mcx_utils.c", "mcx_shapes.c", "mcx_tictoc.c", "mcx.c", "mcx_bench.c", "mcx_lang.c", "cjson/cJSON.c",
+           "ubj/ubjw.c"]
+CPP_FILES = ["mcx_neurojson.cpp", "mcx_mie.cpp"]
+ZMAT_FILES = ["zmat/zmatlib.c", "zmat/miniz/miniz.c", "zmat/lz4/lz4.c", "zmat/lz4/lz4hc.c"]
+
+
+def stage(reference: str | Path = "/root/reference") -> Path:
+    """Copy the reference's src/ tree into baseline/_ref/src (run where the checkout exists)."""
+    src = Path(reference) / "src"
+    if SRC.exists():
+        shutil.rmtree(SRC)
+    SRC.parent.mkdir(parents=True, exist_ok=True)
+    shutil.copytree(src, SRC, ignore=shutil.ignore_patterns("*.o", "*.a", "pybind11", "mcx_doxygen.cfg"))
+    for p in SRC.rglob("*"):
+        if p.is_file():
+            p.chmod(0o644)
+    return SRC
+
+
+def available() -> bool:
+    return SRC.exists() and (SRC / "mcx_core.cu").exists()
+
+
+def _cuda_home() -> Path:
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return Path(nvcc).resolve().parent.parent
+
+
+def _run(cmd: list[str], cwd: Path) -> None:
+    p = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("reference build step failed:\n" + " ".join(cmd) + "\n" + p.stdout[-3000:] + p.stderr[-3000:])
+
+
+def build(force: bool = False) -> Path:
+    """Compile the reference `mcx` binary for sm_103a from baseline/_ref/src."""
+    if BIN.exists() and not force:
+        return BIN
+    if not available():
+        raise RuntimeError("the reference sources are not staged in baseline/_ref/src")
+    cuda = _cuda_home()
+    obj = REF / "obj"
+    obj.mkdir(parents=True, exist_ok=True)
+    inc = ["-Izmat", "-Izmat/easylzma", "-Izmat/miniz", "-Iubj", f"-I{cuda}/include"]
+    jobs = []
+    objs = []
+    o = obj / "mcx_core.o"
+    objs.append(o)
+    jobs.append([str(cuda / "bin" / "nvcc"), "-c", "-DUSE_ATOMIC", "-use_fast_math", "-DSAVE_DETECTORS", "-arch=sm_103a",
+                 "-Xcompiler", "-fopenmp", "-DMCX_TARGET_NAME=\"Kilo-Kelvin\"", "-lineinfo", *inc, "-o", str(o),
+                 "mcx_core.cu"])
+    for f in C_FILES:
+        o = obj / (f.replace("/", "_") + ".o")
+        objs.append(o)
+        jobs.append(["gcc", "-std=c99", "-g", "-fopenmp", *inc, "-c", "-o", str(o), f])
+    for f in CPP_FILES:
+        o = obj / (f.replace("/", "_") + ".o")
+        objs.append(o)
+        jobs.append(["g++", "-g", "-fopenmp", *inc, "-c", "-o", str(o), f])
+    lzma = sorted(str(p.relative_to(SRC)) for p in (SRC / "zmat" / "easylzma").rglob("*.c"))
+    for f in ZMAT_FILES + lzma:
+        o = obj / (f.replace("/", "_") + ".o")
+        objs.append(o)
+        jobs.append(["gcc", "-O3", "-fPIC", "-DNO_ZLIB", "-DNO_ZSTD", "-DNO_BLOSC2", *inc, "-Izmat/easylzma/pavlov",
+                     "-c", "-o", str(o), f])
+    # objects already built from the same sources are kept (the CUDA file dominates the build)
+    jobs = [j for j in jobs if not Path(j[j.index("-o") + 1]).exists()]
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(lambda c: _run(c, SRC), jobs))
+    BIN.parent.mkdir(parents=True, exist_ok=True)
+    _run(["g++", "-o", str(BIN), *map(str, objs), "-fopenmp", f"-L{cuda}/lib64", "-lcudart_static", "-ldl", "-lrt",
+          "-lpthread", "-lm"], SRC)
+    return BIN
+
+
+def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
+    vol = np.asarray(cfg["vol"])
+    prop = np.asarray(cfg["prop"], dtype=float)
+    flag = cfg.get("savedetflag", "dp")
+    issavedet = int(cfg.get("issavedet", 1 if "detpos" in cfg else 0))
+    session_keys = {
+        "ID": session, "Photons": int(cfg["nphoton"]), "RNGSeed": int(cfg.get("seed", 1648335518)),
+        "DoMismatch": int(cfg.get("isreflect", 1)), "DoSaveVolume": 1, "DoNormalize": 1,
+        "DoPartialPath": issavedet, "OutputFormat": "mc2", "OutputType": "x", "DoAutoThread": 1,
+        "SaveDataMask": flag if isinstance(flag, str) else int(flag),
+    }
+    if "maxdetphoton" in cfg:
+        session_keys["MaxDetPhoton"] = int(cfg["maxdetphoton"])
+    out = {
+        "Session": session_keys,
+        "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0, "LengthUnit": 1,
+                   "MediaFormat": "byte", "VolumeFile": volfile,
+                   "Media": [{"mua": float(r[0]), "mus": float(r[1]), "g": float(r[2]), "n": float(r[3])} for r in prop]},
+        "Forward": {"T0": float(cfg["tstart"]), "T1": float(cfg["tend"]), "Dt": float(cfg["tstep"])},
+        "Optode": {"Source": {"Type": "pencil", "Pos": [float(x) for x in cfg["srcpos"][:3]],
+                              "Dir": [float(x) for x in cfg["srcdir"][:3]]}},
+    }
+    if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
+        out["Optode"]["Detector"] = [{"Pos": [float(d[0]), float(d[1]), float(d[2])], "R": float(d[3])}
+                                     for d in np.asarray(cfg["detpos"], float).reshape(-1, 4)]
+    if "bc" in cfg:
+        out["Session"]["BCFlags"] = cfg["bc"]
+    return out
+
+
+def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool = True,
+        timeout: float = 900.0) -> dict[str, Any]:
+    """Run the reference binary on a workload dict; returns its speed report, energies, flux
+    (F-ordered [Nx,Ny,Nz,Nt], normalised as MCX normalises) and detected records."""
+    exe = build()
+    tmp = (Path(workdir) if workdir else Path(tempfile.mkdtemp(prefix="mcxref_"))).resolve()
+    tmp.mkdir(parents=True, exist_ok=True)
+    vol = np.asarray(cfg["vol"]).astype(np.uint8)
+    volfile = tmp / "vol.bin"
+    vol.ravel(order="F").tofile(volfile)
+    session = "ref"
+    (tmp / "in.json").write_text(json.dumps(_json_input(cfg, session, str(volfile))))
+    p = subprocess.run([str(exe), "-f", "in.json"], cwd=tmp, capture_output=True, text=True, timeout=timeout)
+    log = p.stdout + p.stderr
+    (tmp / "stdout.txt").write_text(log)
+    if p.returncode != 0:
+        raise RuntimeError(f"reference mcx failed ({p.returncode}):\n{log[-3000:]}")
+    clean = re.sub(r"\x1b\[[0-9;]*m", "", log)
+    res: dict[str, Any] = {"log": clean}
+    m = re.search(r"MCX simulation speed:\s*([0-9.]+)\s*photon/ms", clean)
+    res["speed"] = float(m.group(1)) if m else None
+    m = re.search(r"kernel complete:\s*([0-9]+)\s*ms", clean)
+    res["kernel_ms_cum"] = int(m.group(1)) if m else None
+    m = re.search(r"data normalization complete\s*:\s*([0-9]+)\s*ms", clean)
+    res["normalized_ms"] = int(m.group(1)) if m else None
+    m = re.search(r"total simulated energy:\s*([0-9.]+)\s*absorbed:\s*([0-9.]+)%", clean)
+    if m:
+        res["energytot"] = float(m.group(1))
+        res["absorbed"] = float(m.group(2)) / 100.0
+    m = re.search(r"detected\s+([0-9]+)\s+photons", clean)
+    res["detected"] = int(m.group(1)) if m else 0
+    m = re.search(r"with\s+([0-9]+)\s+threads", clean)
+    res["threads"] = int(m.group(1)) if m else None
+    if keep_field:
+        ng = max(1, int((cfg["tend"] - cfg["tstart"]) / cfg["tstep"] + 0.5))
+        f = np.fromfile(tmp / f"{session}.mc2", dtype=np.float32)
+        res["flux"] = f.reshape(vol.shape + (ng,), order="F")
+    mch = tmp / f"{session}.mch"
+    if mch.exists():
+        raw = mch.read_bytes()
+        hdr = struct.unpack("<4s14I", raw[:60])   # magic, version..savedetflag
+        colcount = hdr[4]
+        data = np.frombuffer(raw[64:], dtype=np.float32)
+        n = data.size // max(1, colcount)
+        res["detp"] = data[: n * colcount].reshape((colcount, n), order="F")
+    if not workdir:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return res
+
+
+if __name__ == "__main__":
+    import sys
+
+    if len(sys.argv) > 1 and sys.argv[1] == "stage":
+        print(stage(sys.argv[2] if len(sys.argv) > 2 else "/root/reference"))
+    else:
+        print(build(force="--force" in sys.argv))

@@ -1,0 +1,131 @@
+"""The drop-in boundary on CPU: struct layouts, exported symbols, Config preparation."""
+
+from __future__ import annotations
+
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+REFERENCE_SRC = Path("/root/reference/src")
+
+def _probe_offsets(include_dir: Path, header: str, tmp_path: Path) -> dict[str, int]:
+    """Compile a C probe printing offsetof() of every Config field and the struct sizes."""
+    from mcx_gb300 import abi
+
+    lines = [f'#include <stdio.h>\n#include <stddef.h>\n#include "{header}"\nint main(void){{']
+    for name in abi.CONFIG_FIELDS:
+        cname = "lambda" if name == "lambda_" else name
+        lines.append(f'printf("{name} %zu\\n", offsetof(Config, {cname}));')
+    lines.append('printf("sizeof_Config %zu\\n", sizeof(Config));')
+    lines.append('printf("sizeof_GPUInfo %zu\\n", sizeof(GPUInfo));')
+    lines.append('printf("sizeof_History %zu\\n", sizeof(History));')
+    lines.append("return 0;}")
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    cuda_inc = "/usr/local/cuda/include"
+    subprocess.run(["gcc", "-I", str(include_dir), "-I", cuda_inc, str(src), "-o", str(exe)], check=True,
+                   capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (ln.split() for ln in out.splitlines())}
+
+
+def test_ctypes_mirror_matches_header(engine, tmp_path):
+    from mcx_gb300 import abi
+
+    c = _probe_offsets(ROOT / "include", "mcx_abi.h", tmp_path)
+    offs = abi.offsets(abi.Config)
+    for name in abi.CONFIG_FIELDS:
+        assert offs[name] == c[name], name
+    assert C.sizeof(abi.Config) == c["sizeof_Config"]
+    assert C.sizeof(abi.GPUInfo) == c["sizeof_GPUInfo"]
+    assert C.sizeof(abi.History) == c["sizeof_History"]
+
+
+@pytest.mark.skipif(not (REFERENCE_SRC / "mcx_utils.h").exists(), reason="reference headers not present")
+def test_header_matches_reference_layout(engine, tmp_path):
+    """include/mcx_abi.h against MCX's own src/mcx_utils.h, field by field."""
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
+    ours = _probe_offsets(ROOT / "include", "mcx_abi.h", tmp_path / "a")
+    ref = _probe_offsets(REFERENCE_SRC, "mcx_utils.h", tmp_path / "b")
+    assert ours == ref
+
+
+def test_library_exports_every_declared_symbol(engine):
+    """Every function declared in include/*.h is exported by libmcx_gb300.so."""
+    from mcx_gb300._lib import LIB_PATH
+
+    declared = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b((?:mcx|mcxg)_\w+)\s*\(", text, flags=re.M):
+            declared.add(m.group(1))
+    out = subprocess.run(["nm", "-D", "--defined-only", str(LIB_PATH)], check=True, capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    assert {"mcx_run_simulation", "mcx_list_gpu"} <= declared
+    missing = declared - exported
+    assert not missing, missing
+
+
+def test_validatecfg_shifts_and_masks(engine):
+    from mcx_gb300 import problems
+
+    cfg = problems.cube60(1000)
+    cfg["issrcfrom0"] = 0
+    cfg["srcpos"] = [30.0, 30.0, 1.0]
+    pc = engine.prepare(cfg)
+    c = pc.c
+    # origin shift to C indices (src/mcx_utils.c:3761-3773)
+    assert (c.srcpos.x, c.srcpos.y, c.srcpos.z) == (29.0, 29.0, 0.0)
+    assert abs(pc.detpos[0, 0] - 28.0) < 1e-6
+    # launch voxel and label in srcparam2.z/.w as integer bit patterns
+    idx = np.frombuffer(np.float32(c.srcparam2.z).tobytes(), np.uint32)[0]
+    med = np.frombuffer(np.float32(c.srcparam2.w).tobytes(), np.uint32)[0]
+    assert idx == 29 + 29 * 60 and med == 1
+    # mus==0 media become (EPS, g=1)
+    assert pc.prop[0, 1] == np.float32(np.finfo(np.float32).eps) and pc.prop[0, 2] == 1.0
+    # detector voxels are masked only next to the detectors on the z=0 surface
+    det = (pc.vol & 0x80000000).reshape(60, 60, 60, order="F") != 0
+    assert det[:, :, 0].sum() > 0 and det[:, :, 2:].sum() == 0
+    xs, ys, _ = np.nonzero(det)
+    near = np.min([np.hypot(xs + 0.5 - d[0], ys + 0.5 - d[1]) for d in pc.detpos], axis=0)
+    assert near.max() < 3.0
+
+
+def test_maskdet_interior_detector_marks_nothing(engine):
+    from mcx_gb300 import problems
+
+    cfg = problems.cube60(1000)
+    cfg["detpos"] = np.array([[30.0, 30.0, 30.0, 1.0]], np.float32)   # inside the medium, no interface
+    pc = engine.prepare(cfg)
+    assert not np.any(pc.vol & 0x80000000)
+
+
+@pytest.mark.parametrize("bad,msg", [
+    ({"tstart": 5e-9}, "time gate"),
+    ({"srctype": "isotropic"}, "pencil"),
+    ({"respin": 0}, "respin"),
+    ({"srcdir": [0.0, 0.0, 0.0]}, "direction"),
+])
+def test_validatecfg_errors(engine, bad, msg):
+    from mcx_gb300 import problems
+
+    cfg = problems.cube60(1000)
+    cfg.update(bad)
+    with pytest.raises(engine.MCXError, match=msg):
+        engine.prepare(cfg)
+
+
+def test_label_range_checked_on_host(engine):
+    from mcx_gb300 import problems
+
+    cfg = problems.cube60(1000)
+    cfg["vol"] = (cfg["vol"] * 5).astype(np.uint8)
+    with pytest.raises(engine.MCXError, match="labels"):
+        engine.prepare(cfg)
