@@ -2,14 +2,16 @@
 """Plain-MC photon-transport throughput (photons/ms) of the GB300 engine.
 
 One step = one complete simulation of the workload's photon budget.  By default the workload is
-the heterogeneous cube with reflection, 50 time gates and four detectors at 1e8 photons.
+the heterogeneous cube (label-2 sphere, Fresnel reflection, 50 time gates of 0.1 ns, four
+detectors saving id / scattering counts / partial paths) at 1e8 photons.
 
-  value   device-resident: inputs uploaded once into a session, CUDA-event time of the transport
-          launches only (L2 flushed before every timed step)
-  e2e     the public call a user makes, mcx_gb300.run(cfg) -> mcx_run_simulation, with host
-          buffers: Config preparation, volume upload, transport, normalisation, field and
-          detected-photon copy back, all inside the timed region
-  --impl reference   the reference arm (see `reference_arm`)
+  value     device-resident: inputs uploaded once into a session, CUDA-event time of the transport
+            launches only (L2 flushed before every timed step)
+  e2e       the public call a user makes, mcx_gb300.run(cfg) -> mcx_run_simulation, from host
+            buffers: Config preparation, volume upload, transport, normalisation, field and
+            detected-photon copy back, all inside the timed region
+  --impl reference   the reference arm: MCX itself compiled from its sources for sm_103a
+            (oracle/ref_mcx.py) on the same GPU when its sources are staged, else the CPU oracle
 
 Multi-GPU (torchrun, one rank per GPU): every rank simulates its own photon range of the same
 size (weak scaling, no collective in the data path); rank 0 prints.
@@ -33,11 +35,13 @@ import numpy as np  # noqa: E402
 
 METRIC = "photons/ms (plain MC)"
 WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000}
+CPU_SAMPLE = {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}
 
-# Instructions issued per transport step (warp-level, ncu smsp__inst_executed.sum divided by the
-# kernel's own step counter / 32 lanes) from the committed ncu captures under profiles/.
-# None until a capture exists for the workload.
-ISSUE_PER_STEP = {"workload0": None, "workload1": None, "workload2": None}
+# Thread-level instructions per transport step (ncu smsp__thread_inst_executed.sum over the
+# kernel's own step counter) and DRAM bytes per photon (dram__bytes_read.sum + write.sum over
+# photons), from the ncu captures summarised in profiles/transport_<workload>.md.
+NCU_PER_STEP = {"workload0": None, "workload1": None, "workload2": None}
+NCU_DRAM_PER_PHOTON = {"workload0": None, "workload1": None, "workload2": None}
 
 
 def _dist():
@@ -57,6 +61,7 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -68,7 +73,6 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc:
             self.proc.terminate()
             try:
@@ -80,7 +84,7 @@ class Clocks:
     def summary(self) -> dict:
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in (getattr(self, "out", "") or "").splitlines():
+        for line in (self.out or "").splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -126,31 +130,82 @@ def cpu_baseline(name: str, sample: int) -> dict:
 
 
 def reference_arm(args, world, rank) -> None:
-    """The reference arm: MCX's transport exists only as CUDA (src/mcx_core.cu has no CPU path),
-    so the arm times the oracle -- the CPU restatement of that path -- on all host cores, on a
-    bounded sample per step."""
+    """MCX's own CUDA build on this GPU (its kernel-only photon/ms as `value`, photons over its
+    mcx_run_simulation time up to normalised output as `e2e`); the CPU oracle when the reference
+    sources are not staged."""
     if rank != 0:
         return
     name = args.workload
-    sample = args.cpu_sample or {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}[name]
-    vals = []
+    nphoton = int(args.photons) if args.photons else WORKLOAD_PHOTONS[name]
+    from oracle import ref_mcx
+
+    base = {"impl": "reference", "metric": METRIC, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic"}
+    if ref_mcx.available():
+        try:
+            t0 = time.perf_counter()
+            ref_mcx.build()
+            build_s = time.perf_counter() - t0
+            for i in range(args.warmup):
+                ref_mcx.run(make_cfg(name, min(nphoton, 10_000_000), 100 + i), keep_field=False)
+            runs = []
+            for i in range(args.steps):
+                t0 = time.perf_counter()
+                r = ref_mcx.run(make_cfg(name, nphoton, 200 + i), keep_field=False)
+                runs.append((r, time.perf_counter() - t0))
+            speed = statistics.mean(r["speed"] for r, _ in runs)
+            norm_ms = statistics.mean(r["normalized_ms"] for r, _ in runs)
+            wall = statistics.mean(w for _, w in runs)
+            line = dict(base, value=speed, ms_per_step=nphoton / speed,
+                        config={"workload": name, "photons_per_step": nphoton, "threads": runs[0][0]["threads"],
+                                "build": "src/mcx_core.cu -DUSE_ATOMIC -DSAVE_DETECTORS -use_fast_math -arch=sm_103a",
+                                "build_s": round(build_s, 1)},
+                        e2e={"value": nphoton / norm_ms, "unit": "photons/ms", "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0, "ms_per_step": norm_ms, "process_wall_s": wall},
+                        absorbed=[r["absorbed"] for r, _ in runs],
+                        cpu_baseline={"value": speed, "unit": "photons/ms", "cores": os.cpu_count(), "kind": "reference",
+                                      "sample": "the reference MCX CUDA build itself on this GPU"})
+            print(json.dumps(line))
+            return
+        except Exception as e:  # noqa: BLE001 -- fall back to the CPU restatement, say why
+            base["reference_build_error"] = str(e)[:300]
+    sample = args.cpu_sample or CPU_SAMPLE[name]
     for _ in range(args.warmup):
         cpu_baseline(name, max(1000, sample // 10))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(name, sample))
+    vals = [cpu_baseline(name, sample) for _ in range(args.steps)]
     wall = time.perf_counter() - t0
     v = sample * args.steps / (wall * 1e3)
-    line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "photons/ms", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "photons_per_step": sample, "note": "CPU restatement of the CUDA-only path"},
-        "cpu_baseline": {"value": v, "unit": "photons/ms", "cores": vals[0]["cores"], "kind": "port",
-                         "sample": f"{sample} photons of {name} per step"},
-        "e2e": {"value": v, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+    line = dict(base, value=v, ms_per_step=wall * 1e3 / args.steps,
+                config={"workload": name, "photons_per_step": sample, "note": "CPU restatement of the CUDA-only path"},
+                cpu_baseline={"value": v, "unit": "photons/ms", "cores": vals[0]["cores"], "kind": "port",
+                              "sample": f"{sample} photons of {name} per step"},
+                e2e={"value": v, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
     print(json.dumps(line))
+
+
+def roofline(name: str, value: float, world: int, st, f_clk: float, sms: int, atom_rate: float, pk: dict) -> dict:
+    """The transport roofline: the slower of FP32/INT issue (every lane slot issuing a useful
+    instruction) and L2 reduction throughput for the deposits, in photons/ms."""
+    steps = st.n_steps / max(1, st.n_photon)
+    deps = st.n_deposit / max(1, st.n_photon)
+    glob = (st.n_deposit - st.n_tile_deposit) / max(1, st.n_photon)
+    achieved = value / world
+    ips = NCU_PER_STEP.get(name)
+    p_issue = sms * 4 * 32 * f_clk / (ips * steps) / 1e3 if ips else None
+    p_atom = atom_rate / max(glob, 1e-9) / 1e3 if atom_rate else None
+    cands = [(p, b) for p, b in ((p_issue, "fp32-issue"), (p_atom, "l2-atomic")) if p]
+    peak, bound = min(cands) if cands else (None, "fp32-issue")
+    dram = NCU_DRAM_PER_PHOTON.get(name)
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "photons/ms",
+            "frac": achieved / peak if peak else None,
+            "traffic": dram * (st.n_photon / max(1, st.launches)) if dram else None,
+            "traffic_unit": "DRAM bytes per launch",
+            "p_issue": p_issue, "p_atom": p_atom, "steps_per_photon": steps, "deposits_per_photon": deps,
+            "global_reductions_per_photon": glob, "thread_inst_per_step": ips, "sm_clock_hz": f_clk,
+            "l2_reductions_per_s": atom_rate, "peak_source": "issue: SMs x 4 x 32 x measured SM clock; "
+                                                             "atomics: measured on this GPU"}
 
 
 def main() -> None:
@@ -170,6 +225,8 @@ def main() -> None:
         reference_arm(args, world, rank)
         return
 
+    import ctypes as C
+
     import torch
 
     torch.cuda.set_device(local)
@@ -180,6 +237,7 @@ def main() -> None:
 
     import mcx_gb300
     from mcx_gb300 import Session
+    from mcx_gb300._lib import lib
 
     name = args.workload
     nphoton = int(args.photons) if args.photons else WORKLOAD_PHOTONS[name]
@@ -195,6 +253,7 @@ def main() -> None:
             torch.distributed.barrier()
 
     base = rank * nphoton * (args.warmup + args.steps + 1)
+    sess.autotune(nphoton)
     for i in range(args.warmup):
         sess.run(base + i * nphoton, nphoton, seed)
     sess.reset()
@@ -239,17 +298,13 @@ def main() -> None:
     e2e = nphoton * args.steps * world / e2e_tot
 
     pk = peaks()
-    steps_per_photon = st.n_steps / max(1, st.n_photon)
-    dep_per_photon = st.n_deposit / max(1, st.n_photon)
+    clocks = clk.summary()
     props = torch.cuda.get_device_properties(local)
-    f_clk = (clk.summary()["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)) * 1e6
-    ips = ISSUE_PER_STEP.get(name)
-    roof = {"bound": "fp32-issue", "unit": "photons/ms", "achieved": value / world, "peak": None, "frac": None,
-            "traffic": None, "steps_per_photon": steps_per_photon, "deposits_per_photon": dep_per_photon,
-            "issue_per_step": ips, "sm_clock_hz": f_clk, "peak_source": pk.get("_source")}
-    if ips:
-        p_issue = props.multi_processor_count * 4 * f_clk / (ips * steps_per_photon) / 1e3
-        roof.update(peak=p_issue, frac=(value / world) / p_issue)
+    f_clk = (clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)) * 1e6
+    rate = C.c_double(0.0)
+    nvox = int(np.prod(cfg["vol"].shape)) * pc.ngates
+    lib.mcxg_probe_atomic_rate(max(nvox, 1 << 20), C.byref(rate))
+    roof = roofline(name, value, world, st, f_clk, props.multi_processor_count, rate.value, pk)
 
     if rank != 0:
         if world > 1:
@@ -268,11 +323,10 @@ def main() -> None:
         "gpu_launches": args.steps,
         "detected_per_step": ndet / max(1, args.steps),
         "roofline": roof,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if not args.no_cpu_baseline:
-        sample = args.cpu_sample or {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}[name]
-        line["cpu_baseline"] = cpu_baseline(name, sample)
+        line["cpu_baseline"] = cpu_baseline(name, args.cpu_sample or CPU_SAMPLE[name])
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -74,6 +74,11 @@ int mcxg_rng_test(const uint32_t seeds[4], float* out, int n);
 /* n floats of the per-photon stream of photon `pid` under `seed`, generated on the GPU. */
 int mcxg_photon_stream(uint64_t seed, uint64_t pid, float* out, int n);
 
+/* Measured FP32 reduction (atomicAdd without return) throughput into L2 over `nfloats`
+ * distinct addresses, in reductions per second: the deposit-bound term of the transport
+ * roofline, measured on the device in use. */
+int mcxg_probe_atomic_rate(uint64_t nfloats, double* per_second);
+
 /* ---- Device-resident sessions ------------------------------------------------------------ */
 
 /* A prepared simulation held on one device: labels, properties, detectors and output
@@ -91,9 +96,21 @@ int  mcxg_session_run(mcxg_session* s, uint64_t photon_offset, uint64_t nphoton,
  * up to max_records detected records; returns the number of detected photons seen. */
 int64_t mcxg_session_read(mcxg_session* s, float* field, float* detp, uint64_t max_records, mcxg_stats* stats);
 void mcxg_session_destroy(mcxg_session* s);
+/* Pick the session's deposit-tile size from short pilot launches sized for a run of `nphoton`
+ * photons (cached per configuration for the process); clears the session's buffers.
+ * mcx_run_simulation does this itself for runs of 2e7 photons or more unless MCXG_TUNE=0. */
+int  mcxg_session_autotune(mcxg_session* s, uint64_t nphoton);
 
 /* Launch-shape override used by the autotuner (0 = engine default). */
 void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile);
+
+/* RNG seeding of sessions and runs created afterwards.  0 (default): every photon has its own
+ * xorshift128+ stream derived from (seed, photon index) -- results independent of launch shape.
+ * 1: MCX's scheme -- one stream per MCX GPU thread (the count MCX's autopilot picks for the
+ * device), seeded with glibc rand() words after srand(seed), each stream running its share of
+ * photons in sequence (src/mcx_core.cu:3014-3016, 3247-3251, 3381-3387); the same seed then gives
+ * the same random streams as MCX itself.  The environment variable MCXG_SEEDING=mcx selects 1. */
+void mcxg_set_seeding(int mode);
 
 /* ---- Allocation-free transport ----------------------------------------------------------- */
 

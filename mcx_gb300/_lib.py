@@ -62,9 +62,15 @@ lib.mcxg_session_read.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.
 lib.mcxg_session_read.restype = C.c_int64
 lib.mcxg_session_destroy.argtypes = [C.c_void_p]
 lib.mcxg_session_destroy.restype = None
+lib.mcxg_session_autotune.argtypes = [C.c_void_p, C.c_uint64]
+lib.mcxg_session_autotune.restype = C.c_int
 lib.mcxg_set_launch.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
 lib.mcxg_set_launch.restype = None
 
+lib.mcxg_probe_atomic_rate.argtypes = [C.c_uint64, C.POINTER(C.c_double)]
+lib.mcxg_probe_atomic_rate.restype = C.c_int
+lib.mcxg_set_seeding.argtypes = [C.c_int]
+lib.mcxg_set_seeding.restype = None
 lib.mcxg_run_noalloc.argtypes = [_CFG, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64,
                                  C.c_int, C.c_void_p, C.POINTER(abi.Stats)]
 lib.mcxg_run_noalloc.restype = C.c_int
@@ -76,4 +82,6 @@ EXPORTED = [
     "mcxg_maskdet", "mcxg_last_error", "mcxg_last_error_id", "mcxg_clear_error", "mcxg_set_error", "mcxg_get_stats",
     "mcxg_rng_test", "mcxg_photon_stream", "mcxg_session_create", "mcxg_session_reset", "mcxg_session_run",
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
+    "mcxg_set_seeding", "mcxg_probe_atomic_rate",
+    "mcxg_session_autotune",
 ]

@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <stdlib.h>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,23 @@ struct LaunchOverride {
     int block = 0, blocks_per_sm = 0, chunk = 0, tile = -1;
 } g_override;
 std::mutex g_override_mu;
+
+// Autotuner results: deposit-tile budget (KB) per configuration signature.
+std::mutex g_tune_mu;
+std::vector<std::pair<std::string, int>> g_tune_cache;
+
+// RNG seeding of new sessions: -1 = not chosen yet (environment MCXG_SEEDING=mcx selects MCX's
+// per-thread streams), 0 = per-photon streams, 1 = MCX's per-thread streams.
+int g_seeding = -1;
+
+int seeding_mode() {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    if (g_seeding < 0) {
+        const char* e = std::getenv("MCXG_SEEDING");
+        g_seeding = (e && std::strcmp(e, "mcx") == 0) ? 1 : 0;
+    }
+    return g_seeding;
+}
 }  // namespace
 
 [[noreturn]] void raise(int id, const std::string& msg, const char* file, int line) { throw Error{id, msg, file, line}; }
@@ -192,9 +210,18 @@ struct Session {
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos;
     double kernel_ms = 0.0;
     int launches = 0;
+    // MCX per-thread seeding: stream count, host/device seed words and the glibc random_r state
+    // continuing across runs as MCX's rand() sequence does across respins
+    unsigned mcx_streams = 0;
+    DevBuf words;
+    std::vector<uint32_t> hwords;
+    random_data rstate{};
+    char rbuf[128];
+    long long rseed = -1;
 
     ~Session() {
         labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
+        words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -342,8 +369,50 @@ struct Session {
         k.errflag = err.as<unsigned>();
         k.work = work.as<unsigned long long>();
         reset();
+        set_window(cfg->tstart, cfg->tstart + cfg->tstep * (float)k.maxgate);   // first gate group
 
         configure_launch(cfg);
+
+        k.seed_mode = seeding_mode();
+        if (k.seed_mode == 1) {
+            // the thread count MCX's autopilot picks on this device (src/mcx_core.cu:2554-2608,
+            // 2688-2695, 3050-3053), or the user's nthread/nblocksize without autopilot
+            const int v = prop.major * 10 + prop.minor;
+            const int smxblock = v < 30 ? 8 : (v < 50 ? 16 : 32);
+            long long block_ref, threads;
+            if (cfg->autopilot) {
+                block_ref = std::max(prop.maxThreadsPerMultiProcessor / smxblock, 64);
+                threads = block_ref * smxblock * (long long)prop.multiProcessorCount * (v <= 75 ? 1 : 2);
+            } else {
+                block_ref = std::max(1u, cfg->nblocksize);
+                threads = cfg->nthread;
+            }
+            threads -= threads % block_ref;
+            if (threads <= 0) MCXG_RAISE(-6, "invalid thread count for MCX seeding");
+            mcx_streams = (unsigned)threads;
+            k.mcx_streams = mcx_streams;
+            words.alloc((size_t)mcx_streams * 4 * sizeof(uint32_t), stream);
+            k.mcx_words = words.as<uint32_t>();
+            hwords.resize((size_t)mcx_streams * 4);
+        }
+    }
+
+    // MCX's seed words for the next run: (rand()<<16)|(rand()<<1)|(rand()>>14), four per thread,
+    // continuing the sequence srand(seed) started (src/mcx_core.cu:3247-3251, 3381-3387).
+    void mcx_seed_words(uint64_t seed) {
+        if ((long long)seed != rseed) {
+            std::memset(&rstate, 0, sizeof(rstate));
+            initstate_r((unsigned)seed, rbuf, sizeof(rbuf), &rstate);
+            rseed = (long long)seed;
+        }
+        for (auto& wd : hwords) {
+            int32_t a, b, c;
+            random_r(&rstate, &a);
+            random_r(&rstate, &b);
+            random_r(&rstate, &c);
+            wd = ((uint32_t)a << 16) | ((uint32_t)b << 1) | ((uint32_t)c >> 14);
+        }
+        CK(cudaMemcpyAsync(words.p, hwords.data(), hwords.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
     }
 
     // Block size, CTAs per SM and refill chunk; the deposit tile placed over the source.
@@ -402,6 +471,56 @@ struct Session {
         (void)cfg;
     }
 
+    // Configuration signature for the tuning cache: what changes the best launch shape.
+    std::string signature() const {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "%d:%d:%d:%d:%d:%d:%d:%u:%d:%d", kp.nx, kp.ny, kp.nz, kp.maxgate, kp.medianum, (int)reflect,
+                 (int)savedet, kp.src_idx, kp.seed_mode, transport_variant());
+        return buf;
+    }
+
+    // Pick the deposit-tile budget from short pilot launches over {0, 16, 32} KB (cached per
+    // signature).  Pilot photons go to the session's buffers, which are cleared afterwards.
+    void autotune(uint64_t nphoton) {
+        const std::string sig = signature();
+        {
+            std::lock_guard<std::mutex> g(g_tune_mu);
+            for (auto& e : g_tune_cache)
+                if (e.first == sig) {
+                    apply_tile(e.second);
+                    return;
+                }
+        }
+        const uint64_t pilot = std::max<uint64_t>(500000, std::min<uint64_t>(4000000, nphoton / 64));
+        int best_kb = 16;
+        float best = 1e30f;
+        for (int kb : {0, 16, 32}) {
+            apply_tile(kb);
+            run(0, pilot, 0x5eed);          // first launch of a shape warms it up
+            const float ms = run(pilot, pilot, 0x5eed);
+            if (ms < best) {
+                best = ms;
+                best_kb = kb;
+            }
+        }
+        apply_tile(best_kb);
+        reset();
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tune_cache.emplace_back(sig, best_kb);
+    }
+
+    void apply_tile(int kb) {
+        choose_tile(nullptr, kb);
+        smem = transport_smem_bytes(kp, block, savedet);
+        int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        if (bps <= 0) {
+            kp.tile_on = 0;
+            smem = transport_smem_bytes(kp, block, savedet);
+            bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        }
+        grid = std::max(1, bps) * sms;
+    }
+
     void reset() {
         CK(cudaMemsetAsync(field.p, 0, field.bytes, stream));
         if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, stream));
@@ -425,6 +544,11 @@ struct Session {
         kp.photon_offset = offset;
         kp.nphoton = n;
         kp.seed = seed;
+        if (kp.seed_mode == 1) {
+            mcx_seed_words(seed);
+            kp.mcx_per = (unsigned)(n / mcx_streams);
+            kp.mcx_odd = (unsigned)(n - (uint64_t)kp.mcx_per * mcx_streams);
+        }
         CK(cudaMemsetAsync(work.p, 0, sizeof(unsigned long long), stream));
         CK(cudaEventRecord(ev0, stream));
         CK(launch_transport(kp, reflect, savedet, grid, block, smem, stream));
@@ -488,6 +612,11 @@ extern "C" int mcxg_get_stats(mcxg_stats* out) {
     *out = t_stats;
     return 0;
 }
+extern "C" void mcxg_set_seeding(int mode) {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    g_seeding = (mode == 1) ? 1 : 0;
+}
+
 extern "C" void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile) {
     std::lock_guard<std::mutex> g(g_override_mu);
     g_override.block = block;
@@ -596,6 +725,18 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
     std::memset(&t_stats, 0, sizeof(t_stats));
     Session S;
     S.create(cfg, gpuid, fp64_field);
+    {
+        // large runs tune the deposit tile with short pilot launches (cached per configuration)
+        int tile_override;
+        {
+            std::lock_guard<std::mutex> g(g_override_mu);
+            tile_override = g_override.tile;
+        }
+        const char* e = std::getenv("MCXG_TUNE");
+        const bool tune = !(e && std::strcmp(e, "0") == 0);
+        if (tune && tile_override < 0 && cfg->nphoton * (uint64_t)std::abs(cfg->respin) >= 20000000ull)
+            S.autotune(cfg->nphoton);
+    }
     const KParams& k = S.kp;
     const size_t dimxyz = S.nvox;
     const int maxgate = k.maxgate;
@@ -777,6 +918,39 @@ extern "C" int mcxg_photon_stream(uint64_t seed, uint64_t pid, float* out, int n
     }
 }
 
+// Measured FP32 reduction throughput into L2 over `nfloats` distinct addresses (the
+// deposit-bound denominator of the transport roofline), in reductions per second.
+extern "C" int mcxg_probe_atomic_rate(uint64_t nfloats, double* per_second) {
+    mcxg_clear_error();
+    try {
+        int dev = 0, sms = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        float* buf = nullptr;
+        CK(cudaMalloc(&buf, nfloats * sizeof(float)));
+        CK(cudaMemset(buf, 0, nfloats * sizeof(float)));
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        const int block = 256, grid = sms * 8, iters = 256;
+        CK(launch_atomic_probe(buf, (unsigned)nfloats, iters, grid, block, 0));   // warm-up
+        CK(cudaEventRecord(a, 0));
+        CK(launch_atomic_probe(buf, (unsigned)nfloats, iters, grid, block, 0));
+        CK(cudaEventRecord(b, 0));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaFree(buf);
+        *per_second = (double)grid * block * iters / (ms * 1e-3);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Sessions
 // ---------------------------------------------------------------------------------------------
@@ -838,3 +1012,13 @@ extern "C" int64_t mcxg_session_read(mcxg_session* h, float* field, float* detp,
 }
 
 extern "C" void mcxg_session_destroy(mcxg_session* h) { delete h; }
+
+extern "C" int mcxg_session_autotune(mcxg_session* h, uint64_t nphoton) {
+    try {
+        h->s.autotune(nphoton);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return t_err_id;
+    }
+}

@@ -187,13 +187,22 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     unsigned long long r0 = 0ull, r1 = 0ull;
     unsigned c_step = 0u, c_scat = 0u, c_dep = 0u, c_tile = 0u, c_photon = 0u;
 
+    unsigned left = 0u;   // MCX stream mode: photons still to run from this lane's stream
+
     while (true) {
         // ---- relaunch lanes that have no photon (warp-uniform control flow) ------------------
         unsigned need = __ballot_sync(kFull, !alive);
         if (need) {
-            if (!S.drained[warp]) {
-                const unsigned n = __popc(need);
-                const unsigned rank = __popc(need & ((1u << lane) - 1u));
+            bool start = false;
+            // MCX stream mode: a stream with photons left continues with its RNG state
+            if (!alive && left > 0u) {
+                left--;
+                start = true;
+            }
+            const unsigned want = __ballot_sync(kFull, !alive && !start);
+            if (want && !S.drained[warp]) {
+                const unsigned n = __popc(want);
+                const unsigned rank = __popc(want & ((1u << lane) - 1u));
                 unsigned long long pool_next = S.pool[2 * warp], pool_end = S.pool[2 * warp + 1];
                 const unsigned long long avail = pool_end - pool_next;
                 unsigned long long mine = pool_next + rank;
@@ -206,7 +215,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     if (rank >= avail) mine = base + (rank - avail);
                     pool_next = base + (n - avail);
                     pool_end = base + take;
-                    if (lane == 0 && base >= P.nphoton) S.drained[warp] = 1;
+                    if (lane == 0 && base >= P.d_nwork) S.drained[warp] = 1;
                 } else {
                     pool_next += n;
                 }
@@ -215,29 +224,45 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.pool[2 * warp] = pool_next;
                     S.pool[2 * warp + 1] = pool_end;
                 }
-                if (!alive && mine < P.nphoton) {
-                    // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
-                    // skipping and specular loss of skipvoid() are folded into src_* by the host)
-                    seed_photon(P.seed, P.photon_offset + mine, r0, r1);
-                    px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
-                    vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
-                    rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
-                    t = P.src_t * inv_c0;
-                    idx = P.src_idx;
-                    med = (int)(P.src_label & kLabelMask);
-                    det = (P.src_label & kLabelDet) ? kDET_MASK : 0u;
-                    carry = det;
-                    fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
-                    pscat = 0.f; pathlen = 0.f; nscat = -1;
-                    w0 = w; eabs = 0.f; eoth = 0.f; psteps = 0u;
-                    pr = S.prop[med];
-                    if (SAVEDET)
-                        for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
-                    alive = true;
+                if (!alive && !start && mine < P.d_nwork) {
+                    if (P.seed_mode == 1) {
+                        // MCX's per-thread stream `mine`: four host seed words
+                        // (src/mcx_rand_xorshift128p.cu:79-82), then its share of photons in sequence
+                        const unsigned cnt = P.mcx_per + ((unsigned)mine < P.mcx_odd ? 1u : 0u);
+                        if (cnt) {
+                            const uint4 sw = __ldg(reinterpret_cast<const uint4*>(P.mcx_words) + mine);
+                            r0 = ((unsigned long long)sw.x << 32) | sw.y;
+                            r1 = ((unsigned long long)sw.z << 32) | sw.w;
+                            left = cnt - 1u;
+                            start = true;
+                        }
+                    } else {
+                        seed_photon(P.seed, P.photon_offset + mine, r0, r1);
+                        start = true;
+                    }
                 }
-                __syncwarp();
-                need = __ballot_sync(kFull, !alive);
             }
+            if (start) {
+                // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
+                // skipping and specular loss of skipvoid() are folded into src_* by the host)
+                px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
+                vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
+                rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                t = P.src_t * inv_c0;
+                idx = P.src_idx;
+                med = (int)(P.src_label & kLabelMask);
+                det = (P.src_label & kLabelDet) ? kDET_MASK : 0u;
+                carry = det;
+                fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
+                pscat = 0.f; pathlen = 0.f; nscat = -1;
+                w0 = w; eabs = 0.f; eoth = 0.f; psteps = 0u;
+                pr = S.prop[med];
+                if (SAVEDET)
+                    for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
+                alive = true;
+            }
+            __syncwarp();
+            need = __ballot_sync(kFull, !alive);
             if (need == kFull) break;      // no photon left for any lane of this warp
         }
         if (!alive) continue;
@@ -543,6 +568,16 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     }
 }
 
+// Roofline probe: fire-and-forget FP32 reductions to addresses spread over `n` floats (a hash of
+// the thread and iteration), the operation the transport kernel's deposits reduce to.
+__global__ void atomic_probe_kernel(float* buf, unsigned n, int iters) {
+    unsigned h = (blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u;
+    for (int i = 0; i < iters; i++) {
+        h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+        atomicAdd(buf + (h % n), 1.0f);
+    }
+}
+
 // The -D R test kernel: one thread fills `out` from four seed words
 // (src/mcx_core.cu:1731-1742, seeding src/mcx_rand_xorshift128p.cu:79-82).
 __global__ void rng_test_kernel(const uint32_t* seeds, float* out, int n) {
@@ -630,6 +665,7 @@ static KParams finalize(const KParams& in) {
     p.d_tx1 = (float)(p.tx0 + p.tnx); p.d_ty1 = (float)(p.ty0 + p.tny); p.d_tz1 = (float)(p.tz0 + p.tnz);
     p.d_n0 = p.prop[0].w;
     p.d_gscat = (p.gscatter >= 2147483647.f) ? 2147483647 : (int)p.gscatter;
+    p.d_nwork = (p.seed_mode == 1) ? (unsigned long long)p.mcx_streams : p.nphoton;
     return p;
 }
 
@@ -641,6 +677,11 @@ cudaError_t launch_transport(const KParams& in, bool reflect, bool savedet, int 
     if (e != cudaSuccess) return e;
     void* args[] = {const_cast<KParams*>(&p)};
     return cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem_bytes, stream);
+}
+
+cudaError_t launch_atomic_probe(float* buf, unsigned n, int iters, int grid, int block, cudaStream_t stream) {
+    atomic_probe_kernel<<<grid, block, 0, stream>>>(buf, n, iters);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rng_test(const uint32_t* d_seeds, float* d_out, int n, cudaStream_t stream) {

@@ -75,6 +75,12 @@ struct KParams {
     int chunk;                      // photons per warp refill
     unsigned int step_cap;          // safety cap on steps per photon (error flag when hit)
 
+    // --- RNG seeding: 0 = one stream per photon from (seed, photon index); 1 = MCX's scheme, one
+    //     stream per MCX thread seeded with host words, photons split statically over streams
+    int seed_mode;
+    const uint32_t* mcx_words;      // 4 words per stream (seed_mode 1)
+    unsigned int mcx_streams, mcx_per, mcx_odd;
+
     // --- per-CTA shared-memory deposit tile (voxel box x gate range)
     int tile_on;
     int tx0, ty0, tz0, tnx, tny, tnz, tg0, tng;
@@ -87,6 +93,7 @@ struct KParams {
     float d_tx0, d_ty0, d_tz0, d_tx1, d_ty1, d_tz1;   // tile box as floats
     float d_n0;                     // refractive index of medium 0
     int d_gscat;                    // gscatter as an integer threshold
+    unsigned long long d_nwork;     // work items in the pool: photons, or MCX streams
 };
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
@@ -109,6 +116,7 @@ int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_b
 // the host (engine.cu).  Returns the entry voxel or -1.
 int host_skipvoid(const struct MCXConfig* cfg, float4& p, float3& v, float& t, int fd[3]);
 
+cudaError_t launch_atomic_probe(float* buf, unsigned n, int iters, int grid, int block, cudaStream_t stream);
 cudaError_t launch_rng_test(const uint32_t* d_seeds, float* d_out, int n, cudaStream_t stream);
 cudaError_t launch_photon_stream(unsigned long long seed, unsigned long long pid, float* d_out, int n, cudaStream_t stream);
 cudaError_t launch_labels_from_vol(const uint32_t* d_vol, uint8_t* d_labels, size_t n, unsigned int medianum,

@@ -25,6 +25,10 @@ class Session:
         if not self.h:
             raise MCXError(-1, "session creation failed")
 
+    def autotune(self, nphoton: int) -> None:
+        """Pick the deposit-tile size from pilot launches (clears the buffers)."""
+        _check(lib.mcxg_session_autotune(self.h, nphoton))
+
     def reset(self) -> None:
         _check(lib.mcxg_session_reset(self.h))
 

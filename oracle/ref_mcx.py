@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import json
 import os
+import platform
 import re
 import shutil
 import struct
@@ -77,7 +78,11 @@ def build(force: bool = False) -> Path:
         raise RuntimeError("the reference sources are not staged in baseline/_ref/src")
     cuda = _cuda_home()
     obj = REF / "obj"
+    stamp = obj / "machine.txt"
+    if stamp.exists() and stamp.read_text() != platform.machine():
+        shutil.rmtree(obj)          # objects of another host architecture
     obj.mkdir(parents=True, exist_ok=True)
+    stamp.write_text(platform.machine())
     inc = ["-Izmat", "-Izmat/easylzma", "-Izmat/miniz", "-Iubj", f"-I{cuda}/include"]
     jobs = []
     objs = []
@@ -154,7 +159,9 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
     (tmp / "in.json").write_text(json.dumps(_json_input(cfg, session, str(volfile))))
     p = subprocess.run([str(exe), "-f", "in.json"], cwd=tmp, capture_output=True, text=True, timeout=timeout)
     log = p.stdout + p.stderr
-    (tmp / "stdout.txt").write_text(log)
+    # the CLI writes its report to <session>.log (the session is unnamed when the log opens)
+    for lf in sorted(tmp.glob("*.log")):
+        log += lf.read_text(errors="replace")
     if p.returncode != 0:
         raise RuntimeError(f"reference mcx failed ({p.returncode}):\n{log[-3000:]}")
     clean = re.sub(r"\x1b\[[0-9;]*m", "", log)
