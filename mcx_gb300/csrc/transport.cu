@@ -106,6 +106,22 @@ __device__ int find_detector(const KParams& P, float px, float py, float pz) {
     return 0;
 }
 
+// One deposit into the global field: FP64 in the reference-accuracy twin, else FP32 with the
+// two-copy spill of src/mcx_core.cu:2246-2253 -- once the primary copy has grown past
+// kMaxAccum, what it held moves to the shadow copy, so the primary stays small and additions
+// keep their precision (the sum of both copies is conserved exactly under races).
+__device__ __forceinline__ void field_add(const KParams& P, size_t addr, float v) {
+    if (P.field64) {
+        atomicAdd(P.field64 + addr, (double)v);
+        return;
+    }
+    const float old = atomicAdd(P.field + addr, v);
+    if (fabsf(old) > kMaxAccum) {
+        atomicAdd(P.field + addr, -old);
+        atomicAdd(P.shadow + addr, old);
+    }
+}
+
 // Shared-memory carve-up of one CTA.
 struct Smem {
     float4* prop;                 // medianum x (mua, mus, g, n)
@@ -376,16 +392,18 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (weight != 0.f) {
                     rec = true;
                     c_dep++;
+                    const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
                     if (P.tile_on && ox >= tx0 && ox < tx1 && oy >= ty0 && oy < ty1 && oz >= tz0 && oz < tz1 &&
                         (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
                         const int ti = (((tshift - P.tg0) * P.tnz + (int)(oz - tz0)) * P.tny + (int)(oy - ty0)) * P.tnx +
                                        (int)(ox - tx0);
-                        atomicAdd(S.tile + ti, weight);
+                        // keep tile values small so FP32 rounding of many equal deposits stays
+                        // negligible: past kTileSpill the value moves (exactly) to global memory
+                        const float old = atomicAdd(S.tile + ti, weight);
+                        if (old + weight > kTileSpill) field_add(P, addr, atomicExch(S.tile + ti, 0.f));
                         c_tile++;
                     } else {
-                        const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
-                        if (P.field64) atomicAdd(P.field64 + addr, (double)weight);
-                        else atomicAdd(P.field + addr, weight);
+                        field_add(P, addr, weight);
                     }
                 }
             }
@@ -540,17 +558,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         const int g = r;
         const size_t addr = (size_t)((z + P.tz0) * (int)P.dimxy + (y + P.ty0) * P.nx + (x + P.tx0)) +
                             (size_t)(g + P.tg0) * P.nvox;
-        if (P.field64) {
-            atomicAdd(P.field64 + addr, (double)v);
-        } else {
-            // two-copy accumulation (src/mcx_core.cu:2246-2253): once the primary copy grows past
-            // kMaxAccum, move what was there into the shadow copy so the primary stays small
-            const float old = atomicAdd(P.field + addr, v);
-            if (fabsf(old) > kMaxAccum) {
-                atomicAdd(P.field + addr, -old);
-                atomicAdd(P.shadow + addr, old);
-            }
-        }
+        field_add(P, addr, v);
     }
     // FP64 only here: per-thread FP32 partial sums reduced in double
     for (int k = 0; k < kNumEnergy; k++) {

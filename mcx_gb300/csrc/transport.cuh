@@ -98,6 +98,9 @@ struct KParams {
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
 constexpr float kMaxAccum = 1000.f;
+// A shared-memory tile value past this moves to the global field (FP32 increments to values
+// below 64 carry at most 2^-18 relative rounding each).
+constexpr float kTileSpill = 64.f;
 
 // Host-side launch of the transport kernel variant matching the flags.  smem_bytes is the
 // dynamic shared memory per CTA; returns the CUDA error of the launch.

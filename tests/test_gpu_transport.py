@@ -7,8 +7,8 @@ session / RNG entry points) on cuda:0.  Tolerances:
   * per-voxel fluence: 16 independent seeds per side, per-voxel means within 3 standard errors
     (tests/stats.py) in voxels with more than 1e3 oracle deposits;
   * energy balance launched = absorbed + escaped + detected: 1e-5 relative (FP64 tallies);
-  * FP32 field accumulation against the FP64-accumulated twin: 1e-4 relative on the total,
-    2e-3 per voxel in voxels with more than 1e3 deposits.
+  * FP32 field accumulation against the FP64-accumulated twin: 1e-5 relative on the total,
+    2e-5 per voxel in the hottest 1% of voxels.
 """
 
 from __future__ import annotations
@@ -175,23 +175,34 @@ def test_detected_photons_parity(engine, oracle):
                 assert abs(a.mean() - b.mean()) <= 4 * se + 1e-6, (det, row, a.mean(), b.mean())
 
 
-def test_energy_balance_and_fp32_accumulation(engine):
+@pytest.mark.parametrize("tile", [-1, 0, 32])
+def test_energy_balance_and_fp32_accumulation(engine, lib, tile):
+    """FP32 field against the FP64-accumulated twin on identical photon histories, with the
+    default, no and a larger shared-memory tile.  The source voxel of cube60 receives ~1e7 equal
+    first-flight deposits per 1e7 photons: without the two-copy spill FP32 would drift there by
+    ~0.5%; with it the error stays below 2e-5."""
     cfg = problems.workload0(10_000_000, seed=77)
-    r32 = engine.run(cfg)
-    r64 = engine.run(cfg, fp64_field=True)
+    try:
+        lib.mcxg_set_launch(0, 0, 0, tile)
+        r32 = engine.run(cfg)
+        r64 = engine.run(cfg, fp64_field=True)
+    finally:
+        lib.mcxg_set_launch(0, 0, 0, -1)
     s = r32["stat"]
     assert balance(s) < 1e-5 and balance(r64["stat"]) < 1e-5
     # identical photon histories: the only difference is how the field was accumulated
     assert r32["stat"]["n_steps"] == r64["stat"]["n_steps"]
     f32, f64 = r32["flux"].astype(np.float64), r64["flux"].astype(np.float64)
     tot_err = abs(f32.sum() - f64.sum()) / f64.sum()
-    assert tot_err < 1e-4, tot_err
-    hot = f64 > np.quantile(f64, 0.9)
+    assert tot_err < 1e-5, tot_err
+    hot = f64 > np.quantile(f64, 0.99)
     rel = np.abs(f32[hot] - f64[hot]) / f64[hot]
-    assert rel.max() < 2e-3, rel.max()
+    print("tile", tile, "FP32 vs FP64: total", tot_err, "max rel in hottest 1%", rel.max(), "source voxel",
+          f32[29, 29, 0, 0] / f64[29, 29, 0, 0] - 1)
+    assert rel.max() < 2e-5, rel.max()
     # sum of flux*mua*Vvox/normaliser recovers the absorbed weight recorded by the kernel
     raw = f32[..., 0] / s["normalizer"]
-    assert abs(raw.sum() * 0.005 - s["e_absdep"]) / s["e_absdep"] < 1e-4
+    assert abs(raw.sum() * 0.005 - s["e_absdep"]) / s["e_absdep"] < 1e-5
 
 
 def test_diffusion_agreement_gpu(engine):
@@ -220,11 +231,11 @@ def test_launch_shape_independence(engine, lib):
     # same deposits summed in another order (and, in the second run, without the shared-memory
     # tile): the FP32 accumulation tolerance of test_energy_balance_and_fp32_accumulation
     fa, fb = a["flux"].astype(np.float64), b["flux"].astype(np.float64)
-    assert abs(fa.sum() - fb.sum()) / fb.sum() < 1e-4
+    assert abs(fa.sum() - fb.sum()) / fb.sum() < 1e-5
     hot = fb > np.quantile(fb, 0.99)
     rel = np.abs(fa[hot] - fb[hot]) / fb[hot]
     print("launch shape: max rel diff in hot voxels", rel.max())
-    assert rel.max() < 2e-3
+    assert rel.max() < 4e-5
     assert abs(a["stat"]["e_absdep"] - b["stat"]["e_absdep"]) / a["stat"]["e_absdep"] < 1e-9
 
 
