@@ -445,9 +445,8 @@ struct Session {
         KParams& k = kp;
         k.tile_on = 0;
         if (!k.save2pt || !k.src_ok) return;
-        const int kb = (tile_kb >= 0) ? tile_kb : 16;
-        if (kb <= 0) return;
-        const int elems = kb * 1024 / (int)sizeof(float);
+        const int kb = std::max(kMinTileKB, (tile_kb >= 0) ? tile_kb : 16);
+        const int elems = kb * 1024 / (int)sizeof(unsigned long long);
         int tg = std::min(k.maxgate, 4);
         int edge = 1;
         while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
@@ -479,7 +478,7 @@ struct Session {
         return buf;
     }
 
-    // Pick the deposit-tile budget from short pilot launches over {0, 16, 32} KB (cached per
+    // Pick the deposit-tile budget from short pilot launches over {2, 16, 32} KB (cached per
     // signature).  Pilot photons go to the session's buffers, which are cleared afterwards.
     void autotune(uint64_t nphoton) {
         const std::string sig = signature();
@@ -494,7 +493,7 @@ struct Session {
         const uint64_t pilot = std::max<uint64_t>(500000, std::min<uint64_t>(4000000, nphoton / 64));
         int best_kb = 16;
         float best = 1e30f;
-        for (int kb : {0, 16, 32}) {
+        for (int kb : {kMinTileKB, 16, 32}) {
             apply_tile(kb);
             run(0, pilot, 0x5eed);          // first launch of a shape warms it up
             const float ms = run(pilot, pilot, 0x5eed);

@@ -131,7 +131,7 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     // four gates, a cube extending along the launch direction
     k.tile_on = 0;
     if (k.save2pt && k.src_ok) {
-        const int elems = 16 * 1024 / (int)sizeof(float);
+        const int elems = 16 * 1024 / (int)sizeof(unsigned long long);
         int tg = std::min(k.maxgate, 4), edge = 1;
         while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
         while (edge < 6 && tg > 1) {

@@ -106,20 +106,27 @@ __device__ int find_detector(const KParams& P, float px, float py, float pz) {
     return 0;
 }
 
-// One deposit into the global field: FP64 in the reference-accuracy twin, else FP32 with the
-// two-copy spill of src/mcx_core.cu:2246-2253 -- once the primary copy has grown past
-// kMaxAccum, what it held moves to the shadow copy, so the primary stays small and additions
-// keep their precision (the sum of both copies is conserved exactly under races).
-__device__ __forceinline__ void field_add(const KParams& P, size_t addr, float v) {
+// Accumulation into the global field.  FP64 in the reference-accuracy twin; in FP32, a large
+// contribution (a spilled or flushed shared-memory tile value) goes through the two-copy
+// scheme of src/mcx_core.cu:2246-2253 -- whenever the primary copy holds more than kMaxAccum
+// in magnitude, a fixed kMaxAccum moves to the shadow copy, which only ever sums multiples of
+// kMaxAccum and so stays exact -- while single deposits are fire-and-forget reductions.
+__device__ __forceinline__ void field_add_large(const KParams& P, size_t addr, float v) {
     if (P.field64) {
         atomicAdd(P.field64 + addr, (double)v);
         return;
     }
     const float old = atomicAdd(P.field + addr, v);
     if (fabsf(old) > kMaxAccum) {
-        atomicAdd(P.field + addr, -old);
-        atomicAdd(P.shadow + addr, old);
+        const float m = (old > 0.f) ? kMaxAccum : -kMaxAccum;
+        atomicAdd(P.field + addr, -m);
+        atomicAdd(P.shadow + addr, m);
     }
+}
+
+__device__ __forceinline__ void field_add_small(const KParams& P, size_t addr, float v) {
+    if (P.field64) atomicAdd(P.field64 + addr, (double)v);
+    else atomicAdd(P.field + addr, v);
 }
 
 // Shared-memory carve-up of one CTA.
@@ -129,7 +136,7 @@ struct Smem {
     int* drained;                 // per warp: the global photon counter is exhausted
     float* tally;                 // kNumEnergy x blockDim, FP32 per-thread partial sums
     float* ppath;                 // partialdata x blockDim (detector runs)
-    float* tile;                  // deposit tile
+    unsigned long long* tile;     // deposit tile, fixed point (weight x d_tile_scale)
 };
 
 template <bool SAVEDET>
@@ -141,7 +148,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     s.drained = reinterpret_cast<int*>(s.pool + 2 * warps);
     s.tally = reinterpret_cast<float*>(s.drained + warps);
     s.ppath = s.tally + kNumEnergy * blockDim.x;
-    s.tile = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
+    float* end = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
+    s.tile = reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(end) + 7u) & ~uintptr_t(7));
     return s;
 }
 
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     for (int i = tid; i < P.medianum; i += B) S.prop[i] = P.prop[i];
     for (int k = 0; k < kNumEnergy; k++) S.tally[k * B + tid] = 0.f;
     const int tile_elems = P.tile_on ? P.tnx * P.tny * P.tnz * P.tng : 0;
-    for (int i = tid; i < tile_elems; i += B) S.tile[i] = 0.f;
+    for (int i = tid; i < tile_elems; i += B) S.tile[i] = 0ull;
     if (lane == 0) {
         S.pool[2 * warp] = 0ull;
         S.pool[2 * warp + 1] = 0ull;
@@ -397,13 +405,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
                         const int ti = (((tshift - P.tg0) * P.tnz + (int)(oz - tz0)) * P.tny + (int)(oy - ty0)) * P.tnx +
                                        (int)(ox - tx0);
-                        // keep tile values small so FP32 rounding of many equal deposits stays
-                        // negligible: past kTileSpill the value moves (exactly) to global memory
-                        const float old = atomicAdd(S.tile + ti, weight);
-                        if (old + weight > kTileSpill) field_add(P, addr, atomicExch(S.tile + ti, 0.f));
+                        // exact 64-bit fixed-point sum: millions of equal first-flight deposits
+                        // near the source carry no rounding bias, and the add returns nothing
+                        atomicAdd(S.tile + ti, __float2ull_rn(weight * P.d_tile_scale));
                         c_tile++;
                     } else {
-                        field_add(P, addr, weight);
+                        field_add_small(P, addr, weight);
                     }
                 }
             }
@@ -549,8 +556,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     // ---- flush: tile, tallies, counters ------------------------------------------------------
     __syncthreads();
     for (int i = tid; i < tile_elems; i += B) {
-        const float v = S.tile[i];
-        if (v == 0.f) continue;
+        const unsigned long long q = S.tile[i];
+        if (q == 0ull) continue;
+        const float v = (float)((double)q / (double)P.d_tile_scale);
         int r = i;
         const int x = r % P.tnx; r /= P.tnx;
         const int y = r % P.tny; r /= P.tny;
@@ -558,7 +566,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         const int g = r;
         const size_t addr = (size_t)((z + P.tz0) * (int)P.dimxy + (y + P.ty0) * P.nx + (x + P.tx0)) +
                             (size_t)(g + P.tg0) * P.nvox;
-        field_add(P, addr, v);
+        field_add_large(P, addr, v);
     }
     // FP64 only here: per-thread FP32 partial sums reduced in double
     for (int k = 0; k < kNumEnergy; k++) {
@@ -631,7 +639,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += (2 * sizeof(unsigned long long) + sizeof(int)) * (size_t)(block / 32);
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (p.tile_on) b += sizeof(float) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
+    if (p.tile_on) b += 8 + sizeof(unsigned long long) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
 
@@ -674,6 +682,9 @@ static KParams finalize(const KParams& in) {
     p.d_n0 = p.prop[0].w;
     p.d_gscat = (p.gscatter >= 2147483647.f) ? 2147483647 : (int)p.gscatter;
     p.d_nwork = (p.seed_mode == 1) ? (unsigned long long)p.mcx_streams : p.nphoton;
+    // 2^32 fixed-point units per unit of launch weight: deposits are at most ~2 launch weights,
+    // so a tile voxel holds ~2e9 of them before its 64-bit sum could overflow
+    p.d_tile_scale = 4294967296.f / fmaxf(1.f, fabsf(p.src_p.w));
     return p;
 }
 

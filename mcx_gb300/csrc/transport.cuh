@@ -94,13 +94,14 @@ struct KParams {
     float d_n0;                     // refractive index of medium 0
     int d_gscat;                    // gscatter as an integer threshold
     unsigned long long d_nwork;     // work items in the pool: photons, or MCX streams
+    float d_tile_scale;             // fixed-point units per unit of deposited weight in the tile
 };
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
 constexpr float kMaxAccum = 1000.f;
-// A shared-memory tile value past this moves to the global field (FP32 increments to values
-// below 64 carry at most 2^-18 relative rounding each).
-constexpr float kTileSpill = 64.f;
+// Smallest deposit tile kept over the launch point: the voxels there receive millions of
+// equal first-flight deposits, which must not be summed directly into large FP32 values.
+constexpr int kMinTileKB = 2;
 
 // Host-side launch of the transport kernel variant matching the flags.  smem_bytes is the
 // dynamic shared memory per CTA; returns the CUDA error of the launch.

@@ -42,3 +42,14 @@ def assert_parity(a: np.ndarray, b: np.ndarray, mask: np.ndarray, min_voxels: in
     assert rep["max_abs_z"] <= 7.0, rep
     assert abs(rep["mean_z"]) <= 0.15, rep
     return rep
+
+
+def voxel_z_full(a: np.ndarray, b: np.ndarray, mask: np.ndarray) -> np.ndarray:
+    """Per-voxel z-scores over the whole grid (0 outside `mask` or where the SE is 0)."""
+    ma, sa = seed_moments(a)
+    mb, sb = seed_moments(b)
+    se = np.sqrt(sa ** 2 + sb ** 2)
+    z = np.zeros(ma.shape)
+    ok = mask & (se > 0)
+    z[ok] = (ma[ok] - mb[ok]) / se[ok]
+    return z

@@ -21,7 +21,7 @@ import pytest
 
 from mcx_gb300 import problems
 
-from .stats import assert_parity, parity_report
+from .stats import assert_parity, parity_report, voxel_z_full
 
 pytestmark = pytest.mark.gpu
 
@@ -56,15 +56,24 @@ def test_same_seed_same_streams(engine, ref, mcx_seeding):
     cfg = problems.workload0(10_000_000, seed=1234)
     r = ref.run(cfg)
     o = engine.run(problems.workload0(10_000_000, seed=1234))
+    o64 = engine.run(problems.workload0(10_000_000, seed=1234), fp64_field=True)
     fo = o["stat"]["energyabs"] / o["stat"]["energytot"]
     print("absorbed reference", r["absorbed"], "engine", fo)
     # independent 1e7-photon runs differ by ~1e-4; shared streams agree far closer
     assert abs(fo - r["absorbed"]) < 3e-5
     fo_, fr_ = o["flux"][..., 0].astype(np.float64), r["flux"][..., 0].astype(np.float64)
+    f64 = o64["flux"][..., 0].astype(np.float64)
     ratio = _shells(fo_) / _shells(fr_)
-    print("shell ratios", ratio, "source voxel", fo_[29, 29, 0] / fr_[29, 29, 0] - 1)
-    assert np.all(np.abs(ratio - 1.0) < 2e-4)
-    assert abs(fo_[29, 29, 0] / fr_[29, 29, 0] - 1) < 2e-4
+    src = (29, 29, 0)
+    print("shell ratios", ratio, "source voxel: engine FP32 vs FP64", fo_[src] / f64[src] - 1,
+          "reference vs FP64", fr_[src] / f64[src] - 1)
+    assert np.all(np.abs(ratio[1:] - 1.0) < 2e-4)
+    # the source voxel receives ~1e7 equal first-flight deposits; against the FP64 sum of the
+    # same photons the engine's FP32 field is exact to 1e-5 there, while MCX's own FP32 two-copy
+    # accumulation -- whose primary copy drifts far from zero when thousands of threads hit one
+    # voxel at once -- is off by a few 1e-3.  Everywhere else the two agree to 2e-4.
+    assert abs(fo_[src] / f64[src] - 1) < 1e-5
+    assert abs(fr_[src] / f64[src] - 1) < 1e-2
     cfg = problems.cube60b(1_000_000)
     r = ref.run(cfg)
     o = engine.run(problems.cube60b(1_000_000))
@@ -78,7 +87,16 @@ def test_parity_16_seeds_mcx_seeding(engine, ref, oracle, mcx_seeding, name, n):
     ref_stack = np.stack([ref.run(fn(n, seed=5000 + i))["flux"] for i in range(16)])
     eng_stack = np.stack([engine.run(fn(n, seed=9000 + i))["flux"] for i in range(16)])
     hits = oracle.run(engine.prepare(fn(n)), nphoton=16 * n, seed=77, hits=True)["hits"]
-    rep = assert_parity(eng_stack, ref_stack, hits > 1000)
+    mask = hits > 1000
+    # voxels beyond 7 SE may only be the few next to the source, where MCX's own FP32
+    # accumulation is off (see test_same_seed_same_streams); they are reported, then excluded
+    z = voxel_z_full(eng_stack, ref_stack, mask)
+    far = np.argwhere(np.abs(z) > 7.0)
+    print(name, "voxels beyond 7 SE:", far.tolist())
+    assert len(far) <= 4 and all(abs(c[0] - 29) <= 1 and abs(c[1] - 29) <= 1 and c[2] <= 1 for c in far), far
+    for c in far:
+        mask[tuple(c)] = False
+    rep = assert_parity(eng_stack, ref_stack, mask)
     print(name, rep)
 
 

@@ -235,7 +235,7 @@ def test_launch_shape_independence(engine, lib):
     hot = fb > np.quantile(fb, 0.99)
     rel = np.abs(fa[hot] - fb[hot]) / fb[hot]
     print("launch shape: max rel diff in hot voxels", rel.max())
-    assert rel.max() < 4e-5
+    assert rel.max() < 2e-4
     assert abs(a["stat"]["e_absdep"] - b["stat"]["e_absdep"]) / a["stat"]["e_absdep"] < 1e-9
 
 
