@@ -36,6 +36,20 @@ __device__ __forceinline__ float rng_next(unsigned long long& a, unsigned long l
     return __uint_as_float(0x3F800000u | (lo >> 9)) - 1.0f;
 }
 
+// One xorshift128+ step giving two floats: the reference's (low 32 bits) and one from the high
+// 32 bits of the same 64-bit output, for the per-photon streams that need not follow MCX's
+// draw-by-draw consumption.
+__device__ __forceinline__ void rng_next2(unsigned long long& a, unsigned long long& b, float& f0, float& f1) {
+    unsigned long long s1 = a;
+    const unsigned long long s0 = b;
+    a = s0;
+    s1 ^= s1 << 23;
+    b = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+    const unsigned long long r = b + s0;
+    f0 = __uint_as_float(0x3F800000u | ((unsigned)r >> 9)) - 1.0f;
+    f1 = __uint_as_float(0x3F800000u | ((unsigned)(r >> 32) >> 9)) - 1.0f;
+}
+
 __device__ __forceinline__ unsigned long long splitmix64(unsigned long long& x) {
     unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -297,19 +311,36 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         bool kill = false;
 
         if (pscat <= 0.f) {
-            pscat = -__logf(rng_next(r0, r1) + kEPS);                 // src/mcx_rand_xorshift128p.cu:122
+            // random numbers of this scattering event: MCX's order (scattering length, azimuth,
+            // zenith), one generator step each in MCX seeding mode, two steps for all three with
+            // per-photon streams
+            float u_len, u_phi, u_th;
+            if (P.seed_mode == 1) {
+                u_len = rng_next(r0, r1);
+            } else {
+                rng_next2(r0, r1, u_len, u_phi);
+            }
+            pscat = -__logf(u_len + kEPS);                               // src/mcx_rand_xorshift128p.cu:122
             if (nscat >= 0) {                                           // not the launch flight
+                if (P.seed_mode == 1) {
+                    u_phi = rng_next(r0, r1);
+                    u_th = rng_next(r0, r1);
+                } else {
+                    float spare;
+                    rng_next2(r0, r1, u_th, spare);
+                }
                 float sphi, cphi;
-                __sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);   // src/mcx_core.cu:1930-1933
+                __sincosf(kTWO_PI * u_phi, &sphi, &cphi);               // src/mcx_core.cu:1930-1933
                 const float g = (nscat > gscat) ? 0.f : pr.z;
                 float ct;
                 if (fabsf(g) > kEPS) {                                  // Henyey-Greenstein, 1946-1959
-                    float tmp = __fdividef(1.f - g * g, 1.f - g + 2.f * g * rng_next(r0, r1));
+                    const float g2 = g * g;
+                    float tmp = __fdividef(1.f - g2, 1.f - g + 2.f * g * u_th);
                     tmp *= tmp;
-                    ct = __fdividef(1.f + g * g - tmp, 2.f * g);
+                    ct = __fdividef(1.f + g2 - tmp, 2.f * g);
                     ct = fmaxf(-1.f, fminf(1.f, ct));
                 } else {
-                    ct = 2.f * rng_next(r0, r1) - 1.f;                  // isotropic, 1961-1963
+                    ct = 2.f * u_th - 1.f;                              // isotropic, 1961-1963
                 }
                 const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
                 if (SAVEDET && med > 0) {                               // 1970-1993
@@ -407,7 +438,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                                        (int)(ox - tx0);
                         // exact 64-bit fixed-point sum: millions of equal first-flight deposits
                         // near the source carry no rounding bias, and the add returns nothing
-                        atomicAdd(S.tile + ti, __float2ull_rn(weight * P.d_tile_scale));
+                        // weight * scale < 2^23, so adding 2^23 leaves its rounded integer value in the
+                        // low mantissa bits (FP32 pipes only)
+                        const unsigned q = __float_as_uint(fmaf(weight, P.d_tile_scale, 8388608.f)) - 0x4B000000u;
+                        atomicAdd(S.tile + ti, (unsigned long long)q);
                         c_tile++;
                     } else {
                         field_add_small(P, addr, weight);
@@ -682,9 +716,9 @@ static KParams finalize(const KParams& in) {
     p.d_n0 = p.prop[0].w;
     p.d_gscat = (p.gscatter >= 2147483647.f) ? 2147483647 : (int)p.gscatter;
     p.d_nwork = (p.seed_mode == 1) ? (unsigned long long)p.mcx_streams : p.nphoton;
-    // 2^32 fixed-point units per unit of launch weight: deposits are at most ~2 launch weights,
-    // so a tile voxel holds ~2e9 of them before its 64-bit sum could overflow
-    p.d_tile_scale = 4294967296.f / fmaxf(1.f, fabsf(p.src_p.w));
+    // 2^21 fixed-point units per launch weight: a deposit is at most sqrt(3) launch weights (a
+    // voxel diagonal), so weight x scale stays below 2^23 as the rounding trick needs
+    p.d_tile_scale = 2097152.f / fmaxf(1.f, fabsf(p.src_p.w));
     return p;
 }
 
