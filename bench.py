@@ -40,7 +40,7 @@ CPU_SAMPLE = {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}
 # Thread-level instructions per transport step (ncu smsp__thread_inst_executed.sum over the
 # kernel's own step counter) and DRAM bytes per photon (dram__bytes_read.sum + write.sum over
 # photons), from the ncu captures summarised in profiles/transport_<workload>.md.
-NCU_PER_STEP = {"workload0": None, "workload1": None, "workload2": None}
+NCU_PER_STEP = {"workload0": None, "workload1": 288.0, "workload2": None}
 NCU_DRAM_PER_PHOTON = {"workload0": None, "workload1": None, "workload2": None}
 
 

@@ -229,14 +229,15 @@ def test_launch_shape_independence(engine, lib):
     da = a["detp"][:, np.lexsort(a["detp"][::-1])]
     db = b["detp"][:, np.lexsort(b["detp"][::-1])]
     assert np.array_equal(da, db)
-    # same deposits summed in another order (and, in the second run, without the shared-memory
-    # tile): the FP32 accumulation tolerance of test_energy_balance_and_fp32_accumulation
+    # same deposits summed in another order (and, in the second run, with the smallest
+    # shared-memory tile, so most hot voxels take plain FP32 atomics): each run's FP32 sum is
+    # within ~2e-4 of the FP64 sum in the hottest voxels, so two runs differ by up to twice that
     fa, fb = a["flux"].astype(np.float64), b["flux"].astype(np.float64)
     assert abs(fa.sum() - fb.sum()) / fb.sum() < 1e-5
     hot = fb > np.quantile(fb, 0.99)
     rel = np.abs(fa[hot] - fb[hot]) / fb[hot]
     print("launch shape: max rel diff in hot voxels", rel.max())
-    assert rel.max() < 2e-4
+    assert rel.max() < 5e-4
     assert abs(a["stat"]["e_absdep"] - b["stat"]["e_absdep"]) / a["stat"]["e_absdep"] < 1e-9
 
 
