@@ -34,8 +34,9 @@ sys.path.insert(0, str(ROOT))
 import numpy as np  # noqa: E402
 
 METRIC = "photons/ms (plain MC)"
-WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000}
-CPU_SAMPLE = {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000}
+WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000,
+                    "cube60planar": 100_000_000, "batch": 0}
+CPU_SAMPLE = {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000, "cube60planar": 100_000, "batch": 20_000}
 
 # Thread-level instructions per transport step (ncu smsp__thread_inst_executed.sum over the
 # kernel's own step counter) and DRAM bytes per photon (dram__bytes_read.sum + write.sum over
@@ -112,7 +113,60 @@ def peaks() -> dict:
 def make_cfg(name: str, nphoton: int, seed: int):
     from mcx_gb300 import problems
 
+    if name == "cube60planar":
+        cfg = problems.cube60planar(nphoton)
+        cfg["seed"] = seed
+        return cfg
     return problems.WORKLOADS[name](nphoton, seed=seed)
+
+
+def batch_cfgs(scale: float, seed: int = 20251204):
+    from mcx_gb300 import problems
+
+    return problems.batch_instances(256, seed=seed, budget_scale=scale)
+
+
+def batch_main(args, world, rank) -> None:
+    """The batched workload: 256 simulations per step in one CUDA graph (mcxg_run_batch).
+    value = all photons of the batch over the graph's CUDA-event time (volumes already on the
+    device); e2e = the same over the wall time of the whole mcx_gb300.run_batch call (Config
+    preparation, uploads, graph, normalisation, copies back)."""
+    import torch
+
+    import mcx_gb300
+
+    torch.cuda.set_device(0)
+    cfgs = batch_cfgs(args.batch_scale)
+    total = sum(c["nphoton"] for c in cfgs)
+    for _ in range(args.warmup):
+        mcx_gb300.run_batch(batch_cfgs(args.batch_scale), streams=args.streams)
+    graph_ms, wall_ms, h2d, d2h = [], [], 0, 0
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            cs = batch_cfgs(args.batch_scale)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res, ms = mcx_gb300.run_batch(cs, streams=args.streams)
+            wall_ms.append((time.perf_counter() - t0) * 1e3)
+            graph_ms.append(ms)
+            h2d = sum(c["vol"].size * 4 + np.asarray(c["prop"]).nbytes + np.asarray(c["detpos"]).nbytes for c in cs)
+            d2h = sum(r["flux"].nbytes + (r["detp"].nbytes if "detp" in r else 0) for r in res)
+    if rank != 0:
+        return
+    g = sum(graph_ms)
+    line = {
+        "metric": METRIC, "value": total * args.steps / g, "unit": "photons/ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": g / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch", "instances": len(cfgs), "photons_per_step": total,
+                   "budget_scale": args.batch_scale, "streams": args.streams,
+                   "l2": "inputs (256 volumes, 256 fields) larger than L2"},
+        "e2e": {"value": total * args.steps / sum(wall_ms), "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": sum(wall_ms) / args.steps},
+        "gpu_launches": len(cfgs) * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
 
 
 def cpu_baseline(name: str, sample: int) -> dict:
@@ -142,6 +196,29 @@ def reference_arm(args, world, rank) -> None:
     base = {"impl": "reference", "metric": METRIC, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic"}
+    if name == "batch" and ref_mcx.available():
+        # MCX has no batch mode: its front-ends run the simulations one after another.  A bounded
+        # sample of the batch (the first `--ref-sample` instances) runs that way per step.
+        cfgs = batch_cfgs(args.batch_scale)[: args.ref_sample]
+        ref_mcx.build()
+        photons = sum(c["nphoton"] for c in cfgs)
+        kern, norm, wall = 0.0, 0.0, 0.0
+        for _ in range(args.steps):
+            for c in cfgs:
+                t0 = time.perf_counter()
+                r = ref_mcx.run(c, keep_field=False)
+                wall += time.perf_counter() - t0
+                kern += c["nphoton"] / r["speed"]
+                norm += r["normalized_ms"]
+        line = dict(base, value=photons * args.steps / kern, ms_per_step=kern / args.steps,
+                    config={"workload": "batch", "instances": len(cfgs), "photons_per_step": photons,
+                            "budget_scale": args.batch_scale, "note": "the first instances of the batch, run in sequence"},
+                    e2e={"value": photons * args.steps / norm, "unit": "photons/ms", "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0, "ms_per_step": norm / args.steps, "process_wall_s": wall},
+                    cpu_baseline={"value": photons * args.steps / kern, "unit": "photons/ms", "cores": os.cpu_count(),
+                                  "kind": "reference", "sample": f"{len(cfgs)} batch instances, the MCX CUDA build"})
+        print(json.dumps(line))
+        return
     if ref_mcx.available():
         try:
             t0 = time.perf_counter()
@@ -218,8 +295,14 @@ def main() -> None:
     ap.add_argument("--photons", type=float, default=0)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scale", type=float, default=0.1, help="photon-budget scale of the batched workload")
+    ap.add_argument("--streams", type=int, default=4, help="streams of the batched workload's graph")
+    ap.add_argument("--ref-sample", type=int, default=16, help="batch instances the reference arm runs")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.workload == "batch" and args.impl != "reference":
+        batch_main(args, world, rank)
+        return
 
     if args.impl == "reference":
         reference_arm(args, world, rank)

@@ -112,6 +112,19 @@ void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile);
  * the same random streams as MCX itself.  The environment variable MCXG_SEEDING=mcx selects 1. */
 void mcxg_set_seeding(int mode);
 
+/* ---- Batched simulations ------------------------------------------------------------------ */
+
+/* No counterpart in MCX, whose front-ends run one mcx_run_simulation per input (src/mcx.c:62-78).
+ * Runs `count` prepared Configs (each after mcxg_validatecfg or mcx_validatecfg) on the device of
+ * cfgs[0]->deviceid[0], as one CUDA graph of their transport launches over `nstreams` streams
+ * (1..32), largest photon budget first; the block scheduler fills the SMs a finishing launch
+ * frees with the CTAs of launches queued behind it.  Every Config receives exactly the outputs
+ * mcx_run_simulation gives it (exportfield accumulated, exportdetected, energies, normaliser,
+ * detected count); its `runtime` is the whole graph's time.  Each Config must run one repetition
+ * (respin 1) with all its time gates on the device.  `stats` (count entries) and `graph_ms` may
+ * be NULL.  Returns 0 or a negative MCX error id (message via mcxg_last_error). */
+int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms);
+
 /* ---- Allocation-free transport ----------------------------------------------------------- */
 
 /* No counterpart in MCX: an addition for callers that may not call cudaMalloc while they run,

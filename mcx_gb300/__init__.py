@@ -6,7 +6,7 @@ pmcx-style Python front-end (``run``, ``gpuinfo``, ``version``) plus the device-
 session used by the benchmark.
 """
 
-from .api import MCXError, PreparedConfig, gpuinfo, prepare, run, run_prepared, version  # noqa: F401
+from .api import MCXError, PreparedConfig, gpuinfo, prepare, run, run_batch, run_prepared, version  # noqa: F401
 from .session import Session  # noqa: F401
 
-__all__ = ["run", "run_prepared", "prepare", "gpuinfo", "version", "MCXError", "PreparedConfig", "Session"]
+__all__ = ["run", "run_batch", "run_prepared", "prepare", "gpuinfo", "version", "MCXError", "PreparedConfig", "Session"]

@@ -98,6 +98,11 @@ class PreparedConfig:
                 _set_vec(getattr(c, key), cfg[key], n)
         if "steps" in cfg:
             _set_vec(c.steps, cfg["steps"], 3)
+        if "srcpattern" in cfg and cfg["srcpattern"] is not None:
+            # x fastest, as pmcx passes a (param1.w, param2.w) or (nx, ny, nz) array (src/pmcx.cpp)
+            pat = np.asarray(cfg["srcpattern"], dtype=np.float32).ravel(order="F").copy()
+            self.keep.append(pat)
+            c.srcpattern = pat.ctypes.data
 
         if "vol" not in cfg or "prop" not in cfg:
             raise MCXError(-4, "the 'vol' and 'prop' fields are required")
@@ -183,39 +188,44 @@ def run(cfg: dict[str, Any], verbose: bool = False, fp64_field: bool = False) ->
     return run_prepared(pc, fp64_field=fp64_field)
 
 
-def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]:
-    c = pc.c
-    nx, ny, nz = pc.dims
+def _active_devices(c) -> None:
+    """mcx_list_gpu compacts cfg.deviceid into the active-device list, as the front-ends call it."""
     info = C.POINTER(abi.GPUInfo)()
     lib.mcxg_clear_error()
     nact = lib.mcx_list_gpu(C.byref(c), C.byref(info))
     _check()
-    if nact == 0:
-        if info:
-            libc.free(info)
-        raise MCXError(-1, "no active GPU device found")
+    return nact, info
+
+
+def _attach_field(pc: PreparedConfig):
+    c = pc.c
+    nx, ny, nz = pc.dims
     maxgate = pc.ngates if c.maxgate == 0 else min(int(c.maxgate), pc.ngates)
     flux = None
     if c.issave2pt != b"\x00":
         flux = np.zeros(nx * ny * nz * maxgate, dtype=np.float32)
         c.exportfield = flux.ctypes.data
-    try:
-        (lib.mcxg_run_simulation_fp64 if fp64_field else lib.mcx_run_simulation)(C.byref(c), info)
-        _check()
-    finally:
-        libc.free(info)
-        det_ptr = c.exportdetected
-        ndet = int(c.detectedcount)
-        detp = None
-        if det_ptr:
-            reclen = pc.reclen
-            if ndet and reclen:
-                buf = (C.c_float * (reclen * ndet)).from_address(det_ptr)
-                detp = np.frombuffer(buf, dtype=np.float32).copy().reshape((reclen, ndet), order="F")
-            libc.free(C.c_void_p(det_ptr))
-            c.exportdetected = None
-    st = abi.Stats()
-    lib.mcxg_get_stats(C.byref(st))
+    return flux, maxgate
+
+
+def _take_detected(pc: PreparedConfig):
+    c = pc.c
+    det_ptr = c.exportdetected
+    ndet = int(c.detectedcount)
+    detp = None
+    if det_ptr:
+        reclen = pc.reclen
+        if ndet and reclen:
+            buf = (C.c_float * (reclen * ndet)).from_address(det_ptr)
+            detp = np.frombuffer(buf, dtype=np.float32).copy().reshape((reclen, ndet), order="F")
+        libc.free(C.c_void_p(det_ptr))
+        c.exportdetected = None
+    return detp
+
+
+def _result(pc: PreparedConfig, flux, maxgate, detp, st) -> dict[str, Any]:
+    c = pc.c
+    nx, ny, nz = pc.dims
     out: dict[str, Any] = {}
     if flux is not None:
         out["flux"] = flux.reshape((nx, ny, nz, maxgate), order="F")
@@ -241,6 +251,49 @@ def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]
         "error_flags": st.error_flags,
     }
     return out
+
+
+def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]:
+    c = pc.c
+    nact, info = _active_devices(c)
+    if nact == 0:
+        if info:
+            libc.free(info)
+        raise MCXError(-1, "no active GPU device found")
+    flux, maxgate = _attach_field(pc)
+    try:
+        (lib.mcxg_run_simulation_fp64 if fp64_field else lib.mcx_run_simulation)(C.byref(c), info)
+        _check()
+    finally:
+        libc.free(info)
+        detp = _take_detected(pc)
+    st = abi.Stats()
+    lib.mcxg_get_stats(C.byref(st))
+    return _result(pc, flux, maxgate, detp, st)
+
+
+def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[str, Any]], float]:
+    """Run many independent simulations in one CUDA graph on one GPU (``mcxg_run_batch``).
+
+    Returns the per-simulation results -- the same dicts ``run`` gives -- and the graph time in
+    ms.  Each input runs one repetition with all its time gates on the device."""
+    pcs = [prepare(cfg) for cfg in cfgs]
+    for pc in pcs:
+        nact, info = _active_devices(pc.c)
+        if info:
+            libc.free(info)
+        if nact == 0:
+            raise MCXError(-1, "no active GPU device found")
+    fields = [_attach_field(pc) for pc in pcs]
+    arr = (C.POINTER(abi.Config) * len(pcs))(*[C.pointer(pc.c) for pc in pcs])
+    stats = (abi.Stats * len(pcs))()
+    ms = C.c_double(0.0)
+    try:
+        _check(lib.mcxg_run_batch(arr, len(pcs), int(streams), stats, C.byref(ms)))
+    finally:
+        dets = [_take_detected(pc) for pc in pcs]
+    out = [_result(pc, f, g, d, stats[i]) for i, (pc, (f, g), d) in enumerate(zip(pcs, fields, dets))]
+    return out, float(ms.value)
 
 
 def version() -> str:

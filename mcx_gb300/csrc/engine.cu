@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <stdlib.h>
 #include <string>
@@ -194,6 +195,75 @@ uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
 
 }  // namespace
 
+// Source settings the engine takes (src/mcx_core.cu:1261-1640): every MCX_SRC_* shape with one
+// source; not photon sharing (srcnum > 1), extra sources or a launch-angle table.
+void check_source(const Config* cfg) {
+    if ((unsigned char)cfg->srctype >= kNumSrcTypes) MCXG_RAISE(-6, "unknown source type");
+    if (cfg->srcnum > 1) MCXG_RAISE(-6, "photon sharing (srcnum > 1) is not supported by the GB300 engine");
+    if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
+    if (cfg->nangle) MCXG_RAISE(-6, "launch-angle distributions (angleinvcdf) are not supported by the GB300 engine");
+    const int st = (unsigned char)cfg->srctype;
+    if ((st == kSrcPattern || st == kSrcPattern3D) && !cfg->srcpattern)
+        MCXG_RAISE(-4, "the 'srcpattern' field can not be empty when your 'srctype' is 'pattern'");
+    // pattern sizes index the pattern array: whole numbers of pixels / voxels
+    auto whole = [](float x) { return x >= 1.f && x == std::floor(x) && x < 16777216.f; };
+    if (st == kSrcPattern && !(whole(cfg->srcparam1.w) && whole(cfg->srcparam2.w)))
+        MCXG_RAISE(-4, "a pattern source needs whole pattern dimensions in srcparam1.w and srcparam2.w");
+    if (st == kSrcPattern3D && !(whole(cfg->srcparam1.x) && whole(cfg->srcparam1.y) && whole(cfg->srcparam1.z)))
+        MCXG_RAISE(-4, "a pattern3d source needs whole pattern dimensions in srcparam1.x/y/z");
+    if (st == kSrcPencilArray && !(cfg->srcparam1.w >= 2.f && cfg->srcparam2.w >= 2.f))
+        MCXG_RAISE(-4, "a pencil-array source needs at least 2 beams along each side (srcparam1.w, srcparam2.w)");
+}
+
+size_t source_pattern_len(const Config* cfg) {
+    if (!cfg->srcpattern) return 0;
+    if ((unsigned char)cfg->srctype == kSrcPattern) return (size_t)cfg->srcparam1.w * (size_t)cfg->srcparam2.w;
+    if ((unsigned char)cfg->srctype == kSrcPattern3D) return (size_t)cfg->srcparam1.x * (size_t)cfg->srcparam1.y * (size_t)cfg->srcparam1.z;
+    return 0;
+}
+
+void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
+    float4 p = cfg->srcpos;
+    float3 v = f3(cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z);
+    float t = 0.f;
+    k.srctype = (unsigned char)cfg->srctype;
+    k.src_param1 = cfg->srcparam1;
+    k.src_param2 = cfg->srcparam2;
+    k.src_focal = cfg->srcdir.w;
+    k.srcpattern = d_pattern;
+    k.isspecular = cfg->isspecular ? 1 : 0;
+    k.voidtime = cfg->voidtime;
+    k.src_ok = 1;
+    uint32_t sidx = 0, smed = 0;
+    if (src_is_point(k.srctype)) {          // launch voxel from preprocessing (srcparam2.z/.w)
+        std::memcpy(&sidx, &cfg->srcparam2.z, 4);
+        std::memcpy(&smed, &cfg->srcparam2.w, 4);
+    }
+    int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
+    if (k.srctype == kSrcPencil) {
+        // every pencil photon follows the same path through the void: traced once here, the
+        // photons start from its end (src/mcx_core.cu:1236-1243, 1652-1672)
+        if ((smed & kMED_MASK) == 0) {
+            const int id = host_skipvoid(cfg, p, v, t, fd);
+            if (id < 0) {
+                k.src_ok = 0;
+            } else {
+                sidx = (uint32_t)id;
+                smed = host_label(cfg, id);
+            }
+        }
+        if (std::fabs(p.w) <= cfg->minenergy) k.src_ok = 0;
+    }
+    k.src_p = p;
+    k.src_v = make_float4(v.x, v.y, v.z, 0.f);
+    k.src_t = t;
+    k.src_idx = sidx;
+    k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
+    if (k.src_ok) {
+        k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Session: one prepared simulation on one device.
 // ---------------------------------------------------------------------------------------------
@@ -207,7 +277,7 @@ struct Session {
     size_t smem = 0;
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
-    DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos;
+    DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
     double kernel_ms = 0.0;
     int launches = 0;
     // MCX per-thread seeding: stream count, host/device seed words and the glibc random_r state
@@ -223,6 +293,8 @@ struct Session {
         labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
+        pattern.release();
+        // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -317,33 +389,13 @@ struct Session {
             k.detpos = detpos.as<float4>();
         }
 
-        // launch state of the pencil beam, void skipping folded in (src/mcx_core.cu:1236-1243, 1652-1672)
-        float4 p = cfg->srcpos;
-        float3 v = f3(cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z);
-        float t = 0.f;
-        uint32_t sidx, smed;
-        std::memcpy(&sidx, &cfg->srcparam2.z, 4);
-        std::memcpy(&smed, &cfg->srcparam2.w, 4);
-        int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
-        k.src_ok = 1;
-        if ((smed & kMED_MASK) == 0) {
-            const int id = host_skipvoid(cfg, p, v, t, fd);
-            if (id < 0) {
-                k.src_ok = 0;
-            } else {
-                sidx = (uint32_t)id;
-                smed = host_label(cfg, id);
-            }
+        // source: pattern intensities on the device, launch state
+        const size_t npat = source_pattern_len(cfg);
+        if (npat) {
+            pattern.alloc(npat * sizeof(float), stream);
+            CK(cudaMemcpyAsync(pattern.p, cfg->srcpattern, npat * sizeof(float), cudaMemcpyHostToDevice, stream));
         }
-        if (std::fabs(p.w) <= cfg->minenergy) k.src_ok = 0;
-        k.src_p = p;
-        k.src_v = make_float4(v.x, v.y, v.z, 0.f);
-        k.src_t = t;
-        k.src_idx = sidx;
-        k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
-        if (k.src_ok) {
-            k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
-        }
+        fill_source(k, cfg, pattern.as<float>());
         k.step_cap = 20000000u;   // a photon longer than this is a fault: flagged and stopped
 
         // output and scratch buffers
@@ -427,11 +479,11 @@ struct Session {
         set_transport_variant((o.blocks_per_sm > 0 && o.blocks_per_sm <= 3) ? 3 : 4);
         choose_tile(cfg, o.tile);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
         }
         if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
         if (o.blocks_per_sm > 0) bps = std::min(bps, o.blocks_per_sm);
@@ -439,34 +491,9 @@ struct Session {
         kp.chunk = o.chunk > 0 ? o.chunk : 64;
     }
 
-    // Deposit tile: a box of voxels x gates around the point where photons enter the medium,
-    // extending along the launch direction, sized to a shared-memory budget.
+    // Deposit tile over the entry point in a shared-memory budget of tile_kb KB (default 16).
     void choose_tile(const Config* cfg, int tile_kb) {
-        KParams& k = kp;
-        k.tile_on = 0;
-        if (!k.save2pt || !k.src_ok) return;
-        const int kb = std::max(kMinTileKB, (tile_kb >= 0) ? tile_kb : 16);
-        const int elems = kb * 1024 / (int)sizeof(unsigned long long);
-        int tg = std::min(k.maxgate, 4);
-        int edge = 1;
-        while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
-        while (edge < 6 && tg > 1) {
-            tg--;
-            edge = 1;
-            while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
-        }
-        edge = std::min(edge, std::max(k.nx, std::max(k.ny, k.nz)));
-        const int tnx = std::min(edge, k.nx), tny = std::min(edge, k.ny), tnz = std::min(edge, k.nz);
-        const float c[3] = {k.src_p.x + 0.5f * edge * k.src_v.x, k.src_p.y + 0.5f * edge * k.src_v.y,
-                            k.src_p.z + 0.5f * edge * k.src_v.z};
-        auto place = [](float center, int n, int dim) { return std::max(0, std::min(dim - n, (int)std::floor(center - 0.5f * n))); };
-        k.tnx = tnx; k.tny = tny; k.tnz = tnz;
-        k.tx0 = place(c[0], tnx, k.nx);
-        k.ty0 = place(c[1], tny, k.ny);
-        k.tz0 = place(c[2], tnz, k.nz);
-        k.tg0 = 0;
-        k.tng = tg;
-        k.tile_on = 1;
+        place_tile(kp, std::max(kMinTileKB, (tile_kb >= 0) ? tile_kb : 16));
         (void)cfg;
     }
 
@@ -511,11 +538,11 @@ struct Session {
     void apply_tile(int kb) {
         choose_tile(nullptr, kb);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
         }
         grid = std::max(1, bps) * sms;
     }
@@ -558,6 +585,28 @@ struct Session {
         kernel_ms += ms;
         launches++;
         return ms;
+    }
+
+    // Queue a cleared-buffer launch over photons [offset, offset + n) on stream `s` without
+    // waiting (the batch captures these into one graph).  MCX seeding words must be in place.
+    void enqueue(cudaStream_t s, uint64_t offset, uint64_t n, uint64_t seed) {
+        kp.photon_offset = offset;
+        kp.nphoton = n;
+        kp.seed = seed;
+        if (kp.seed_mode == 1) {
+            kp.mcx_per = (unsigned)(n / mcx_streams);
+            kp.mcx_odd = (unsigned)(n - (uint64_t)kp.mcx_per * mcx_streams);
+        }
+        CK(cudaMemsetAsync(field.p, 0, field.bytes, s));
+        if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, s));
+        if (field64.p) CK(cudaMemsetAsync(field64.p, 0, field64.bytes, s));
+        if (detcount.p) CK(cudaMemsetAsync(detcount.p, 0, detcount.bytes, s));
+        CK(cudaMemsetAsync(energy.p, 0, energy.bytes, s));
+        CK(cudaMemsetAsync(counters.p, 0, counters.bytes, s));
+        CK(cudaMemsetAsync(err.p, 0, err.bytes, s));
+        CK(cudaMemsetAsync(work.p, 0, sizeof(unsigned long long), s));
+        CK(launch_transport(kp, reflect, savedet, grid, block, smem, s));
+        launches = 1;
     }
 
     // Merge shadow copies, optionally scale, and copy the field out.
@@ -703,144 +752,106 @@ extern "C" int mcx_list_gpu(Config* cfg, GPUInfo** info) {
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
-    const auto t_start = std::chrono::steady_clock::now();
-    const int threadid = omp_get_thread_num ? omp_get_thread_num() : 0;
-    if (threadid >= MCXG_MAX_DEVICE || cfg->deviceid[threadid] == '\0') return;
-    if (threadid > 0) {
-        // one device per call: replicas on further devices are left to the caller
-        if (cfg->flog) fprintf(cfg->flog, "WARNING: the GB300 engine runs on one device per call; thread %d idle\n", threadid);
-        return;
-    }
-    const int gpuid = cfg->deviceid[threadid] - 1;
-    if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
-    (void)gpu;
+// Settings every run path rejects (MCX error ids).
+void check_config(const Config* cfg) {
     if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "photon replay is not supported by the GB300 engine");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
-    if (cfg->srctype != 0) MCXG_RAISE(-6, "the GB300 engine supports the pencil source only");
     if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media are supported by the GB300 engine");
     if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
+    check_source(cfg);
+}
 
-    std::memset(&t_stats, 0, sizeof(t_stats));
-    Session S;
-    S.create(cfg, gpuid, fp64_field);
-    {
-        // large runs tune the deposit tile with short pilot launches (cached per configuration)
-        int tile_override;
-        {
-            std::lock_guard<std::mutex> g(g_override_mu);
-            tile_override = g_override.tile;
-        }
-        const char* e = std::getenv("MCXG_TUNE");
-        const bool tune = !(e && std::strcmp(e, "0") == 0);
-        if (tune && tile_override < 0 && cfg->nphoton * (uint64_t)std::abs(cfg->respin) >= 20000000ull)
-            S.autotune(cfg->nphoton);
-    }
-    const KParams& k = S.kp;
-    const size_t dimxyz = S.nvox;
-    const int maxgate = k.maxgate;
-    const unsigned hostdetreclen = k.reclen;
-
+// Output buffers and counters of a run, as mcx_run_simulation leaves them before its first
+// launch (src/mcx_core.cu:2907-2921): exportfield is accumulated into, exportdetected grows.
+void begin_outputs(Config* cfg, const Session& S) {
     if (cfg->exportfield == nullptr && cfg->issave2pt)
-        cfg->exportfield = (float*)calloc(dimxyz * (size_t)maxgate, sizeof(float));
+        cfg->exportfield = (float*)calloc(S.nvox * (size_t)S.kp.maxgate, sizeof(float));
     if (cfg->exportdetected == nullptr)
-        cfg->exportdetected = (float*)malloc((size_t)hostdetreclen * std::max(1u, cfg->maxdetphoton) * sizeof(float));
+        cfg->exportdetected = (float*)malloc((size_t)S.kp.reclen * std::max(1u, cfg->maxdetphoton) * sizeof(float));
     cfg->detectedcount = 0;
     cfg->his.detected = 0;
     cfg->his.respin = cfg->respin;
-    cfg->his.colcount = hostdetreclen;
+    cfg->his.colcount = S.kp.reclen;
     cfg->energytot = 0.0;
     cfg->energyabs = 0.0;
     cfg->energyesc = 0.0;
     cfg->runtime = 0;
-
-    if (S.totalgates > maxgate && cfg->isnormalized) {
+    if (S.totalgates > S.kp.maxgate && cfg->isnormalized) {
         if (cfg->flog)
             fprintf(cfg->flog, "WARNING: GPU memory can not hold all time gates, disabling normalization to allow multiple runs\n");
         cfg->isnormalized = 0;
     }
-    const int reps = std::abs(cfg->respin);
-    const uint64_t nper = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps;
-    const uint64_t seed = (uint64_t)(uint32_t)cfg->seed;
-    if (cfg->flog && cfg->printnum >= 0)
-        fprintf(cfg->flog, "GPU=%d (%s) np=%.0f grid=%d block=%d chunk=%d maxgate=%d repetition=%d\n", gpuid + 1,
-                gpu ? gpu[gpuid].name : "", (double)cfg->nphoton, S.grid, S.block, k.chunk, maxgate, reps);
+}
 
-    std::vector<float> host_field(cfg->issave2pt ? S.fieldlen : 0);
-    std::vector<float> host_det;
-    mcxg_stats total{};
-    uint64_t run_index = 0;
-    for (int gate0 = 0; gate0 < S.totalgates; gate0 += maxgate) {
-        const float twin0 = cfg->tstart + cfg->tstep * gate0;
-        S.set_window(twin0, twin0 + cfg->tstep * maxgate);
-        S.reset();
-        for (int it = 0; it < reps; it++) {
-            if (S.savedet) CK(cudaMemsetAsync(S.detcount.p, 0, sizeof(unsigned), S.stream));
-            S.run(run_index * nper, nper, seed);
-            run_index++;
-            if (S.savedet) {
-                const unsigned det = S.detected();
-                cfg->his.detected += det;
-                const unsigned keep = std::min(det, cfg->maxdetphoton);
-                if (det > cfg->maxdetphoton && cfg->flog)
-                    fprintf(cfg->flog, "WARNING: the detected photon number is more than what your have specified (%u > %u), please use the -H option to specify a greater number\n",
-                            det, cfg->maxdetphoton);
-                if (keep && cfg->exportdetected) {
-                    cfg->exportdetected = (float*)realloc(cfg->exportdetected,
-                                                          (cfg->detectedcount + keep) * (size_t)hostdetreclen * sizeof(float));
-                    CK(cudaMemcpyAsync(cfg->exportdetected + cfg->detectedcount * hostdetreclen, S.detp.p,
-                                       (size_t)keep * hostdetreclen * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
-                    CK(cudaStreamSynchronize(S.stream));
-                    cfg->detectedcount += keep;
-                }
-            }
-        }
-        mcxg_stats st{};
-        S.read_stats(&st);
-        if (st.error_flags & kErrStepCap)
-            MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
-        total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
-        total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
-        total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;
-        total.n_launch += st.n_launch; total.n_photon += st.n_photon; total.n_detected += st.n_detected;
-        total.n_tile_deposit += st.n_tile_deposit;
-        total.grid = st.grid; total.block = st.block; total.chunk = st.chunk; total.launches += st.launches;
-        total.error_flags |= st.error_flags;
-        cfg->energytot += st.e_launch;
-        cfg->energyesc += st.e_escape + st.e_detect;
-
-        if (cfg->issave2pt) {
-            // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
-            float scale = 1.f;
-            if (cfg->isnormalized && st.e_launch > 0.0) {
-                const double Vvox = (double)cfg->steps.x * cfg->steps.y * cfg->steps.z;
-                if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
-                    double s = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
-                    if (cfg->outputtype == otFluence) s *= cfg->tstep;
-                    scale = (float)s;
-                } else {
-                    scale = (float)(1.0 / cfg->energytot);
-                }
-                cfg->normalizer = scale;
-                cfg->his.normalizer = scale;
-            }
-            S.read_field(host_field.data(), scale, cfg->isnormalized == 2);
-            float* out = cfg->exportfield;
-            for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
-        }
+// Detected photons of the last launch appended to exportdetected (src/mcx_core.cu:3645-3666).
+void append_detected(Config* cfg, Session& S) {
+    if (!S.savedet) return;
+    const unsigned reclen = S.kp.reclen;
+    const unsigned det = S.detected();
+    cfg->his.detected += det;
+    const unsigned keep = std::min(det, cfg->maxdetphoton);
+    if (det > cfg->maxdetphoton && cfg->flog)
+        fprintf(cfg->flog, "WARNING: the detected photon number is more than what your have specified (%u > %u), please use the -H option to specify a greater number\n",
+                det, cfg->maxdetphoton);
+    if (keep && cfg->exportdetected) {
+        cfg->exportdetected = (float*)realloc(cfg->exportdetected, (cfg->detectedcount + keep) * (size_t)reclen * sizeof(float));
+        CK(cudaMemcpyAsync(cfg->exportdetected + cfg->detectedcount * reclen, S.detp.p, (size_t)keep * reclen * sizeof(float),
+                           cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        cfg->detectedcount += keep;
     }
-    cfg->runtime = (unsigned)std::ceil(S.kernel_ms);
-    cfg->energyabs = cfg->energytot - cfg->energyesc;
-    total.kernel_ms = S.kernel_ms;
-    total.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
-    t_stats = total;
+}
 
+// End of one gate window: statistics, energies, normalised field added to exportfield
+// (src/mcx_core.cu:3716-3770, 3823-3925).
+void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg_stats& total) {
+    mcxg_stats st{};
+    S.read_stats(&st);
+    if (st.error_flags & kErrStepCap)
+        MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
+    total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
+    total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
+    total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;
+    total.n_launch += st.n_launch; total.n_photon += st.n_photon; total.n_detected += st.n_detected;
+    total.n_tile_deposit += st.n_tile_deposit;
+    total.grid = st.grid; total.block = st.block; total.chunk = st.chunk; total.launches += st.launches;
+    total.error_flags |= st.error_flags;
+    cfg->energytot += st.e_launch;
+    cfg->energyesc += st.e_escape + st.e_detect;
+
+    if (cfg->issave2pt) {
+        // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
+        float scale = 1.f;
+        if (cfg->isnormalized && st.e_launch > 0.0) {
+            const double Vvox = (double)cfg->steps.x * cfg->steps.y * cfg->steps.z;
+            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+                double sc = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
+                if (cfg->outputtype == otFluence) sc *= cfg->tstep;
+                scale = (float)sc;
+            } else {
+                scale = (float)(1.0 / cfg->energytot);
+            }
+            cfg->normalizer = scale;
+            cfg->his.normalizer = scale;
+        }
+        host_field.resize(S.fieldlen);
+        S.read_field(host_field.data(), scale, cfg->isnormalized == 2);
+        float* out = cfg->exportfield;
+        for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
+    }
+}
+
+// End of a run: runtime, absorbed energy, the log lines and the standalone file output
+// (src/mcx_core.cu:3932-4030).
+void end_outputs(Config* cfg, Session& S, double kernel_ms, int reps) {
+    cfg->runtime = (unsigned)std::ceil(kernel_ms);
+    cfg->energyabs = cfg->energytot - cfg->energyesc;
     if (cfg->flog && cfg->printnum >= 0) {
+        const double np = (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1);
         if (S.savedet) fprintf(cfg->flog, "detected %u photons, total: %lu\n", cfg->his.detected, (unsigned long)cfg->detectedcount);
-        fprintf(cfg->flog, "kernel complete:  \t%.3f ms\n", S.kernel_ms);
+        fprintf(cfg->flog, "kernel complete:  \t%.3f ms\n", kernel_ms);
         fprintf(cfg->flog, "simulated %.0f photons (%.0f) with %d threads (repeat x%d)\nMCX simulation speed: %.2f photon/ms\n",
-                (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1), (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1),
-                S.grid * S.block, reps, (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1) / std::max(1e-3, S.kernel_ms));
+                np, np, S.grid * S.block, reps, np / std::max(1e-3, kernel_ms));
         fprintf(cfg->flog, "total simulated energy: %.2f\tabsorbed: %5.5f%%\n(loss due to initial specular reflection is excluded in the total)\n",
                 cfg->energytot, cfg->energytot > 0 ? (cfg->energytot - cfg->energyesc) / cfg->energytot * 100.0 : 0.0);
         fflush(cfg->flog);
@@ -858,7 +869,170 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
     }
 }
 
+void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
+    const auto t_start = std::chrono::steady_clock::now();
+    const int threadid = omp_get_thread_num ? omp_get_thread_num() : 0;
+    if (threadid >= MCXG_MAX_DEVICE || cfg->deviceid[threadid] == '\0') return;
+    if (threadid > 0) {
+        // one device per call: replicas on further devices are left to the caller
+        if (cfg->flog) fprintf(cfg->flog, "WARNING: the GB300 engine runs on one device per call; thread %d idle\n", threadid);
+        return;
+    }
+    const int gpuid = cfg->deviceid[threadid] - 1;
+    if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
+    check_config(cfg);
+
+    std::memset(&t_stats, 0, sizeof(t_stats));
+    Session S;
+    S.create(cfg, gpuid, fp64_field);
+    {
+        // large runs tune the deposit tile with short pilot launches (cached per configuration)
+        int tile_override;
+        {
+            std::lock_guard<std::mutex> g(g_override_mu);
+            tile_override = g_override.tile;
+        }
+        const char* e = std::getenv("MCXG_TUNE");
+        const bool tune = !(e && std::strcmp(e, "0") == 0);
+        if (tune && tile_override < 0 && cfg->nphoton * (uint64_t)std::abs(cfg->respin) >= 20000000ull)
+            S.autotune(cfg->nphoton);
+    }
+    const int maxgate = S.kp.maxgate;
+    begin_outputs(cfg, S);
+    const int reps = std::abs(cfg->respin);
+    const uint64_t nper = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps;
+    const uint64_t seed = (uint64_t)(uint32_t)cfg->seed;
+    if (cfg->flog && cfg->printnum >= 0)
+        fprintf(cfg->flog, "GPU=%d (%s) np=%.0f grid=%d block=%d chunk=%d maxgate=%d repetition=%d\n", gpuid + 1,
+                gpu ? gpu[gpuid].name : "", (double)cfg->nphoton, S.grid, S.block, S.kp.chunk, maxgate, reps);
+
+    std::vector<float> host_field;
+    mcxg_stats total{};
+    uint64_t run_index = 0;
+    for (int gate0 = 0; gate0 < S.totalgates; gate0 += maxgate) {
+        const float twin0 = cfg->tstart + cfg->tstep * gate0;
+        S.set_window(twin0, twin0 + cfg->tstep * maxgate);
+        S.reset();
+        for (int it = 0; it < reps; it++) {
+            if (S.savedet) CK(cudaMemsetAsync(S.detcount.p, 0, sizeof(unsigned), S.stream));
+            S.run(run_index * nper, nper, seed);
+            run_index++;
+            append_detected(cfg, S);
+        }
+        finish_window(cfg, S, host_field, total);
+    }
+    total.kernel_ms = S.kernel_ms;
+    total.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    t_stats = total;
+    end_outputs(cfg, S, S.kernel_ms, reps);
+}
+
+// Many independent simulations on one device (the batched workload): every Config gets its
+// own session -- volume, media, source and field on the device -- and all transport launches
+// go into one CUDA graph over `nstreams` streams, largest photon budget first.  A launch is a
+// full-device persistent grid drawing on its own photon counter; as the CTAs of one launch run
+// out of photons, the block scheduler fills the freed SMs with CTAs of the launches queued on
+// the other streams, so the tail of one simulation overlaps the next.  Each Config's outputs are
+// those of mcx_run_simulation; `runtime` is the batch's graph time.
+void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms) {
+    if (count <= 0 || !cfgs) MCXG_RAISE(-4, "an empty batch");
+    nstreams = std::max(1, std::min(nstreams, 32));
+    const int gpuid = cfgs[0]->deviceid[0] - 1;
+    if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
+    std::vector<std::unique_ptr<Session>> S(count);
+    for (int i = 0; i < count; i++) {
+        Config* cfg = cfgs[i];
+        check_config(cfg);
+        if (std::abs(cfg->respin) != 1) MCXG_RAISE(-6, "batched simulations run one repetition (respin 1) each");
+        S[i] = std::make_unique<Session>();
+        S[i]->create(cfg, gpuid, false);
+        if (S[i]->totalgates > S[i]->kp.maxgate) MCXG_RAISE(-6, "batched simulations must hold all their time gates on the device");
+        S[i]->apply_tile(kMinTileKB);
+        S[i]->set_window(cfg->tstart, cfg->tstart + cfg->tstep * S[i]->kp.maxgate);
+        if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
+        begin_outputs(cfg, *S[i]);
+    }
+    for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
+
+    std::vector<int> order(count);
+    for (int i = 0; i < count; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cfgs[a]->nphoton > cfgs[b]->nphoton; });
+
+    std::vector<cudaStream_t> st(nstreams, nullptr);
+    std::vector<cudaEvent_t> joins(nstreams, nullptr);
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto e : joins) if (e) cudaEventDestroy(e);
+        for (auto x : st) if (x) cudaStreamDestroy(x);
+        if (fork) cudaEventDestroy(fork);
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+        if (origin) cudaStreamDestroy(origin);
+    };
+    try {
+        CK(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        CK(cudaEventCreate(&t0));
+        CK(cudaEventCreate(&t1));
+        for (int k = 0; k < nstreams; k++) {
+            CK(cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&joins[k], cudaEventDisableTiming));
+        }
+        CK(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
+        CK(cudaEventRecord(fork, origin));
+        for (int k = 0; k < nstreams; k++) CK(cudaStreamWaitEvent(st[k], fork, 0));
+        for (int j = 0; j < count; j++) {
+            Session& s = *S[order[j]];
+            const Config* cfg = cfgs[order[j]];
+            s.enqueue(st[j % nstreams], 0, (uint64_t)cfg->nphoton, (uint64_t)(uint32_t)cfg->seed);
+        }
+        for (int k = 0; k < nstreams; k++) {
+            CK(cudaEventRecord(joins[k], st[k]));
+            CK(cudaStreamWaitEvent(origin, joins[k], 0));
+        }
+        CK(cudaStreamEndCapture(origin, &graph));
+        CK(cudaGraphInstantiate(&exec, graph, 0));
+        CK(cudaEventRecord(t0, origin));
+        CK(cudaGraphLaunch(exec, origin));
+        CK(cudaEventRecord(t1, origin));
+        CK(cudaEventSynchronize(t1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, t0, t1));
+        if (graph_ms) *graph_ms = ms;
+        for (int i = 0; i < count; i++) {
+            std::vector<float> host_field;
+            mcxg_stats total{};
+            append_detected(cfgs[i], *S[i]);
+            finish_window(cfgs[i], *S[i], host_field, total);
+            total.kernel_ms = ms;
+            if (stats) stats[i] = total;
+            end_outputs(cfgs[i], *S[i], ms, 1);
+        }
+    } catch (...) {
+        cudaStreamEndCapture(origin, &graph);      // leaves capture mode if an error came mid-capture
+        cleanup();
+        throw;
+    }
+    cleanup();
+}
+
 }  // namespace
+
+extern "C" int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms) {
+    mcxg_clear_error();
+    try {
+        run_batch(cfgs, count, nstreams, stats, graph_ms);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return e.id ? e.id : -1;
+    }
+}
 
 extern "C" void mcx_run_simulation(Config* cfg, GPUInfo* gpu) {
     mcxg_clear_error();

@@ -98,57 +98,12 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     k.maxdet = cfg->maxdetphoton;
     k.ndet = (int)cfg->detnum;
 
-    float4 p = cfg->srcpos;
-    float3 v = make_float3(cfg->srcdir.x, cfg->srcdir.y, cfg->srcdir.z);
-    float t = 0.f;
-    uint32_t sidx, smed;
-    std::memcpy(&sidx, &cfg->srcparam2.z, 4);
-    std::memcpy(&smed, &cfg->srcparam2.w, 4);
-    int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
-    k.src_ok = 1;
-    if ((smed & kMED_MASK) == 0) {
-        const int id = host_skipvoid(cfg, p, v, t, fd);
-        if (id < 0) {
-            k.src_ok = 0;
-        } else {
-            sidx = (uint32_t)id;
-            smed = cfg->vol[id];
-        }
-    }
-    if (std::fabs(p.w) <= cfg->minenergy) k.src_ok = 0;
-    k.src_p = p;
-    k.src_v = make_float4(v.x, v.y, v.z, 0.f);
-    k.src_t = t;
-    k.src_idx = sidx;
-    k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
-    if (k.src_ok) {
-        k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
-    }
+    fill_source(k, cfg, nullptr);
     k.step_cap = 20000000u;
     k.chunk = 64;
 
-    // shared-memory deposit tile over the entry point, as the session places it: 16 KB, up to
-    // four gates, a cube extending along the launch direction
-    k.tile_on = 0;
-    if (k.save2pt && k.src_ok) {
-        const int elems = 16 * 1024 / (int)sizeof(unsigned long long);
-        int tg = std::min(k.maxgate, 4), edge = 1;
-        while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
-        while (edge < 6 && tg > 1) {
-            tg--;
-            edge = 1;
-            while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
-        }
-        edge = std::min(edge, std::max(k.nx, std::max(k.ny, k.nz)));
-        k.tnx = std::min(edge, k.nx); k.tny = std::min(edge, k.ny); k.tnz = std::min(edge, k.nz);
-        auto place = [](float c, int n, int dim) { return std::max(0, std::min(dim - n, (int)std::floor(c - 0.5f * n))); };
-        k.tx0 = place(k.src_p.x + 0.5f * edge * k.src_v.x, k.tnx, k.nx);
-        k.ty0 = place(k.src_p.y + 0.5f * edge * k.src_v.y, k.tny, k.ny);
-        k.tz0 = place(k.src_p.z + 0.5f * edge * k.src_v.z, k.tnz, k.nz);
-        k.tg0 = 0;
-        k.tng = tg;
-        k.tile_on = 1;
-    }
+    // shared-memory deposit tile over the entry point, as the session places it by default
+    place_tile(k, 16);
 }
 
 #define NCK(call)                                                                \
@@ -160,7 +115,8 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
 void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, float* d_spill, float* d_detp,
                  uint64_t photon_offset, uint64_t nphoton, int gate_group, cudaStream_t stream, mcxg_stats* stats) {
     if (!cfg || !d_labels || !d_field || !d_spill) MCXG_RAISE(-4, "labels, field and spill buffers are required");
-    if (cfg->srctype != 0) MCXG_RAISE(-6, "the GB300 engine supports the pencil source only");
+    if (cfg->srctype == kSrcPattern || cfg->srctype == kSrcPattern3D)
+        MCXG_RAISE(-6, "pattern sources need a device pattern buffer, which the allocation-free entry point does not take");
     if (cfg->medianum < 1 || cfg->medianum > (unsigned)kMaxMedia) MCXG_RAISE(-6, "the GB300 engine supports 1 to 128 media labels");
     if (cfg->detnum > (unsigned)kMaxDetectors)
         MCXG_RAISE(-6, "the allocation-free entry point holds at most 256 detectors in its static scratch");
@@ -198,7 +154,7 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
 
     const int block = 256;
     const size_t smem = transport_smem_bytes(k, block, savedet);
-    const int bps = transport_blocks_per_sm(reflect, savedet, block, smem);
+    const int bps = transport_blocks_per_sm(reflect, savedet, k.srctype != kSrcPencil, block, smem);
     if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
     int sms = 0;
     NCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));

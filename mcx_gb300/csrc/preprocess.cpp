@@ -22,6 +22,7 @@
 #include "../../include/mcx_abi.h"
 #include "../../include/mcx_gb300.h"
 #include "mcxg_common.h"
+#include "transport.cuh"
 
 using namespace mcxg;
 
@@ -179,7 +180,7 @@ void validate(Config* cfg) {
     if (cfg->medianum == 0) MCXG_RAISE(-4, "you must define the 'prop' field in the input structure");
     if (cfg->dim.x == 0 || cfg->dim.y == 0 || cfg->dim.z == 0) MCXG_RAISE(-4, "the 'vol' field in the input structure can not be empty");
     if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media (mediabyte 1, 2 or 4) are supported by the GB300 engine");
-    if (cfg->srctype != 0) MCXG_RAISE(-6, "the GB300 engine supports the pencil source only");
+    check_source(cfg);
 
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) cfg->unitinmm = cfg->steps.x;
     if (cfg->unitinmm != 1.f) {
@@ -219,16 +220,19 @@ void validate(Config* cfg) {
     for (size_t i = 0; i < nvox; i++) maxlabel = std::max(maxlabel, cfg->vol[i] & kMED_MASK);
     if (cfg->medianum <= maxlabel) MCXG_RAISE(-4, "input media optical properties are less than the labels in the volume");
 
-    // launch voxel and medium of the pencil source (src/mcx_utils.c:1737-1760)
+    // launch voxel and medium of point sources (src/mcx_utils.c:1737-1760); the other shapes keep
+    // srcparam2 as their parameters
     uint32_t idx = 0, med = 0;
-    if (!(cfg->srcpos.x < 0.f || cfg->srcpos.y < 0.f || cfg->srcpos.z < 0.f || cfg->srcpos.x >= cfg->dim.x ||
+    if (src_is_point((unsigned char)cfg->srctype) && !(cfg->srcpos.x < 0.f || cfg->srcpos.y < 0.f || cfg->srcpos.z < 0.f || cfg->srcpos.x >= cfg->dim.x ||
           cfg->srcpos.y >= cfg->dim.y || cfg->srcpos.z >= cfg->dim.z)) {
         idx = (uint32_t)((int)std::floor(cfg->srcpos.z) * (cfg->dim.y * cfg->dim.x) + (int)std::floor(cfg->srcpos.y) * cfg->dim.x +
                          (int)std::floor(cfg->srcpos.x));
         med = cfg->vol[idx] & kMED_MASK;
     }
-    std::memcpy(&cfg->srcparam2.z, &idx, 4);
-    std::memcpy(&cfg->srcparam2.w, &med, 4);
+    if (src_is_point((unsigned char)cfg->srctype)) {
+        std::memcpy(&cfg->srcparam2.z, &idx, 4);
+        std::memcpy(&cfg->srcparam2.w, &med, 4);
+    }
 
     if (cfg->issavedet) mcxg_maskdet(cfg);
     for (int i = 0; i < MCXG_MAX_DEVICE; i++)

@@ -17,6 +17,8 @@
 // Semantics that must match the reference step for step are annotated with its file:line.
 
 #include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include "transport.cuh"
 
@@ -36,18 +38,20 @@ __device__ __forceinline__ float rng_next(unsigned long long& a, unsigned long l
     return __uint_as_float(0x3F800000u | (lo >> 9)) - 1.0f;
 }
 
-// One xorshift128+ step giving two floats: the reference's (low 32 bits) and one from the high
-// 32 bits of the same 64-bit output, for the per-photon streams that need not follow MCX's
-// draw-by-draw consumption.
-__device__ __forceinline__ void rng_next2(unsigned long long& a, unsigned long long& b, float& f0, float& f1) {
+// One xorshift128+ step giving three uniforms in [0, 1) with 21-bit resolution, from bits 43-63,
+// 22-42 and 1-21 of the 64-bit output: the random numbers of one scattering event for the
+// per-photon streams, which need not follow MCX's draw-by-draw consumption.
+__device__ __forceinline__ void rng_next3(unsigned long long& a, unsigned long long& b, float& f0, float& f1,
+                                          float& f2) {
     unsigned long long s1 = a;
     const unsigned long long s0 = b;
     a = s0;
     s1 ^= s1 << 23;
     b = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
     const unsigned long long r = b + s0;
-    f0 = __uint_as_float(0x3F800000u | ((unsigned)r >> 9)) - 1.0f;
-    f1 = __uint_as_float(0x3F800000u | ((unsigned)(r >> 32) >> 9)) - 1.0f;
+    f0 = __uint_as_float(0x3F800000u | (((unsigned)(r >> 32) >> 9) & 0x7FFFFCu)) - 1.0f;
+    f1 = __uint_as_float(0x3F800000u | ((unsigned)(r >> 20) & 0x7FFFFCu)) - 1.0f;
+    f2 = __uint_as_float(0x3F800000u | (((unsigned)r << 1) & 0x7FFFFCu)) - 1.0f;
 }
 
 __device__ __forceinline__ unsigned long long splitmix64(unsigned long long& x) {
@@ -120,6 +124,310 @@ __device__ int find_detector(const KParams& P, float px, float py, float pz) {
     return 0;
 }
 
+// ---- sources other than the pencil beam -------------------------------------------------------
+// A launched photon: position, weight, direction, time (grid units), voxel and its label byte.
+struct Launch {
+    float px, py, pz, w, vx, vy, vz, t;
+    unsigned idx, label;
+};
+
+// src/mcx_core.cu:552-570 (reflectcoeff): unpolarised Fresnel reflectance at a face normal to
+// `axis` going from index n1 to n2.
+__device__ __forceinline__ float reflect_coeff(float vx, float vy, float vz, float n1, float n2, int axis) {
+    const float Icos = fabsf(axis == 0 ? vx : (axis == 1 ? vy : vz));
+    const float a = n1 * n1, b = n2 * n2;
+    float c = 1.f - __fdividef(a, b) * (1.f - Icos * Icos);
+    if (c <= 0.f) return 1.f;
+    float Re = a * Icos * Icos + b * c;
+    c = sqrtf(c);
+    const float Im = 2.f * n1 * n2 * Icos * c;
+    float R = __fdividef(Re - Im, Re + Im);
+    Re = b * Icos * Icos + a * c * c;
+    return (R + __fdividef(Re - Im, Re + Im)) * 0.5f;
+}
+
+__device__ __forceinline__ unsigned label_at(const KParams& P, int x, int y, int z) {
+    return __ldg(P.labels + ((unsigned)z * P.dimxy + (unsigned)y * (unsigned)P.nx + (unsigned)x));
+}
+
+__device__ __forceinline__ bool in_grid(const KParams& P, int x, int y, int z) {
+    return (unsigned)x < (unsigned)P.nx && (unsigned)y < (unsigned)P.ny && (unsigned)z < (unsigned)P.nz;
+}
+
+// src/mcx_core.cu:866-956 (skipvoid): march a photon launched outside the volume or in a 0 voxel
+// in unit steps until it is inside a non-zero voxel, back up one step and find the exact entry
+// face with voxel-to-voxel steps; optional specular loss and refraction there.  Returns the
+// entry voxel, or -1 when the photon misses the volume.
+__device__ int skip_void(const KParams& P, Launch& L) {
+    const float rvx = __fdividef(1.f, L.vx), rvy = __fdividef(1.f, L.vy), rvz = __fdividef(1.f, L.vz);
+    int fx = (int)floorf(L.px), fy = (int)floorf(L.py), fz = (int)floorf(L.pz);
+    int count = 1;
+    while (true) {
+        if (in_grid(P, fx, fy, fz) && (label_at(P, fx, fy, fz) & kLabelMask)) {
+            L.px -= L.vx; L.py -= L.vy; L.pz -= L.vz;
+            fx = (int)floorf(L.px); fy = (int)floorf(L.py); fz = (int)floorf(L.pz);
+            L.t -= 1.f;
+            int axis = -1;
+            for (int k = 0; k <= 4 && !(in_grid(P, fx, fy, fz) && (label_at(P, fx, fy, fz) & kLabelMask)); k++) {
+                const float hx = fabsf((fx + (L.vx > 0.f ? 1.f : 0.f) - L.px) * rvx);
+                const float hy = fabsf((fy + (L.vy > 0.f ? 1.f : 0.f) - L.py) * rvy);
+                const float hz = fabsf((fz + (L.vz > 0.f ? 1.f : 0.f) - L.pz) * rvz);
+                const float d = fminf(fminf(hx, hy), hz);
+                axis = (d == hx) ? 0 : ((d == hy) ? 1 : 2);
+                L.t += d;
+                L.px += d * L.vx; L.py += d * L.vy; L.pz += d * L.vz;
+                if (axis == 0) fx += (L.vx > 0.f) ? 1 : -1;
+                else if (axis == 1) fy += (L.vy > 0.f) ? 1 : -1;
+                else fz += (L.vz > 0.f) ? 1 : -1;
+            }
+            if (!in_grid(P, fx, fy, fz)) return -1;
+            if (!P.voidtime) L.t = 0.f;
+            const unsigned lab = label_at(P, fx, fy, fz);
+            const float n2 = P.prop[lab & kLabelMask].w, n0 = P.prop[0].w;
+            if (P.isspecular && axis >= 0 && n2 != n0) {
+                L.w *= 1.f - reflect_coeff(L.vx, L.vy, L.vz, n0, n2, axis);
+                if (L.w > kEPS) transmit(L.vx, L.vy, L.vz, n0, n2, axis);
+            }
+            return (int)((unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx);
+        }
+        if ((L.px < 0.f && L.vx <= 0.f) || (L.px >= P.d_fnx && L.vx >= 0.f) || (L.py < 0.f && L.vy <= 0.f) ||
+            (L.py >= P.d_fny && L.vy >= 0.f) || (L.pz < 0.f && L.vz <= 0.f) || (L.pz >= P.d_fnz && L.vz >= 0.f))
+            return -1;
+        L.px += L.vx; L.py += L.vy; L.pz += L.vz;
+        fx = (int)floorf(L.px); fy = (int)floorf(L.py); fz = (int)floorf(L.pz);
+        L.t += 1.f;
+        if (count++ > (int)P.maxvoidstep) return -1;
+    }
+}
+
+// Position shift by r along the azimuth (cphi, sphi) of the plane normal to v (the disk and
+// Gaussian branches of src/mcx_core.cu:1372-1420).
+__device__ __forceinline__ void offset_normal(Launch& L, float r, float sphi, float cphi) {
+    if (L.vz > -1.f + kEPS && L.vz < 1.f - kEPS) {
+        const float t0 = 1.f - L.vz * L.vz;
+        const float t1 = r * rsqrtf(t0);
+        L.px += t1 * (L.vx * L.vz * cphi - L.vy * sphi);
+        L.py += t1 * (L.vy * L.vz * cphi + L.vx * sphi);
+        L.pz -= t1 * t0 * cphi;
+    } else {
+        L.px += r * cphi;
+        L.py += r * sphi;
+    }
+}
+
+// One launch of a non-pencil source, drawing from the photon's stream in MCX's order
+// (launchnewphoton, src/mcx_core.cu:1236-1672).  Retries a photon that misses the volume up to
+// maxvoidstep times; false when every attempt missed.
+__device__ __forceinline__ bool launch_source(const KParams& P, unsigned long long& r0, unsigned long long& r1, Launch& L) {
+    const float4 p1 = P.src_param1, p2 = P.src_param2;
+    constexpr float kJustBelowOne = 0.9998f;                      // src/mcx_const.h:50
+    for (int attempt = 1; attempt <= (int)P.maxvoidstep; attempt++) {
+        L.px = P.src_p.x; L.py = P.src_p.y; L.pz = P.src_p.z; L.w = P.src_p.w;
+        L.vx = P.src_v.x; L.vy = P.src_v.y; L.vz = P.src_v.z;
+        L.t = 0.f;
+        float ox = P.src_p.x, oy = P.src_p.y, oz = P.src_p.z;     // focus origin
+        bool canfocus = true, located = false;
+        switch (P.srctype) {
+        case kSrcPlanar: case kSrcPattern: case kSrcPattern3D: case kSrcFourier: case kSrcPencilArray: {
+            const float rx = rng_next(r0, r1), ry = rng_next(r0, r1);
+            if (P.srctype == kSrcPattern3D) {
+                const float rz = rng_next(r0, r1);
+                L.px += rx * p1.x; L.py += ry * p1.y; L.pz += rz * p1.z;
+                const int nx = (int)p1.x, ny = (int)p1.y;
+                L.w = P.src_p.w * __ldg(P.srcpattern + (int)(rz * kJustBelowOne * p1.z) * ny * nx +
+                                        (int)(ry * kJustBelowOne * p1.y) * nx + (int)(rx * kJustBelowOne * p1.x));
+            } else {
+                L.px += rx * p1.x + ry * p2.x; L.py += rx * p1.y + ry * p2.y; L.pz += rx * p1.z + ry * p2.z;
+                if (P.srctype == kSrcPattern) {
+                    L.w = P.src_p.w * __ldg(P.srcpattern + (int)(ry * kJustBelowOne * p2.w) * (int)p1.w +
+                                            (int)(rx * kJustBelowOne * p1.w));
+                } else if (P.srctype == kSrcFourier) {
+                    L.w = P.src_p.w * (cosf((floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w)) * kTWO_PI) *
+                                           (1.f - p2.w + floorf(p2.w)) + 1.f) * 0.5f;
+                } else if (P.srctype == kSrcPencilArray) {
+                    const float ix = floorf(rx * p1.w) / (p1.w - 1.f), iy = floorf(ry * p2.w) / (p2.w - 1.f);
+                    L.px = P.src_p.x + ix * p1.x + iy * p2.x;
+                    L.py = P.src_p.y + ix * p1.y + iy * p2.y;
+                    L.pz = P.src_p.z + ix * p1.z + iy * p2.z;
+                }
+            }
+            ox += (p1.x + p2.x) * 0.5f; oy += (p1.y + p2.y) * 0.5f; oz += (p1.z + p2.z) * 0.5f;
+            break;
+        }
+        case kSrcFourierX: case kSrcFourierX2D: {
+            const float rx = rng_next(r0, r1), ry = rng_next(r0, r1);
+            const float s = p1.w * rsqrtf(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z);
+            const float v2x = s * (L.vy * p1.z - L.vz * p1.y), v2y = s * (L.vz * p1.x - L.vx * p1.z),
+                        v2z = s * (L.vx * p1.y - L.vy * p1.x);
+            L.px += rx * p1.x + ry * v2x; L.py += rx * p1.y + ry * v2y; L.pz += rx * p1.z + ry * v2z;
+            if (P.srctype == kSrcFourierX2D)
+                L.w = P.src_p.w * (sinf((p2.x * rx + p2.z) * kTWO_PI) * sinf((p2.y * ry + p2.w) * kTWO_PI) + 1.f) * 0.5f;
+            else
+                L.w = P.src_p.w * (cosf((p2.x * rx + p2.y * ry + p2.z) * kTWO_PI) * (1.f - p2.w) + 1.f) * 0.5f;
+            ox += (p1.x + v2x) * 0.5f; oy += (p1.y + v2y) * 0.5f; oz += (p1.z + v2z) * 0.5f;
+            break;
+        }
+        case kSrcDisk: case kSrcRing: case kSrcGaussian: {
+            float phi;
+            if (P.srctype == kSrcRing && (p1.z > 0.f || p1.w > 0.f))
+                phi = fabsf(p1.z - p1.w) * rng_next(r0, r1) + fminf(p1.z, p1.w);
+            else
+                phi = kTWO_PI * rng_next(r0, r1);
+            float sphi, cphi;
+            sincosf(phi, &sphi, &cphi);
+            float r;
+            if (P.srctype != kSrcGaussian) {
+                r = sqrtf(rng_next(r0, r1) * fabsf(p1.x * p1.x - p1.y * p1.y) + p1.y * p1.y);
+            } else if (fabsf(P.src_focal) < 1e-5f || fabsf(p1.y) < 1e-5f) {
+                r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS)) * p1.x;
+            } else {
+                const float zr = p1.x * p1.x * 3.14159265358979f / p1.y;        // Rayleigh range
+                r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS) * (1.f + P.src_focal * P.src_focal / (zr * zr))) * p1.x;
+            }
+            offset_normal(L, r, sphi, cphi);
+            break;
+        }
+        case kSrcCone: case kSrcIsotropic: case kSrcArcsine: {
+            float sphi, cphi, st, ct, ang = kTWO_PI * rng_next(r0, r1);
+            sincosf(ang, &sphi, &cphi);
+            if (P.srctype == kSrcCone) {
+                const float c = cosf(p1.x);
+                ang = (p1.y > 0.f) ? rng_next(r0, r1) * p1.x : acosf(rng_next(r0, r1) * (1.f - c) + c);
+            } else if (P.srctype == kSrcIsotropic) {
+                ang = acosf(2.f * rng_next(r0, r1) - 1.f);
+            } else {
+                ang = 3.14159265358979f * rng_next(r0, r1);
+            }
+            sincosf(ang, &st, &ct);
+            rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
+            canfocus = false;
+            located = true;
+            break;
+        }
+        case kSrcZGaussian: {
+            float sphi, cphi, st, ct, ang = kTWO_PI * rng_next(r0, r1);
+            sincosf(ang, &sphi, &cphi);
+            ang = sqrtf(2.f * -logf(rng_next(r0, r1) + kEPS));
+            ang *= (1.f - 2.f * rng_next(r0, r1)) * p1.x;
+            sincosf(ang, &st, &ct);
+            rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
+            canfocus = false;
+            located = true;
+            break;
+        }
+        case kSrcHyperboloid: {
+            float sphi, cphi;
+            sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+            const float r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS)) * p1.x;
+            const float a = __fdividef(-p1.y, p1.z), b = rsqrtf(r * r + p1.z * p1.z);
+            // displacement from the source and direction, in the beam's frame (beam along +z)
+            float qx = r * (cphi - a * sphi), qy = r * (sphi + a * cphi), qz = 0.f;
+            const float dx = -r * sphi * b, dy = r * cphi * b, dz = p1.z * b;
+            if (L.vz > -1.f + kEPS && L.vz < 1.f - kEPS) {
+                float t = 1.f - L.vz * L.vz;
+                const float st = sqrtf(t);
+                t = rsqrtf(t);
+                const float cp = L.vx * t, sp = L.vy * t, vz = L.vz;
+                const float ax = qx * cp * vz - qy * sp, ay = qx * sp * vz + qy * cp, az = -qx * st;
+                qx = ax; qy = ay; qz = az;
+                L.vx = dx * cp * vz - dy * sp + dz * cp * st;
+                L.vy = dx * sp * vz + dy * cp + dz * sp * st;
+                L.vz = -dx * st + dz * vz;
+            } else {
+                L.vx = dx; L.vy = dy; L.vz = (L.vz > 0.f) ? dz : -dz;
+            }
+            L.px += qx; L.py += qy; L.pz += qz;
+            canfocus = false;
+            break;
+        }
+        case kSrcLine: case kSrcSlit: {
+            float r = rng_next(r0, r1);
+            L.px += r * p1.x; L.py += r * p1.y; L.pz += r * p1.z;
+            if (P.srctype == kSrcLine) {
+                float sphi, cphi;
+                r = rsqrtf(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z);
+                const float ax = p1.x * r, ay = p1.y * r, az = p1.z * r;
+                if (p2.x > 0.f) {
+                    // direction: srcdir made normal to the line, turned about it by up to p2.x
+                    r = L.vx * ax + L.vy * ay + L.vz * az;
+                    L.vx -= r * ax; L.vy -= r * ay; L.vz -= r * az;
+                    r = rsqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+                    L.vx *= r; L.vy *= r; L.vz *= r;
+                    sincosf(p2.x * (2.f * rng_next(r0, r1) - 1.f), &sphi, &cphi);
+                    const float cx = ay * L.vz - az * L.vy, cy = az * L.vx - ax * L.vz, cz = ax * L.vy - ay * L.vx;
+                    L.vx = L.vx * cphi + cx * sphi; L.vy = L.vy * cphi + cy * sphi; L.vz = L.vz * cphi + cz * sphi;
+                } else {
+                    L.vx = ax; L.vy = ay; L.vz = az;
+                    sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+                    rotate(L.vx, L.vy, L.vz, 1.f, 0.f, sphi, cphi);
+                }
+            } else if (p2.x > 0.f || p2.y > 0.f) {
+                float sphi, cphi;
+                sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+                r = sqrtf(2.f * -logf(rng_next(r0, r1) + kEPS));
+                cphi *= p2.x * r;
+                sphi *= p2.y * r * rsqrtf(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z);
+                const float nx = p1.y * L.vz - p1.z * L.vy, ny = p1.z * L.vx - p1.x * L.vz, nz = p1.x * L.vy - p1.y * L.vx;
+                cphi *= rsqrtf(nx * nx + ny * ny + nz * nz);
+                L.vx += cphi * nx + sphi * p1.x;
+                L.vy += cphi * ny + sphi * p1.y;
+                L.vz += cphi * nz + sphi * p1.z;
+                r = rsqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+                L.vx *= r; L.vy *= r; L.vz *= r;
+            }
+            ox = P.src_p.x + p1.x * 0.5f; oy = P.src_p.y + p1.y * 0.5f; oz = P.src_p.z + p1.z * 0.5f;
+            canfocus = (P.srctype == kSrcSlit);
+            break;
+        }
+        default:
+            return false;
+        }
+        if (fabsf(L.w) <= P.minenergy) continue;
+        if (canfocus) {
+            const float f = P.src_focal;
+            float sphi, cphi, st, ct;
+            if (isnan(f)) {                                             // isotropic
+                sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+                sincosf(acosf(2.f * rng_next(r0, r1) - 1.f), &st, &ct);
+                rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
+            } else if (f < 0.f && isinf(f)) {                           // Lambertian
+                sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+                st = sqrtf(rng_next(r0, r1));
+                ct = sqrtf(1.f - st * st);
+                rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
+            } else if (f != 0.f) {                                      // converging / diverging
+                const float sg = (f > 0.f) ? 1.f : -1.f;
+                ox += f * L.vx; oy += f * L.vy; oz += f * L.vz;
+                L.vx = sg * (ox - L.px); L.vy = sg * (oy - L.py); L.vz = sg * (oz - L.pz);
+                const float k = rsqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+                L.vx *= k; L.vy *= k; L.vz *= k;
+            }
+        }
+        // launch voxel: the host's for point sources, else where the photon stands
+        unsigned lab = 0u;
+        if (located) {
+            L.idx = P.src_idx;
+            lab = P.src_label;
+        } else {
+            const int fx = (int)floorf(L.px), fy = (int)floorf(L.py), fz = (int)floorf(L.pz);
+            if (L.px >= 0.f && L.py >= 0.f && L.pz >= 0.f && L.px < P.d_fnx && L.py < P.d_fny && L.pz < P.d_fnz) {
+                L.idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
+                lab = __ldg(P.labels + L.idx);
+            }
+        }
+        if ((lab & kLabelMask) == 0u) {
+            const int id = skip_void(P, L);
+            if (id < 0) continue;
+            L.idx = (unsigned)id;
+            lab = __ldg(P.labels + L.idx);
+        }
+        if ((lab & kLabelMask) == 0u || fabsf(L.w) <= P.minenergy) continue;
+        L.label = lab;
+        return true;
+    }
+    return false;
+}
+
 // Accumulation into the global field.  FP64 in the reference-accuracy twin; in FP32, a large
 // contribution (a spilled or flushed shared-memory tile value) goes through the two-copy
 // scheme of src/mcx_core.cu:2246-2253 -- whenever the primary copy holds more than kMaxAccum
@@ -148,9 +456,14 @@ struct Smem {
     float4* prop;                 // medianum x (mua, mus, g, n)
     unsigned long long* pool;     // per warp: next, end of its photon-index pool
     int* drained;                 // per warp: the global photon counter is exhausted
+    unsigned* wcount;             // per warp: launches tried, deposits into the tile, photons run
+    float* wlaunch;               // per thread: launch weight of its photon
+    unsigned* left;               // per thread, MCX stream mode: photons still to run from its stream
+    unsigned* step0;              // per thread: the lane's step count when its photon started
+    int* nscat0;                  // per thread, detector runs: nscat at the last change of medium
     float* tally;                 // kNumEnergy x blockDim, FP32 per-thread partial sums
     float* ppath;                 // partialdata x blockDim (detector runs)
-    unsigned long long* tile;     // deposit tile, fixed point (weight x d_tile_scale)
+    unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
 template <bool SAVEDET>
@@ -160,15 +473,35 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     s.prop = reinterpret_cast<float4*>(raw);
     s.pool = reinterpret_cast<unsigned long long*>(s.prop + P.medianum);
     s.drained = reinterpret_cast<int*>(s.pool + 2 * warps);
-    s.tally = reinterpret_cast<float*>(s.drained + warps);
+    s.wcount = reinterpret_cast<unsigned*>(s.drained + warps);
+    s.left = s.wcount + 3 * warps;
+    s.step0 = s.left + blockDim.x;
+    s.nscat0 = reinterpret_cast<int*>(s.step0 + blockDim.x);
+    s.wlaunch = reinterpret_cast<float*>(s.nscat0 + blockDim.x);
+    s.tally = s.wlaunch + blockDim.x;
     s.ppath = s.tally + kNumEnergy * blockDim.x;
     float* end = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
-    s.tile = reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(end) + 7u) & ~uintptr_t(7));
+    s.tile = reinterpret_cast<unsigned*>(end);
     return s;
 }
 
+// Per-medium partial path (flag P) and scattering count (flag S) of a detector run
+// (src/mcx_core.cu:1970-1981, 2152-2165): the reference adds every step's length and every
+// scattering event to the slot of the current medium; here they are summed in registers while
+// the medium stays the same and added to the slot of medium `m` when it changes.
+__device__ __forceinline__ void flush_segment(const KParams& P, const Smem& S, int tid, int B, int m, float& segp,
+                                              int nscat) {
+    if (m > 0) {
+        const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
+        if (fS) S.ppath[(unsigned)(m - 1) * B + tid] += (float)(nscat - S.nscat0[tid]);
+        if (fP) S.ppath[((unsigned)P.nmedia_det * fS + (unsigned)(m - 1)) * B + tid] += segp;
+    }
+    S.nscat0[tid] = nscat;
+    segp = 0.f;
+}
+
 // MINB: CTAs of 256 threads the register budget is sized for (4 -> 64 registers, 3 -> 85).
-template <bool REFLECT, bool SAVEDET, int MINB>
+template <bool REFLECT, bool SAVEDET, int MINB, bool AREA>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Smem S = carve<SAVEDET>(P, smem_raw);
@@ -180,11 +513,14 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     for (int i = tid; i < P.medianum; i += B) S.prop[i] = P.prop[i];
     for (int k = 0; k < kNumEnergy; k++) S.tally[k * B + tid] = 0.f;
     const int tile_elems = P.tile_on ? P.tnx * P.tny * P.tnz * P.tng : 0;
-    for (int i = tid; i < tile_elems; i += B) S.tile[i] = 0ull;
+    for (int i = tid; i < tile_elems; i += B) S.tile[i] = 0u;
     if (lane == 0) {
         S.pool[2 * warp] = 0ull;
         S.pool[2 * warp + 1] = 0ull;
         S.drained[warp] = (P.src_ok == 0);
+        S.wcount[3 * warp] = 0u;
+        S.wcount[3 * warp + 1] = 0u;
+        S.wcount[3 * warp + 2] = 0u;
     }
     __syncthreads();
 
@@ -213,19 +549,24 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     float px = 0.f, py = 0.f, pz = 0.f, w = 0.f;
     float vx = 0.f, vy = 0.f, vz = 1.f, rvx = 0.f, rvy = 0.f, rvz = 0.f;
     float pscat = 0.f, t = 0.f, pathlen = 0.f, w0 = 0.f;
-    float eabs = 0.f, eoth = 0.f;       // absorbed weight recorded / not recorded in the field
+    float eabs = 0.f;                   // absorbed weight recorded in the field (the rest goes to the
+                                        // kEAbsOther tally as it happens)
     float fx = 0.f, fy = 0.f, fz = 0.f; // integer voxel coordinates, as floats
+    // detector runs: path length in the current medium since the last change of medium (the
+    // scattering count since then is nscat minus its value then, kept in shared memory)
+    float segp = 0.f;
     int nscat = -1;
-    // det: detector bit of the current voxel.  carry: the reference's `isdet` as it stands at the
-    // end of a step -- the new voxel's bit (or the boundary code outside), which after a
-    // reflection still describes the voxel bounced off; it feeds the next step's mediaidold.
-    unsigned idx = 0u, det = 0u, carry = 0u, psteps = 0u;
+    // det: the current voxel has the detector bit.  carry: the detector bit of the reference's
+    // `isdet` as it stands at the end of a step -- the new voxel's (clear outside, where isdet
+    // holds a boundary code), which after a reflection still describes the voxel bounced off;
+    // it feeds the next step's mediaidold.
+    unsigned idx = 0u;
+    bool det = false, carry = false;
     int med = 0;
     float4 pr = make_float4(0.f, 0.f, 0.f, 1.f);
     unsigned long long r0 = 0ull, r1 = 0ull;
-    unsigned c_step = 0u, c_scat = 0u, c_dep = 0u, c_tile = 0u, c_photon = 0u;
-
-    unsigned left = 0u;   // MCX stream mode: photons still to run from this lane's stream
+    unsigned c_step = 0u, c_scat = 0u, c_dep = 0u;
+    S.left[tid] = 0u;
 
     while (true) {
         // ---- relaunch lanes that have no photon (warp-uniform control flow) ------------------
@@ -233,9 +574,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         if (need) {
             bool start = false;
             // MCX stream mode: a stream with photons left continues with its RNG state
-            if (!alive && left > 0u) {
-                left--;
-                start = true;
+            if (!alive && P.seed_mode == 1) {
+                const unsigned left = S.left[tid];
+                if (left > 0u) {
+                    S.left[tid] = left - 1u;
+                    start = true;
+                }
             }
             const unsigned want = __ballot_sync(kFull, !alive && !start);
             if (want && !S.drained[warp]) {
@@ -271,7 +615,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                             const uint4 sw = __ldg(reinterpret_cast<const uint4*>(P.mcx_words) + mine);
                             r0 = ((unsigned long long)sw.x << 32) | sw.y;
                             r1 = ((unsigned long long)sw.z << 32) | sw.w;
-                            left = cnt - 1u;
+                            S.left[tid] = cnt - 1u;
                             start = true;
                         }
                     } else {
@@ -280,28 +624,52 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     }
                 }
             }
-            if (start) {
+            bool entered = false;
+            if (start && P.srctype == kSrcPencil) {
                 // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
                 // skipping and specular loss of skipvoid() are folded into src_* by the host)
                 px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
                 vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
-                rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                 t = P.src_t * inv_c0;
                 idx = P.src_idx;
                 med = (int)(P.src_label & kLabelMask);
-                det = (P.src_label & kLabelDet) ? kDET_MASK : 0u;
-                carry = det;
+                det = (P.src_label & kLabelDet) != 0u;
                 fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
+                entered = true;
+            } else if (AREA && start) {
+                Launch L;
+                entered = launch_source(P, r0, r1, L);
+                if (entered) {
+                    px = L.px; py = L.py; pz = L.pz; w = L.w;
+                    vx = L.vx; vy = L.vy; vz = L.vz;
+                    t = L.t;
+                    idx = L.idx;
+                    med = (int)(L.label & kLabelMask);
+                    det = (L.label & kLabelDet) != 0u;
+                    fx = floorf(px); fy = floorf(py); fz = floorf(pz);
+                }
+            }
+            if (entered) {
+                rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                carry = det;
+                S.wlaunch[tid] = w;
                 pscat = 0.f; pathlen = 0.f; nscat = -1;
-                w0 = w; eabs = 0.f; eoth = 0.f; psteps = 0u;
+                segp = 0.f;
+                if (SAVEDET) S.nscat0[tid] = 0;
+                w0 = w; eabs = 0.f;
+                S.step0[tid] = c_step;
                 pr = S.prop[med];
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
                 alive = true;
             }
-            __syncwarp();
+            const unsigned attempted = __ballot_sync(kFull, start), ran = __ballot_sync(kFull, entered);
+            if (lane == 0) {
+                S.wcount[3 * warp] += __popc(attempted);
+                S.wcount[3 * warp + 2] += __popc(ran);
+            }
             need = __ballot_sync(kFull, !alive);
-            if (need == kFull) break;      // no photon left for any lane of this warp
+            if (need == kFull && attempted == 0u) break;   // no photon left for any lane of this warp
         }
         if (!alive) continue;
 
@@ -312,22 +680,19 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
 
         if (pscat <= 0.f) {
             // random numbers of this scattering event: MCX's order (scattering length, azimuth,
-            // zenith), one generator step each in MCX seeding mode, two steps for all three with
+            // zenith), one generator step each in MCX seeding mode, one step for all three with
             // per-photon streams
             float u_len, u_phi, u_th;
             if (P.seed_mode == 1) {
                 u_len = rng_next(r0, r1);
             } else {
-                rng_next2(r0, r1, u_len, u_phi);
+                rng_next3(r0, r1, u_len, u_phi, u_th);
             }
             pscat = -__logf(u_len + kEPS);                               // src/mcx_rand_xorshift128p.cu:122
             if (nscat >= 0) {                                           // not the launch flight
                 if (P.seed_mode == 1) {
                     u_phi = rng_next(r0, r1);
                     u_th = rng_next(r0, r1);
-                } else {
-                    float spare;
-                    rng_next2(r0, r1, u_th, spare);
                 }
                 float sphi, cphi;
                 __sincosf(kTWO_PI * u_phi, &sphi, &cphi);               // src/mcx_core.cu:1930-1933
@@ -343,11 +708,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     ct = 2.f * u_th - 1.f;                              // isotropic, 1961-1963
                 }
                 const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
-                if (SAVEDET && med > 0) {                               // 1970-1993
-                    const unsigned M = (unsigned)P.nmedia_det;
+                if (SAVEDET && med > 0 && ((P.savedetflag >> 3) & 1u)) {   // momentum transfer, 1970-1993
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
-                    if (fS) S.ppath[(unsigned)(med - 1) * B + tid] += 1.f;
-                    if ((P.savedetflag >> 3) & 1u) S.ppath[(M * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
+                    S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
                 }
                 rotate(vx, vy, vz, st, ct, sphi, cphi);
                 nscat++;
@@ -382,16 +745,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         pscat -= slen;
         t = fmaf(len, pr.w, t);                                         // t += len*n/c0, in grid units
         pathlen += len;
-        if (SAVEDET && med > 0 && ((P.savedetflag >> 2) & 1u)) {
-            const unsigned fS = (P.savedetflag >> 1) & 1u;
-            S.ppath[((unsigned)P.nmedia_det * fS + (unsigned)(med - 1)) * B + tid] += len;
-        }
-        if (++psteps >= P.step_cap) {
+        // step cap, checked every 1024 steps of the lane against its step count at launch
+        if ((c_step & 1023u) == 0u && c_step - S.step0[tid] >= P.step_cap) {
             atomicOr(P.errflag, kErrStepCap);
             kill = true;
         }
 
-        const unsigned detold = carry;   // mediaidold's detector bit (src/mcx_core.cu:2167)
+        const unsigned detold = carry ? kDET_MASK : 0u;   // mediaidold's detector bit (src/mcx_core.cu:2167)
         const int medold = med;
         bool inside = true;
         int bcf = BC_UNKNOWN;
@@ -412,12 +772,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 idx = (sg > 0.f) ? idx + stride : idx - stride;
                 const unsigned lab = __ldg(P.labels + idx);
                 med = (int)(lab & kLabelMask);
-                det = (lab & kLabelDet) ? kDET_MASK : 0u;
+                det = (lab & kLabelDet) != 0u;
             } else {
                 med = 0;
                 idx = (c < 0.f) ? kOUT_MIN : kOUT_MAX;
                 bcf = P.bc[(idx == kOUT_MAX) * 3 + axis];
-                det = (unsigned)bcf;
+                det = false;                // a boundary code, never the detector bit
             }
             carry = det;
 
@@ -432,24 +792,31 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     rec = true;
                     c_dep++;
                     const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
-                    if (P.tile_on && ox >= tx0 && ox < tx1 && oy >= ty0 && oy < ty1 && oz >= tz0 && oz < tz1 &&
-                        (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
+                    if (P.tile_on && weight > 0.f && ox >= tx0 && ox < tx1 && oy >= ty0 && oy < ty1 && oz >= tz0 &&
+                        oz < tz1 && (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
                         const int ti = (((tshift - P.tg0) * P.tnz + (int)(oz - tz0)) * P.tny + (int)(oy - ty0)) * P.tnx +
                                        (int)(ox - tx0);
-                        // exact 64-bit fixed-point sum: millions of equal first-flight deposits
-                        // near the source carry no rounding bias, and the add returns nothing
-                        // weight * scale < 2^23, so adding 2^23 leaves its rounded integer value in the
-                        // low mantissa bits (FP32 pipes only)
+                        // exact fixed-point sum: millions of equal first-flight deposits near the
+                        // source carry no rounding bias.  0 <= weight * scale < 2^23, so adding 2^23
+                        // leaves its rounded integer value in the low mantissa bits (FP32 pipes only).
+                        // The add whose result crosses kTileFlushUnits moves that many units to the
+                        // global field; the slot never exceeds 2^31 + 256 * 2^23 < 2^32.
                         const unsigned q = __float_as_uint(fmaf(weight, P.d_tile_scale, 8388608.f)) - 0x4B000000u;
-                        atomicAdd(S.tile + ti, (unsigned long long)q);
-                        c_tile++;
+                        const unsigned old = atomicAdd(S.tile + ti, q);
+                        if (old < kTileFlushUnits && old + q >= kTileFlushUnits) {
+                            atomicSub(S.tile + ti, kTileFlushUnits);
+                            field_add_large(P, addr, P.d_tile_flush);
+                        }
+                        atomicAdd(S.wcount + 3 * warp + 1, 1u);
                     } else {
                         field_add_small(P, addr, weight);
                     }
                 }
             }
-            if (rec) eabs += w0 - w; else eoth += w0 - w;
+            if (rec) eabs += w0 - w;
+            else S.tally[kEAbsOther * B + tid] += w0 - w;
             w0 = w;
+            segp += pathlen;
             pathlen = 0.f;
 
             // leaving into a 0 voxel or the outside without reflection (2307-2354)
@@ -469,8 +836,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
                 const unsigned lab = __ldg(P.labels + idx);
                 med = (int)(lab & kLabelMask);
-                det = (lab & kLabelDet) ? kDET_MASK : 0u;
+                det = (lab & kLabelDet) != 0u;
                 carry = det;
+                if (SAVEDET && med != medold) flush_segment(P, S, tid, B, medold, segp, nscat);
                 continue;
             }
         }
@@ -533,7 +901,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         idx = idxold;
                         const unsigned lab = __ldg(P.labels + idx);
                         med = (int)(lab & kLabelMask);
-                        det = (lab & kLabelDet) ? kDET_MASK : 0u;   // carry keeps the bounced-off value
+                        det = (lab & kLabelDet) != 0u;   // carry keeps the bounced-off value
                         pr = S.prop[med];
                     }
                 } else {
@@ -542,6 +910,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             }
         }
 
+        if (SAVEDET && (kill || med != medold)) {
+            segp += pathlen;        // the last voxel's path when the photon ends inside it, else 0
+            flush_segment(P, S, tid, B, medold, segp, nscat);
+        }
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
             bool detected = false;
@@ -557,15 +929,14 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         for (unsigned i = 0; i < P.partialdata; i++) rec[k++] = S.ppath[i * B + tid];
                         if (P.savedetflag & 0x10u) { rec[k++] = px; rec[k++] = py; rec[k++] = pz; }
                         if (P.savedetflag & 0x20u) { rec[k++] = vx; rec[k++] = vy; rec[k++] = vz; }
-                        if (P.savedetflag & 0x40u) rec[k++] = P.src_p.w;
+                        if (P.savedetflag & 0x40u) rec[k++] = S.wlaunch[tid];
                     }
                 }
             }
-            S.tally[kELaunch * B + tid] += P.src_p.w;
+            S.tally[kELaunch * B + tid] += S.wlaunch[tid];
             S.tally[(detected ? kEDetect : kEEscape) * B + tid] += w;
             S.tally[kEAbsDep * B + tid] += eabs;
-            S.tally[kEAbsOther * B + tid] += eoth + (w0 - w);
-            c_photon++;
+            S.tally[kEAbsOther * B + tid] += w0 - w;
             alive = false;
         }
     }
@@ -590,8 +961,8 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     // ---- flush: tile, tallies, counters ------------------------------------------------------
     __syncthreads();
     for (int i = tid; i < tile_elems; i += B) {
-        const unsigned long long q = S.tile[i];
-        if (q == 0ull) continue;
+        const unsigned q = S.tile[i];
+        if (q == 0u) continue;
         const float v = (float)((double)q / (double)P.d_tile_scale);
         int r = i;
         const int x = r % P.tnx; r /= P.tnx;
@@ -608,7 +979,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
         if (lane == 0 && v != 0.0) atomicAdd(P.energy + k, v);
     }
-    unsigned cnt[6] = {c_step, c_scat, c_dep, c_photon, c_photon, c_tile};
+    const unsigned c_launch = (lane == 0) ? S.wcount[3 * warp] : 0u;
+    const unsigned c_tile = (lane == 0) ? S.wcount[3 * warp + 1] : 0u;
+    const unsigned c_photon = (lane == 0) ? S.wcount[3 * warp + 2] : 0u;
+    unsigned cnt[6] = {c_step, c_scat, c_dep, c_launch, c_photon, c_tile};
     const int cidx[6] = {kCntSteps, kCntScatter, kCntDeposit, kCntLaunch, kCntPhoton, kCntTileDeposit};
 #pragma unroll
     for (int k = 0; k < 6; k++) {
@@ -670,36 +1044,71 @@ __global__ void merge_kernel(float* __restrict__ out, const float* __restrict__ 
 
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     size_t b = sizeof(float4) * (size_t)p.medianum;
-    b += (2 * sizeof(unsigned long long) + sizeof(int)) * (size_t)(block / 32);
+    b += (2 * sizeof(unsigned long long) + sizeof(int) + 3 * sizeof(unsigned)) * (size_t)(block / 32);
+    b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (p.tile_on) b += 8 + sizeof(unsigned long long) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
+    if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
 
-template <bool R, bool D, int M>
-static const void* kernel_ptr() { return (const void*)transport_kernel<R, D, M>; }
+template <bool R, bool D, int M, bool A>
+static const void* kernel_ptr() { return (const void*)transport_kernel<R, D, M, A>; }
 
 static int g_minb = 4;   // register budget of the variant launched (set by the launch tuner)
 
 void set_transport_variant(int minb) { g_minb = (minb == 3) ? 3 : 4; }
 int transport_variant() { return g_minb; }
 
-static const void* pick(bool reflect, bool savedet) {
-    if (g_minb == 3) {
-        if (reflect) return savedet ? kernel_ptr<true, true, 3>() : kernel_ptr<true, false, 3>();
-        return savedet ? kernel_ptr<false, true, 3>() : kernel_ptr<false, false, 3>();
+// Pencil sources run the variants without the per-photon source sampling; the others run the
+// variants with it, at the larger register budget its launch code needs.
+static const void* pick(bool reflect, bool savedet, bool area) {
+    if (area) {
+        if (reflect) return savedet ? kernel_ptr<true, true, 3, true>() : kernel_ptr<true, false, 3, true>();
+        return savedet ? kernel_ptr<false, true, 3, true>() : kernel_ptr<false, false, 3, true>();
     }
-    if (reflect) return savedet ? kernel_ptr<true, true, 4>() : kernel_ptr<true, false, 4>();
-    return savedet ? kernel_ptr<false, true, 4>() : kernel_ptr<false, false, 4>();
+    if (g_minb == 3) {
+        if (reflect) return savedet ? kernel_ptr<true, true, 3, false>() : kernel_ptr<true, false, 3, false>();
+        return savedet ? kernel_ptr<false, true, 3, false>() : kernel_ptr<false, false, 3, false>();
+    }
+    if (reflect) return savedet ? kernel_ptr<true, true, 4, false>() : kernel_ptr<true, false, 4, false>();
+    return savedet ? kernel_ptr<false, true, 4, false>() : kernel_ptr<false, false, 4, false>();
 }
 
-int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_bytes) {
-    const void* k = pick(reflect, savedet);
+int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, size_t smem_bytes) {
+    const void* k = pick(reflect, savedet, area);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem_bytes) != cudaSuccess) return 0;
     return n;
+}
+
+void place_tile(KParams& k, int kb) {
+    k.tile_on = 0;
+    // area sources spread their deposits: only point sources get a tile
+    if (!k.save2pt || !k.src_ok || !src_is_point(k.srctype)) return;
+    const int elems = kb * 1024 / (int)sizeof(unsigned);
+    int tg = std::min(k.maxgate, 4);
+    int edge = 1;
+    while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+    while (edge < 6 && tg > 1) {        // prefer a deeper box over more gates
+        tg--;
+        edge = 1;
+        while ((edge + 1) * (edge + 1) * (edge + 1) * tg <= elems) edge++;
+    }
+    edge = std::min(edge, std::max(k.nx, std::max(k.ny, k.nz)));
+    k.tnx = std::min(edge, k.nx);
+    k.tny = std::min(edge, k.ny);
+    k.tnz = std::min(edge, k.nz);
+    auto place = [](float c, int n, int dim) { return std::max(0, std::min(dim - n, (int)std::floor(c - 0.5f * n))); };
+    // a pencil beam deposits along its direction; the other point sources all around the source
+    const float ahead = (k.srctype == kSrcPencil) ? 0.5f * edge : 0.f;
+    k.tx0 = place(k.src_p.x + ahead * k.src_v.x, k.tnx, k.nx);
+    k.ty0 = place(k.src_p.y + ahead * k.src_v.y, k.tny, k.ny);
+    k.tz0 = place(k.src_p.z + ahead * k.src_v.z, k.tnz, k.nz);
+    k.tg0 = 0;
+    k.tng = tg;
+    k.tile_on = 1;
 }
 
 // Fill the derived block of KParams from its base fields.
@@ -719,13 +1128,14 @@ static KParams finalize(const KParams& in) {
     // 2^21 fixed-point units per launch weight: a deposit is at most sqrt(3) launch weights (a
     // voxel diagonal), so weight x scale stays below 2^23 as the rounding trick needs
     p.d_tile_scale = 2097152.f / fmaxf(1.f, fabsf(p.src_p.w));
+    p.d_tile_flush = (float)((double)kTileFlushUnits / (double)p.d_tile_scale);
     return p;
 }
 
 cudaError_t launch_transport(const KParams& in, bool reflect, bool savedet, int grid, int block, size_t smem_bytes,
                              cudaStream_t stream) {
     const KParams p = finalize(in);
-    const void* k = pick(reflect, savedet);
+    const void* k = pick(reflect, savedet, p.srctype != kSrcPencil);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e != cudaSuccess) return e;
     void* args[] = {const_cast<KParams*>(&p)};

@@ -10,7 +10,19 @@ namespace mcxg {
 // Indices into the device counter array.
 enum Counter : int {
     kCntSteps = 0, kCntScatter, kCntDeposit, kCntLaunch, kCntPhoton, kCntDetected, kCntTileDeposit, kCntWork, kNumCounters
+    // kCntLaunch: photons whose launch was attempted; kCntPhoton: photons that entered the
+    // medium (the rest missed the volume after maxvoidstep attempts)
 };
+// Source types, MCX's MCX_SRC_* numbering (src/mcx_const.h:84-101).
+enum SrcType : int {
+    kSrcPencil = 0, kSrcIsotropic, kSrcCone, kSrcGaussian, kSrcPlanar, kSrcPattern, kSrcFourier, kSrcArcsine,
+    kSrcDisk, kSrcFourierX, kSrcFourierX2D, kSrcZGaussian, kSrcLine, kSrcSlit, kSrcPencilArray, kSrcPattern3D,
+    kSrcHyperboloid, kSrcRing, kNumSrcTypes
+};
+// Point sources: the launch voxel is the host's (srcparam2.z/.w after preprocessing).
+__host__ __device__ constexpr bool src_is_point(int t) {
+    return t == kSrcPencil || t == kSrcIsotropic || t == kSrcCone || t == kSrcArcsine || t == kSrcZGaussian;
+}
 // Indices into the device FP64 energy array.
 enum Energy : int { kELaunch = 0, kEEscape, kEDetect, kEAbsDep, kEAbsOther, kNumEnergy };
 // Bits of the device error word.
@@ -36,7 +48,7 @@ struct KParams {
     int nx, ny, nz;
     unsigned int dimxy, nvox;
 
-    // --- launch state every photon starts from (pencil beam, after void skipping)
+    // --- launch state every photon starts from (pencil beam: after void skipping on the host)
     float4 src_p;                   // x, y, z, initial weight
     float4 src_v;                   // unit direction
     float src_t;                    // time already spent in the void
@@ -44,6 +56,14 @@ struct KParams {
     unsigned int src_label;         // its label byte (detector bit included)
     int src_fx, src_fy, src_fz;     // integer voxel coordinates of the launch voxel
     int src_ok;                     // 0: photons cannot enter the volume (all launches fail)
+
+    // --- other source shapes (src/mcx_core.cu:1261-1640): sampled per photon on the device,
+    //     void skipping and specular loss per photon as well
+    int srctype;                    // MCX_SRC_* (0 = pencil, the fixed launch state above)
+    float4 src_param1, src_param2;  // srcparam1, srcparam2
+    float src_focal;                // srcdir.w: focal length (NaN isotropic, -inf Lambertian)
+    const float* srcpattern;        // pattern (param1.w x param2.w) or pattern3d intensities
+    int isspecular, voidtime;
 
     // --- time gates
     float twin0, twin1, Rtstep, oneoverc0;
@@ -95,6 +115,7 @@ struct KParams {
     int d_gscat;                    // gscatter as an integer threshold
     unsigned long long d_nwork;     // work items in the pool: photons, or MCX streams
     float d_tile_scale;             // fixed-point units per unit of deposited weight in the tile
+    float d_tile_flush;             // weight of kTileFlushUnits units
 };
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).
@@ -102,6 +123,13 @@ constexpr float kMaxAccum = 1000.f;
 // Smallest deposit tile kept over the launch point: the voxels there receive millions of
 // equal first-flight deposits, which must not be summed directly into large FP32 values.
 constexpr int kMinTileKB = 2;
+// Fixed-point units a tile slot hands to the global field at once (32-bit slots).
+constexpr unsigned kTileFlushUnits = 1u << 30;
+
+// Place the deposit tile: a box of voxels x gates around the point where photons enter the
+// medium, extending along the launch direction, in `kb` KB of 32-bit slots (off when nothing
+// is saved or the source misses the volume).
+void place_tile(KParams& k, int kb);
 
 // Host-side launch of the transport kernel variant matching the flags.  smem_bytes is the
 // dynamic shared memory per CTA; returns the CUDA error of the launch.
@@ -114,7 +142,15 @@ int transport_variant();
 // Shared memory the kernel needs for a given block size and parameter set.
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
 // Occupancy-derived CTAs per SM for the chosen variant.
-int transport_blocks_per_sm(bool reflect, bool savedet, int block, size_t smem_bytes);
+int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, size_t smem_bytes);
+
+// Source fields of KParams from a preprocessed Config: shape parameters, the pencil's launch
+// state (void skipping traced on the host), the point sources' launch voxel.  d_pattern holds
+// the pattern intensities on the device (source_pattern_len floats) or is null.
+void fill_source(KParams& k, const struct MCXConfig* cfg, const float* d_pattern);
+size_t source_pattern_len(const struct MCXConfig* cfg);
+// Rejects source settings the engine does not run (MCX error -6).
+void check_source(const struct MCXConfig* cfg);
 
 // Void skipping of a pencil source launched outside the volume or in a 0 voxel, traced once on
 // the host (engine.cu).  Returns the entry voxel or -1.

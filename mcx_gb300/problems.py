@@ -39,12 +39,32 @@ def cube60b(nphoton: float = 1e6) -> dict:
     return _cube60(nphoton, True, 1.0)
 
 
+def cube60planar(nphoton: float = 1e6) -> dict:
+    """The cube with reflection and a 40 x 40 planar source 10 mm in front of the z=0 face
+    (src/mcx_bench.c:155-215); every photon crosses the void before it enters."""
+    cfg = _cube60(nphoton, True, 1.0)
+    cfg.update(srctype="planar", srcpos=[10.0, 10.0, -10.0], srcdir=[0.0, 0.0, 1.0],
+               srcparam1=[40.0, 0.0, 0.0, 0.0], srcparam2=[0.0, 40.0, 0.0, 0.0])
+    return cfg
+
+
 def sphere60b(nphoton: float = 1e6) -> dict:
     """cube60 plus a label-2 sphere (R=15 at (30,30,30), medium 2 = (0.002, 5.0, 0.9, 1.0)) with
     reflection on: the second deck of MCX's speed benchmark (mcxlab/examples/mcx_gpu_benchmarks.m:47-87)."""
     cfg = _cube60(nphoton, True, 1.0)
     cfg["seed"] = 29012392
     sphere_labels((60, 60, 60), (30.0, 30.0, 30.0), 15.0, 2, cfg["vol"])
+    return cfg
+
+
+def source_deck(g: dict, nphoton: float | None = None) -> dict:
+    """The deck of a source-shape golden entry: its base deck with the entry's overrides."""
+    cfg = {"cube60": cube60, "cube60planar": cube60planar}[g["deck"]](nphoton or g["nphoton"])
+    for k, v in g["set"].items():
+        cfg[k] = np.array(v, np.float32) if k == "prop" else v
+    if g.get("nosave"):
+        cfg.pop("detpos", None)
+        cfg["issavedet"] = 0
     return cfg
 
 
@@ -134,3 +154,49 @@ def workload2(nphoton: float = 1e9, seed: int = CUBE60_SEED, n: int = 256) -> di
 
 
 WORKLOADS = {"workload0": workload0, "workload1": workload1, "workload2": workload2}
+
+
+BATCH_EDGES = (32, 48, 64, 96, 128)
+
+
+def batch_instances(count: int = 256, seed: int = 20251204, budget_scale: float = 1.0) -> list[dict]:
+    """The batched workload: `count` independent simulations drawn from one master seed.
+
+    Each instance: a cube of edge uniform over {32, 48, 64, 96, 128} voxels (1 mm) of medium 1
+    with 1-4 random axis-aligned ellipsoids (labels 2..5, later ones overwrite earlier ones); every
+    medium has mua log-uniform in [1e-3, 5e-2]/mm, mus uniform in [0.5, 20]/mm, g uniform in
+    [0.7, 0.95] and n = 1.37 (background n = 1, Fresnel reflection on); a photon budget
+    log-uniform in [1e6, 1e8] (times `budget_scale`); a pencil source entering the z = 0 face
+    along +z at a random point of its central half; two radius-1 detectors on that face 5 and
+    10 mm from the source (detector id and per-medium partial paths saved); one 0-5 ns gate."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.choice(BATCH_EDGES))
+        vol = np.ones((n, n, n), dtype=np.uint8)
+        nell = int(rng.integers(1, 5))
+        idx = np.arange(n, dtype=np.float32) + 0.5
+        for e in range(nell):
+            c = rng.uniform(0.2 * n, 0.8 * n, 3)
+            r = rng.uniform(0.08 * n, 0.3 * n, 3)
+            X, Y, Z = np.meshgrid((idx - c[0]) / r[0], (idx - c[1]) / r[1], (idx - c[2]) / r[2], indexing="ij")
+            vol[X * X + Y * Y + Z * Z <= 1.0] = 2 + e
+        nmed = 1 + nell
+        prop = np.zeros((nmed + 1, 4), np.float32)
+        prop[0] = [0.0, 0.0, 1.0, 1.0]
+        for m in range(1, nmed + 1):
+            prop[m] = [np.exp(rng.uniform(np.log(1e-3), np.log(5e-2))), rng.uniform(0.5, 20.0),
+                       rng.uniform(0.7, 0.95), 1.37]
+        budget = float(np.exp(rng.uniform(np.log(1e6), np.log(1e8)))) * budget_scale
+        sx, sy = (float(np.floor(v)) for v in rng.uniform(0.25 * n, 0.75 * n, 2))
+        ang = rng.uniform(0, 2 * np.pi)
+        det = [[sx + d * np.cos(ang), sy + d * np.sin(ang), 0.0, 1.0] for d in (5.0, 10.0)]
+        out.append({
+            "nphoton": max(1, int(budget)), "seed": int(rng.integers(1, 2**31 - 1)),
+            "vol": vol, "prop": prop,
+            "tstart": 0.0, "tend": 5e-9, "tstep": 5e-9,
+            "srcpos": [sx, sy, 0.0], "srcdir": [0.0, 0.0, 1.0], "issrcfrom0": 1,
+            "isreflect": 1, "issavedet": 1, "savedetflag": "dp", "detpos": np.array(det, np.float32),
+            "maxdetphoton": max(1000, int(budget * 0.005)),
+        })
+    return out

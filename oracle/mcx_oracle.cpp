@@ -299,7 +299,200 @@ struct Runner {
     }
 
     // Launch a pencil-beam photon (src/mcx_core.cu:1236-1243, 1646-1717).  Returns false on failure.
-    bool launch(Photon& ph, Tally& T) {
+    // Shape of a non-pencil source: position, weight and direction of one photon, drawn in the
+    // reference's order (launchnewphoton, src/mcx_core.cu:1261-1640; no launch-angle table).
+    // Sets the launch voxel for shapes that move the photon.  False when the weight is at or
+    // below minenergy (the reference then draws again without counting an attempt).
+    bool sample_source(Photon& ph, Rng& rng) {
+        const OracleProblem* P = C.P;
+        const float* a = P->srcparam1;
+        const float* b = P->srcparam2;
+        const float W = P->srcpos[3];
+        const float kJBO = 0.9998f;            // JUST_BELOW_ONE, src/mcx_const.h:50
+        float origin[3] = {P->srcpos[0], P->srcpos[1], P->srcpos[2]};
+        bool canfocus = true, moved = true;
+        auto U = [&]() { return rng.next(); };
+        auto scatlen = [&]() { return -std::log(rng.next() + kEPS); };
+        auto rotate_to = [&](float st, float ct, float sp, float cp) { rotatevector(ph.v, st, ct, sp, cp); };
+        switch (P->srctype) {
+        case 4: case 5: case 15: case 6: case 14: {          // planar, pattern, pattern3d, fourier, pencilarray
+            const float rx = U(), ry = U();
+            if (P->srctype == 15) {
+                const float rz = U();
+                ph.p[0] += rx * a[0]; ph.p[1] += ry * a[1]; ph.p[2] += rz * a[2];
+                const int nx = (int)a[0], ny = (int)a[1];
+                ph.w = W * P->srcpattern[(int)(rz * kJBO * a[2]) * ny * nx + (int)(ry * kJBO * a[1]) * nx + (int)(rx * kJBO * a[0])];
+            } else {
+                for (int i = 0; i < 3; i++) ph.p[i] += rx * a[i] + ry * b[i];
+                if (P->srctype == 5) {
+                    ph.w = W * P->srcpattern[(int)(ry * kJBO * b[3]) * (int)a[3] + (int)(rx * kJBO * a[3])];
+                } else if (P->srctype == 6) {
+                    ph.w = W * (std::cos((std::floor(a[3]) * rx + std::floor(b[3]) * ry + a[3] - std::floor(a[3])) * kTWO_PI) *
+                                    (1.f - b[3] + std::floor(b[3])) + 1.f) * 0.5f;
+                } else if (P->srctype == 14) {
+                    const float i = std::floor(rx * a[3]) / (a[3] - 1.f), j = std::floor(ry * b[3]) / (b[3] - 1.f);
+                    for (int k = 0; k < 3; k++) ph.p[k] = P->srcpos[k] + i * a[k] + j * b[k];
+                }
+            }
+            for (int i = 0; i < 3; i++) origin[i] += (a[i] + b[i]) * 0.5f;
+            break;
+        }
+        case 9: case 10: {                                     // fourierx, fourierx2d
+            const float rx = U(), ry = U();
+            const float s = a[3] / std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+            const float d[3] = {P->srcdir[0], P->srcdir[1], P->srcdir[2]};
+            const float v2[3] = {s * (d[1] * a[2] - d[2] * a[1]), s * (d[2] * a[0] - d[0] * a[2]), s * (d[0] * a[1] - d[1] * a[0])};
+            for (int i = 0; i < 3; i++) ph.p[i] += rx * a[i] + ry * v2[i];
+            if (P->srctype == 10)
+                ph.w = W * (std::sin((b[0] * rx + b[2]) * kTWO_PI) * std::sin((b[1] * ry + b[3]) * kTWO_PI) + 1.f) * 0.5f;
+            else
+                ph.w = W * (std::cos((b[0] * rx + b[1] * ry + b[2]) * kTWO_PI) * (1.f - b[3]) + 1.f) * 0.5f;
+            for (int i = 0; i < 3; i++) origin[i] += (a[i] + v2[i]) * 0.5f;
+            break;
+        }
+        case 8: case 17: case 3: {                             // disk, ring, gaussian
+            const float phi = (P->srctype == 17 && (a[2] > 0.f || a[3] > 0.f))
+                                  ? std::fabs(a[2] - a[3]) * U() + std::fmin(a[2], a[3]) : kTWO_PI * U();
+            const float sp = std::sin(phi), cp = std::cos(phi);
+            float r;
+            if (P->srctype != 3) {
+                r = std::sqrt(U() * std::fabs(a[0] * a[0] - a[1] * a[1]) + a[1] * a[1]);
+            } else if (std::fabs(P->srcdir[3]) < 1e-5f || std::fabs(a[1]) < 1e-5f) {
+                r = std::sqrt(0.5f * scatlen()) * a[0];
+            } else {
+                const float zr = a[0] * a[0] * 3.14159265358979f / a[1];
+                r = std::sqrt(0.5f * scatlen() * (1.f + P->srcdir[3] * P->srcdir[3] / (zr * zr))) * a[0];
+            }
+            const float* v = ph.v;
+            if (v[2] > -1.f + kEPS && v[2] < 1.f - kEPS) {
+                const float t0 = 1.f - v[2] * v[2], t1 = r / std::sqrt(t0);
+                ph.p[0] += t1 * (v[0] * v[2] * cp - v[1] * sp);
+                ph.p[1] += t1 * (v[1] * v[2] * cp + v[0] * sp);
+                ph.p[2] -= t1 * t0 * cp;
+            } else {
+                ph.p[0] += r * cp;
+                ph.p[1] += r * sp;
+            }
+            break;
+        }
+        case 2: case 1: case 7: {                              // cone, isotropic, arcsine
+            float ang = kTWO_PI * U();
+            const float sp = std::sin(ang), cp = std::cos(ang);
+            if (P->srctype == 2) {
+                const float c = std::cos(a[0]);
+                ang = (a[1] > 0.f) ? U() * a[0] : std::acos(U() * (1.f - c) + c);
+            } else if (P->srctype == 1) {
+                ang = std::acos(2.f * U() - 1.f);
+            } else {
+                ang = 3.14159265358979f * U();
+            }
+            rotate_to(std::sin(ang), std::cos(ang), sp, cp);
+            canfocus = false;
+            moved = false;
+            break;
+        }
+        case 11: {                                             // zgaussian
+            float ang = kTWO_PI * U();
+            const float sp = std::sin(ang), cp = std::cos(ang);
+            ang = std::sqrt(2.f * scatlen());
+            ang *= (1.f - 2.f * U()) * a[0];
+            rotate_to(std::sin(ang), std::cos(ang), sp, cp);
+            canfocus = false;
+            moved = false;
+            break;
+        }
+        case 16: {                                             // hyperboloid gaussian
+            const float phi = kTWO_PI * U();
+            const float sp = std::sin(phi), cp = std::cos(phi);
+            const float r = std::sqrt(0.5f * scatlen()) * a[0];
+            const float q = -a[1] / a[2], k = 1.f / std::sqrt(r * r + a[2] * a[2]);
+            float d[3] = {r * (cp - q * sp), r * (sp + q * cp), 0.f};           // displacement
+            const float u[3] = {-r * sp * k, r * cp * k, a[2] * k};            // direction, beam frame
+            const float* v = ph.v;
+            if (v[2] > -1.f + kEPS && v[2] < 1.f - kEPS) {
+                const float st = std::sqrt(1.f - v[2] * v[2]);
+                const float c = v[0] / st, s_ = v[1] / st, vz = v[2];
+                const float dd[3] = {d[0] * c * vz - d[1] * s_, d[0] * s_ * vz + d[1] * c, -d[0] * st};
+                ph.v[0] = u[0] * c * vz - u[1] * s_ + u[2] * c * st;
+                ph.v[1] = u[0] * s_ * vz + u[1] * c + u[2] * s_ * st;
+                ph.v[2] = -u[0] * st + u[2] * vz;
+                d[0] = dd[0]; d[1] = dd[1]; d[2] = dd[2];
+            } else {
+                ph.v[0] = u[0]; ph.v[1] = u[1]; ph.v[2] = (v[2] > 0.f) ? u[2] : -u[2];
+            }
+            for (int i = 0; i < 3; i++) ph.p[i] += d[i];
+            canfocus = false;
+            break;
+        }
+        case 12: case 13: {                                    // line, slit
+            const float r = U();
+            for (int i = 0; i < 3; i++) ph.p[i] += r * a[i];
+            const float len = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+            if (P->srctype == 12) {
+                const float ax[3] = {a[0] / len, a[1] / len, a[2] / len};
+                if (b[0] > 0.f) {
+                    float* v = ph.v;
+                    const float dot = v[0] * ax[0] + v[1] * ax[1] + v[2] * ax[2];
+                    for (int i = 0; i < 3; i++) v[i] -= dot * ax[i];
+                    const float n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                    for (int i = 0; i < 3; i++) v[i] /= n;
+                    const float ang = b[0] * (2.f * U() - 1.f), sp = std::sin(ang), cp = std::cos(ang);
+                    const float cr[3] = {ax[1] * v[2] - ax[2] * v[1], ax[2] * v[0] - ax[0] * v[2], ax[0] * v[1] - ax[1] * v[0]};
+                    for (int i = 0; i < 3; i++) v[i] = v[i] * cp + cr[i] * sp;
+                } else {
+                    for (int i = 0; i < 3; i++) ph.v[i] = ax[i];
+                    const float ang = kTWO_PI * U();
+                    rotate_to(1.f, 0.f, std::sin(ang), std::cos(ang));
+                }
+            } else if (b[0] > 0.f || b[1] > 0.f) {
+                const float ang = kTWO_PI * U();
+                float sp = std::sin(ang), cp = std::cos(ang);
+                const float g = std::sqrt(2.f * scatlen());
+                cp *= b[0] * g;
+                sp *= b[1] * g / len;
+                float* v = ph.v;
+                const float nv[3] = {a[1] * v[2] - a[2] * v[1], a[2] * v[0] - a[0] * v[2], a[0] * v[1] - a[1] * v[0]};
+                cp /= std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+                for (int i = 0; i < 3; i++) v[i] += cp * nv[i] + sp * a[i];
+                const float n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                for (int i = 0; i < 3; i++) v[i] /= n;
+            }
+            for (int i = 0; i < 3; i++) origin[i] = P->srcpos[i] + a[i] * 0.5f;
+            canfocus = (P->srctype == 13);
+            break;
+        }
+        default:
+            break;
+        }
+        if (std::fabs(ph.w) <= P->minenergy) return false;
+        const float f = P->srcdir[3];
+        if (canfocus) {
+            if (std::isnan(f)) {
+                const float phi = kTWO_PI * U(), th = std::acos(2.f * U() - 1.f);
+                rotate_to(std::sin(th), std::cos(th), std::sin(phi), std::cos(phi));
+            } else if (f < 0.f && std::isinf(f)) {
+                const float phi = kTWO_PI * U(), st = std::sqrt(U());
+                rotate_to(st, std::sqrt(1.f - st * st), std::sin(phi), std::cos(phi));
+            } else if (f != 0.f) {
+                const float sg = (f > 0.f) ? 1.f : -1.f;
+                for (int i = 0; i < 3; i++) origin[i] += f * ph.v[i];
+                for (int i = 0; i < 3; i++) ph.v[i] = sg * (origin[i] - ph.p[i]);
+                const float n = std::sqrt(ph.v[0] * ph.v[0] + ph.v[1] * ph.v[1] + ph.v[2] * ph.v[2]);
+                for (int i = 0; i < 3; i++) ph.v[i] /= n;
+            }
+        }
+        if (moved) {
+            if (ph.p[0] < 0.f || ph.p[1] < 0.f || ph.p[2] < 0.f || ph.p[0] >= C.maxx || ph.p[1] >= C.maxy || ph.p[2] >= C.maxz) {
+                ph.mediaid = 0;
+            } else {
+                ph.idx1d = (uint32_t)((int)std::floor(ph.p[2]) * C.dimxy + (int)std::floor(ph.p[1]) * C.nx + (int)std::floor(ph.p[0]));
+                ph.mediaid = P->vol[ph.idx1d];
+            }
+        }
+        return true;
+    }
+
+    bool launch(Photon& ph, Tally& T, Rng& rng) {
         const OracleProblem* P = C.P;
         float attempts = 1.f;
         do {
@@ -308,6 +501,12 @@ struct Runner {
             ph.pscat = 0.f; ph.t = 0.f; ph.pathlen = C.minaccumtime;
             ph.idx1d = P->src_idx;
             ph.mediaid = P->src_med;
+            if (P->srctype != 0 && !sample_source(ph, rng)) {
+                // weight at or below minenergy: draw again (bounded here, unlike the reference)
+                attempts += 1.f;
+                if (attempts > (float)P->maxvoidstep) return false;
+                continue;
+            }
             ph.rv[0] = 1.f / ph.v[0]; ph.rv[1] = 1.f / ph.v[1]; ph.rv[2] = 1.f / ph.v[2];
             if ((ph.mediaid & kMED_MASK) == 0) {
                 int id = skipvoid(C, ph);
@@ -349,7 +548,7 @@ struct Runner {
         Photon ph;
         std::memset(&ph, 0, sizeof(ph));
         ph.fd[3] = -1;
-        if (!launch(ph, T)) return;
+        if (!launch(ph, T, rng)) return;
         const uint32_t flag = P->savedetflag;
         const int save_nscat = P->savedet && (flag & 0x2);
         const int save_ppath = P->savedet && (flag & 0x4);

@@ -38,6 +38,11 @@ typedef struct OracleProblem {
      * nphoton/mcx_threads photons (+1 for the first nphoton%mcx_threads streams) in sequence. */
     int seed_mode;
     uint32_t mcx_threads;
+    /* source shape (MCX_SRC_* numbering, src/mcx_const.h:84-101); src_idx/src_med are the launch
+     * voxel of point sources; srcpattern holds pattern / pattern3d intensities, x fastest */
+    int srctype;
+    float srcparam1[4], srcparam2[4];
+    const float* srcpattern;
 } OracleProblem;
 
 /* Outputs: raw (unnormalised) field in FP64, optional per-voxel deposit counts, detected

@@ -31,7 +31,8 @@ class OracleProblem(C.Structure):
         ("outputtype", C.c_int), ("minenergy", C.c_float), ("gscatter", C.c_uint32), ("bc", C.c_uint8 * 12),
         ("savedet", C.c_int), ("savedetflag", C.c_uint32), ("maxdetphoton", C.c_uint32), ("nphoton", C.c_uint64),
         ("photon_offset", C.c_uint64), ("seed", C.c_uint64), ("nthreads", C.c_int), ("seed_mode", C.c_int),
-        ("mcx_threads", C.c_uint32),
+        ("mcx_threads", C.c_uint32), ("srctype", C.c_int), ("srcparam1", C.c_float * 4),
+        ("srcparam2", C.c_float * 4), ("srcpattern", C.c_void_p),
     ]
 
 
@@ -101,8 +102,9 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
     P.detnum = int(c.detnum)
     P.srcpos[:] = [c.srcpos.x, c.srcpos.y, c.srcpos.z, c.srcpos.w]
     P.srcdir[:] = [c.srcdir.x, c.srcdir.y, c.srcdir.z, c.srcdir.w]
-    P.src_idx = struct.unpack("<I", struct.pack("<f", c.srcparam2.z))[0]
-    P.src_med = struct.unpack("<I", struct.pack("<f", c.srcparam2.w))[0]
+    if ord(c.srctype) in (0, 1, 2, 7, 11):     # point sources: launch voxel from preprocessing
+        P.src_idx = struct.unpack("<I", struct.pack("<f", c.srcparam2.z))[0]
+        P.src_med = struct.unpack("<I", struct.pack("<f", c.srcparam2.w))[0]
     P.twin0 = c.tstart + c.tstep * maxgate * gate_group
     P.twin1 = P.twin0 + c.tstep * maxgate
     P.tstep = c.tstep
@@ -127,6 +129,10 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
     P.nthreads = threads or os.cpu_count() or 1
     P.seed_mode = 1 if mcx_threads else 0
     P.mcx_threads = int(mcx_threads)
+    P.srctype = ord(c.srctype)
+    P.srcparam1[:] = [c.srcparam1.x, c.srcparam1.y, c.srcparam1.z, c.srcparam1.w]
+    P.srcparam2[:] = [c.srcparam2.x, c.srcparam2.y, c.srcparam2.z, c.srcparam2.w]
+    P.srcpattern = c.srcpattern
 
     field = np.zeros(nvox * maxgate, dtype=np.float64)
     hit = np.zeros(nvox * maxgate, dtype=np.uint64) if hits else None

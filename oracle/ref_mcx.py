@@ -115,6 +115,15 @@ def build(force: bool = False) -> Path:
     return BIN
 
 
+_SRC_NAMES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
+              "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid", "ring"]
+
+
+def _src_name(t) -> str:
+    """MCX's source-type keyword (src/mcx_utils.c:211)."""
+    return t.lower() if isinstance(t, str) else _SRC_NAMES[int(t)]
+
+
 def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
     vol = np.asarray(cfg["vol"])
     prop = np.asarray(cfg["prop"], dtype=float)
@@ -134,9 +143,13 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
                    "MediaFormat": "byte", "VolumeFile": volfile,
                    "Media": [{"mua": float(r[0]), "mus": float(r[1]), "g": float(r[2]), "n": float(r[3])} for r in prop]},
         "Forward": {"T0": float(cfg["tstart"]), "T1": float(cfg["tend"]), "Dt": float(cfg["tstep"])},
-        "Optode": {"Source": {"Type": "pencil", "Pos": [float(x) for x in cfg["srcpos"][:3]],
-                              "Dir": [float(x) for x in cfg["srcdir"][:3]]}},
+        "Optode": {"Source": {"Type": _src_name(cfg.get("srctype", "pencil")),
+                              "Pos": [float(x) for x in cfg["srcpos"][:3]],
+                              "Dir": [float(x) for x in list(cfg["srcdir"])[:4]]}},
     }
+    for key, name in (("srcparam1", "Param1"), ("srcparam2", "Param2")):
+        if key in cfg:
+            out["Optode"]["Source"][name] = [float(x) for x in cfg[key]]
     if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
         out["Optode"]["Detector"] = [{"Pos": [float(d[0]), float(d[1]), float(d[2])], "R": float(d[3])}
                                      for d in np.asarray(cfg["detpos"], float).reshape(-1, 4)]

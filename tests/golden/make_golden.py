@@ -67,6 +67,26 @@ def main(ref: Path) -> None:
                    "source": f"test/testmcx.sh:{_line_of(sh, 'cccccc')}"},
         "reflect_bc": {"deck": "cube60", "bc": "aarraa", "isreflect": 0, "nphoton": 1e6, "pattern": "27.x%",
                        "lo": 0.27, "hi": 0.28, "source": f"test/testmcx.sh:{_line_of(sh, '-B aarraa')}"},
+        # source shapes (test/testmcx.sh "test ... source" blocks): deck, overrides of its
+        # Optode/Domain, the absorbed-fraction window the reference's test greps for
+        "sources": [
+            {"name": "planar", "deck": "cube60planar", "set": {}, "nphoton": 1e6, "pattern": "25.x%",
+             "lo": 0.25, "hi": 0.26, "source": f"test/testmcx.sh:{_line_of(sh, 'cube60planar $PARAM')}"},
+            {"name": "isotropic", "deck": "cube60", "set": {"srctype": "isotropic", "srcpos": [29, 29, 29]},
+             "nosave": True, "nphoton": 1e6, "pattern": "88.x%", "lo": 0.88, "hi": 0.89,
+             "source": f"test/testmcx.sh:{_line_of(sh, 'absorbed:.*88')}"},
+            {"name": "cone", "deck": "cube60",
+             "set": {"srctype": "cone", "srcparam1": [0.5, 0, 0, 0], "prop": [[0, 0, 1, 1], [0.001, 0.001, 0, 1]]},
+             "nosave": True, "nphoton": 1e6, "pattern": "6.x%", "lo": 0.06, "hi": 0.07,
+             "source": f"test/testmcx.sh:{_line_of(sh, 'absorbed:.*6')}"},
+            {"name": "fourier", "deck": "cube60planar", "set": {"srctype": "fourier", "srcparam1": [40, 0, 0, 2]},
+             "nosave": True, "nphoton": 1e6, "pattern": "25.x%", "lo": 0.25, "hi": 0.26,
+             "source": f"test/testmcx.sh:{_line_of(sh, 'fourier')}"},
+            {"name": "pencilarray", "deck": "cube60planar",
+             "set": {"srctype": "pencilarray", "srcparam1": [40, 0, 0, 4], "srcparam2": [0, 20, 0, 2]},
+             "nosave": True, "nphoton": 1e6, "pattern": "23.x%", "lo": 0.23, "hi": 0.24,
+             "source": f"test/testmcx.sh:{_line_of(sh, 'pencilarray')}"},
+        ],
     }
     (HERE / "reference_goldens.json").write_text(json.dumps(out, indent=1) + "\n")
     print("wrote", HERE / "reference_goldens.json")

@@ -109,7 +109,8 @@ def test_maskdet_interior_detector_marks_nothing(engine):
 
 @pytest.mark.parametrize("bad,msg", [
     ({"tstart": 5e-9}, "time gate"),
-    ({"srctype": "isotropic"}, "pencil"),
+    ({"srctype": "pattern"}, "srcpattern"),
+    ({"srcnum": 2}, "photon sharing"),
     ({"respin": 0}, "respin"),
     ({"srcdir": [0.0, 0.0, 0.0]}, "direction"),
 ])

@@ -149,3 +149,14 @@ def test_energy_balance_and_field_consistency(engine, oracle):
     assert abs(lhs - rhs) / lhs < 1e-9
     mua = pc.prop[:, 0][pc.vol.reshape(pc.dims, order="F") & 0x7FFFFFFF]
     assert abs((r["raw"][..., 0] * mua).sum() - s["e_absdep"]) / s["e_absdep"] < 1e-6
+
+
+@pytest.mark.parametrize("name", ["planar", "isotropic", "cone", "fourier", "pencilarray"])
+def test_source_shapes_absorbed(engine, oracle, goldens, name):
+    """Absorbed fraction of each source shape the reference's tests check (test/testmcx.sh:84-102),
+    from the oracle's restatement of launchnewphoton at 3e5 photons with a fixed seed."""
+    g = next(x for x in goldens["sources"] if x["name"] == name)
+    pc = engine.prepare(problems.source_deck(g))
+    s = oracle.run(pc, nphoton=300_000, seed=123)["stat"]
+    frac = s["energyabs"] / s["energytot"]
+    assert g["lo"] <= frac < g["hi"], (name, frac, g["source"])
