@@ -199,6 +199,8 @@ uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
 // source; not photon sharing (srcnum > 1), extra sources or a launch-angle table.
 void check_source(const Config* cfg) {
     if ((unsigned char)cfg->srctype >= kNumSrcTypes) MCXG_RAISE(-6, "unknown source type");
+    if (std::isinf(cfg->srcdir.w) && cfg->srcdir.w > 0.f)
+        MCXG_RAISE(-4, "a focal length of +inf is not a valid source setting (srcdir.w)");
     if (cfg->srcnum > 1) MCXG_RAISE(-6, "photon sharing (srcnum > 1) is not supported by the GB300 engine");
     if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
     if (cfg->nangle) MCXG_RAISE(-6, "launch-angle distributions (angleinvcdf) are not supported by the GB300 engine");
@@ -229,7 +231,11 @@ void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
     k.srctype = (unsigned char)cfg->srctype;
     k.src_param1 = cfg->srcparam1;
     k.src_param2 = cfg->srcparam2;
-    k.src_focal = cfg->srcdir.w;
+    const float f = cfg->srcdir.w;
+    k.src_focus = std::isnan(f) ? kFocusIsotropic
+                : std::isinf(f) ? kFocusLambertian          // -inf; +inf is rejected by check_source
+                : (f != 0.f) ? kFocusLength : kFocusNone;
+    k.src_focal = std::isfinite(f) ? f : 0.f;
     k.srcpattern = d_pattern;
     k.isspecular = cfg->isspecular ? 1 : 0;
     k.voidtime = cfg->voidtime;
@@ -947,7 +953,6 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
         S[i] = std::make_unique<Session>();
         S[i]->create(cfg, gpuid, false);
         if (S[i]->totalgates > S[i]->kp.maxgate) MCXG_RAISE(-6, "batched simulations must hold all their time gates on the device");
-        S[i]->apply_tile(kMinTileKB);
         S[i]->set_window(cfg->tstart, cfg->tstart + cfg->tstep * S[i]->kp.maxgate);
         if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
         begin_outputs(cfg, *S[i]);

@@ -383,19 +383,20 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
             return false;
         }
         if (fabsf(L.w) <= P.minenergy) continue;
-        if (canfocus) {
+        if (canfocus && P.src_focus != kFocusNone) {
+            // the host classifies the focal length: fast-math code must not test for NaN or inf
             const float f = P.src_focal;
             float sphi, cphi, st, ct;
-            if (isnan(f)) {                                             // isotropic
+            if (P.src_focus == kFocusIsotropic) {                       // NaN focal length
                 sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
                 sincosf(acosf(2.f * rng_next(r0, r1) - 1.f), &st, &ct);
                 rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
-            } else if (f < 0.f && isinf(f)) {                           // Lambertian
+            } else if (P.src_focus == kFocusLambertian) {               // -inf focal length
                 sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
                 st = sqrtf(rng_next(r0, r1));
                 ct = sqrtf(1.f - st * st);
                 rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
-            } else if (f != 0.f) {                                      // converging / diverging
+            } else {                                                    // converging / diverging
                 const float sg = (f > 0.f) ? 1.f : -1.f;
                 ox += f * L.vx; oy += f * L.vy; oz += f * L.vz;
                 L.vx = sg * (ox - L.px); L.vy = sg * (oy - L.py); L.vz = sg * (oz - L.pz);
@@ -792,8 +793,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     rec = true;
                     c_dep++;
                     const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
-                    if (P.tile_on && weight > 0.f && ox >= tx0 && ox < tx1 && oy >= ty0 && oy < ty1 && oz >= tz0 &&
-                        oz < tz1 && (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
+                    // the index range of the tile box (empty without a tile) screens most deposits out
+                    // with one compare before the box test
+                    if (idxold - P.d_tile_lo < P.d_tile_span && weight > 0.f && ox >= tx0 && ox < tx1 && oy >= ty0 &&
+                        oy < ty1 && oz >= tz0 && oz < tz1 && (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
                         const int ti = (((tshift - P.tg0) * P.tnz + (int)(oz - tz0)) * P.tny + (int)(oy - ty0)) * P.tnx +
                                        (int)(ox - tx0);
                         // exact fixed-point sum: millions of equal first-flight deposits near the
@@ -1129,6 +1132,8 @@ static KParams finalize(const KParams& in) {
     // voxel diagonal), so weight x scale stays below 2^23 as the rounding trick needs
     p.d_tile_scale = 2097152.f / fmaxf(1.f, fabsf(p.src_p.w));
     p.d_tile_flush = (float)((double)kTileFlushUnits / (double)p.d_tile_scale);
+    p.d_tile_lo = p.tile_on ? (unsigned)(p.tz0 * (int)p.dimxy + p.ty0 * p.nx + p.tx0) : 0u;
+    p.d_tile_span = p.tile_on ? (unsigned)((p.tnz - 1) * (int)p.dimxy + (p.tny - 1) * p.nx + p.tnx) : 0u;
     return p;
 }
 

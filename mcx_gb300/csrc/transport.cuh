@@ -19,6 +19,9 @@ enum SrcType : int {
     kSrcDisk, kSrcFourierX, kSrcFourierX2D, kSrcZGaussian, kSrcLine, kSrcSlit, kSrcPencilArray, kSrcPattern3D,
     kSrcHyperboloid, kSrcRing, kNumSrcTypes
 };
+// Launch-direction options of area sources, from srcdir.w (src/mcx_core.cu:1672-1710): 0 =
+// along srcdir, a finite value = focal length, NaN = isotropic, -inf = Lambertian.
+enum FocusMode : int { kFocusNone = 0, kFocusLength, kFocusIsotropic, kFocusLambertian };
 // Point sources: the launch voxel is the host's (srcparam2.z/.w after preprocessing).
 __host__ __device__ constexpr bool src_is_point(int t) {
     return t == kSrcPencil || t == kSrcIsotropic || t == kSrcCone || t == kSrcArcsine || t == kSrcZGaussian;
@@ -61,7 +64,8 @@ struct KParams {
     //     void skipping and specular loss per photon as well
     int srctype;                    // MCX_SRC_* (0 = pencil, the fixed launch state above)
     float4 src_param1, src_param2;  // srcparam1, srcparam2
-    float src_focal;                // srcdir.w: focal length (NaN isotropic, -inf Lambertian)
+    float src_focal;                // srcdir.w when finite: focal length
+    int src_focus;                  // kFocus*: what srcdir.w asks of the area sources
     const float* srcpattern;        // pattern (param1.w x param2.w) or pattern3d intensities
     int isspecular, voidtime;
 
@@ -116,6 +120,7 @@ struct KParams {
     unsigned long long d_nwork;     // work items in the pool: photons, or MCX streams
     float d_tile_scale;             // fixed-point units per unit of deposited weight in the tile
     float d_tile_flush;             // weight of kTileFlushUnits units
+    unsigned d_tile_lo, d_tile_span;  // voxel-index range [lo, lo + span) holding the tile box
 };
 
 // Spill threshold of the two-copy accumulation (src/mcx_core.h:53, MAX_ACCUM).

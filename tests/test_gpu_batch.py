@@ -38,10 +38,11 @@ def test_batch_matches_single_runs(engine):
             da = ra["detp"][:, np.lexsort(ra["detp"][::-1])]
             db = rb["detp"][:, np.lexsort(rb["detp"][::-1])]
             assert np.array_equal(da, db)
+        # same deposits summed in another order: the FP32 accumulation tolerance
         fa, fb = ra["flux"].astype(np.float64), rb["flux"].astype(np.float64)
         assert abs(fa.sum() - fb.sum()) <= 1e-5 * fa.sum()
         hot = fa > np.quantile(fa, 0.99)
-        assert np.max(np.abs(fa[hot] - fb[hot]) / fa[hot]) < 1e-3
+        assert np.max(np.abs(fa[hot] - fb[hot]) / fa[hot]) < 5e-4
         assert sb["runtime"] >= 1
 
 
@@ -57,7 +58,8 @@ def test_batch_energy_balance_and_normalisation(engine):
         prop = np.asarray(cfg["prop"], np.float32)
         mua = prop[:, 0][cfg["vol"].astype(int)]
         deposited = float((r["flux"][..., 0].astype(np.float64) * mua).sum() * 5e-9)
-        assert abs(deposited - s["e_absdep"] / s["e_launch"]) <= 1e-4 * deposited
+        # FP32 field sums against the FP64 tally of the same deposits
+        assert abs(deposited - s["e_absdep"] / s["e_launch"]) <= 1e-3 * deposited
 
 
 def test_batch_rejects_repetitions(engine):

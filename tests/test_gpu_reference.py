@@ -111,3 +111,25 @@ def test_default_seeding_totals(engine, ref):
     assert abs(tot_o - tot_r) / tot_r < 0.005
     print("default seeding vs reference", parity_report(o["flux"][None], r["flux"][None], np.zeros(1, bool)),
           "absorbed", r["absorbed"], fo)
+
+
+@pytest.mark.parametrize("name,setting", [
+    ("planar", {}),
+    ("disk", {"srctype": "disk", "srcpos": [29.0, 29.0, 0.0], "srcparam1": [6.0, 0.0, 0.0, 0.0]}),
+    ("isotropic", {"srctype": "isotropic", "srcpos": [29.0, 29.0, 29.0]}),
+])
+def test_source_shapes_same_seed(engine, ref, mcx_seeding, name, setting):
+    """Area and angular sources draw their launch numbers from the photon's stream in MCX's order,
+    so in MCX seeding mode the engine and MCX simulate the same photons."""
+    def deck():
+        cfg = problems.cube60planar(1_000_000)
+        cfg.update(setting)
+        cfg["seed"] = 4711
+        return cfg
+
+    r = ref.run(deck(), keep_field=False)
+    o = engine.run(deck())
+    fo = o["stat"]["energyabs"] / o["stat"]["energytot"]
+    print(name, "absorbed reference", r["absorbed"], "engine", fo, "detected", r["detected"], o["stat"]["detected"])
+    assert abs(fo - r["absorbed"]) < 5e-5
+    assert abs(o["stat"]["detected"] - r["detected"]) <= max(10, 0.003 * r["detected"])

@@ -267,8 +267,8 @@ def test_errors_are_reported_not_faulted(engine):
     with pytest.raises(engine.MCXError):
         engine.run(cfg)
     cfg = problems.workload0(1000)
-    cfg["srctype"] = "planar"
-    with pytest.raises(engine.MCXError):
+    cfg["srctype"] = "pattern"                        # a pattern source without its pattern
+    with pytest.raises(engine.MCXError, match="srcpattern"):
         engine.run(cfg)
     # the context is still usable
     assert engine.run(problems.workload0(1000))["stat"]["n_photon"] == 1000
