@@ -112,6 +112,14 @@ void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile);
  * the same random streams as MCX itself.  The environment variable MCXG_SEEDING=mcx selects 1. */
 void mcxg_set_seeding(int mode);
 
+/* Restatement of mcx_replayinit (src/mcx_utils.c:3624-3690) for front-ends that do not link
+ * mcx_utils.c: prepares a replay (cfg->seed == SEED_FROM_FILE) from the baseline run's detected
+ * photons `detps` (dimdetps[1] records of dimdetps[0] floats, saved with savedetflag 'dp') and
+ * their seeds in cfg->replay.seed (seedbyte bytes each, compacted in place): keeps the photons of
+ * detector cfg->replaydet (all when <= 0) detected within [tstart, tend] and fills
+ * cfg->replay.weight / tof / detid and cfg->nphoton.  Returns 0 or a negative MCX error id. */
+int mcxg_replayinit(Config* cfg, const float* detps, const int dimdetps[2], int seedbyte);
+
 /* ---- Batched simulations ------------------------------------------------------------------ */
 
 /* No counterpart in MCX, whose front-ends run one mcx_run_simulation per input (src/mcx.c:62-78).

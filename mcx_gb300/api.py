@@ -19,7 +19,11 @@ import numpy as np
 from . import abi
 from ._lib import lib, libc
 
-_OUTPUT_TYPES = {"x": 0, "flux": 0, "f": 1, "fluence": 1, "e": 2, "energy": 2}
+# MCX's output-type letters (src/mcx_utils.c:150) and pmcx's long names
+_OUTPUT_TYPES = {"x": 0, "flux": 0, "f": 1, "fluence": 1, "e": 2, "energy": 2, "j": 3, "jacobian": 3, "p": 4,
+                 "nscat": 4, "m": 5, "r": 6, "l": 7, "length": 7, "s": 8, "t": 9, "b": 10}
+SEED_FROM_FILE = -999
+SEED_BYTES = 16          # xorshift128+ state saved per detected photon
 _SRC_TYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
               "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid", "ring"]
 _SAVEDET_CHARS = "dspmxvwi"      # detid, nscat, ppath, momentum, exit pos, exit dir, w0, iquv (src/mcx_utils.c)
@@ -73,11 +77,21 @@ class PreparedConfig:
         for k in _SCALARS_CHAR:
             if k in cfg:
                 setattr(c, k, bytes([int(cfg[k]) & 0xFF]))
+        self.seeds = None
         if "seed" in cfg:
             seed = cfg["seed"]
             if isinstance(seed, np.ndarray) or isinstance(seed, (list, tuple)):
-                raise MCXError(-6, "photon replay is not supported by the GB300 engine")
-            c.seed = int(seed)
+                # replay: the seeds pmcx returns, (16, n) uint8 -- one column per detected photon
+                sd = np.asarray(seed, dtype=np.uint8)
+                if sd.ndim == 2 and sd.shape[0] == SEED_BYTES and sd.shape[1] != SEED_BYTES:
+                    sd = sd.T
+                # a private copy: mcxg_replayinit compacts it in place
+                self.seeds = np.array(sd.reshape(-1, SEED_BYTES), dtype=np.uint8, order="C", copy=True)
+                c.seed = SEED_FROM_FILE
+                c.replay.seed = self.seeds.ctypes.data
+                c.nphoton = self.seeds.shape[0]
+            else:
+                c.seed = int(seed)
         if "session" in cfg:
             c.session = str(cfg["session"]).encode()[: abi.SESSION_LEN - 1]
         if "srctype" in cfg:
@@ -139,6 +153,25 @@ class PreparedConfig:
         lib.mcxg_clear_error()
         rc = lib.mcxg_validatecfg(C.byref(c))
         _check(rc)
+        if self.seeds is not None:
+            if "detphotons" not in cfg:
+                raise MCXError(-6, "you give cfg.seed for replay, but did not specify cfg.detphotons")
+            dp = np.asarray(cfg["detphotons"], dtype=np.float32)
+            dims = (C.c_int * 2)(dp.shape[0], dp.shape[1])
+            self.detps = np.ascontiguousarray(dp.T)       # one detected record after another
+            _check(lib.mcxg_replayinit(C.byref(c), self.detps.ctypes.data_as(C.POINTER(C.c_float)), dims, SEED_BYTES))
+            # MCX allocates these with malloc; they live as long as this object
+            self._replay_bufs = (c.replay.weight, c.replay.tof, c.replay.detid)
+
+    def __del__(self):
+        # replay buffers mcxg_replayinit allocated with malloc (MCX frees them in mcx_clearcfg)
+        c = getattr(self, "c", None)
+        if c is not None and getattr(self, "seeds", None) is not None:
+            for name in ("weight", "tof", "detid"):
+                ptr = getattr(c.replay, name)
+                if ptr:
+                    libc.free(C.c_void_p(ptr))
+                    setattr(c.replay, name, None)
 
     @property
     def dims(self) -> tuple[int, int, int]:
@@ -201,11 +234,29 @@ def _attach_field(pc: PreparedConfig):
     c = pc.c
     nx, ny, nz = pc.dims
     maxgate = pc.ngates if c.maxgate == 0 else min(int(c.maxgate), pc.ngates)
+    if int(c.seed) == SEED_FROM_FILE and int(c.replaydet) == -1:
+        maxgate *= max(1, int(c.detnum))     # one block of gates per detector
     flux = None
     if c.issave2pt != b"\x00":
         flux = np.zeros(nx * ny * nz * maxgate, dtype=np.float32)
         c.exportfield = flux.ctypes.data
     return flux, maxgate
+
+
+def _take_seeds(pc: PreparedConfig):
+    """The saved seeds of the detected photons, (16, n) uint8 as pmcx returns them."""
+    c = pc.c
+    ptr = c.seeddata
+    if not ptr:
+        return None
+    n = int(c.detectedcount)
+    seeds = None
+    if n and c.issaveseed != b"\x00":
+        buf = (C.c_uint8 * (SEED_BYTES * n)).from_address(ptr)
+        seeds = np.frombuffer(buf, dtype=np.uint8).copy().reshape(n, SEED_BYTES).T
+    libc.free(C.c_void_p(ptr))
+    c.seeddata = None
+    return seeds
 
 
 def _take_detected(pc: PreparedConfig):
@@ -266,10 +317,14 @@ def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]
         _check()
     finally:
         libc.free(info)
+        seeds = _take_seeds(pc)
         detp = _take_detected(pc)
     st = abi.Stats()
     lib.mcxg_get_stats(C.byref(st))
-    return _result(pc, flux, maxgate, detp, st)
+    out = _result(pc, flux, maxgate, detp, st)
+    if seeds is not None:
+        out["seeds"] = seeds
+    return out
 
 
 def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[str, Any]], float]:
@@ -291,6 +346,8 @@ def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[s
     try:
         _check(lib.mcxg_run_batch(arr, len(pcs), int(streams), stats, C.byref(ms)))
     finally:
+        for pc in pcs:
+            _take_seeds(pc)
         dets = [_take_detected(pc) for pc in pcs]
     out = [_result(pc, f, g, d, stats[i]) for i, (pc, (f, g), d) in enumerate(zip(pcs, fields, dets))]
     return out, float(ms.value)

@@ -284,6 +284,8 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
+    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata;
+    unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     double kernel_ms = 0.0;
     int launches = 0;
     // MCX per-thread seeding: stream count, host/device seed words and the glibc random_r state
@@ -299,7 +301,8 @@ struct Session {
         labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
-        pattern.release();
+        pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
+        seeddata.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -339,7 +342,11 @@ struct Session {
         const size_t per_gate = nvox * (use64 ? sizeof(double) : 2 * sizeof(float)) + nvox * sizeof(float);
         const size_t budget = freeb > (size_t)(1u << 30) ? freeb - (size_t)(1u << 30) : freeb / 2;
         if ((size_t)maxgate * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / per_gate));
-        fieldlen = nvox * (size_t)maxgate;
+        // a replay of every detector at once keeps one block of gates per detector
+        // (src/mcx_core.cu:2907-2913)
+        blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
+        if ((size_t)maxgate * blocks * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / (per_gate * blocks)));
+        fieldlen = nvox * (size_t)maxgate * blocks;
 
         // labels: upload the uint32 volume, pack to one byte per voxel on the device
         {
@@ -370,8 +377,6 @@ struct Session {
         k.doreflect = cfg->isreflect ? 1 : 0;
         k.save2pt = cfg->issave2pt ? 1 : 0;
         k.outputtype = cfg->outputtype;
-        if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
-            MCXG_RAISE(-6, "the GB300 engine supports flux, fluence and energy outputs");
         k.minenergy = cfg->minenergy;
         k.gscatter = (float)cfg->gscatter;
         k.maxvoidstep = (float)cfg->maxvoidstep;
@@ -404,6 +409,27 @@ struct Session {
         fill_source(k, cfg, pattern.as<float>());
         k.step_cap = 20000000u;   // a photon longer than this is a fault: flagged and stopped
 
+        // photon replay (MCX's SEED_FROM_FILE, prepared by mcx_replayinit) and seed saving
+        k.replay = (cfg->seed == kSEED_FROM_FILE) ? 1 : 0;
+        k.replaydet = cfg->replaydet;
+        k.detnum = (int)cfg->detnum;
+        if (k.replay) {
+            const size_t n = (size_t)cfg->nphoton;
+            replay_seed.alloc(n * kSeedBytes, stream);
+            replay_w.alloc(n * sizeof(float), stream);
+            replay_tof.alloc(n * sizeof(float), stream);
+            replay_detid.alloc(n * sizeof(int), stream);
+            CK(cudaMemcpyAsync(replay_seed.p, cfg->replay.seed, n * kSeedBytes, cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(replay_w.p, cfg->replay.weight, n * sizeof(float), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(replay_tof.p, cfg->replay.tof, n * sizeof(float), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(replay_detid.p, cfg->replay.detid, n * sizeof(int), cudaMemcpyHostToDevice, stream));
+            k.replay_seed = replay_seed.as<unsigned long long>();
+            k.replay_w = replay_w.as<float>();
+            k.replay_tof = replay_tof.as<float>();
+            k.replay_detid = replay_detid.as<int>();
+        }
+        k.saveseed = (cfg->issaveseed && savedet) ? 1 : 0;
+
         // output and scratch buffers
         field.alloc(fieldlen * sizeof(float), stream);
         outbuf.alloc(fieldlen * sizeof(float), stream);
@@ -412,6 +438,10 @@ struct Session {
         if (savedet) {
             detp.alloc((size_t)k.maxdet * k.reclen * sizeof(float), stream);
             detcount.alloc(sizeof(unsigned), stream);
+        }
+        if (k.saveseed) {
+            seeddata.alloc((size_t)k.maxdet * kSeedBytes, stream);
+            k.seeddata = seeddata.as<unsigned long long>();
         }
         energy.alloc(sizeof(double) * kNumEnergy, stream);
         counters.alloc(sizeof(unsigned long long) * kNumCounters, stream);
@@ -485,11 +515,11 @@ struct Session {
         set_transport_variant((o.blocks_per_sm > 0 && o.blocks_per_sm <= 3) ? 3 : 4);
         choose_tile(cfg, o.tile);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
         }
         if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
         if (o.blocks_per_sm > 0) bps = std::min(bps, o.blocks_per_sm);
@@ -544,11 +574,11 @@ struct Session {
     void apply_tile(int kb) {
         choose_tile(nullptr, kb);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, kp.srctype != kSrcPencil, block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
         }
         grid = std::max(1, bps) * sms;
     }
@@ -760,7 +790,14 @@ namespace {
 
 // Settings every run path rejects (MCX error ids).
 void check_config(const Config* cfg) {
-    if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "photon replay is not supported by the GB300 engine");
+    if (cfg->seed == kSEED_FROM_FILE &&
+        !(cfg->replay.seed && cfg->replay.weight && cfg->replay.tof && cfg->replay.detid))
+        MCXG_RAISE(-6, "a replay needs the detected photons' seeds, weights, times of flight and detector ids (mcx_replayinit)");
+    const int ot = cfg->outputtype;
+    if (ot == otRF || ot == otRFmus) MCXG_RAISE(-6, "frequency-domain (RF) replay outputs are not supported by the GB300 engine");
+    if ((ot == otJacobian || ot == otWP || ot == otDCS || ot == otWLTOF || ot == otWPTOF) && cfg->seed != kSEED_FROM_FILE)
+        MCXG_RAISE(-6, "the Jacobian and scattering-count outputs need a replay run (seed from the detected photons)");
+    if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
     if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media are supported by the GB300 engine");
     if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
@@ -770,10 +807,12 @@ void check_config(const Config* cfg) {
 // Output buffers and counters of a run, as mcx_run_simulation leaves them before its first
 // launch (src/mcx_core.cu:2907-2921): exportfield is accumulated into, exportdetected grows.
 void begin_outputs(Config* cfg, const Session& S) {
-    if (cfg->exportfield == nullptr && cfg->issave2pt)
-        cfg->exportfield = (float*)calloc(S.nvox * (size_t)S.kp.maxgate, sizeof(float));
+    if (cfg->exportfield == nullptr && cfg->issave2pt) cfg->exportfield = (float*)calloc(S.fieldlen, sizeof(float));
     if (cfg->exportdetected == nullptr)
         cfg->exportdetected = (float*)malloc((size_t)S.kp.reclen * std::max(1u, cfg->maxdetphoton) * sizeof(float));
+    if (S.kp.saveseed && cfg->seeddata == nullptr)
+        cfg->seeddata = malloc((size_t)std::max(1u, cfg->maxdetphoton) * kSeedBytes);
+    cfg->his.seedbyte = S.kp.saveseed ? (unsigned)kSeedBytes : 0u;
     cfg->detectedcount = 0;
     cfg->his.detected = 0;
     cfg->his.respin = cfg->respin;
@@ -803,6 +842,11 @@ void append_detected(Config* cfg, Session& S) {
         cfg->exportdetected = (float*)realloc(cfg->exportdetected, (cfg->detectedcount + keep) * (size_t)reclen * sizeof(float));
         CK(cudaMemcpyAsync(cfg->exportdetected + cfg->detectedcount * reclen, S.detp.p, (size_t)keep * reclen * sizeof(float),
                            cudaMemcpyDeviceToHost, S.stream));
+        if (S.kp.saveseed && cfg->seeddata) {      // the seeds of the same photons (src/mcx_core.cu:3628-3655)
+            cfg->seeddata = realloc(cfg->seeddata, (cfg->detectedcount + keep) * kSeedBytes);
+            CK(cudaMemcpyAsync((char*)cfg->seeddata + cfg->detectedcount * kSeedBytes, S.seeddata.p, (size_t)keep * kSeedBytes,
+                               cudaMemcpyDeviceToHost, S.stream));
+        }
         CK(cudaStreamSynchronize(S.stream));
         cfg->detectedcount += keep;
     }
@@ -828,22 +872,50 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
     if (cfg->issave2pt) {
         // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
         float scale = 1.f;
+        std::vector<float> block_scale;         // all-detector replay: one scale per detector block
+        const int ot = cfg->outputtype;
+        const bool path_units = (ot == otJacobian || ot == otRF || ot == otWLTOF);
         if (cfg->isnormalized && st.e_launch > 0.0) {
             const double Vvox = (double)cfg->steps.x * cfg->steps.y * cfg->steps.z;
-            if (cfg->outputtype == otFlux || cfg->outputtype == otFluence) {
+            if (ot == otFlux || ot == otFluence) {
                 double sc = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
-                if (cfg->outputtype == otFluence) sc *= cfg->tstep;
+                if (ot == otFluence) sc *= cfg->tstep;
                 scale = (float)sc;
-            } else {
+            } else if (ot == otEnergy || ot == otL) {
                 scale = (float)(1.0 / cfg->energytot);
+            } else if (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) {
+                // each detector's block over its replayed weight; paths carry unitinmm
+                for (unsigned d = 1; d <= S.blocks; d++) {
+                    float sd = path_units ? cfg->unitinmm : 1.f;
+                    if (cfg->isnormalized != 2) {
+                        double sum = 0.0;
+                        for (size_t i = 0; i < (size_t)cfg->nphoton; i++)
+                            if ((unsigned)(cfg->replay.detid[i] & 0xFFFF) == d) sum += cfg->replay.weight[i];
+                        sd = (sum > 0.0) ? (float)((path_units ? cfg->unitinmm : 1.0) / sum) : 0.f;
+                    }
+                    block_scale.push_back(sd);
+                }
+                scale = block_scale.empty() ? 1.f : block_scale.back();
+            } else {
+                double sum = 0.0;
+                for (size_t i = 0; i < (size_t)cfg->nphoton; i++) sum += cfg->replay.weight[i];
+                scale = (sum > 0.0) ? (float)(cfg->unitinmm / sum) : 0.f;
             }
             cfg->normalizer = scale;
             cfg->his.normalizer = scale;
         }
         host_field.resize(S.fieldlen);
-        S.read_field(host_field.data(), scale, cfg->isnormalized == 2);
+        S.read_field(host_field.data(), block_scale.empty() ? scale : 1.f, cfg->isnormalized == 2);
         float* out = cfg->exportfield;
-        for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
+        if (block_scale.empty()) {
+            for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
+        } else {
+            const size_t per = S.fieldlen / S.blocks;
+            for (size_t i = 0; i < S.fieldlen; i++) {
+                const float v = host_field[i];
+                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * block_scale[i / per];
+            }
+        }
     }
 }
 

@@ -17,6 +17,7 @@ constexpr float    kR_C0      = 3.335640951981520e-12f;   // 1/c in s/mm
 constexpr float    kTWO_PI    = 6.28318530717959f;
 constexpr int      kSEED_FROM_FILE = -999;
 constexpr int      kFILL_MAXDETPHOTON = 3;
+constexpr size_t   kSeedBytes = 16;                      // saved generator state per photon: RAND_BUF_LEN x 8 B
 
 // Engine limits.  The GB300 engine keeps one byte per voxel: bit 7 is the detector mask and
 // bits 0-6 the medium label, so a run may use at most 128 property rows (labels 0..127).

@@ -79,7 +79,9 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     k.save2pt = cfg->issave2pt ? 1 : 0;
     k.outputtype = cfg->outputtype;
     if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
-        MCXG_RAISE(-6, "the GB300 engine supports flux, fluence and energy outputs");
+        MCXG_RAISE(-6, "the allocation-free entry point supports flux, fluence and energy outputs");
+    if (cfg->seed == kSEED_FROM_FILE || cfg->issaveseed)
+        MCXG_RAISE(-6, "the allocation-free entry point runs no replay and saves no seeds");
     k.minenergy = cfg->minenergy;
     k.gscatter = (float)cfg->gscatter;
     k.maxvoidstep = (float)cfg->maxvoidstep;
@@ -154,7 +156,7 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
 
     const int block = 256;
     const size_t smem = transport_smem_bytes(k, block, savedet);
-    const int bps = transport_blocks_per_sm(reflect, savedet, k.srctype != kSrcPencil, block, smem);
+    const int bps = transport_blocks_per_sm(reflect, savedet, transport_general(k), block, smem);
     if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
     int sms = 0;
     NCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));

@@ -9,8 +9,8 @@
 //   mcxg_validatecfg  <- mcx_validatecfg    src/mcx_utils.c:3748-3857 (origin shift, time gates)
 //                        mcx_preprocess     src/mcx_utils.c:1525-1820 (direction, media, launch voxel)
 //   mcxg_maskdet      <- mcx_maskdet        src/mcx_utils.c:4214-4340 (label-media branch)
-// Out of this restatement (and rejected by the engine): replay/seed files, polarised and
-// split-voxel media, pattern and extra sources, shapes/JSON parsing.
+// Out of this restatement (and rejected by the engine): seed files, polarised and
+// split-voxel media, extra sources, shapes/JSON parsing.
 
 #include <cmath>
 #include <cstdlib>
@@ -144,7 +144,13 @@ extern "C" void mcxg_maskdet(Config* cfg) {
 namespace {
 
 void validate(Config* cfg) {
-    if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "photon replay is not supported by the GB300 engine");
+    // replay of saved photons (src/mcx_utils.c:1651-1664)
+    if (cfg->seed == kSEED_FROM_FILE && (cfg->respin > 1 || cfg->respin < 0)) {
+        cfg->respin = 1;
+        if (cfg->flog) fprintf(cfg->flog, "WARNING: respin is disabled in the replay mode\n");
+    }
+    if (cfg->replaydet > (int)cfg->detnum) MCXG_RAISE(-4, "replay detector ID exceeds the maximum detector number");
+    if (cfg->replaydet == -1 && cfg->detnum == 1) cfg->replaydet = 1;
     if (cfg->polprop || cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
     if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
 
@@ -161,7 +167,7 @@ void validate(Config* cfg) {
     if (cfg->steps.x == 0.f || cfg->steps.y == 0.f || cfg->steps.z == 0.f) MCXG_RAISE(-6, "field 'steps' can not have zero elements");
     const int gates = (int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5f);
     if ((int)cfg->maxgate > gates) cfg->maxgate = gates;
-    if (cfg->seed < 0) cfg->seed = (int)time(nullptr);
+    if (cfg->seed < 0 && cfg->seed != kSEED_FROM_FILE) cfg->seed = (int)time(nullptr);
 
     // mcx_preprocess (src/mcx_utils.c:1525-1820), label-media subset
     double len = std::sqrt((double)cfg->srcdir.x * cfg->srcdir.x + (double)cfg->srcdir.y * cfg->srcdir.y +
@@ -254,6 +260,58 @@ void validate(Config* cfg) {
 }
 
 }  // namespace
+
+// mcx_replayinit (src/mcx_utils.c:3624-3690): keep the detected photons of detector `replaydet`
+// (all when <= 0) whose time of flight lies in [tstart, tend], with their seeds, detected weight
+// exp(-sum mua_m ppath_m), time of flight sum ppath_m n_m / c0 and detector id.  detps holds
+// dimdetps[1] records of dimdetps[0] floats (savedetflag with D and P); seeds arrive in
+// cfg->replay.seed, seedbyte bytes per photon, and are compacted in place.  Sets nphoton.
+extern "C" int mcxg_replayinit(Config* cfg, const float* detps, const int dimdetps[2], int seedbyte) {
+    mcxg_clear_error();
+    try {
+        if (cfg->seed != kSEED_FROM_FILE) return 0;
+        if (!detps) MCXG_RAISE(-6, "a replay needs the detected photons of the baseline run (detphotons)");
+        if ((uint64_t)cfg->nphoton != (uint64_t)dimdetps[1]) MCXG_RAISE(-6, "the column numbers of detphotons and seed do not match");
+        if (seedbyte == 0 || !cfg->replay.seed) MCXG_RAISE(-6, "the seed input is empty");
+        const unsigned f = cfg->savedetflag;
+        const int hasdetid = (int)(f & 0x1u);
+        const int offset = (int)((f >> 1) & 1u) * ((int)cfg->medianum - 1);
+        if ((!hasdetid && cfg->detnum > 1) || !((f >> 2) & 1u))
+            MCXG_RAISE(-6, "please rerun the baseline simulation and save detector ID (D) and partial-path (P) using cfg.savedetflag='dp'");
+        const int n = dimdetps[1], rec = dimdetps[0];
+        free(cfg->replay.weight);
+        free(cfg->replay.tof);
+        free(cfg->replay.detid);
+        cfg->replay.weight = (float*)malloc(std::max(1, n) * sizeof(float));
+        cfg->replay.tof = (float*)calloc(std::max(1, n), sizeof(float));
+        cfg->replay.detid = (int*)calloc(std::max(1, n), sizeof(int));
+        int kept = 0;
+        char* seeds = (char*)cfg->replay.seed;
+        for (int i = 0; i < n; i++) {
+            const float* r = detps + (size_t)i * rec;
+            const int id = hasdetid ? (int)r[0] : 1;
+            if (cfg->replaydet > 0 && cfg->replaydet != (id & 0xFFFF)) continue;
+            float w = 1.f, tof = 0.f;
+            for (int j = hasdetid; j < (int)cfg->medianum - 1 + hasdetid; j++) {
+                float plen = r[offset + j];
+                w *= expf(-cfg->prop[j - hasdetid + 1].mua * plen);
+                plen *= cfg->unitinmm;
+                tof += plen * kR_C0 * cfg->prop[j - hasdetid + 1].n;
+            }
+            if (tof < cfg->tstart || tof > cfg->tend) continue;
+            if (i != kept) std::memmove(seeds + (size_t)kept * seedbyte, seeds + (size_t)i * seedbyte, seedbyte);
+            cfg->replay.weight[kept] = w;
+            cfg->replay.tof[kept] = tof;
+            cfg->replay.detid[kept] = id;
+            kept++;
+        }
+        cfg->nphoton = kept;
+        return 0;
+    } catch (const Error& e) {
+        mcxg_set_error(e.id, e.msg.c_str());
+        return e.id ? e.id : -1;
+    }
+}
 
 extern "C" int mcxg_validatecfg(Config* cfg) {
     mcxg_clear_error();

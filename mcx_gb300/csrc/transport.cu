@@ -464,10 +464,14 @@ struct Smem {
     int* nscat0;                  // per thread, detector runs: nscat at the last change of medium
     float* tally;                 // kNumEnergy x blockDim, FP32 per-thread partial sums
     float* ppath;                 // partialdata x blockDim (detector runs)
+    unsigned long long* seed0;    // 2 x blockDim, general variant: generator state at launch
+    float* rw;                    // per thread, replay: detected weight of the photon
+    float* rtof;                  // per thread, replay: its time of flight
+    int* rbin;                    // per thread, replay: its field block (gate + detector offset), -1 none
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
-template <bool SAVEDET>
+template <bool SAVEDET, bool GENERAL>
 __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     Smem s;
     const unsigned warps = blockDim.x >> 5;
@@ -482,6 +486,14 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     s.tally = s.wlaunch + blockDim.x;
     s.ppath = s.tally + kNumEnergy * blockDim.x;
     float* end = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
+    if (GENERAL) {
+        // 8-byte aligned: everything before is a multiple of 4 bytes
+        s.seed0 = reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(end) + 7u) & ~uintptr_t(7));
+        s.rw = reinterpret_cast<float*>(s.seed0 + 2 * blockDim.x);
+        s.rtof = s.rw + blockDim.x;
+        s.rbin = reinterpret_cast<int*>(s.rtof + blockDim.x);
+        end = reinterpret_cast<float*>(s.rbin + blockDim.x);
+    }
     s.tile = reinterpret_cast<unsigned*>(end);
     return s;
 }
@@ -502,10 +514,11 @@ __device__ __forceinline__ void flush_segment(const KParams& P, const Smem& S, i
 }
 
 // MINB: CTAs of 256 threads the register budget is sized for (4 -> 64 registers, 3 -> 85).
-template <bool REFLECT, bool SAVEDET, int MINB, bool AREA>
+// GENERAL: per-photon source sampling, replay, seed saving and the replay / path-length outputs.
+template <bool REFLECT, bool SAVEDET, int MINB, bool GENERAL>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const Smem S = carve<SAVEDET>(P, smem_raw);
+    const Smem S = carve<SAVEDET, GENERAL>(P, smem_raw);
     const int tid = threadIdx.x;
     const int B = blockDim.x;
     const unsigned lane = tid & 31u;
@@ -608,7 +621,23 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.pool[2 * warp + 1] = pool_end;
                 }
                 if (!alive && !start && mine < P.d_nwork) {
-                    if (P.seed_mode == 1) {
+                    if (GENERAL && P.replay) {
+                        // a detected photon again: its saved launch state and detection record
+                        // (src/mcx_core.cu:1203-1211)
+                        r0 = __ldg(P.replay_seed + 2 * mine);
+                        r1 = __ldg(P.replay_seed + 2 * mine + 1);
+                        const float tof = __ldg(P.replay_tof + mine);
+                        int bin = (int)floorf((tof - P.twin0) * P.Rtstep);
+                        if (bin < 0 || bin >= P.maxgate) {
+                            bin = -1;           // detected outside this gate group: nothing to add
+                        } else if (P.replaydet == -1) {
+                            bin += ((__ldg(P.replay_detid + mine) & 0xFFFF) - 1) * P.maxgate;
+                        }
+                        S.rw[tid] = __ldg(P.replay_w + mine);
+                        S.rtof[tid] = tof;
+                        S.rbin[tid] = bin;
+                        start = true;
+                    } else if (P.seed_mode == 1) {
                         // MCX's per-thread stream `mine`: four host seed words
                         // (src/mcx_rand_xorshift128p.cu:79-82), then its share of photons in sequence
                         const unsigned cnt = P.mcx_per + ((unsigned)mine < P.mcx_odd ? 1u : 0u);
@@ -625,6 +654,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     }
                 }
             }
+            if (GENERAL && start && P.saveseed) {      // state at launch (src/mcx_core.cu:1213-1215)
+                S.seed0[2 * tid] = r0;
+                S.seed0[2 * tid + 1] = r1;
+            }
             bool entered = false;
             if (start && P.srctype == kSrcPencil) {
                 // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
@@ -637,7 +670,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 det = (P.src_label & kLabelDet) != 0u;
                 fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
                 entered = true;
-            } else if (AREA && start) {
+            } else if (GENERAL && start) {
                 Launch L;
                 entered = launch_source(P, r0, r1, L);
                 if (entered) {
@@ -713,6 +746,18 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
                     S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
                 }
+                if (GENERAL && P.replay &&
+                    (P.outputtype == kOutWP || P.outputtype == kOutDCS || P.outputtype == kOutWPTOF)) {
+                    // replay outputs at scattering events (src/mcx_core.cu:2018-2066): detected weight
+                    // x (1, momentum transfer 1 - cos, or time of flight) in the current voxel
+                    const int rb = S.rbin[tid];
+                    if (rb >= 0) {
+                        float q = S.rw[tid];
+                        if (P.outputtype == kOutDCS) q *= 1.f - ct;
+                        else if (P.outputtype == kOutWPTOF) q *= S.rtof[tid];
+                        field_add_small(P, (size_t)idx + (size_t)rb * P.nvox, q);
+                    }
+                }
                 rotate(vx, vy, vz, st, ct, sphi, cphi);
                 nscat++;
                 rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
@@ -785,10 +830,22 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             // deposit into the voxel just left, time bin taken at exit (2191-2292)
             bool rec = false;
             if (P.save2pt && t >= tw0 && t < tw1) {
-                const int tshift = (P.maxgate > 1) ? min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b))) : 0;
+                int tshift = (P.maxgate > 1) ? min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b))) : 0;
                 float weight;
-                if (P.outputtype == 2) weight = w0 - w;
-                else weight = (pr.x < kEPS) ? (w0 * pathlen) : __fdividef(w0 - w, pr.x);
+                if (P.outputtype == kOutEnergy) {
+                    weight = w0 - w;
+                } else if (!GENERAL || P.outputtype <= kOutFluence) {
+                    weight = (pr.x < kEPS) ? (w0 * pathlen) : __fdividef(w0 - w, pr.x);
+                } else if (P.outputtype == kOutL) {
+                    weight = w0 * pathlen;                  // total path length per voxel
+                } else if (P.replay && (P.outputtype == kOutJacobian || P.outputtype == kOutWLTOF)) {
+                    // mua Jacobian: detected weight x path in the voxel (x time of flight)
+                    const int rb = S.rbin[tid];
+                    weight = (rb < 0) ? 0.f : S.rw[tid] * pathlen * (P.outputtype == kOutWLTOF ? S.rtof[tid] : 1.f);
+                    tshift = rb;
+                } else {
+                    weight = 0.f;                           // scattering-event outputs (below)
+                }
                 if (weight != 0.f) {
                     rec = true;
                     c_dep++;
@@ -925,6 +982,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (detid) {
                     detected = true;
                     const unsigned slot = atomicAdd(P.detcount, 1u);
+                    if (GENERAL && P.saveseed && slot < P.maxdet) {    // src/mcx_core.cu:375-377
+                        P.seeddata[2 * slot] = S.seed0[2 * tid];
+                        P.seeddata[2 * slot + 1] = S.seed0[2 * tid + 1];
+                    }
                     if (slot < P.maxdet) {
                         float* rec = P.detp + (size_t)slot * P.reclen;
                         unsigned k = 0;
@@ -1051,6 +1112,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
+    if (transport_general(p)) b += 8 + (2 * sizeof(unsigned long long) + 3 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1063,8 +1125,12 @@ static int g_minb = 4;   // register budget of the variant launched (set by the 
 void set_transport_variant(int minb) { g_minb = (minb == 3) ? 3 : 4; }
 int transport_variant() { return g_minb; }
 
-// Pencil sources run the variants without the per-photon source sampling; the others run the
-// variants with it, at the larger register budget its launch code needs.
+bool transport_general(const KParams& p) {
+    return p.srctype != kSrcPencil || p.replay || p.saveseed || p.outputtype > kOutEnergy;
+}
+
+// Pencil-beam flux/fluence/energy runs use the variants without the general launch; the others
+// use the general variants, at the larger register budget their launch code needs.
 static const void* pick(bool reflect, bool savedet, bool area) {
     if (area) {
         if (reflect) return savedet ? kernel_ptr<true, true, 3, true>() : kernel_ptr<true, false, 3, true>();
@@ -1088,8 +1154,9 @@ int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, si
 
 void place_tile(KParams& k, int kb) {
     k.tile_on = 0;
-    // area sources spread their deposits: only point sources get a tile
-    if (!k.save2pt || !k.src_ok || !src_is_point(k.srctype)) return;
+    // area sources spread their deposits: only point sources get a tile; replay and path-length
+    // outputs add other quantities than the absorbed weight the tile's scale is sized for
+    if (!k.save2pt || !k.src_ok || !src_is_point(k.srctype) || k.replay || k.outputtype > kOutEnergy) return;
     const int elems = kb * 1024 / (int)sizeof(unsigned);
     int tg = std::min(k.maxgate, 4);
     int edge = 1;
@@ -1127,7 +1194,7 @@ static KParams finalize(const KParams& in) {
     p.d_tx1 = (float)(p.tx0 + p.tnx); p.d_ty1 = (float)(p.ty0 + p.tny); p.d_tz1 = (float)(p.tz0 + p.tnz);
     p.d_n0 = p.prop[0].w;
     p.d_gscat = (p.gscatter >= 2147483647.f) ? 2147483647 : (int)p.gscatter;
-    p.d_nwork = (p.seed_mode == 1) ? (unsigned long long)p.mcx_streams : p.nphoton;
+    p.d_nwork = (p.seed_mode == 1 && !p.replay) ? (unsigned long long)p.mcx_streams : p.nphoton;
     // 2^21 fixed-point units per launch weight: a deposit is at most sqrt(3) launch weights (a
     // voxel diagonal), so weight x scale stays below 2^23 as the rounding trick needs
     p.d_tile_scale = 2097152.f / fmaxf(1.f, fabsf(p.src_p.w));
@@ -1140,7 +1207,7 @@ static KParams finalize(const KParams& in) {
 cudaError_t launch_transport(const KParams& in, bool reflect, bool savedet, int grid, int block, size_t smem_bytes,
                              cudaStream_t stream) {
     const KParams p = finalize(in);
-    const void* k = pick(reflect, savedet, p.srctype != kSrcPencil);
+    const void* k = pick(reflect, savedet, transport_general(p));
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e != cudaSuccess) return e;
     void* args[] = {const_cast<KParams*>(&p)};

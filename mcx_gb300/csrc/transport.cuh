@@ -21,6 +21,10 @@ enum SrcType : int {
 };
 // Launch-direction options of area sources, from srcdir.w (src/mcx_core.cu:1672-1710): 0 =
 // along srcdir, a finite value = focal length, NaN = isotropic, -inf = Lambertian.
+// MCX's output types (src/mcx_utils.h:70).
+enum OutputType : int {
+    kOutFlux = 0, kOutFluence, kOutEnergy, kOutJacobian, kOutWP, kOutDCS, kOutRF, kOutL, kOutRFmus, kOutWLTOF, kOutWPTOF
+};
 enum FocusMode : int { kFocusNone = 0, kFocusLength, kFocusIsotropic, kFocusLambertian };
 // Point sources: the launch voxel is the host's (srcparam2.z/.w after preprocessing).
 __host__ __device__ constexpr bool src_is_point(int t) {
@@ -68,6 +72,17 @@ struct KParams {
     int src_focus;                  // kFocus*: what srcdir.w asks of the area sources
     const float* srcpattern;        // pattern (param1.w x param2.w) or pattern3d intensities
     int isspecular, voidtime;
+
+    // --- seed saving and photon replay (src/mcx_core.cu:375-377, 1203-1215, 2018-2066, 2207-2226)
+    int saveseed;                   // store each detected photon's generator state at launch
+    unsigned long long* seeddata;   // maxdet x 2 words (xorshift128+ state)
+    int replay;                     // photons start from saved states (MCX's SEED_FROM_FILE)
+    const unsigned long long* replay_seed;  // nphoton x 2 words
+    const float* replay_w;          // detected weight of each replayed photon
+    const float* replay_tof;        // its time of flight (s)
+    const int* replay_detid;        // its detector id
+    int replaydet;                  // -1: one field block of maxgate gates per detector
+    int detnum;
 
     // --- time gates
     float twin0, twin1, Rtstep, oneoverc0;
@@ -146,6 +161,9 @@ void set_transport_variant(int minb);
 int transport_variant();
 // Shared memory the kernel needs for a given block size and parameter set.
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
+// The kernel variant with per-photon source sampling, replay, seed saving and the replay and
+// path-length outputs; the pencil-beam flux/fluence/energy runs use the leaner one.
+bool transport_general(const KParams& p);
 // Occupancy-derived CTAs per SM for the chosen variant.
 int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, size_t smem_bytes);
 

@@ -130,3 +130,34 @@ def test_label_range_checked_on_host(engine):
     cfg["vol"] = (cfg["vol"] * 5).astype(np.uint8)
     with pytest.raises(engine.MCXError, match="labels"):
         engine.prepare(cfg)
+
+
+def test_replayinit_filters_and_weights(engine):
+    """mcxg_replayinit (restating src/mcx_utils.c:3624-3690) on hand-made records."""
+    import ctypes as C
+
+    from mcx_gb300 import problems
+
+    cfg = problems.sphere60b(10)
+    cfg.update(savedetflag="dp")
+    rng = np.random.default_rng(3)
+    n = 6
+    detp = np.zeros((3, n), np.float32)                  # detid | ppath(2)
+    detp[0] = [1, 2, 3, 2, 4, 2]
+    detp[1] = rng.uniform(1, 50, n)
+    detp[2] = rng.uniform(0, 20, n)
+    detp[1, 5] = 5000.0                                  # time of flight beyond the 5 ns window
+    seeds = np.arange(16 * n, dtype=np.uint8).reshape(n, 16).T
+    cfg.update(seed=seeds, detphotons=detp, replaydet=2)
+    pc = engine.prepare(cfg)
+    c = pc.c
+    assert c.nphoton == 2 and c.seed == -999             # detector 2, in time: records 1 and 3
+    w = np.frombuffer((C.c_float * 2).from_address(c.replay.weight), np.float32)
+    tof = np.frombuffer((C.c_float * 2).from_address(c.replay.tof), np.float32)
+    mua = np.asarray(cfg["prop"], np.float32)[1:, 0]
+    nidx = np.asarray(cfg["prop"], np.float32)[1:, 3]
+    for k, i in enumerate((1, 3)):
+        assert abs(w[k] - np.exp(-(mua * detp[1:, i]).sum())) < 1e-6
+        assert abs(tof[k] - (detp[1:, i] * nidx).sum() * 3.335640951981520e-12) < 1e-15
+    got = np.frombuffer((C.c_uint8 * 32).from_address(c.replay.seed), np.uint8).reshape(2, 16)
+    assert np.array_equal(got, seeds.T[[1, 3]])
