@@ -859,6 +859,8 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
     S.read_stats(&st);
     if (st.error_flags & kErrStepCap)
         MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
+    if (st.error_flags & kErrIndex)
+        MCXG_RAISE(-6, "internal error: a photon's voxel index left the volume; the photon was stopped");
     total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
     total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
     total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include "transport.cuh"
 
@@ -129,6 +130,7 @@ __device__ int find_detector(const KParams& P, float px, float py, float pz) {
 struct Launch {
     float px, py, pz, w, vx, vy, vz, t;
     unsigned idx, label;
+    int ix, iy, iz;             // integer coordinates of voxel idx (the position may sit on its face)
 };
 
 // src/mcx_core.cu:552-570 (reflectcoeff): unpolarised Fresnel reflectance at a face normal to
@@ -188,6 +190,9 @@ __device__ int skip_void(const KParams& P, Launch& L) {
                 L.w *= 1.f - reflect_coeff(L.vx, L.vy, L.vz, n0, n2, axis);
                 if (L.w > kEPS) transmit(L.vx, L.vy, L.vz, n0, n2, axis);
             }
+            // the entry voxel as the search found it: the position lies on its face, possibly a
+            // rounding error outside, so the photon's voxel coordinates are these, not floor(p)
+            L.ix = fx; L.iy = fy; L.iz = fz;
             return (int)((unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx);
         }
         if ((L.px < 0.f && L.vx <= 0.f) || (L.px >= P.d_fnx && L.vx >= 0.f) || (L.py < 0.f && L.vy <= 0.f) ||
@@ -408,11 +413,14 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
         unsigned lab = 0u;
         if (located) {
             L.idx = P.src_idx;
+            L.ix = P.src_fx; L.iy = P.src_fy; L.iz = P.src_fz;
             lab = P.src_label;
         } else {
             const int fx = (int)floorf(L.px), fy = (int)floorf(L.py), fz = (int)floorf(L.pz);
-            if (L.px >= 0.f && L.py >= 0.f && L.pz >= 0.f && L.px < P.d_fnx && L.py < P.d_fny && L.pz < P.d_fnz) {
+            if (L.px >= 0.f && L.py >= 0.f && L.pz >= 0.f && L.px < P.d_fnx && L.py < P.d_fny && L.pz < P.d_fnz &&
+                in_grid(P, fx, fy, fz)) {
                 L.idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
+                L.ix = fx; L.iy = fy; L.iz = fz;
                 lab = __ldg(P.labels + L.idx);
             }
         }
@@ -513,7 +521,7 @@ __device__ __forceinline__ void flush_segment(const KParams& P, const Smem& S, i
     segp = 0.f;
 }
 
-// MINB: CTAs of 256 threads the register budget is sized for (4 -> 64 registers, 3 -> 85).
+// MINB: CTAs of 256 threads the register budget is sized for (4 -> 64 registers, 3 -> 85, 2 -> 128).
 // GENERAL: per-photon source sampling, replay, seed saving and the replay / path-length outputs.
 template <bool REFLECT, bool SAVEDET, int MINB, bool GENERAL>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
@@ -680,7 +688,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     idx = L.idx;
                     med = (int)(L.label & kLabelMask);
                     det = (L.label & kLabelDet) != 0u;
-                    fx = floorf(px); fy = floorf(py); fz = floorf(pz);
+                    fx = (float)L.ix; fy = (float)L.iy; fz = (float)L.iz;
                 }
             }
             if (entered) {
@@ -816,6 +824,14 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             inside = (c >= 0.f) && (c < lim);
             if (inside) {
                 idx = (sg > 0.f) ? idx + stride : idx - stride;
+                if (idx >= P.nvox) {
+                    // the voxel index has lost step with the coordinates: never read or write out
+                    // of the volume; the photon leaves and the host reports the error
+                    atomicOr(P.errflag, kErrIndex);
+                    inside = false;
+                }
+            }
+            if (inside) {
                 const unsigned lab = __ldg(P.labels + idx);
                 med = (int)(lab & kLabelMask);
                 det = (lab & kLabelDet) != 0u;
@@ -1131,10 +1147,24 @@ bool transport_general(const KParams& p) {
 
 // Pencil-beam flux/fluence/energy runs use the variants without the general launch; the others
 // use the general variants, at the larger register budget their launch code needs.
+// Register budget of the general variants: 2 CTAs of 256 per SM (up to 128 registers, no
+// spills) or 3 (80 registers, some spills); MCXG_GENERAL_CTAS=3 selects the latter.
+static int general_minb() {
+    static const int v = [] {
+        const char* e = std::getenv("MCXG_GENERAL_CTAS");
+        return (e && std::atoi(e) == 3) ? 3 : 2;
+    }();
+    return v;
+}
+
 static const void* pick(bool reflect, bool savedet, bool area) {
-    if (area) {
+    if (area && general_minb() == 3) {
         if (reflect) return savedet ? kernel_ptr<true, true, 3, true>() : kernel_ptr<true, false, 3, true>();
         return savedet ? kernel_ptr<false, true, 3, true>() : kernel_ptr<false, false, 3, true>();
+    }
+    if (area) {
+        if (reflect) return savedet ? kernel_ptr<true, true, 2, true>() : kernel_ptr<true, false, 2, true>();
+        return savedet ? kernel_ptr<false, true, 2, true>() : kernel_ptr<false, false, 2, true>();
     }
     if (g_minb == 3) {
         if (reflect) return savedet ? kernel_ptr<true, true, 3, false>() : kernel_ptr<true, false, 3, false>();

@@ -33,7 +33,7 @@ __host__ __device__ constexpr bool src_is_point(int t) {
 // Indices into the device FP64 energy array.
 enum Energy : int { kELaunch = 0, kEEscape, kEDetect, kEAbsDep, kEAbsOther, kNumEnergy };
 // Bits of the device error word.
-enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow = 4u };
+enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow = 4u, kErrIndex = 8u };
 
 // Everything one transport launch needs.  Passed as a __grid_constant__ kernel parameter, so
 // uniform reads come from the constant bank; the per-medium table is copied to shared memory

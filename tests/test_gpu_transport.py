@@ -272,3 +272,18 @@ def test_errors_are_reported_not_faulted(engine):
         engine.run(cfg)
     # the context is still usable
     assert engine.run(problems.workload0(1000))["stat"]["n_photon"] == 1000
+
+
+def test_path_length_output_matches_oracle(engine, oracle):
+    """Output type 'l' (src/mcx_core.cu:2221-2223): w0 x path per voxel, normalised by the
+    launched energy (src/mcx_core.cu:3837-3838); its total is the weighted path length per photon."""
+    cfg = problems.workload0(1_000_000, seed=5)
+    cfg["outputtype"] = "l"
+    g = engine.run(cfg)
+    tot_g = float(g["flux"].astype(np.float64).sum())
+    pc = engine.prepare(problems.workload0(200_000, seed=6) | {"outputtype": "l"})
+    o = oracle.run(pc, seed=6)
+    tot_o = float(o["flux"].astype(np.float64).sum())
+    assert g["stat"]["error_flags"] == 0
+    # per-photon weighted path lengths have a coefficient of variation near 1: 5 SE ~ 1.2%
+    assert abs(tot_g - tot_o) <= 0.012 * tot_o, (tot_g, tot_o)
