@@ -36,13 +36,18 @@ import numpy as np  # noqa: E402
 METRIC = "photons/ms (plain MC)"
 WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000,
                     "cube60planar": 100_000_000, "batch": 0}
-CPU_SAMPLE = {"workload0": 200_000, "workload1": 50_000, "workload2": 5_000, "cube60planar": 100_000, "batch": 20_000}
+# photons of the CPU-oracle sample per workload: about 10 s on 16 cores
+CPU_SAMPLE = {"workload0": 8_000_000, "workload1": 4_000_000, "workload2": 1_000_000, "cube60planar": 6_000_000,
+              "batch": 20_000}
 
-# Thread-level instructions per transport step (ncu smsp__thread_inst_executed.sum over the
-# kernel's own step counter) and DRAM bytes per photon (dram__bytes_read.sum + write.sum over
-# photons), from the ncu captures summarised in profiles/transport_<workload>.md.
-NCU_PER_STEP = {"workload0": None, "workload1": 288.0, "workload2": None}
-NCU_DRAM_PER_PHOTON = {"workload0": None, "workload1": None, "workload2": None}
+# Thread-level instructions per transport step (ncu smsp__inst_executed.sum x
+# smsp__thread_inst_executed_per_inst_executed.ratio over the kernel's own step counter) and
+# DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum), from one ncu capture
+# of `bench.py --workload W --photons 20000000 --steps 1 --warmup 1`.  The DRAM bytes are the
+# field's first read and its write-back: the field and labels stay in L2, so they do not grow
+# with the photon count.
+NCU_PER_STEP = {"workload0": None, "workload1": 272.0, "workload2": None}
+NCU_DRAM_PER_LAUNCH = {"workload0": None, "workload1": 41.59e6, "workload2": None}
 
 
 def _dist():
@@ -274,11 +279,11 @@ def roofline(name: str, value: float, world: int, st, f_clk: float, sms: int, at
     p_atom = atom_rate / max(glob, 1e-9) / 1e3 if atom_rate else None
     cands = [(p, b) for p, b in ((p_issue, "fp32-issue"), (p_atom, "l2-atomic")) if p]
     peak, bound = min(cands) if cands else (None, "fp32-issue")
-    dram = NCU_DRAM_PER_PHOTON.get(name)
+    dram = NCU_DRAM_PER_LAUNCH.get(name)
     return {"bound": bound, "achieved": achieved, "peak": peak, "unit": "photons/ms",
             "frac": achieved / peak if peak else None,
-            "traffic": dram * (st.n_photon / max(1, st.launches)) if dram else None,
-            "traffic_unit": "DRAM bytes per launch",
+            "traffic": dram,
+            "traffic_unit": "DRAM bytes per launch (ncu capture of a 2e7-photon launch; independent of the photon count)",
             "p_issue": p_issue, "p_atom": p_atom, "steps_per_photon": steps, "deposits_per_photon": deps,
             "global_reductions_per_photon": glob, "thread_inst_per_step": ips, "sm_clock_hz": f_clk,
             "l2_reductions_per_s": atom_rate, "peak_source": "issue: SMs x 4 x 32 x measured SM clock; "
