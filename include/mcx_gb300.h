@@ -120,6 +120,12 @@ void mcxg_set_seeding(int mode);
  * cfg->replay.weight / tof / detid and cfg->nphoton.  Returns 0 or a negative MCX error id. */
 int mcxg_replayinit(Config* cfg, const float* detps, const int dimdetps[2], int seedbyte);
 
+/* Per-photon step cap of the simulations started after the call (0 restores the default 2e7).
+ * A photon still running after that many steps (checked every 1024 steps of its GPU thread) is
+ * stopped and the run fails with MCX error -6; it guards against inputs that would keep a
+ * photon alive forever.  No counterpart in MCX. */
+void mcxg_set_step_cap(unsigned int steps);
+
 /* ---- Batched simulations ------------------------------------------------------------------ */
 
 /* No counterpart in MCX, whose front-ends run one mcx_run_simulation per input (src/mcx.c:62-78).

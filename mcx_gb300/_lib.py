@@ -53,6 +53,8 @@ lib.mcxg_photon_stream.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_float),
 lib.mcxg_photon_stream.restype = C.c_int
 lib.mcxg_replayinit.argtypes = [_CFG, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_int]
 lib.mcxg_replayinit.restype = C.c_int
+lib.mcxg_set_step_cap.argtypes = [C.c_uint]
+lib.mcxg_set_step_cap.restype = None
 lib.mcxg_run_batch.argtypes = [C.POINTER(C.POINTER(abi.Config)), C.c_int, C.c_int, C.POINTER(abi.Stats),
                                 C.POINTER(C.c_double)]
 lib.mcxg_run_batch.restype = C.c_int
@@ -88,5 +90,5 @@ EXPORTED = [
     "mcxg_rng_test", "mcxg_photon_stream", "mcxg_session_create", "mcxg_session_reset", "mcxg_session_run",
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
     "mcxg_set_seeding", "mcxg_probe_atomic_rate",
-    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit",
+    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap",
 ]

@@ -59,6 +59,10 @@ std::vector<std::pair<std::string, int>> g_tune_cache;
 // per-thread streams), 0 = per-photon streams, 1 = MCX's per-thread streams.
 int g_seeding = -1;
 
+// Per-photon step cap of new sessions (a photon longer than this is stopped and reported).
+constexpr unsigned kDefaultStepCap = 20000000u;
+unsigned g_step_cap = kDefaultStepCap;
+
 int seeding_mode() {
     std::lock_guard<std::mutex> g(g_override_mu);
     if (g_seeding < 0) {
@@ -407,7 +411,10 @@ struct Session {
             CK(cudaMemcpyAsync(pattern.p, cfg->srcpattern, npat * sizeof(float), cudaMemcpyHostToDevice, stream));
         }
         fill_source(k, cfg, pattern.as<float>());
-        k.step_cap = 20000000u;   // a photon longer than this is a fault: flagged and stopped
+        {
+            std::lock_guard<std::mutex> g(g_override_mu);
+            k.step_cap = g_step_cap;      // a photon longer than this is a fault: flagged and stopped
+        }
 
         // photon replay (MCX's SEED_FROM_FILE, prepared by mcx_replayinit) and seed saving
         k.replay = (cfg->seed == kSEED_FROM_FILE) ? 1 : 0;
@@ -515,11 +522,11 @@ struct Session {
         set_transport_variant((o.blocks_per_sm > 0 && o.blocks_per_sm <= 3) ? 3 : 4);
         choose_tile(cfg, o.tile);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, transport_mode(kp), block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, transport_mode(kp), block, smem);
         }
         if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
         if (o.blocks_per_sm > 0) bps = std::min(bps, o.blocks_per_sm);
@@ -574,11 +581,11 @@ struct Session {
     void apply_tile(int kb) {
         choose_tile(nullptr, kb);
         smem = transport_smem_bytes(kp, block, savedet);
-        int bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
+        int bps = transport_blocks_per_sm(reflect, savedet, transport_mode(kp), block, smem);
         if (bps <= 0) {
             kp.tile_on = 0;
             smem = transport_smem_bytes(kp, block, savedet);
-            bps = transport_blocks_per_sm(reflect, savedet, transport_general(kp), block, smem);
+            bps = transport_blocks_per_sm(reflect, savedet, transport_mode(kp), block, smem);
         }
         grid = std::max(1, bps) * sms;
     }
@@ -699,6 +706,11 @@ extern "C" int mcxg_get_stats(mcxg_stats* out) {
 extern "C" void mcxg_set_seeding(int mode) {
     std::lock_guard<std::mutex> g(g_override_mu);
     g_seeding = (mode == 1) ? 1 : 0;
+}
+
+extern "C" void mcxg_set_step_cap(unsigned int steps) {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    g_step_cap = steps ? steps : kDefaultStepCap;
 }
 
 extern "C" void mcxg_set_launch(int block, int blocks_per_sm, int chunk, int tile) {

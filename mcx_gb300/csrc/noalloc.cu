@@ -156,7 +156,7 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
 
     const int block = 256;
     const size_t smem = transport_smem_bytes(k, block, savedet);
-    const int bps = transport_blocks_per_sm(reflect, savedet, transport_general(k), block, smem);
+    const int bps = transport_blocks_per_sm(reflect, savedet, transport_mode(k), block, smem);
     if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
     int sms = 0;
     NCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));

@@ -479,7 +479,7 @@ struct Smem {
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
-template <bool SAVEDET, bool GENERAL>
+template <bool SAVEDET, bool FULL>
 __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     Smem s;
     const unsigned warps = blockDim.x >> 5;
@@ -494,7 +494,7 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
     s.tally = s.wlaunch + blockDim.x;
     s.ppath = s.tally + kNumEnergy * blockDim.x;
     float* end = s.ppath + (SAVEDET ? P.partialdata * blockDim.x : 0u);
-    if (GENERAL) {
+    if (FULL) {
         // 8-byte aligned: everything before is a multiple of 4 bytes
         s.seed0 = reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(end) + 7u) & ~uintptr_t(7));
         s.rw = reinterpret_cast<float*>(s.seed0 + 2 * blockDim.x);
@@ -522,11 +522,14 @@ __device__ __forceinline__ void flush_segment(const KParams& P, const Smem& S, i
 }
 
 // MINB: CTAs of 256 threads the register budget is sized for (4 -> 64 registers, 3 -> 85, 2 -> 128).
-// GENERAL: per-photon source sampling, replay, seed saving and the replay / path-length outputs.
-template <bool REFLECT, bool SAVEDET, int MINB, bool GENERAL>
+// MODE 0: pencil beam, flux / fluence / energy.  MODE 1: adds per-photon sampling of the other
+// source shapes.  MODE 2: adds replay, seed saving and the replay / path-length outputs.
+template <bool REFLECT, bool SAVEDET, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
+    constexpr bool AREA = MODE >= 1;
+    constexpr bool FULL = MODE == 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const Smem S = carve<SAVEDET, GENERAL>(P, smem_raw);
+    const Smem S = carve<SAVEDET, FULL>(P, smem_raw);
     const int tid = threadIdx.x;
     const int B = blockDim.x;
     const unsigned lane = tid & 31u;
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.pool[2 * warp + 1] = pool_end;
                 }
                 if (!alive && !start && mine < P.d_nwork) {
-                    if (GENERAL && P.replay) {
+                    if (FULL && P.replay) {
                         // a detected photon again: its saved launch state and detection record
                         // (src/mcx_core.cu:1203-1211)
                         r0 = __ldg(P.replay_seed + 2 * mine);
@@ -662,7 +665,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     }
                 }
             }
-            if (GENERAL && start && P.saveseed) {      // state at launch (src/mcx_core.cu:1213-1215)
+            if (FULL && start && P.saveseed) {      // state at launch (src/mcx_core.cu:1213-1215)
                 S.seed0[2 * tid] = r0;
                 S.seed0[2 * tid + 1] = r1;
             }
@@ -678,7 +681,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 det = (P.src_label & kLabelDet) != 0u;
                 fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
                 entered = true;
-            } else if (GENERAL && start) {
+            } else if (AREA && start) {
                 Launch L;
                 entered = launch_source(P, r0, r1, L);
                 if (entered) {
@@ -754,7 +757,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
                     S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
                 }
-                if (GENERAL && P.replay &&
+                if (FULL && P.replay &&
                     (P.outputtype == kOutWP || P.outputtype == kOutDCS || P.outputtype == kOutWPTOF)) {
                     // replay outputs at scattering events (src/mcx_core.cu:2018-2066): detected weight
                     // x (1, momentum transfer 1 - cos, or time of flight) in the current voxel
@@ -850,7 +853,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 float weight;
                 if (P.outputtype == kOutEnergy) {
                     weight = w0 - w;
-                } else if (!GENERAL || P.outputtype <= kOutFluence) {
+                } else if (!FULL || P.outputtype <= kOutFluence) {
                     weight = (pr.x < kEPS) ? (w0 * pathlen) : __fdividef(w0 - w, pr.x);
                 } else if (P.outputtype == kOutL) {
                     weight = w0 * pathlen;                  // total path length per voxel
@@ -998,7 +1001,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (detid) {
                     detected = true;
                     const unsigned slot = atomicAdd(P.detcount, 1u);
-                    if (GENERAL && P.saveseed && slot < P.maxdet) {    // src/mcx_core.cu:375-377
+                    if (FULL && P.saveseed && slot < P.maxdet) {    // src/mcx_core.cu:375-377
                         P.seeddata[2 * slot] = S.seed0[2 * tid];
                         P.seeddata[2 * slot + 1] = S.seed0[2 * tid + 1];
                     }
@@ -1128,54 +1131,42 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_general(p)) b += 8 + (2 * sizeof(unsigned long long) + 3 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) == 2) b += 8 + (2 * sizeof(unsigned long long) + 3 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
 
-template <bool R, bool D, int M, bool A>
-static const void* kernel_ptr() { return (const void*)transport_kernel<R, D, M, A>; }
+template <bool R, bool D, int M, int K>
+static const void* kernel_ptr() { return (const void*)transport_kernel<R, D, M, K>; }
 
-static int g_minb = 4;   // register budget of the variant launched (set by the launch tuner)
+static int g_minb = 4;   // register budget of the pencil variants (set by the launch tuner)
 
 void set_transport_variant(int minb) { g_minb = (minb == 3) ? 3 : 4; }
 int transport_variant() { return g_minb; }
 
-bool transport_general(const KParams& p) {
-    return p.srctype != kSrcPencil || p.replay || p.saveseed || p.outputtype > kOutEnergy;
+bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
+
+int transport_mode(const KParams& p) {
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy) return 2;
+    return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 
-// Pencil-beam flux/fluence/energy runs use the variants without the general launch; the others
-// use the general variants, at the larger register budget their launch code needs.
-// Register budget of the general variants: 2 CTAs of 256 per SM (up to 128 registers, no
-// spills) or 3 (80 registers, some spills); MCXG_GENERAL_CTAS=3 selects the latter.
-static int general_minb() {
-    static const int v = [] {
-        const char* e = std::getenv("MCXG_GENERAL_CTAS");
-        return (e && std::atoi(e) == 3) ? 3 : 2;
-    }();
-    return v;
+template <int M, int K>
+static const void* pick_flags(bool reflect, bool savedet) {
+    if (reflect) return savedet ? kernel_ptr<true, true, M, K>() : kernel_ptr<true, false, M, K>();
+    return savedet ? kernel_ptr<false, true, M, K>() : kernel_ptr<false, false, M, K>();
 }
 
-static const void* pick(bool reflect, bool savedet, bool area) {
-    if (area && general_minb() == 3) {
-        if (reflect) return savedet ? kernel_ptr<true, true, 3, true>() : kernel_ptr<true, false, 3, true>();
-        return savedet ? kernel_ptr<false, true, 3, true>() : kernel_ptr<false, false, 3, true>();
-    }
-    if (area) {
-        if (reflect) return savedet ? kernel_ptr<true, true, 2, true>() : kernel_ptr<true, false, 2, true>();
-        return savedet ? kernel_ptr<false, true, 2, true>() : kernel_ptr<false, false, 2, true>();
-    }
-    if (g_minb == 3) {
-        if (reflect) return savedet ? kernel_ptr<true, true, 3, false>() : kernel_ptr<true, false, 3, false>();
-        return savedet ? kernel_ptr<false, true, 3, false>() : kernel_ptr<false, false, 3, false>();
-    }
-    if (reflect) return savedet ? kernel_ptr<true, true, 4, false>() : kernel_ptr<true, false, 4, false>();
-    return savedet ? kernel_ptr<false, true, 4, false>() : kernel_ptr<false, false, 4, false>();
+// The pencil variants run at 4 CTAs of 256 per SM (64 registers) unless the tuner asks for 3;
+// the variants with the general launch need more registers and run at 3 (80 registers).
+static const void* pick(bool reflect, bool savedet, int mode) {
+    if (mode == 2) return pick_flags<3, 2>(reflect, savedet);
+    if (mode == 1) return pick_flags<3, 1>(reflect, savedet);
+    return (g_minb == 3) ? pick_flags<3, 0>(reflect, savedet) : pick_flags<4, 0>(reflect, savedet);
 }
 
-int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, size_t smem_bytes) {
-    const void* k = pick(reflect, savedet, area);
+int transport_blocks_per_sm(bool reflect, bool savedet, int mode, int block, size_t smem_bytes) {
+    const void* k = pick(reflect, savedet, mode);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem_bytes) != cudaSuccess) return 0;
@@ -1237,7 +1228,7 @@ static KParams finalize(const KParams& in) {
 cudaError_t launch_transport(const KParams& in, bool reflect, bool savedet, int grid, int block, size_t smem_bytes,
                              cudaStream_t stream) {
     const KParams p = finalize(in);
-    const void* k = pick(reflect, savedet, transport_general(p));
+    const void* k = pick(reflect, savedet, transport_mode(p));
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e != cudaSuccess) return e;
     void* args[] = {const_cast<KParams*>(&p)};

@@ -161,11 +161,12 @@ void set_transport_variant(int minb);
 int transport_variant();
 // Shared memory the kernel needs for a given block size and parameter set.
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
-// The kernel variant with per-photon source sampling, replay, seed saving and the replay and
-// path-length outputs; the pencil-beam flux/fluence/energy runs use the leaner one.
+// Kernel variant of a parameter set: 0 = pencil beam with flux/fluence/energy output, 1 = other
+// source shapes sampled per photon, 2 = replay, seed saving or the replay / path-length outputs.
+int transport_mode(const KParams& p);
 bool transport_general(const KParams& p);
 // Occupancy-derived CTAs per SM for the chosen variant.
-int transport_blocks_per_sm(bool reflect, bool savedet, bool area, int block, size_t smem_bytes);
+int transport_blocks_per_sm(bool reflect, bool savedet, int mode, int block, size_t smem_bytes);
 
 // Source fields of KParams from a preprocessed Config: shape parameters, the pencil's launch
 // state (void skipping traced on the host), the point sources' launch voxel.  d_pattern holds

@@ -287,3 +287,17 @@ def test_path_length_output_matches_oracle(engine, oracle):
     assert g["stat"]["error_flags"] == 0
     # per-photon weighted path lengths have a coefficient of variation near 1: 5 SE ~ 1.2%
     assert abs(tot_g - tot_o) <= 0.012 * tot_o, (tot_g, tot_o)
+
+
+def test_step_cap_stops_photons_and_reports(engine, lib):
+    """Failure detection without a GPU fault: a step cap far below what the photons need stops
+    them on the device; the kernel returns, the host reports MCX error -6, and the context keeps
+    working."""
+    try:
+        lib.mcxg_set_step_cap(100)
+        with pytest.raises(engine.MCXError, match="step cap"):
+            engine.run(problems.workload1(200_000, seed=3))
+    finally:
+        lib.mcxg_set_step_cap(0)
+    r = engine.run(problems.workload0(100_000))
+    assert r["stat"]["error_flags"] == 0 and r["stat"]["n_photon"] == 100_000
