@@ -160,3 +160,21 @@ def test_source_shapes_absorbed(engine, oracle, goldens, name):
     s = oracle.run(pc, nphoton=300_000, seed=123)["stat"]
     frac = s["energyabs"] / s["energytot"]
     assert g["lo"] <= frac < g["hi"], (name, frac, g["source"])
+
+
+def test_batch_workload_ranges():
+    """The batched workload's 256 instances follow their stated distributions (deterministic)."""
+    a = problems.batch_instances(256, budget_scale=1.0)
+    b = problems.batch_instances(256, budget_scale=1.0)
+    assert len(a) == 256
+    assert all(np.array_equal(x["vol"], y["vol"]) and x["nphoton"] == y["nphoton"] for x, y in zip(a, b))
+    edges = {x["vol"].shape[0] for x in a}
+    assert edges <= set(problems.BATCH_EDGES) and len(edges) == 5
+    for x in a:
+        prop = x["prop"]
+        assert 2 <= prop.shape[0] - 1 <= 5                        # medium 1 + 1..4 inclusions
+        assert np.all((prop[1:, 0] >= 1e-3) & (prop[1:, 0] <= 5e-2))
+        assert np.all((prop[1:, 1] >= 0.5) & (prop[1:, 1] <= 20.0))
+        assert np.all((prop[1:, 2] >= 0.7) & (prop[1:, 2] <= 0.95)) and np.all(prop[1:, 3] == np.float32(1.37))
+        assert 1e6 <= x["nphoton"] <= 1e8
+        assert x["vol"].max() <= prop.shape[0] - 1 and x["detpos"].shape == (2, 4)
