@@ -46,8 +46,8 @@ CPU_SAMPLE = {"workload0": 8_000_000, "workload1": 4_000_000, "workload2": 1_000
 # of `bench.py --workload W --photons 20000000 --steps 1 --warmup 1`.  The DRAM bytes are the
 # field's first read and its write-back: the field and labels stay in L2, so they do not grow
 # with the photon count.
-NCU_PER_STEP = {"workload0": None, "workload1": 272.0, "workload2": None}
-NCU_DRAM_PER_LAUNCH = {"workload0": None, "workload1": 41.59e6, "workload2": None}
+NCU_PER_STEP = {"workload0": 222.8, "workload1": 272.0, "workload2": None}
+NCU_DRAM_PER_LAUNCH = {"workload0": 1.63e6, "workload1": 41.59e6, "workload2": None}
 
 
 def _dist():

@@ -7,13 +7,14 @@
 // on the device before a single copy back, FP64 energy tallies, stream-ordered allocations
 // that are reused across calls.
 //
-// Config fields read: nphoton, seed, srcpos, srcdir, srcparam2 (launch voxel/label), tstart,
-// tstep, tend, steps, dim, medianum, prop, detnum, detpos, maxdetphoton, maxgate, respin,
-// vol, isreflect, isnormalized, issavedet, issave2pt, isspecular, outputtype, minenergy,
-// unitinmm, flog, maxvoidstep, voidtime, savedetflag, deviceid, parentid, gscatter, bc.
-// Config fields written: exportfield (+=), exportdetected (realloc), detectedcount, runtime,
-// energytot, energyabs, energyesc, normalizer, his.{normalizer,detected,respin,colcount,...},
-// deviceid (compacted by mcx_list_gpu).
+// Config fields read: nphoton, seed, srctype, srcpos, srcdir, srcparam1, srcparam2, srcpattern,
+// tstart, tstep, tend, steps, dim, medianum, prop, detnum, detpos, maxdetphoton, maxgate, respin,
+// vol, isreflect, isnormalized, issavedet, issaveseed, issave2pt, isspecular, outputtype,
+// minenergy, unitinmm, flog, maxvoidstep, voidtime, savedetflag, deviceid, parentid, gscatter,
+// bc, replay, replaydet.
+// Config fields written: exportfield (+=), exportdetected and seeddata (realloc), detectedcount,
+// runtime, energytot, energyabs, energyesc, normalizer, his.{normalizer,detected,respin,colcount,
+// seedbyte,...}, deviceid (compacted by mcx_list_gpu).
 
 #include <cuda_runtime.h>
 #include <algorithm>

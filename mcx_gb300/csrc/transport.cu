@@ -1,18 +1,21 @@
 // transport.cu -- the GB300 photon-transport kernel (sm_103a).
 //
-// Algorithm: MCX's voxel Monte Carlo (src/mcx_core.cu:1767-2528, pencil source, label media),
-// one photon per thread, re-organised for Blackwell:
+// Algorithm: MCX's voxel Monte Carlo (src/mcx_core.cu:1767-2528, label media) with its photon
+// launch (src/mcx_core.cu:1089-1717, every source shape), one photon per thread, re-organised
+// for Blackwell:
 //   * persistent CTAs (grid = SMs x resident CTAs) whose warps refill dead lanes from a
 //     warp-private pool of photon indices, topped up with one global atomic per `chunk`
 //     photons -- no lane waits for a slow photon of another lane to finish a static quota;
 //   * every photon owns an xorshift128+ state in registers, seeded from (seed, photon index)
-//     so results do not depend on grid shape or scheduling;
+//     so results do not depend on grid shape or scheduling (or MCX's own per-thread streams);
 //   * labels are one byte per voxel (bit 7 = detector mask) read through the read-only
-//     path; the (mua, mus, g, n) table and derived constants live in shared memory because
-//     lanes index them with divergent labels;
-//   * fluence deposits inside a per-CTA voxel x gate box (sized and placed by the host over
-//     the densest deposit region) go to a shared-memory tile and reach L2 once per CTA; the
-//     rest are fire-and-forget FP32 reductions;
+//     path; the (mua, mus, g, n) table lives in shared memory because lanes index it with
+//     divergent labels;
+//   * fluence deposits inside a per-CTA voxel x gate box over the launch point go to an exact
+//     32-bit fixed-point shared-memory tile and reach L2 once per CTA; the rest are
+//     fire-and-forget FP32 reductions;
+//   * three variants per flag set: pencil beam (mode 0), other source shapes sampled per
+//     photon (1), replay / seed saving / replay outputs (2), so each carries only its state;
 //   * FP64 is used only for the energy tallies.
 // Semantics that must match the reference step for step are annotated with its file:line.
 
