@@ -303,6 +303,8 @@ def main() -> None:
     ap.add_argument("--batch-scale", type=float, default=0.1, help="photon-budget scale of the batched workload")
     ap.add_argument("--streams", type=int, default=4, help="streams of the batched workload's graph")
     ap.add_argument("--ref-sample", type=int, default=16, help="batch instances the reference arm runs")
+    ap.add_argument("--no-detectors", action="store_true",
+                    help="drop the deck's detectors (measures the cost of detected-photon bookkeeping)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.workload == "batch" and args.impl != "reference":
@@ -331,6 +333,9 @@ def main() -> None:
     nphoton = int(args.photons) if args.photons else WORKLOAD_PHOTONS[name]
     seed = 20251203
     cfg = make_cfg(name, nphoton, seed)
+    if args.no_detectors:
+        cfg.pop("detpos", None)
+        cfg["issavedet"] = 0
     pc = mcx_gb300.prepare(cfg)
     sess = Session(pc, device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
@@ -369,6 +374,9 @@ def main() -> None:
     h2d = d2h = 0
     for i in range(1 + args.steps):
         c = make_cfg(name, nphoton, seed + 1 + i)
+        if args.no_detectors:
+            c.pop("detpos", None)
+            c["issavedet"] = 0
         barrier()
         t0 = time.perf_counter()
         r = mcx_gb300.run(c)
@@ -404,7 +412,8 @@ def main() -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": name, "photons_per_step": nphoton, "volume": list(cfg["vol"].shape),
                    "gates": pc.ngates, "parallelism": f"replicas{world}", "l2": "flushed before each timed step",
-                   "grid": st.grid, "block": st.block, "chunk": st.chunk},
+                   "grid": st.grid, "block": st.block, "chunk": st.chunk,
+                   "detectors": int(pc.c.detnum)},
         "e2e": {"value": e2e, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_tot / args.steps},
         "wall_ms_per_step": wall_ms / args.steps,

@@ -1230,7 +1230,11 @@ static KParams finalize(const KParams& in) {
 
 cudaError_t launch_transport(const KParams& in, bool reflect, bool savedet, int grid, int block, size_t smem_bytes,
                              cudaStream_t stream) {
-    const KParams p = finalize(in);
+    KParams p = finalize(in);
+    // a launch of fewer than 16 photons per thread reserves nothing beyond what its dead lanes
+    // need: whole-chunk reservations would leave some warps with two rounds of photons while
+    // others have none, and the launch would end on their tail
+    if (p.d_nwork < (unsigned long long)grid * (unsigned long long)block * 16ull) p.chunk = 1;
     const void* k = pick(reflect, savedet, transport_mode(p));
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e != cudaSuccess) return e;

@@ -137,6 +137,8 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
     }
     if "maxdetphoton" in cfg:
         session_keys["MaxDetPhoton"] = int(cfg["maxdetphoton"])
+    if cfg.get("issaveseed"):
+        session_keys["DoSaveSeed"] = 1
     out = {
         "Session": session_keys,
         "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0, "LengthUnit": 1,
@@ -200,11 +202,15 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
     mch = tmp / f"{session}.mch"
     if mch.exists():
         raw = mch.read_bytes()
-        hdr = struct.unpack("<4s14I", raw[:60])   # magic, version..savedetflag
-        colcount = hdr[4]
-        data = np.frombuffer(raw[64:], dtype=np.float32)
-        n = data.size // max(1, colcount)
-        res["detp"] = data[: n * colcount].reshape((colcount, n), order="F")
+        # History header (src/mcx_utils.h:115-132): magic, version, maxmedia, detnum, colcount,
+        # totalphoton, detected, savedphoton, unitinmm, seedbyte, ...
+        hdr = struct.unpack("<4s7If1I", raw[:40])
+        colcount, saved, seedbyte = hdr[4], hdr[7], hdr[9]
+        body = raw[64:64 + 4 * colcount * saved]
+        res["detp"] = np.frombuffer(body, dtype=np.float32).reshape((colcount, saved), order="F")
+        if seedbyte and cfg.get("issaveseed"):
+            sd = np.frombuffer(raw[64 + 4 * colcount * saved:64 + (4 * colcount + seedbyte) * saved], dtype=np.uint8)
+            res["seeds"] = sd.reshape(saved, seedbyte).T       # (seedbyte, n), as pmcx returns
     if not workdir:
         shutil.rmtree(tmp, ignore_errors=True)
     return res

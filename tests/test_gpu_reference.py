@@ -133,3 +133,24 @@ def test_source_shapes_same_seed(engine, ref, mcx_seeding, name, setting):
     print(name, "absorbed reference", r["absorbed"], "engine", fo, "detected", r["detected"], o["stat"]["detected"])
     assert abs(fo - r["absorbed"]) < 5e-5
     assert abs(o["stat"]["detected"] - r["detected"]) <= max(10, 0.003 * r["detected"])
+
+
+def test_replay_of_reference_seeds(engine, ref, mcx_seeding):
+    """Seeds saved by MCX itself are xorshift128+ states in MCX's layout: replayed by the engine in
+    MCX seeding mode, MCX's detected photons are detected again with the same records."""
+    cfg = problems.cube60b(1_000_000)
+    cfg.update(issaveseed=1, savedetflag="dp", seed=2024)
+    r = ref.run(cfg, keep_field=False)
+    assert r["seeds"].shape == (16, r["detp"].shape[1])
+    rep = problems.cube60b(1)
+    rep.update(seed=r["seeds"], detphotons=r["detp"], savedetflag="dp", outputtype="j")
+    o = engine.run(rep)
+    n = o["stat"]["nphoton"]
+    assert n > 0.99 * r["detp"].shape[1]
+    # the same arithmetic on the same random numbers: nearly every photon retraces MCX's path
+    again = set(map(tuple, np.round(r["detp"].T.astype(np.float64), 3).tolist()))
+    mine = [tuple(x) for x in np.round(o["detp"].T.astype(np.float64), 3).tolist()]
+    same = sum(1 for x in mine if x in again)
+    print("replayed", n, "detected again", o["stat"]["detected"], "with MCX's record", same)
+    assert o["stat"]["detected"] >= 0.98 * n
+    assert same >= 0.95 * n
