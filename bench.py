@@ -35,10 +35,14 @@ import numpy as np  # noqa: E402
 
 METRIC = "photons/ms (plain MC)"
 WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000,
-                    "cube60planar": 100_000_000, "batch": 0}
+                    "cube60planar": 100_000_000, "batch": 0, "contest": 100_000_000}
 # photons of the CPU-oracle sample per workload: about 10 s on 16 cores
 CPU_SAMPLE = {"workload0": 8_000_000, "workload1": 4_000_000, "workload2": 1_000_000, "cube60planar": 6_000_000,
-              "batch": 20_000}
+              "batch": 20_000, "contest": 4_000_000}
+# MCX's speed contest (manpage/mcxcontest.1:13, mcxlab/examples/mcx_gpu_benchmarks.m:124-130): the
+# built-in cube60, cube60b and cube60planar decks at 1e8 photons; the score is the sum of the three
+# photons/ms figures.
+CONTEST_DECKS = ("cube60", "cube60b", "cube60planar")
 
 # Thread-level instructions per transport step (ncu smsp__inst_executed.sum x
 # smsp__thread_inst_executed_per_inst_executed.ratio over the kernel's own step counter) and
@@ -125,6 +129,67 @@ def make_cfg(name: str, nphoton: int, seed: int):
     return problems.WORKLOADS[name](nphoton, seed=seed)
 
 
+def contest_cfg(deck: str, nphoton: int, seed: int):
+    from mcx_gb300 import problems
+
+    cfg = getattr(problems, deck)(nphoton)
+    cfg["seed"] = seed
+    return cfg
+
+
+def contest_main(args, world, rank) -> None:
+    """The speed contest: each deck timed like the single workloads (device-resident `value`,
+    `e2e` through mcx_gb300.run), the line's value and e2e being the sums of the three."""
+    import torch
+
+    import mcx_gb300
+    from mcx_gb300 import Session
+
+    torch.cuda.set_device(0)
+    nphoton = int(args.photons) if args.photons else WORKLOAD_PHOTONS["contest"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    per, e2e, h2d, d2h = {}, {}, 0, 0
+    with Clocks(0) as clk:
+        for k, deck in enumerate(CONTEST_DECKS):
+            sess = Session(mcx_gb300.prepare(contest_cfg(deck, nphoton, 1648335518)))
+            sess.autotune(nphoton)
+            for i in range(args.warmup):
+                sess.run(i * nphoton, nphoton, 1648335518)
+            ms = []
+            for i in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ms.append(sess.run((args.warmup + i) * nphoton, nphoton, 1648335518))
+            sess.close()
+            per[deck] = nphoton * args.steps / sum(ms)
+            wall = []
+            for i in range(1 + args.steps):
+                c = contest_cfg(deck, nphoton, 1648335518 + i)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r = mcx_gb300.run(c)
+                if i:
+                    wall.append((time.perf_counter() - t0) * 1e3)
+                h2d += (c["vol"].size * 4 + np.asarray(c["prop"]).nbytes) * (i > 0)
+                d2h += (r["flux"].nbytes + (r["detp"].nbytes if "detp" in r else 0)) * (i > 0)
+            e2e[deck] = nphoton * args.steps / sum(wall)
+    if rank != 0:
+        return
+    value = sum(per.values())
+    line = {
+        "metric": METRIC + ", summed over MCX's contest decks", "value": value, "unit": "photons/ms", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(nphoton / v for v in per.values()),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "contest", "decks": list(CONTEST_DECKS), "photons_per_deck": nphoton,
+                   "per_deck": per, "l2": "flushed before each timed step"},
+        "e2e": {"value": sum(e2e.values()), "unit": "photons/ms", "per_deck": e2e,
+                "h2d_bytes_per_step": int(h2d / max(1, args.steps)), "d2h_bytes_per_step": int(d2h / max(1, args.steps))},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def batch_cfgs(scale: float, seed: int = 20251204):
     from mcx_gb300 import problems
 
@@ -201,6 +266,26 @@ def reference_arm(args, world, rank) -> None:
     base = {"impl": "reference", "metric": METRIC, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic"}
+    if name == "contest" and ref_mcx.available():
+        ref_mcx.build()
+        per, e2e = {}, {}
+        for deck in CONTEST_DECKS:
+            for i in range(args.warmup):
+                ref_mcx.run(contest_cfg(deck, min(nphoton, 10_000_000), 100 + i), keep_field=False)
+            runs = [ref_mcx.run(contest_cfg(deck, nphoton, 1648335518 + i), keep_field=False) for i in range(args.steps)]
+            per[deck] = statistics.mean(r["speed"] for r in runs)
+            e2e[deck] = nphoton / statistics.mean(r["normalized_ms"] for r in runs)
+        v = sum(per.values())
+        line = dict(base, metric=METRIC + ", summed over MCX's contest decks", value=v,
+                    ms_per_step=sum(nphoton / x for x in per.values()),
+                    config={"workload": "contest", "decks": list(CONTEST_DECKS), "photons_per_deck": nphoton,
+                            "per_deck": per},
+                    e2e={"value": sum(e2e.values()), "unit": "photons/ms", "per_deck": e2e, "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0},
+                    cpu_baseline={"value": v, "unit": "photons/ms", "cores": os.cpu_count(), "kind": "reference",
+                                  "sample": "the reference MCX CUDA build itself on this GPU"})
+        print(json.dumps(line))
+        return
     if name == "batch" and ref_mcx.available():
         # MCX has no batch mode: its front-ends run the simulations one after another.  A bounded
         # sample of the batch (the first `--ref-sample` instances) runs that way per step.
@@ -309,6 +394,9 @@ def main() -> None:
     world, rank, local = _dist()
     if args.workload == "batch" and args.impl != "reference":
         batch_main(args, world, rank)
+        return
+    if args.workload == "contest" and args.impl != "reference":
+        contest_main(args, world, rank)
         return
 
     if args.impl == "reference":
