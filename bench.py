@@ -13,6 +13,11 @@ detectors saving id / scattering counts / partial paths) at 1e8 photons.
   --impl reference   the reference arm: MCX itself compiled from its sources for sm_103a
             (oracle/ref_mcx.py) on the same GPU when its sources are staged, else the CPU oracle
 
+Other workloads (--workload): workload0 (homogeneous cube), workload2 (256^3 layered volume),
+cube60planar (planar source), batch (256 simulations in one CUDA graph), contest (MCX's speed
+contest: cube60 + cube60b + cube60planar at 1e8 photons, the score being the sum of the three
+photons/ms).
+
 Multi-GPU (torchrun, one rank per GPU): every rank simulates its own photon range of the same
 size (weak scaling, no collective in the data path); rank 0 prints.
 """
