@@ -723,8 +723,8 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
 
         // ---- one step (src/mcx_core.cu:1888-2514) --------------------------------------------
         c_step++;
+        unsigned detflag = 0u;
         bool kill = false;
-        bool rkill = false;      // ended by Russian roulette (no boundary code for detection)
 
         if (pscat <= 0.f) {
             // random numbers of this scattering event: MCX's order (scattering length, azimuth,
@@ -924,14 +924,16 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 continue;
             }
         }
-        if (!kill) {
+        if (kill) {
+            detflag = (!inside && P.bc[((idx == kOUT_MAX) ? 9 : 6) + axis]) ? kOUT_MIN : (detold & kDET_MASK);
+        } else {
             // Russian roulette (2357-2378); off when minenergy is 0
             if (P.minenergy > 0.f && fabsf(w) < P.minenergy) {
                 if (rng_next(r0, r1) * 10.f <= 1.f) {
                     w *= 10.f;
                 } else {
                     kill = true;
-                    rkill = true;
+                    detflag = detold & kDET_MASK;
                 }
             }
             // Fresnel reflection / refraction on crossing (2381-2503)
@@ -958,6 +960,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         transmit(vx, vy, vz, n1, prn.w, axis);
                         if (med == 0) {
                             kill = true;
+                            detflag = (!inside && P.bc[((idx == kOUT_MAX) ? 9 : 6) + axis]) ? kOUT_MIN : (detold & kDET_MASK);
                         } else {
                             rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                         }
@@ -989,17 +992,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             }
         }
 
-        if (SAVEDET && !kill && med != medold) flush_segment(P, S, tid, B, medold, segp, nscat);
+        if (SAVEDET && (kill || med != medold)) {
+            segp += pathlen;        // the last voxel's path when the photon ends inside it, else 0
+            flush_segment(P, S, tid, B, medold, segp, nscat);
+        }
         if (kill) {
-            // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417).
-            // detflag: a boundary-detector face the photon left through (kOUT_MIN), else the
-            // detector bit of the voxel it ended in
-            const unsigned detflag =
-                (!rkill && !inside && P.bc[((idx == kOUT_MAX) ? 9 : 6) + axis]) ? kOUT_MIN : (detold & kDET_MASK);
-            if (SAVEDET) {
-                segp += pathlen;    // the last voxel's path when the photon ends inside it, else 0
-                flush_segment(P, S, tid, B, medold, segp, nscat);
-            }
+            // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
             bool detected = false;
             if (SAVEDET && (detflag & kDET_MASK) && med == 0) {
                 const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
