@@ -126,6 +126,12 @@ int mcxg_replayinit(Config* cfg, const float* detps, const int dimdetps[2], int 
  * photon alive forever.  No counterpart in MCX. */
 void mcxg_set_step_cap(unsigned int steps);
 
+/* mcx_run_simulation with the fluence accumulated in FP64 on the device instead of MCX's FP32
+ * two-copy scheme: the reference-accuracy twin the FP32 accumulation error is stated against.
+ * Same inputs, outputs and errors as mcx_run_simulation (src/mcx_core.h:200).  No counterpart
+ * in MCX. */
+void mcxg_run_simulation_fp64(Config* cfg, GPUInfo* gpu);
+
 /* ---- Batched simulations ------------------------------------------------------------------ */
 
 /* No counterpart in MCX, whose front-ends run one mcx_run_simulation per input (src/mcx.c:62-78).
