@@ -236,6 +236,8 @@ def _attach_field(pc: PreparedConfig):
     maxgate = pc.ngates if c.maxgate == 0 else min(int(c.maxgate), pc.ngates)
     if int(c.seed) == SEED_FROM_FILE and int(c.replaydet) == -1:
         maxgate *= max(1, int(c.detnum))     # one block of gates per detector
+    if ord(c.outputtype) in (6, 8):
+        maxgate *= 2                         # RF replay: real blocks, then imaginary blocks
     flux = None
     if c.issave2pt != b"\x00":
         flux = np.zeros(nx * ny * nz * maxgate, dtype=np.float32)

@@ -291,6 +291,7 @@ struct Session {
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
     DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
+    unsigned halves = 1;       // 2: RF replay, real then imaginary part
     double kernel_ms = 0.0;
     int launches = 0;
     // MCX per-thread seeding: stream count, host/device seed words and the glibc random_r state
@@ -350,8 +351,11 @@ struct Session {
         // a replay of every detector at once keeps one block of gates per detector
         // (src/mcx_core.cu:2907-2913)
         blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
-        if ((size_t)maxgate * blocks * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / (per_gate * blocks)));
-        fieldlen = nvox * (size_t)maxgate * blocks;
+        // RF replay outputs carry a real and an imaginary field (src/mcx_core.cu:2908-2913)
+        halves = (cfg->outputtype == otRF || cfg->outputtype == otRFmus) ? 2 : 1;
+        if ((size_t)maxgate * blocks * halves * per_gate > budget)
+            maxgate = std::max<int>(1, (int)(budget / (per_gate * blocks * halves)));
+        fieldlen = nvox * (size_t)maxgate * blocks * halves;
 
         // labels: upload the uint32 volume, pack to one byte per voxel on the device
         {
@@ -421,6 +425,8 @@ struct Session {
         k.replay = (cfg->seed == kSEED_FROM_FILE) ? 1 : 0;
         k.replaydet = cfg->replaydet;
         k.detnum = (int)cfg->detnum;
+        k.omega = cfg->omega;
+        k.rf_offset = fieldlen / halves;
         if (k.replay) {
             const size_t n = (size_t)cfg->nphoton;
             replay_seed.alloc(n * kSeedBytes, stream);
@@ -807,8 +813,8 @@ void check_config(const Config* cfg) {
         !(cfg->replay.seed && cfg->replay.weight && cfg->replay.tof && cfg->replay.detid))
         MCXG_RAISE(-6, "a replay needs the detected photons' seeds, weights, times of flight and detector ids (mcx_replayinit)");
     const int ot = cfg->outputtype;
-    if (ot == otRF || ot == otRFmus) MCXG_RAISE(-6, "frequency-domain (RF) replay outputs are not supported by the GB300 engine");
-    if ((ot == otJacobian || ot == otWP || ot == otDCS || ot == otWLTOF || ot == otWPTOF) && cfg->seed != kSEED_FROM_FILE)
+    if ((ot == otJacobian || ot == otWP || ot == otDCS || ot == otRF || ot == otRFmus || ot == otWLTOF || ot == otWPTOF) &&
+        cfg->seed != kSEED_FROM_FILE)
         MCXG_RAISE(-6, "the Jacobian and scattering-count outputs need a replay run (seed from the detected photons)");
     if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
@@ -925,10 +931,10 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
         if (block_scale.empty()) {
             for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
         } else {
-            const size_t per = S.fieldlen / S.blocks;
+            const size_t per = S.fieldlen / (S.blocks * S.halves);     // one detector's gates
             for (size_t i = 0; i < S.fieldlen; i++) {
                 const float v = host_field[i];
-                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * block_scale[i / per];
+                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * block_scale[(i / per) % S.blocks];
             }
         }
     }

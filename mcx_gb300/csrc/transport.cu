@@ -478,6 +478,7 @@ struct Smem {
     unsigned long long* seed0;    // 2 x blockDim, general variant: generator state at launch
     float* rw;                    // per thread, replay: detected weight of the photon
     float* rtof;                  // per thread, replay: its time of flight
+    float* rcos;                  // per thread, RF replay: cos and sin of omega x time of flight
     int* rbin;                    // per thread, replay: its field block (gate + detector offset), -1 none
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
@@ -502,7 +503,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
         s.seed0 = reinterpret_cast<unsigned long long*>((reinterpret_cast<uintptr_t>(end) + 7u) & ~uintptr_t(7));
         s.rw = reinterpret_cast<float*>(s.seed0 + 2 * blockDim.x);
         s.rtof = s.rw + blockDim.x;
-        s.rbin = reinterpret_cast<int*>(s.rtof + blockDim.x);
+        s.rcos = s.rtof + blockDim.x;                 // cos, then sin, blockDim.x each
+        s.rbin = reinterpret_cast<int*>(s.rcos + 2 * blockDim.x);
         end = reinterpret_cast<float*>(s.rbin + blockDim.x);
     }
     s.tile = reinterpret_cast<unsigned*>(end);
@@ -650,6 +652,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         S.rw[tid] = __ldg(P.replay_w + mine);
                         S.rtof[tid] = tof;
                         S.rbin[tid] = bin;
+                        if (P.outputtype == kOutRF || P.outputtype == kOutRFmus) {
+                            // modulation phase of the detected photon (src/mcx_core.cu:1700-1703)
+                            float sn, cs;
+                            sincosf(P.omega * tof, &sn, &cs);
+                            S.rcos[tid] = cs;
+                            S.rcos[B + tid] = sn;
+                        }
                         start = true;
                     } else if (P.seed_mode == 1) {
                         // MCX's per-thread stream `mine`: four host seed words
@@ -760,16 +769,22 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
                     S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
                 }
-                if (FULL && P.replay &&
-                    (P.outputtype == kOutWP || P.outputtype == kOutDCS || P.outputtype == kOutWPTOF)) {
+                if (FULL && P.replay && (P.outputtype == kOutWP || P.outputtype == kOutDCS ||
+                                         P.outputtype == kOutWPTOF || P.outputtype == kOutRFmus)) {
                     // replay outputs at scattering events (src/mcx_core.cu:2018-2066): detected weight
-                    // x (1, momentum transfer 1 - cos, or time of flight) in the current voxel
+                    // x (1, momentum transfer 1 - cos, time of flight, or cos / sin of the RF phase)
+                    // in the current voxel
                     const int rb = S.rbin[tid];
                     if (rb >= 0) {
                         float q = S.rw[tid];
+                        const size_t at = (size_t)idx + (size_t)rb * P.nvox;
                         if (P.outputtype == kOutDCS) q *= 1.f - ct;
                         else if (P.outputtype == kOutWPTOF) q *= S.rtof[tid];
-                        field_add_small(P, (size_t)idx + (size_t)rb * P.nvox, q);
+                        if (P.outputtype == kOutRFmus) {
+                            field_add_small(P, at + P.rf_offset, q * S.rcos[B + tid]);
+                            q *= S.rcos[tid];
+                        }
+                        field_add_small(P, at, q);
                     }
                 }
                 rotate(vx, vy, vz, st, ct, sphi, cphi);
@@ -864,6 +879,15 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     // mua Jacobian: detected weight x path in the voxel (x time of flight)
                     const int rb = S.rbin[tid];
                     weight = (rb < 0) ? 0.f : S.rw[tid] * pathlen * (P.outputtype == kOutWLTOF ? S.rtof[tid] : 1.f);
+                    tshift = rb;
+                } else if (P.replay && P.outputtype == kOutRF) {
+                    // RF mua Jacobian (src/mcx_core.cu:2207-2256): -(detected weight x path) x
+                    // cos(omega t) here, x sin(omega t) in the imaginary half
+                    const int rb = S.rbin[tid];
+                    weight = (rb < 0) ? 0.f : -S.rw[tid] * pathlen * S.rcos[tid];
+                    if (rb >= 0)
+                        field_add_small(P, (size_t)idxold + (size_t)rb * P.nvox + P.rf_offset,
+                                        -S.rw[tid] * pathlen * S.rcos[B + tid]);
                     tshift = rb;
                 } else {
                     weight = 0.f;                           // scattering-event outputs (below)
@@ -1134,7 +1158,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) == 2) b += 8 + (2 * sizeof(unsigned long long) + 3 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) == 2) b += 8 + (2 * sizeof(unsigned long long) + 5 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }

@@ -83,6 +83,8 @@ struct KParams {
     const int* replay_detid;        // its detector id
     int replaydet;                  // -1: one field block of maxgate gates per detector
     int detnum;
+    float omega;                    // RF replay: angular modulation frequency (rad/s)
+    size_t rf_offset;               // RF replay: offset of the imaginary half of the field
 
     // --- time gates
     float twin0, twin1, Rtstep, oneoverc0;

@@ -101,3 +101,28 @@ def test_replay_in_mcx_seeding_mode(engine):
     assert r["stat"]["detected"] == r["stat"]["nphoton"] > 0.99 * b["detp"].shape[1]
     baseline = set(map(tuple, b["detp"].T.tolist()))
     assert all(rec in baseline for rec in map(tuple, r["detp"].T.tolist()))
+
+
+@pytest.mark.parametrize("ot,col,sign", [("r", "ppath", -1.0), ("s", "nscat", 1.0)])
+def test_rf_replay_outputs(engine, base, ot, col, sign):
+    """Frequency-domain replay (src/mcx_core.cu:1700-1703, 2018-2066, 2207-2256): the real half of
+    the field holds sign x w_i cos(omega t_i) x (path or scattering count), the imaginary half the
+    same with sin; t_i the detected photon's time of flight from its partial paths."""
+    omega = 2 * np.pi * 100e6
+    cfg = _baseline(1)
+    cfg.update(seed=base["seeds"], detphotons=base["detp"], outputtype=ot, isnormalized=0, omega=omega)
+    r = engine.run(cfg)
+    prop = np.asarray(cfg["prop"], np.float32)
+    M = prop.shape[0] - 1
+    det = r["detp"].astype(np.float64)
+    ppath = det[1 + M:1 + 2 * M]
+    w = np.exp(-(prop[1:, 0:1].astype(np.float64) * ppath).sum(axis=0))
+    tof = (ppath * prop[1:, 3:4].astype(np.float64)).sum(axis=0) * 3.335640951981520e-12
+    q = det[1 + M:1 + 2 * M] if col == "ppath" else det[1:1 + M]
+    assert r["flux"].shape[-1] == 2
+    labels = cfg["vol"]
+    for half, trig in ((0, np.cos), (1, np.sin)):
+        field = r["flux"][..., half].astype(np.float64)
+        got = np.array([field[labels == m].sum() for m in range(1, M + 1)])
+        expect = sign * (q * (w * trig(omega * tof))).sum(axis=1)
+        np.testing.assert_allclose(got, expect, rtol=1e-4, atol=1e-6 * np.abs(expect).max())
