@@ -52,6 +52,57 @@ def _check(rc: int | None = None) -> None:
         raise MCXError(rc, "engine call failed")
 
 
+def _f2h_mcx(x: np.ndarray) -> np.ndarray:
+    """float32 -> binary16 bits as MCX packs them (mcx_float2half2, src/mcx_utils.c:5490-5540):
+    the mantissa truncated, values below 2^-14 handled by its denormal branch."""
+    i = np.asarray(x, np.float32).view(np.uint32).astype(np.int64)
+    m = (i >> 13) & 0x3FF
+    e = (i >> 23) & 0xFF
+    normal = e > 0x70
+    h = np.where(normal, ((i >> 31) << 15) | (((e - 0x70) & 0x1F) << 10) | m, 0)
+    sign = (i >> 16) & 0x8000
+    md = ((i >> 12) & 0x7FF) | 0x800
+    s1 = np.clip(114 - e, 0, 31)
+    s2 = np.clip(113 - e, 0, 31)
+    den = sign | ((md >> s1) + ((md >> s2) & 1))
+    h = np.where(~normal & (m < 0x10), den, np.where(normal, h, ((i >> 31) << 15) | m))
+    return (h & 0xFFFF).astype(np.uint32)
+
+
+def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]:
+    """The 32-bit voxel words and MCX mediabyte of a volume, as pmcx and mcx_utils.c pack them
+    (src/pmcx.cpp:120-380, src/mcx_utils.c:3537-3594):
+
+      integer (nx, ny, nz)        labels (mediabyte 1, 2 or 4)
+      float   (nx, ny, nz)        mua per voxel, MEDIA_MUA_FLOAT (101): float bits of mua x unitinmm,
+                                  0 -> FLT_EPSILON (not void), NaN -> 0 (void)
+      float   (2, nx, ny, nz)     mua, mus per voxel, MEDIA_AS_F2H (100): two binary16 halves
+      uint8   (4, nx, ny, nz)     interpolation bytes for mua, mus, g, n, MEDIA_ASGN_BYTE (103)
+      uint16  (2, nx, ny, nz)     interpolation shorts for mua, mus, MEDIA_AS_SHORT (104)"""
+    v = np.asarray(vol)
+    if v.ndim == 3 and v.dtype.kind in "iub":
+        return np.asfortranarray(v.astype(np.uint32, copy=False)), {1: 1, 2: 2, 4: 4, 8: 4}[v.dtype.itemsize]
+    if v.ndim == 3 and v.dtype.kind == "f":
+        f = (v.astype(np.float32) * np.float32(unitinmm)).astype(np.float32)
+        w = f.view(np.uint32).copy()
+        w[w == 0] = np.array(np.finfo(np.float32).eps, np.float32).view(np.uint32)
+        w[np.isnan(f) | (w == 0x80000000)] = 0
+        return np.asfortranarray(w), 101
+    if v.ndim == 4 and v.dtype.kind == "f" and v.shape[0] == 2:
+        mua = (v[0].astype(np.float32) * np.float32(unitinmm)).astype(np.float32)
+        mus = (v[1].astype(np.float32) * np.float32(unitinmm)).astype(np.float32)
+        w = _f2h_mcx(mua) | (_f2h_mcx(mus) << 16)
+        w[np.isnan(mua) | np.isnan(mus)] = 0
+        return np.asfortranarray(w.astype(np.uint32)), 100
+    if v.ndim == 4 and v.dtype == np.uint8 and v.shape[0] == 4:
+        b = v.astype(np.uint32)
+        return np.asfortranarray(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24)), 103
+    if v.ndim == 4 and v.dtype == np.uint16 and v.shape[0] == 2:
+        b = v.astype(np.uint32)
+        return np.asfortranarray(b[0] | (b[1] << 16)), 104
+    raise MCXError(-4, "the 'vol' field must be a 3-D label array, a 3-D float mua array, or a 4-D per-voxel property array")
+
+
 def _set_vec(dst, vals, n) -> None:
     vals = list(np.asarray(vals, dtype=np.float64).ravel())
     for i, name in enumerate("xyzw"[:n]):
@@ -121,13 +172,10 @@ class PreparedConfig:
         if "vol" not in cfg or "prop" not in cfg:
             raise MCXError(-4, "the 'vol' and 'prop' fields are required")
         vol = np.asarray(cfg["vol"])
-        if vol.ndim != 3:
-            raise MCXError(-4, "the 'vol' field must be a 3-D label array")
-        if vol.dtype.kind == "f":
-            raise MCXError(-6, "only label-based media are supported by the GB300 engine")
-        vol32 = np.asfortranarray(vol.astype(np.uint32, copy=False)).ravel(order="F").copy()
-        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in vol.shape)
-        c.mediabyte = {1: 1, 2: 2, 4: 4, 8: 4}[vol.dtype.itemsize]
+        words, mediabyte = pack_media(vol, float(cfg.get("unitinmm", 1.0)))
+        vol32 = words.ravel(order="F").copy()
+        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in words.shape)
+        c.mediabyte = mediabyte
         self.vol = vol32
         c.vol = vol32.ctypes.data
 

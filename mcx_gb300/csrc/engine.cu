@@ -269,7 +269,8 @@ void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
     k.src_v = make_float4(v.x, v.y, v.z, 0.f);
     k.src_t = t;
     k.src_idx = sidx;
-    k.src_label = (smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u);
+    // byte-label form, or the raw word for the per-voxel media formats
+    k.src_label = media_words(cfg->mediabyte) ? smed : ((smed & kLabelMask) | ((smed & kDET_MASK) ? kLabelDet : 0u));
     if (k.src_ok) {
         k.src_fx = fd[0]; k.src_fy = fd[1]; k.src_fz = fd[2];
     }
@@ -289,7 +290,7 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
-    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata;
+    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
     double kernel_ms = 0.0;
@@ -308,7 +309,7 @@ struct Session {
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
         pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
-        seeddata.release();
+        seeddata.release(); voxwords.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -357,8 +358,14 @@ struct Session {
             maxgate = std::max<int>(1, (int)(budget / (per_gate * blocks * halves)));
         fieldlen = nvox * (size_t)maxgate * blocks * halves;
 
-        // labels: upload the uint32 volume, pack to one byte per voxel on the device
-        {
+        // labels: upload the uint32 volume, pack to one byte per voxel on the device; the
+        // per-voxel media formats keep MCX's 32-bit words
+        const bool words_mode = media_words(cfg->mediabyte);
+        if (words_mode) {
+            voxwords.alloc(nvox * sizeof(uint32_t), stream);
+            err.alloc(sizeof(unsigned), stream);
+            CK(cudaMemcpyAsync(voxwords.p, cfg->vol, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+        } else {
             DevBuf vol32;
             vol32.alloc(nvox * sizeof(uint32_t), stream);
             CK(cudaMemcpyAsync(vol32.p, cfg->vol, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
@@ -374,6 +381,8 @@ struct Session {
 
         KParams& k = kp;
         std::memset(&k, 0, sizeof(k));
+        k.mediaformat = cfg->mediabyte;
+        k.words = voxwords.as<uint32_t>();
         k.nx = (int)cfg->dim.x; k.ny = (int)cfg->dim.y; k.nz = (int)cfg->dim.z;
         k.dimxy = cfg->dim.x * cfg->dim.y;
         k.nvox = (unsigned)nvox;
@@ -818,7 +827,12 @@ void check_config(const Config* cfg) {
         MCXG_RAISE(-6, "the Jacobian and scattering-count outputs need a replay run (seed from the detected photons)");
     if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
-    if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media are supported by the GB300 engine");
+    if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 100-104");
+    if ((cfg->mediabyte == kMediaAsF2H || cfg->mediabyte == kMediaMuaFloat || cfg->mediabyte == kMediaAsHalf) && cfg->medianum < 2)
+        MCXG_RAISE(-4, "the per-voxel media format needs the 2nd row of prop for the properties it does not store");
+    if ((cfg->mediabyte == kMediaAsgnByte || cfg->mediabyte == kMediaAsShort) && cfg->medianum < 3)
+        MCXG_RAISE(-4, "the interpolating media formats need prop rows 2 and 3 as their end points");
     if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
     check_source(cfg);
 }

@@ -80,6 +80,8 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     k.outputtype = cfg->outputtype;
     if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
         MCXG_RAISE(-6, "the allocation-free entry point supports flux, fluence and energy outputs");
+    if (cfg->mediabyte > 4)
+        MCXG_RAISE(-6, "the allocation-free entry point takes byte labels: no per-voxel media formats");
     if (cfg->seed == kSEED_FROM_FILE || cfg->issaveseed)
         MCXG_RAISE(-6, "the allocation-free entry point runs no replay and saves no seeds");
     k.minenergy = cfg->minenergy;

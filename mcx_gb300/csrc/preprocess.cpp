@@ -185,7 +185,8 @@ void validate(Config* cfg) {
     }
     if (cfg->medianum == 0) MCXG_RAISE(-4, "you must define the 'prop' field in the input structure");
     if (cfg->dim.x == 0 || cfg->dim.y == 0 || cfg->dim.z == 0) MCXG_RAISE(-4, "the 'vol' field in the input structure can not be empty");
-    if (cfg->mediabyte > 4) MCXG_RAISE(-6, "only label-based media (mediabyte 1, 2 or 4) are supported by the GB300 engine");
+    if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 100-104");
     check_source(cfg);
 
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) cfg->unitinmm = cfg->steps.x;
@@ -222,9 +223,11 @@ void validate(Config* cfg) {
     }
     if (cfg->srcpos.w == 0.f) cfg->srcpos.w = 1.f;
     const size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
-    uint32_t maxlabel = 0;
-    for (size_t i = 0; i < nvox; i++) maxlabel = std::max(maxlabel, cfg->vol[i] & kMED_MASK);
-    if (cfg->medianum <= maxlabel) MCXG_RAISE(-4, "input media optical properties are less than the labels in the volume");
+    if (cfg->mediabyte <= 4) {
+        uint32_t maxlabel = 0;
+        for (size_t i = 0; i < nvox; i++) maxlabel = std::max(maxlabel, cfg->vol[i] & kMED_MASK);
+        if (cfg->medianum <= maxlabel) MCXG_RAISE(-4, "input media optical properties are less than the labels in the volume");
+    }
 
     // launch voxel and medium of point sources (src/mcx_utils.c:1737-1760); the other shapes keep
     // srcparam2 as their parameters
@@ -247,6 +250,8 @@ void validate(Config* cfg) {
     if (cfg->issaveexit) cfg->savedetflag |= 0x30;
     cfg->savedetflag &= ~0x80u;       // no Stokes vector without polarisation
     if (cfg->issavedet && cfg->savedetflag == 0) cfg->savedetflag = 0x5;
+    // per-voxel media have no labels: no per-medium record columns (src/mcx_utils.c:1801-1806)
+    if (cfg->mediabyte >= 100 && cfg->savedetflag) cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u | 0x80u);
     if (cfg->issaveref) MCXG_RAISE(-6, "diffuse-reflectance output (issaveref) is not supported by the GB300 engine");
 
     // history header bookkeeping done at the end of mcx_validatecfg (src/mcx_utils.c:3853-3857)

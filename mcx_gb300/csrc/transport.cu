@@ -20,6 +20,7 @@
 // Semantics that must match the reference step for step are annotated with its file:line.
 
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -151,8 +152,43 @@ __device__ __forceinline__ float reflect_coeff(float vx, float vy, float vz, flo
     return (R + __fdividef(Re - Im, Re + Im)) * 0.5f;
 }
 
-__device__ __forceinline__ unsigned label_at(const KParams& P, int x, int y, int z) {
-    return __ldg(P.labels + ((unsigned)z * P.dimxy + (unsigned)y * (unsigned)P.nx + (unsigned)x));
+// Voxel contents: a byte label (bit 7 detector mask, bits 0-6 medium) or, for the per-voxel media
+// formats, MCX's 32-bit word (bit 31 detector mask, bits 0-30 the encoded properties; 0 = void).
+template <bool WORDS>
+__device__ __forceinline__ unsigned voxel_load(const KParams& P, unsigned idx) {
+    if (WORDS) return __ldg(P.words + idx);
+    return (unsigned)__ldg(P.labels + idx);
+}
+template <bool WORDS>
+__device__ __forceinline__ unsigned voxel_med(unsigned v) { return WORDS ? (v & kMED_MASK) : (v & kLabelMask); }
+template <bool WORDS>
+__device__ __forceinline__ bool voxel_det(unsigned v) { return WORDS ? (v >> 31) != 0u : (v & kLabelDet) != 0u; }
+
+__device__ __forceinline__ float half_bits(unsigned h) { return __half2float(__ushort_as_half((unsigned short)h)); }
+
+// Optical properties (mua, mus, g, n) of a voxel's medium value m (src/mcx_core.cu:582-730):
+// the table row for labels; decoded from the word for the per-voxel formats, whose missing
+// fields come from table rows 1 and 2.  A void or outside voxel (m = 0) takes row 0 in every
+// format; MCX decodes it like any word, which for MEDIA_ASGN_BYTE gives the outside row 2's n
+// and mus, so photons there scatter outside the volume.
+template <bool WORDS>
+__device__ __forceinline__ float4 props_of(const KParams& P, const float4* tab, unsigned m) {
+    if (!WORDS || m == 0u) return tab[m];     // void and outside: row 1 of prop, as for labels
+    const float4 r1 = tab[1];
+    const float n = r1.w;
+    if (P.mediaformat == kMediaMuaFloat) return make_float4(__uint_as_float(m), r1.y, r1.z, n);
+    if (P.mediaformat == kMediaAsF2H || P.mediaformat == kMediaAsHalf)
+        return make_float4(fabsf(half_bits(m & 0xFFFFu)), fabsf(half_bits(m >> 16)), r1.z, n);
+    const float4 r2 = tab[2];
+    if (P.mediaformat == kMediaAsgnByte) {
+        return make_float4((m & 0xFFu) * (1.f / 255.f) * (r2.x - r1.x) + r1.x,
+                           ((m >> 8) & 0xFFu) * (1.f / 255.f) * (r2.y - r1.y) + r1.y,
+                           ((m >> 16) & 0xFFu) * (1.f / 255.f) * (r2.z - r1.z) + r1.z,
+                           (m >> 24) * (1.f / 127.f) * (r2.w - r1.w) + r1.w);
+    }
+    // kMediaAsShort
+    return make_float4((m & 0xFFFFu) * (1.f / 65535.f) * (r2.x - r1.x) + r1.x,
+                       (m >> 16) * (1.f / 65535.f) * (r2.y - r1.y) + r1.y, r1.z, n);
 }
 
 __device__ __forceinline__ bool in_grid(const KParams& P, int x, int y, int z) {
@@ -163,17 +199,21 @@ __device__ __forceinline__ bool in_grid(const KParams& P, int x, int y, int z) {
 // in unit steps until it is inside a non-zero voxel, back up one step and find the exact entry
 // face with voxel-to-voxel steps; optional specular loss and refraction there.  Returns the
 // entry voxel, or -1 when the photon misses the volume.
+template <bool WORDS>
 __device__ int skip_void(const KParams& P, Launch& L) {
     const float rvx = __fdividef(1.f, L.vx), rvy = __fdividef(1.f, L.vy), rvz = __fdividef(1.f, L.vz);
     int fx = (int)floorf(L.px), fy = (int)floorf(L.py), fz = (int)floorf(L.pz);
     int count = 1;
     while (true) {
-        if (in_grid(P, fx, fy, fz) && (label_at(P, fx, fy, fz) & kLabelMask)) {
+        const auto at = [&](int x, int y, int z) {
+            return voxel_load<WORDS>(P, (unsigned)z * P.dimxy + (unsigned)y * (unsigned)P.nx + (unsigned)x);
+        };
+        if (in_grid(P, fx, fy, fz) && voxel_med<WORDS>(at(fx, fy, fz))) {
             L.px -= L.vx; L.py -= L.vy; L.pz -= L.vz;
             fx = (int)floorf(L.px); fy = (int)floorf(L.py); fz = (int)floorf(L.pz);
             L.t -= 1.f;
             int axis = -1;
-            for (int k = 0; k <= 4 && !(in_grid(P, fx, fy, fz) && (label_at(P, fx, fy, fz) & kLabelMask)); k++) {
+            for (int k = 0; k <= 4 && !(in_grid(P, fx, fy, fz) && voxel_med<WORDS>(at(fx, fy, fz))); k++) {
                 const float hx = fabsf((fx + (L.vx > 0.f ? 1.f : 0.f) - L.px) * rvx);
                 const float hy = fabsf((fy + (L.vy > 0.f ? 1.f : 0.f) - L.py) * rvy);
                 const float hz = fabsf((fz + (L.vz > 0.f ? 1.f : 0.f) - L.pz) * rvz);
@@ -187,8 +227,8 @@ __device__ int skip_void(const KParams& P, Launch& L) {
             }
             if (!in_grid(P, fx, fy, fz)) return -1;
             if (!P.voidtime) L.t = 0.f;
-            const unsigned lab = label_at(P, fx, fy, fz);
-            const float n2 = P.prop[lab & kLabelMask].w, n0 = P.prop[0].w;
+            const unsigned lab = at(fx, fy, fz);
+            const float n2 = props_of<WORDS>(P, P.prop, voxel_med<WORDS>(lab)).w, n0 = P.prop[0].w;
             if (P.isspecular && axis >= 0 && n2 != n0) {
                 L.w *= 1.f - reflect_coeff(L.vx, L.vy, L.vz, n0, n2, axis);
                 if (L.w > kEPS) transmit(L.vx, L.vy, L.vz, n0, n2, axis);
@@ -226,6 +266,7 @@ __device__ __forceinline__ void offset_normal(Launch& L, float r, float sphi, fl
 // One launch of a non-pencil source, drawing from the photon's stream in MCX's order
 // (launchnewphoton, src/mcx_core.cu:1236-1672).  Retries a photon that misses the volume up to
 // maxvoidstep times; false when every attempt missed.
+template <bool WORDS>
 __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long long& r0, unsigned long long& r1, Launch& L) {
     const float4 p1 = P.src_param1, p2 = P.src_param2;
     constexpr float kJustBelowOne = 0.9998f;                      // src/mcx_const.h:50
@@ -424,16 +465,16 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                 in_grid(P, fx, fy, fz)) {
                 L.idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
                 L.ix = fx; L.iy = fy; L.iz = fz;
-                lab = __ldg(P.labels + L.idx);
+                lab = voxel_load<WORDS>(P, L.idx);
             }
         }
-        if ((lab & kLabelMask) == 0u) {
-            const int id = skip_void(P, L);
+        if (voxel_med<WORDS>(lab) == 0u) {
+            const int id = skip_void<WORDS>(P, L);
             if (id < 0) continue;
             L.idx = (unsigned)id;
-            lab = __ldg(P.labels + L.idx);
+            lab = voxel_load<WORDS>(P, L.idx);
         }
-        if ((lab & kLabelMask) == 0u || fabsf(L.w) <= P.minenergy) continue;
+        if (voxel_med<WORDS>(lab) == 0u || fabsf(L.w) <= P.minenergy) continue;
         L.label = lab;
         return true;
     }
@@ -532,7 +573,8 @@ __device__ __forceinline__ void flush_segment(const KParams& P, const Smem& S, i
 template <bool REFLECT, bool SAVEDET, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
     constexpr bool AREA = MODE >= 1;
-    constexpr bool FULL = MODE == 2;
+    constexpr bool FULL = MODE >= 2;
+    constexpr bool WORDS = MODE == 3;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Smem S = carve<SAVEDET, FULL>(P, smem_raw);
     const int tid = threadIdx.x;
@@ -689,20 +731,20 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
                 t = P.src_t * inv_c0;
                 idx = P.src_idx;
-                med = (int)(P.src_label & kLabelMask);
-                det = (P.src_label & kLabelDet) != 0u;
+                med = (int)voxel_med<WORDS>(P.src_label);
+                det = voxel_det<WORDS>(P.src_label);
                 fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
                 entered = true;
             } else if (AREA && start) {
                 Launch L;
-                entered = launch_source(P, r0, r1, L);
+                entered = launch_source<WORDS>(P, r0, r1, L);
                 if (entered) {
                     px = L.px; py = L.py; pz = L.pz; w = L.w;
                     vx = L.vx; vy = L.vy; vz = L.vz;
                     t = L.t;
                     idx = L.idx;
-                    med = (int)(L.label & kLabelMask);
-                    det = (L.label & kLabelDet) != 0u;
+                    med = (int)voxel_med<WORDS>(L.label);
+                    det = voxel_det<WORDS>(L.label);
                     fx = (float)L.ix; fy = (float)L.iy; fz = (float)L.iz;
                 }
             }
@@ -715,7 +757,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (SAVEDET) S.nscat0[tid] = 0;
                 w0 = w; eabs = 0.f;
                 S.step0[tid] = c_step;
-                pr = S.prop[med];
+                pr = props_of<WORDS>(P, S.prop, (unsigned)med);
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
                 alive = true;
@@ -765,7 +807,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     ct = 2.f * u_th - 1.f;                              // isotropic, 1961-1963
                 }
                 const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
-                if (SAVEDET && med > 0 && ((P.savedetflag >> 3) & 1u)) {   // momentum transfer, 1970-1993
+                if (SAVEDET && !WORDS && med > 0 && ((P.savedetflag >> 3) & 1u)) {   // momentum transfer, 1970-1993
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
                     S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
                 }
@@ -797,7 +839,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
 
         const float n1 = pr.w;
-        pr = S.prop[med];
+        pr = props_of<WORDS>(P, S.prop, (unsigned)med);
 
         // distance to the nearest voxel face (hitgrid, src/mcx_core.cu:493-507)
         const float hx = fabsf((fx + (vx > 0.f ? 1.f : 0.f) - px) * rvx);
@@ -853,9 +895,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 }
             }
             if (inside) {
-                const unsigned lab = __ldg(P.labels + idx);
-                med = (int)(lab & kLabelMask);
-                det = (lab & kLabelDet) != 0u;
+                const unsigned lab = voxel_load<WORDS>(P, idx);
+                med = (int)voxel_med<WORDS>(lab);
+                det = voxel_det<WORDS>(lab);
             } else {
                 med = 0;
                 idx = (c < 0.f) ? kOUT_MIN : kOUT_MAX;
@@ -940,11 +982,11 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             else { pz = nextafter_mcx(roundf(pz + shift), (vz > 0.f) - (vz < 0.f), P.maxvoidstep); fz = floorf(pz); }
             if (fx >= 0.f && fx < fnx && fy >= 0.f && fy < fny && fz >= 0.f && fz < fnz) {
                 idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
-                const unsigned lab = __ldg(P.labels + idx);
-                med = (int)(lab & kLabelMask);
-                det = (lab & kLabelDet) != 0u;
+                const unsigned lab = voxel_load<WORDS>(P, idx);
+                med = (int)voxel_med<WORDS>(lab);
+                det = voxel_det<WORDS>(lab);
                 carry = det;
-                if (SAVEDET && med != medold) flush_segment(P, S, tid, B, medold, segp, nscat);
+                if (SAVEDET && !WORDS && med != medold) flush_segment(P, S, tid, B, medold, segp, nscat);
                 continue;
             }
         }
@@ -962,7 +1004,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             }
             // Fresnel reflection / refraction on crossing (2381-2503)
             if (REFLECT && !kill && !stay) {
-                const float4 prn = S.prop[med];
+                const float4 prn = props_of<WORDS>(P, S.prop, (unsigned)med);
                 pr = prn;
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
@@ -1005,18 +1047,18 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         }
                         rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                         idx = idxold;
-                        const unsigned lab = __ldg(P.labels + idx);
-                        med = (int)(lab & kLabelMask);
-                        det = (lab & kLabelDet) != 0u;   // carry keeps the bounced-off value
-                        pr = S.prop[med];
+                        const unsigned lab = voxel_load<WORDS>(P, idx);
+                        med = (int)voxel_med<WORDS>(lab);
+                        det = voxel_det<WORDS>(lab);     // carry keeps the bounced-off value
+                        pr = props_of<WORDS>(P, S.prop, (unsigned)med);
                     }
                 } else {
-                    pr = S.prop[medold];
+                    pr = props_of<WORDS>(P, S.prop, (unsigned)medold);
                 }
             }
         }
 
-        if (SAVEDET && (kill || med != medold)) {
+        if (SAVEDET && !WORDS && (kill || med != medold)) {
             segp += pathlen;        // the last voxel's path when the photon ends inside it, else 0
             flush_segment(P, S, tid, B, medold, segp, nscat);
         }
@@ -1158,7 +1200,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) == 2) b += 8 + (2 * sizeof(unsigned long long) + 5 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 5 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1174,6 +1216,7 @@ int transport_variant() { return g_minb; }
 bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 
 int transport_mode(const KParams& p) {
+    if (media_words(p.mediaformat)) return 3;
     if (p.replay || p.saveseed || p.outputtype > kOutEnergy) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
@@ -1187,6 +1230,7 @@ static const void* pick_flags(bool reflect, bool savedet) {
 // The pencil variants run at 4 CTAs of 256 per SM (64 registers) unless the tuner asks for 3;
 // the variants with the general launch need more registers and run at 3 (80 registers).
 static const void* pick(bool reflect, bool savedet, int mode) {
+    if (mode == 3) return pick_flags<3, 3>(reflect, savedet);
     if (mode == 2) return pick_flags<3, 2>(reflect, savedet);
     if (mode == 1) return pick_flags<3, 1>(reflect, savedet);
     return (g_minb == 3) ? pick_flags<3, 0>(reflect, savedet) : pick_flags<4, 0>(reflect, savedet);

@@ -19,6 +19,12 @@ enum SrcType : int {
     kSrcDisk, kSrcFourierX, kSrcFourierX2D, kSrcZGaussian, kSrcLine, kSrcSlit, kSrcPencilArray, kSrcPattern3D,
     kSrcHyperboloid, kSrcRing, kNumSrcTypes
 };
+// Per-voxel media formats (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730 does).
+enum MediaFormat : int {
+    kMediaAsF2H = 100, kMediaMuaFloat = 101, kMediaAsHalf = 102, kMediaAsgnByte = 103, kMediaAsShort = 104
+};
+__host__ __device__ constexpr bool media_words(int f) { return f >= kMediaAsF2H && f <= kMediaAsShort; }
+
 // Launch-direction options of area sources, from srcdir.w (src/mcx_core.cu:1672-1710): 0 =
 // along srcdir, a finite value = focal length, NaN = isotropic, -inf = Lambertian.
 // MCX's output types (src/mcx_utils.h:70).
@@ -41,6 +47,8 @@ enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow =
 struct KParams {
     // --- buffers (device pointers)
     const uint8_t* labels;          // Nvox bytes: bit 7 detector mask, bits 0-6 medium label
+    const uint32_t* words;          // per-voxel media formats: MCX's 32-bit voxel words instead
+    int mediaformat;                // MCX mediabyte: 1/2/4 labels, kMedia* per-voxel formats
     float* field;                   // maxgate x Nvox raw flux accumulator
     float* shadow;                  // maxgate x Nvox spill copy (values moved out past kMaxAccum)
     double* field64;                // FP64 accumulator (reference-accuracy runs only), else null
@@ -164,7 +172,8 @@ int transport_variant();
 // Shared memory the kernel needs for a given block size and parameter set.
 size_t transport_smem_bytes(const KParams& p, int block, bool savedet);
 // Kernel variant of a parameter set: 0 = pencil beam with flux/fluence/energy output, 1 = other
-// source shapes sampled per photon, 2 = replay, seed saving or the replay / path-length outputs.
+// source shapes sampled per photon, 2 = replay, seed saving or the replay / path-length outputs,
+// 3 = everything of 2 on a per-voxel media format.
 int transport_mode(const KParams& p);
 bool transport_general(const KParams& p);
 // Occupancy-derived CTAs per SM for the chosen variant.

@@ -99,6 +99,39 @@ struct Ctx {
     uint32_t partialdata, reclen;
     int isreflect;                 // template flag of the reference (isreflect or any r/m face)
     const Prop* prop;
+
+    // Properties of a voxel's medium value m: the table row for labels; for the per-voxel formats
+    // decoded from the word, the fields a format does not store taken from row 1 (MCX's kernel
+    // starts from row 1 and never overwrites them), n from row 1 (src/mcx_core.cu:614-695).  A
+    // void or outside voxel (m = 0) takes row 0 in every format, unlike MCX's decode of a zero
+    // MEDIA_ASGN_BYTE word (the engine's rule, restated here).
+    Prop prop_of(uint32_t m) const {
+        const int f = P->mediaformat;
+        if (f <= 4 || m == 0) return prop[m];
+        const Prop r1 = prop[1];
+        const float n = r1.n;
+        if (f == 101) {
+            float mua;
+            std::memcpy(&mua, &m, 4);
+            return {std::fabs(mua), r1.mus, r1.g, n};
+        }
+        if (f == 100 || f == 102) return {std::fabs(half_to_float(m & 0xFFFF)), std::fabs(half_to_float(m >> 16)), r1.g, n};
+        const Prop r2 = prop[2];
+        if (f == 103)
+            return {(m & 0xFF) * (1.f / 255.f) * (r2.mua - r1.mua) + r1.mua, ((m >> 8) & 0xFF) * (1.f / 255.f) * (r2.mus - r1.mus) + r1.mus,
+                    ((m >> 16) & 0xFF) * (1.f / 255.f) * (r2.g - r1.g) + r1.g, (m >> 24) * (1.f / 127.f) * (r2.n - r1.n) + r1.n};
+        return {(m & 0xFFFF) * (1.f / 65535.f) * (r2.mua - r1.mua) + r1.mua, (m >> 16) * (1.f / 65535.f) * (r2.mus - r1.mus) + r1.mus,
+                r1.g, n};
+    }
+
+    // IEEE 754 binary16 bits to float (normals, subnormals, zero; the formats store no inf/NaN)
+    static float half_to_float(uint32_t h) {
+        const uint32_t sign = (h >> 15) & 1u, e = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+        float v;
+        if (e == 0) v = std::ldexp((float)man, -24);
+        else v = std::ldexp((float)(man | 0x400u), (int)e - 25);
+        return sign ? -v : v;
+    }
 };
 
 // src/mcx_core.cu:470-478
@@ -221,7 +254,7 @@ int skipvoid(const Ctx& C, Photon& ph) {
                     if (count++ > 3) break;
                 }
                 ph.t = P->voidtime ? ph.t : 0.f;
-                const Prop& np = C.prop[P->vol[id] & kMED_MASK];
+                const Prop np = C.prop_of(P->vol[id] & kMED_MASK);
                 if (P->isspecular && np.n != C.prop[0].n) {
                     ph.w *= 1.f - reflectcoeff(ph.v, C.prop[0].n, np.n, fd[3]);
                     if (ph.w > kEPS) transmit(ph.v, C.prop[0].n, np.n, fd[3]);
@@ -521,7 +554,7 @@ struct Runner {
             attempts += 1.f;
             if (attempts > (float)P->maxvoidstep) return false;
         } while ((ph.mediaid & kMED_MASK) == 0 || std::fabs(ph.w) <= P->minenergy);
-        ph.prop = C.prop[ph.mediaid & kMED_MASK];
+        ph.prop = C.prop_of(ph.mediaid & kMED_MASK);
         T.e_launch += ph.w;
         T.launches++;
         ph.w0 = ph.w;
@@ -590,7 +623,7 @@ struct Runner {
             }
 
             float n1 = ph.prop.n;
-            ph.prop = C.prop[ph.mediaid];
+            ph.prop = C.prop_of(ph.mediaid);
 
             float len = hitgrid(ph.p, ph.v, ph.rv, ph.fd);
             float musp = ph.prop.mus * ((ph.nscat + 1.f > (float)P->gscatter) ? (1.f - ph.prop.g) : 1.f);
@@ -691,7 +724,7 @@ struct Runner {
             }
 
             if (C.isreflect) {
-                ph.prop = C.prop[med];
+                ph.prop = C.prop_of(med);
                 if (((med && P->isreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P->isreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != ph.prop.n)) {
@@ -726,10 +759,10 @@ struct Runner {
                         ph.fd[a] = (short)std::floor(ph.p[a]);
                         ph.idx1d = idx1dold;
                         ph.mediaid = P->vol[ph.idx1d] & kMED_MASK;
-                        ph.prop = C.prop[ph.mediaid];
+                        ph.prop = C.prop_of(ph.mediaid);
                     }
                 } else {
-                    ph.prop = C.prop[mediaidold & kMED_MASK];
+                    ph.prop = C.prop_of(mediaidold & kMED_MASK);
                 }
             }
         }

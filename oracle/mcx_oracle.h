@@ -43,6 +43,9 @@ typedef struct OracleProblem {
     int srctype;
     float srcparam1[4], srcparam2[4];
     const float* srcpattern;
+    /* MCX mediabyte: 1/2/4 label volumes; 100-104 per-voxel formats whose 32-bit words encode the
+     * properties (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730) */
+    int mediaformat;
 } OracleProblem;
 
 /* Outputs: raw (unnormalised) field in FP64, optional per-voxel deposit counts, detected

@@ -32,7 +32,7 @@ class OracleProblem(C.Structure):
         ("savedet", C.c_int), ("savedetflag", C.c_uint32), ("maxdetphoton", C.c_uint32), ("nphoton", C.c_uint64),
         ("photon_offset", C.c_uint64), ("seed", C.c_uint64), ("nthreads", C.c_int), ("seed_mode", C.c_int),
         ("mcx_threads", C.c_uint32), ("srctype", C.c_int), ("srcparam1", C.c_float * 4),
-        ("srcparam2", C.c_float * 4), ("srcpattern", C.c_void_p),
+        ("srcparam2", C.c_float * 4), ("srcpattern", C.c_void_p), ("mediaformat", C.c_int),
     ]
 
 
@@ -133,6 +133,7 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
     P.srcparam1[:] = [c.srcparam1.x, c.srcparam1.y, c.srcparam1.z, c.srcparam1.w]
     P.srcparam2[:] = [c.srcparam2.x, c.srcparam2.y, c.srcparam2.z, c.srcparam2.w]
     P.srcpattern = c.srcpattern
+    P.mediaformat = int(c.mediabyte)
 
     field = np.zeros(nvox * maxgate, dtype=np.float64)
     hit = np.zeros(nvox * maxgate, dtype=np.uint64) if hits else None

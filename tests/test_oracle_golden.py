@@ -178,3 +178,28 @@ def test_batch_workload_ranges():
         assert np.all((prop[1:, 2] >= 0.7) & (prop[1:, 2] <= 0.95)) and np.all(prop[1:, 3] == np.float32(1.37))
         assert 1e6 <= x["nphoton"] <= 1e8
         assert x["vol"].max() <= prop.shape[0] - 1 and x["detpos"].shape == (2, 4)
+
+
+def test_per_voxel_media_formats_in_the_oracle(engine, oracle):
+    """A label volume and the same media written per voxel (MEDIA_MUA_FLOAT: mua per voxel, mus / g /
+    n from prop row 1) describe identical physics: the oracle's histories are the same photon for
+    photon.  MEDIA_AS_F2H keeps mua and mus as binary16, so only agrees statistically."""
+    from mcx_gb300.api import pack_media
+
+    base = problems.cube60(100_000)
+    base.update(issavedet=0)
+    base.pop("detpos")
+    lab = oracle.run(engine.prepare(base), nphoton=100_000, seed=5)["stat"]
+    mua = np.full((60, 60, 60), 0.005, np.float32)
+    words = dict(base, vol=mua)
+    w = oracle.run(engine.prepare(words), nphoton=100_000, seed=5)["stat"]
+    assert engine.prepare(words).c.mediabyte == 101
+    assert w["energyabs"] == lab["energyabs"] and w["n_steps"] == lab["n_steps"]
+    f2h = dict(base, vol=np.stack([mua, np.full((60, 60, 60), 1.0, np.float32)]))
+    h = oracle.run(engine.prepare(f2h), nphoton=100_000, seed=5)["stat"]
+    assert engine.prepare(f2h).c.mediabyte == 100
+    assert abs(h["energyabs"] / h["energytot"] - lab["energyabs"] / lab["energytot"]) < 3e-3
+    # packing: truncated binary16 of 0.005 and 1.0, NaN -> void word
+    wv, fmt = pack_media(np.stack([np.array([[[0.005, np.nan]]], np.float32), np.array([[[1.0, 1.0]]], np.float32)]))
+    assert fmt == 100 and wv[0, 0, 1] == 0 and (wv[0, 0, 0] >> 16) == 0x3C00
+    assert abs(np.array([wv[0, 0, 0] & 0xFFFF], np.uint16).view(np.float16)[0] - 0.005) < 5e-6
