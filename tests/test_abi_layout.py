@@ -161,3 +161,26 @@ def test_replayinit_filters_and_weights(engine):
         assert abs(tof[k] - (detp[1:, i] * nidx).sum() * 3.335640951981520e-12) < 1e-15
     got = np.frombuffer((C.c_uint8 * 32).from_address(c.replay.seed), np.uint8).reshape(2, 16)
     assert np.array_equal(got, seeds.T[[1, 3]])
+
+
+def test_pack_media_layouts():
+    """pack_media: the 32-bit words and mediabyte of each per-voxel format (pmcx's packing)."""
+    from mcx_gb300.api import pack_media
+
+    b = np.zeros((4, 1, 1, 2), np.uint8)
+    b[:, 0, 0, 0] = [1, 2, 3, 4]
+    w, f = pack_media(b)
+    assert f == 103 and w[0, 0, 0] == 0x04030201 and w[0, 0, 1] == 0
+    s = np.zeros((2, 1, 1, 1), np.uint16)
+    s[:, 0, 0, 0] = [0x1234, 0x5678]
+    w, f = pack_media(s)
+    assert f == 104 and w[0, 0, 0] == 0x56781234
+    m = np.array([[[0.0, 0.25, np.nan]]], np.float32)
+    w, f = pack_media(m, unitinmm=2.0)
+    assert f == 101
+    assert w[0, 0, 0] == np.array(np.finfo(np.float32).eps, np.float32).view(np.uint32)   # 0 is not void
+    assert w[0, 0, 1] == np.array(0.5, np.float32).view(np.uint32) and w[0, 0, 2] == 0  # scaled; NaN void
+    w, f = pack_media(np.ones((3, 3, 3), np.uint16))
+    assert f == 2 and w.dtype == np.uint32
+    with pytest.raises(Exception):
+        pack_media(np.ones((3, 3, 3, 3), np.float32))
