@@ -154,3 +154,23 @@ def test_replay_of_reference_seeds(engine, ref, mcx_seeding):
     print("replayed", n, "detected again", o["stat"]["detected"], "with MCX's record", same)
     assert o["stat"]["detected"] >= 0.98 * n
     assert same >= 0.95 * n
+
+
+@pytest.mark.parametrize("seed", list(range(8)))
+def test_random_decks_against_the_reference(engine, ref, seed):
+    """The randomised decks of tests/test_gpu_fuzz.py (volume, inclusions, void pocket, media,
+    boundary conditions, reflection, gates, source shape, detectors) run by MCX itself: absorbed
+    fraction and detected count within 5 standard errors of the engine's."""
+    from .test_gpu_fuzz import deck
+
+    n = 1_000_000
+    cfg = deck(seed, n)
+    cfg["outputtype"] = "x"
+    r = ref.run(cfg, keep_field=False)
+    g = engine.run(deck(seed, n) | {"outputtype": "x"})["stat"]
+    fg, fr = g["energyabs"] / g["energytot"], r["absorbed"]
+    se = np.sqrt(2 * max(fg * (1 - fg), 1e-4) / n)
+    print(seed, cfg["srctype"], cfg["bc"], "absorbed engine", fg, "reference", fr, "detected", g["detected"], r["detected"])
+    assert abs(fg - fr) <= 5 * se + 2e-4, (seed, fg, fr)
+    if g["detected"] or r["detected"]:
+        assert abs(g["detected"] - r["detected"]) <= 5 * np.sqrt(g["detected"] + r["detected"]) + 3, (seed, g["detected"], r["detected"])
