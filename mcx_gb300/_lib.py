@@ -84,11 +84,31 @@ lib.mcxg_run_noalloc.restype = C.c_int
 lib.mcxg_noalloc_scratch_bytes.argtypes = []
 lib.mcxg_noalloc_scratch_bytes.restype = C.c_size_t
 
+# fluence denoiser kernels (include/mcxg_denoise.h); pointers are device addresses
+_P, _I, _LL, _F = C.c_void_p, C.c_int, C.c_longlong, C.c_float
+_DN = {
+    "mcxg_dn_conv_fwd": [_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_conv_wgrad": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_bias_grad": [_P, _P, _LL, _I, _P],
+    "mcxg_dn_pool": [_P, _P, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_upcat": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_upcat_bwd": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_unpool_add": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P],
+    "mcxg_dn_head": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _LL, _F, _P],
+    "mcxg_dn_pack": [_P, _P, _P, _P, _P, _P, _I, _LL, _I, _P],
+    "mcxg_dn_adamw": [_P, _P, _P, _P, _P, _P, _LL, _I, _I, _I, _F, _F, _F, _F, _F, _I, _P],
+}
+for _name, _args in _DN.items():
+    getattr(lib, _name).argtypes = _args
+    getattr(lib, _name).restype = C.c_int
+lib.mcxg_dn_last_error.argtypes = []
+lib.mcxg_dn_last_error.restype = C.c_char_p
+
 EXPORTED = [
     "mcx_run_simulation", "mcx_list_gpu", "mcxg_run_simulation_fp64", "mcxg_initcfg", "mcxg_validatecfg",
     "mcxg_maskdet", "mcxg_last_error", "mcxg_last_error_id", "mcxg_clear_error", "mcxg_set_error", "mcxg_get_stats",
     "mcxg_rng_test", "mcxg_photon_stream", "mcxg_session_create", "mcxg_session_reset", "mcxg_session_run",
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
     "mcxg_set_seeding", "mcxg_probe_atomic_rate",
-    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap",
-]
+    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap", "mcxg_dn_last_error",
+] + list(_DN)

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "--use_fast_math"] + ARCH
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["transport.cu", "engine.cu", "noalloc.cu"]
+CU_SOURCES = ["transport.cu", "engine.cu", "noalloc.cu", "denoise.cu"]
 CPP_SOURCES = ["preprocess.cpp"]
 
 

@@ -1,0 +1,819 @@
+// Kernels of the fluence denoiser: a 4-level 3D U-Net (16/32/64/128 channels, 3x3x3 convolutions,
+// ReLU, 2x2x2 average pooling, nearest upsampling with skip concatenation, a 1x1x1 head added to
+// the input log-fluence) trained on pairs of low- and high-photon fluence maps from this engine.
+//
+// Layout: activations are channels-last bf16, [volumes][z][y][x][channels] with x fastest over
+// voxels (MCX's own voxel order, so a fluence map is used in place); convolution weights are
+// bf16 [Cout][taps][Cin] with tap = dz*9 + dy*3 + dx; master weights, gradients and Adam moments
+// are fp32 in the same order.
+//
+// Convolutions are implicit GEMMs on the BF16 tensor cores (mma.sync m16n8k16, fp32 accumulate):
+//   forward   Y[v, co]  = sum_{t, ci} X[v + off(t), ci] * W[co, t, ci]      (M = voxels, N = Cout)
+//   data grad dX[v, ci] = sum_{t, co} dY[v + off(t), co] * W[co, 26-t, ci] (the forward kernel run
+//             on the flipped, transposed copy of W that the optimiser writes beside the weights)
+//   weight gr dW[co, t, ci] = sum_v dY[v, co] * X[v + off(t), ci]         (M = Cout, N = taps*Cin,
+//             K = voxels split across CTAs, fp32 atomics)
+// Operand tiles are staged through a 4-deep cp.async pipeline into XOR-swizzled shared memory and
+// fed to the tensor cores with ldmatrix (.trans for the weight gradient's voxel-major operands).
+// Zero padding of the 3x3x3 stencil is the cp.async zero fill.  The ReLU backward is fused: a data
+// gradient is multiplied by (layer input > 0) in its epilogue, so every gradient handed to a
+// weight-gradient launch is already the pre-activation gradient.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "mcxg_denoise.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// 16-byte asynchronous copy global -> shared; `valid` false copies nothing and fills zeros.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    int n = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t a, uint32_t (&r)[4]) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t a, uint32_t (&r)[4]) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Shared-memory tiles are rows of CPR 16-byte chunks; chunk c of row r is stored at
+// c ^ swz(r) so that the 8 rows one ldmatrix phase reads fall in 8 different bank groups.
+template <int CPR>
+__device__ __forceinline__ int swz(int r) {
+    if constexpr (CPR >= 8) return r & 7;
+    else if constexpr (CPR == 4) return (r >> 1) & 3;
+    else return (r >> 2) & 1;
+}
+
+struct Geo {
+    int nvol, d, h, w;
+    long long m;  // voxels over all volumes
+};
+
+// Neighbour of voxel (z, y, x) at tap t of a 3x3x3 stencil (t = dz*9 + dy*3 + dx), or -1 outside.
+__device__ __forceinline__ long long tap_voxel(const Geo& g, long long v, int z, int y, int x, int t, int taps) {
+    if (taps == 1) return v;
+    int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+    int zz = z + dz, yy = y + dy, xx = x + dx;
+    if (zz < 0 || zz >= g.d || yy < 0 || yy >= g.h || xx < 0 || xx >= g.w) return -1;
+    return v + (long long)dz * g.h * g.w + dy * g.w + dx;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Forward convolution (and data gradient): Y[v, n0:n0+BN] over a tile of BM = 128 voxels.
+// 256 threads; warps tile the BM x BN output as WARPS_M x WARPS_N.
+template <int BN, int BK, int STAGES>
+__global__ void __launch_bounds__(256) conv_fwd_kernel(const bf16* __restrict__ x, const bf16* __restrict__ wt,
+                                                       const float* __restrict__ bias, const bf16* __restrict__ mask,
+                                                       bf16* __restrict__ y, Geo g, int cin, int cout, int taps,
+                                                       int relu) {
+    constexpr int BM = 128;
+    constexpr int CPR = BK / 8;
+    constexpr int WARPS_N = BN >= 64 ? BN / 32 : 1;
+    constexpr int WARPS_M = 8 / WARPS_N;
+    constexpr int WM = BM / WARPS_M, WN = BN / WARPS_N;
+    constexpr int MI = WM / 16, NI = WN / 8;
+    constexpr int A_ELEMS = BM * BK, B_ELEMS = BN * BK;
+    constexpr int STAGE = A_ELEMS + B_ELEMS;
+    constexpr int A_IT = BM * CPR / 256;
+    static_assert(NI % 2 == 0 && MI >= 1 && A_IT >= 1, "tile shape");
+
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    bf16* sm = reinterpret_cast<bf16*>(dyn_smem);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm0 = (warp / WARPS_N) * WM, wn0 = (warp % WARPS_N) * WN;
+    const long long m0 = (long long)blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+    const int kc = cin / BK;
+    const int ktiles = taps * kc;
+
+    // voxel coordinates of the A rows this thread loads (fixed over the K loop)
+    long long av[A_IT];
+    int az[A_IT], ay[A_IT], ax[A_IT];
+#pragma unroll
+    for (int i = 0; i < A_IT; ++i) {
+        int row = (tid + i * 256) / CPR;
+        long long v = m0 + row;
+        av[i] = v < g.m ? v : -1;
+        long long r = v % ((long long)g.d * g.h * g.w);
+        ax[i] = (int)(r % g.w);
+        ay[i] = (int)((r / g.w) % g.h);
+        az[i] = (int)(r / ((long long)g.w * g.h));
+    }
+
+    auto load_stage = [&](int stage, int kt) {
+        bf16* sa = sm + stage * STAGE;
+        bf16* sb = sa + A_ELEMS;
+        const int t = kt / kc, c0 = (kt % kc) * BK;
+#pragma unroll
+        for (int i = 0; i < A_IT; ++i) {
+            int q = tid + i * 256, row = q / CPR, c = q % CPR;
+            long long src = av[i] >= 0 ? tap_voxel(g, av[i], az[i], ay[i], ax[i], t, taps) : -1;
+            const bf16* p = src >= 0 ? x + src * cin + c0 + c * 8 : x;
+            cp_async16(smem_addr(sa + row * BK + ((c ^ swz<CPR>(row)) << 3)), p, src >= 0);
+        }
+        for (int q = tid; q < BN * CPR; q += 256) {
+            int row = q / CPR, c = q % CPR;
+            const bf16* p = wt + ((long long)(n0 + row) * taps + t) * cin + c0 + c * 8;
+            cp_async16(smem_addr(sb + row * BK + ((c ^ swz<CPR>(row)) << 3)), p, true);
+        }
+    };
+
+    float acc[MI][NI][4];
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < ktiles) load_stage(s, s);
+        cp_commit();
+    }
+    for (int kt = 0; kt < ktiles; ++kt) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        const bf16* sa = sm + (kt % STAGES) * STAGE;
+        const bf16* sb = sa + A_ELEMS;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+            uint32_t af[MI][4];
+#pragma unroll
+            for (int i = 0; i < MI; ++i) {
+                int row = wm0 + i * 16 + (lane & 15), c = kk * 2 + (lane >> 4);
+                ldsm_x4(smem_addr(sa + row * BK + ((c ^ swz<CPR>(row)) << 3)), af[i]);
+            }
+#pragma unroll
+            for (int jj = 0; jj < NI / 2; ++jj) {
+                uint32_t bfr[4];
+                int row = wn0 + jj * 16 + (lane & 7) + ((lane >> 4) << 3), c = kk * 2 + ((lane >> 3) & 1);
+                ldsm_x4(smem_addr(sb + row * BK + ((c ^ swz<CPR>(row)) << 3)), bfr);
+#pragma unroll
+                for (int i = 0; i < MI; ++i) {
+                    mma_bf16(acc[i][2 * jj], af[i], bfr[0], bfr[1]);
+                    mma_bf16(acc[i][2 * jj + 1], af[i], bfr[2], bfr[3]);
+                }
+            }
+        }
+        int nk = kt + STAGES - 1;
+        if (nk < ktiles) load_stage(nk % STAGES, nk);
+        cp_commit();
+    }
+    cp_wait<0>();
+    __syncthreads();
+
+    // epilogue: bias + ReLU into a padded shared tile, then 16-byte rows to global (times the mask)
+    constexpr int EP = BN + 8;
+    bf16* se = sm;
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+            int row = wm0 + i * 16 + (lane >> 2), col = wn0 + j * 8 + (lane & 3) * 2;
+            float b0 = bias ? bias[n0 + col] : 0.f, b1 = bias ? bias[n0 + col + 1] : 0.f;
+            float v0 = acc[i][j][0] + b0, v1 = acc[i][j][1] + b1, v2 = acc[i][j][2] + b0, v3 = acc[i][j][3] + b1;
+            if (relu) {
+                v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f);
+            }
+            *reinterpret_cast<__nv_bfloat162*>(se + row * EP + col) = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162*>(se + (row + 8) * EP + col) = __floats2bfloat162_rn(v2, v3);
+        }
+    __syncthreads();
+    constexpr int CH = BN / 8;
+    for (int q = tid; q < BM * CH; q += 256) {
+        int row = q / CH, c = q % CH;
+        long long v = m0 + row;
+        if (v >= g.m) continue;
+        uint4 val = *reinterpret_cast<const uint4*>(se + row * EP + c * 8);
+        long long off = v * cout + n0 + c * 8;
+        if (mask) {
+            uint4 mk = *reinterpret_cast<const uint4*>(mask + off);
+            uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
+            const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                // keep each bf16 where the mask's bf16 is > 0 (sign bit clear and not +0)
+                uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
+                uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
+                                ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
+                pv[e] &= keep;
+            }
+        }
+        *reinterpret_cast<uint4*>(y + off) = val;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Weight gradient: dW[co, n] += sum_v dY[v, co] * X[v + off(t), ci], n = t*Cin + ci, over the
+// voxel slice [blockIdx.y*kslice, +kslice).  BM = Cout (the whole output-channel range), BN = 64
+// columns of (tap, ci); 128 threads; K staged 32 voxels at a time.
+template <int BM, int STAGES>
+__global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict__ dy, const bf16* __restrict__ x,
+                                                         float* __restrict__ dw, Geo g, int cin, int taps,
+                                                         long long kslice) {
+    constexpr int BN = 64, BK = 32;
+    constexpr int CPA = BM / 8, CPB = BN / 8;
+    constexpr int WARPS_M = BM >= 32 ? 2 : 1;
+    constexpr int WARPS_N = 4 / WARPS_M;
+    constexpr int WM = BM / WARPS_M, WN = BN / WARPS_N;
+    constexpr int MI = WM / 16, NI = WN / 8;
+    constexpr int A_ELEMS = BK * BM, B_ELEMS = BK * BN;
+    constexpr int STAGE = A_ELEMS + B_ELEMS;
+    static_assert(NI % 2 == 0 && MI >= 1, "tile shape");
+
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    bf16* sm = reinterpret_cast<bf16*>(dyn_smem);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm0 = (warp / WARPS_N) * WM, wn0 = (warp % WARPS_N) * WN;
+    const int ntot = taps * cin;
+    const int nt0 = blockIdx.x * BN;
+    const long long kbeg = (long long)blockIdx.y * kslice;
+    const long long kend = min(g.m, kbeg + kslice);
+    if (kbeg >= kend) return;
+    const int ktiles = (int)((kend - kbeg + BK - 1) / BK);
+    const long long vvol = (long long)g.d * g.h * g.w;
+
+    auto load_stage = [&](int stage, int kt) {
+        bf16* sa = sm + stage * STAGE;
+        bf16* sb = sa + A_ELEMS;
+        const long long vb = kbeg + (long long)kt * BK;
+        for (int q = tid; q < BK * CPA; q += 128) {
+            int row = q / CPA, c = q % CPA;
+            long long v = vb + row;
+            bool ok = v < kend;
+            const bf16* p = ok ? dy + v * BM + c * 8 : dy;
+            cp_async16(smem_addr(sa + row * BM + ((c ^ swz<CPA>(row)) << 3)), p, ok);
+        }
+#pragma unroll
+        for (int i = 0; i < BK * CPB / 128; ++i) {
+            int q = tid + i * 128, row = q / CPB, c = q % CPB;
+            long long v = vb + row;
+            int n = nt0 + c * 8;
+            long long src = -1;
+            if (v < kend && n < ntot) {
+                int t = n / cin;
+                long long r = v % vvol;
+                int xx = (int)(r % g.w), yy = (int)((r / g.w) % g.h), zz = (int)(r / ((long long)g.w * g.h));
+                src = tap_voxel(g, v, zz, yy, xx, t, taps);
+            }
+            const bf16* p = src >= 0 ? x + src * cin + (n % cin) : x;
+            cp_async16(smem_addr(sb + row * BN + ((c ^ swz<CPB>(row)) << 3)), p, src >= 0);
+        }
+    };
+
+    float acc[MI][NI][4];
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < ktiles) load_stage(s, s);
+        cp_commit();
+    }
+    for (int kt = 0; kt < ktiles; ++kt) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        const bf16* sa = sm + (kt % STAGES) * STAGE;
+        const bf16* sb = sa + A_ELEMS;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+            const int qm = lane >> 3, r8 = lane & 7;
+            uint32_t af[MI][4];
+#pragma unroll
+            for (int i = 0; i < MI; ++i) {
+                int row = kk * 16 + r8 + ((qm >> 1) << 3);
+                int c = (wm0 + i * 16) / 8 + (qm & 1);
+                ldsm_x4_t(smem_addr(sa + row * BM + ((c ^ swz<CPA>(row)) << 3)), af[i]);
+            }
+#pragma unroll
+            for (int jj = 0; jj < NI / 2; ++jj) {
+                uint32_t bfr[4];
+                int row = kk * 16 + r8 + ((qm & 1) << 3);
+                int c = (wn0 + jj * 16) / 8 + (qm >> 1);
+                ldsm_x4_t(smem_addr(sb + row * BN + ((c ^ swz<CPB>(row)) << 3)), bfr);
+#pragma unroll
+                for (int i = 0; i < MI; ++i) {
+                    mma_bf16(acc[i][2 * jj], af[i], bfr[0], bfr[1]);
+                    mma_bf16(acc[i][2 * jj + 1], af[i], bfr[2], bfr[3]);
+                }
+            }
+        }
+        int nk = kt + STAGES - 1;
+        if (nk < ktiles) load_stage(nk % STAGES, nk);
+        cp_commit();
+    }
+    cp_wait<0>();
+
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+            int co = wm0 + i * 16 + (lane >> 2);
+            int n = nt0 + wn0 + j * 8 + (lane & 3) * 2;
+            if (n < ntot) {
+                atomicAdd(dw + (long long)co * ntot + n, acc[i][j][0]);
+                atomicAdd(dw + (long long)(co + 8) * ntot + n, acc[i][j][2]);
+            }
+            if (n + 1 < ntot) {
+                atomicAdd(dw + (long long)co * ntot + n + 1, acc[i][j][1]);
+                atomicAdd(dw + (long long)(co + 8) * ntot + n + 1, acc[i][j][3]);
+            }
+        }
+}
+
+// db[c] += sum_v dY[v, c]
+__global__ void bias_grad_kernel(const bf16* __restrict__ dy, float* __restrict__ db, long long m, int c,
+                                 long long rows_per_block) {
+    const int lanes = blockDim.x / c;  // rows processed side by side
+    const int ch = threadIdx.x % c, r0 = threadIdx.x / c;
+    long long beg = blockIdx.x * rows_per_block, end = min(m, beg + rows_per_block);
+    float s = 0.f;
+    for (long long v = beg + r0; v < end; v += lanes) s += __bfloat162float(dy[v * c + ch]);
+    atomicAdd(db + ch, s);
+}
+
+__device__ __forceinline__ void load8(const bf16* p, float (&f)[8]) {
+    uint4 u = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float2 t = __bfloat1622float2(h[e]);
+        f[2 * e] = t.x;
+        f[2 * e + 1] = t.y;
+    }
+}
+__device__ __forceinline__ void store8(bf16* p, const float (&f)[8]) {
+    uint4 u;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(f[2 * e], f[2 * e + 1]);
+    *reinterpret_cast<uint4*>(p) = u;
+}
+
+// 2x2x2 average pooling; (d, h, w) are the fine grid's sizes.  One thread per coarse voxel and
+// 8-channel chunk.
+__global__ void pool_kernel(const bf16* __restrict__ x, bf16* __restrict__ y, int nvol, int d, int h, int w, int c) {
+    const int d2 = d / 2, h2 = h / 2, w2 = w / 2, cc = c / 8;
+    long long total = (long long)nvol * d2 * h2 * w2 * cc;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        int ch = (int)(q % cc);
+        long long v = q / cc;
+        int xx = (int)(v % w2), yy = (int)((v / w2) % h2), zz = (int)((v / ((long long)w2 * h2)) % d2);
+        long long n = v / ((long long)w2 * h2 * d2);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 8; ++k) {
+            long long fv = ((n * d + 2 * zz + (k >> 2)) * h + 2 * yy + ((k >> 1) & 1)) * w + 2 * xx + (k & 1);
+            float f[8];
+            load8(x + fv * c + ch * 8, f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[e] += f[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] *= 0.125f;
+        store8(y + v * c + ch * 8, s);
+    }
+}
+
+// cat[v, 0:c1] = low[parent(v)], cat[v, c1:c1+c2] = skip[v]; (d, h, w) fine sizes.
+__global__ void upcat_kernel(const bf16* __restrict__ low, const bf16* __restrict__ skip, bf16* __restrict__ cat,
+                             int nvol, int d, int h, int w, int c1, int c2) {
+    const int ct = (c1 + c2) / 8;
+    long long total = (long long)nvol * d * h * w * ct;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        int ch = (int)(q % ct);
+        long long v = q / ct;
+        const bf16* src;
+        if (ch * 8 < c1) {
+            int xx = (int)(v % w), yy = (int)((v / w) % h), zz = (int)((v / ((long long)w * h)) % d);
+            long long n = v / ((long long)w * h * d);
+            long long pv = ((n * (d / 2) + zz / 2) * (h / 2) + yy / 2) * (w / 2) + xx / 2;
+            src = low + pv * c1 + ch * 8;
+        } else {
+            src = skip + v * c2 + (ch * 8 - c1);
+        }
+        *reinterpret_cast<uint4*>(cat + v * (c1 + c2) + ch * 8) = *reinterpret_cast<const uint4*>(src);
+    }
+}
+
+// dlow[u, c] = (sum over the 8 children of dcat[child, c]) * (low[u, c] > 0), c < c1.
+__global__ void upcat_bwd_kernel(const bf16* __restrict__ dcat, const bf16* __restrict__ low, bf16* __restrict__ dlow,
+                                 int nvol, int d, int h, int w, int c1, int c2) {
+    const int d2 = d / 2, h2 = h / 2, w2 = w / 2, cc = c1 / 8, ct = c1 + c2;
+    long long total = (long long)nvol * d2 * h2 * w2 * cc;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        int ch = (int)(q % cc);
+        long long u = q / cc;
+        int xx = (int)(u % w2), yy = (int)((u / w2) % h2), zz = (int)((u / ((long long)w2 * h2)) % d2);
+        long long n = u / ((long long)w2 * h2 * d2);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 8; ++k) {
+            long long fv = ((n * d + 2 * zz + (k >> 2)) * h + 2 * yy + ((k >> 1) & 1)) * w + 2 * xx + (k & 1);
+            float f[8];
+            load8(dcat + fv * ct + ch * 8, f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[e] += f[e];
+        }
+        float lv[8];
+        load8(low + u * c1 + ch * 8, lv);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] = lv[e] > 0.f ? s[e] : 0.f;
+        store8(dlow + u * c1 + ch * 8, s);
+    }
+}
+
+// denc[v, c] = (dpool[parent(v), c] / 8 + dcat[v, c1 + c]) * (enc[v, c] > 0); dcat may be null
+// (no skip path).  (d, h, w) fine sizes; c = encoder channels.
+__global__ void unpool_add_kernel(const bf16* __restrict__ dpool, const bf16* __restrict__ dcat,
+                                  const bf16* __restrict__ enc, bf16* __restrict__ denc, int nvol, int d, int h, int w,
+                                  int c1, int c) {
+    const int cc = c / 8;
+    long long total = (long long)nvol * d * h * w * cc;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        int ch = (int)(q % cc);
+        long long v = q / cc;
+        int xx = (int)(v % w), yy = (int)((v / w) % h), zz = (int)((v / ((long long)w * h)) % d);
+        long long n = v / ((long long)w * h * d);
+        long long pv = ((n * (d / 2) + zz / 2) * (h / 2) + yy / 2) * (w / 2) + xx / 2;
+        float a[8], b[8], e8[8];
+        load8(dpool + pv * c + ch * 8, a);
+        if (dcat) load8(dcat + v * (c1 + c) + c1 + ch * 8, b);
+        else
+            for (int e = 0; e < 8; ++e) b[e] = 0.f;
+        load8(enc + v * c + ch * 8, e8);
+        float o[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) o[e] = e8[e] > 0.f ? a[e] * 0.125f + b[e] : 0.f;
+        store8(denc + v * c + ch * 8, o);
+    }
+}
+
+// Head: out[v] = xres[v] + b + sum_c w[c] * act[v, c] (16 channels).  With a target, also the
+// masked L1 loss, dact = g * w * (act > 0), dw += g * act, db += g, g = sign(out - t) * valid * inv.
+__global__ void __launch_bounds__(256) head_kernel(const bf16* __restrict__ act, const float* __restrict__ xres,
+                                                   const float* __restrict__ w, const float* __restrict__ b,
+                                                   const float* __restrict__ target, const float* __restrict__ valid,
+                                                   float* __restrict__ out, bf16* __restrict__ dact,
+                                                   float* __restrict__ dw, float* __restrict__ db,
+                                                   float* __restrict__ loss, long long m, float inv) {
+    __shared__ float red[8][18];
+    float gw[16], gb = 0.f, ls = 0.f;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) gw[c] = 0.f;
+    float wc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) wc[c] = w[c];
+    const float bias = b[0];
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < m; v += (long long)gridDim.x * blockDim.x) {
+        float a[16];
+        float lo[8], hi[8];
+        load8(act + v * 16, lo);
+        load8(act + v * 16 + 8, hi);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            a[e] = lo[e];
+            a[8 + e] = hi[e];
+        }
+        float o = xres[v] + bias;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) o = fmaf(wc[c], a[c], o);
+        if (out) out[v] = o;
+        if (target) {
+            float diff = o - target[v], vl = valid[v];
+            ls += fabsf(diff) * vl;
+            float gr = (diff > 0.f ? 1.f : (diff < 0.f ? -1.f : 0.f)) * vl * inv;
+            gb += gr;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) gw[c] += gr * a[c];
+            float da[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) da[c] = a[c] > 0.f ? gr * wc[c] : 0.f;
+            float d0[8], d1[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                d0[e] = da[e];
+                d1[e] = da[8 + e];
+            }
+            store8(dact + v * 16, d0);
+            store8(dact + v * 16 + 8, d1);
+        }
+    }
+    if (!target) return;
+    // block reduction of the 18 sums (16 weights, bias, loss)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float vals[18];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) vals[c] = gw[c];
+    vals[16] = gb;
+    vals[17] = ls;
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+        float s = vals[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[warp][k] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 18) {
+        float s = 0.f;
+        for (int k = 0; k < (int)(blockDim.x / 32); ++k) s += red[k][threadIdx.x];
+        if (threadIdx.x < 16) atomicAdd(dw + threadIdx.x, s);
+        else if (threadIdx.x == 16) atomicAdd(db, s);
+        else atomicAdd(loss, s);
+    }
+}
+
+// Input features of one voxel (16 channels, 0..4 used):
+//   0: (log10(F + 1e-10) + 5) / 3 of the noisy fluence F
+//   1: log10(mua) + 2        2: log10(mus * (1 - g))        3: (log10(photons) - 5.5) * 2
+// and xres[v] = log10(F + 1e-10), the residual base the head adds its correction to.
+__global__ void pack_kernel(const float* __restrict__ flux, const uint8_t* __restrict__ label,
+                            const float* __restrict__ props, const float* __restrict__ log_photons,
+                            bf16* __restrict__ x0, float* __restrict__ xres, int nvol, long long vox, int nprop) {
+    long long total = (long long)nvol * vox;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < total; v += (long long)gridDim.x * blockDim.x) {
+        int n = (int)(v / vox);
+        int lab = label[v];
+        if (lab >= nprop) lab = nprop - 1;
+        const float* pr = props + ((long long)n * nprop + lab) * 4;
+        float l = log10f(fmaxf(flux[v], 0.f) + 1e-10f);
+        float f[8], z[8];
+        f[0] = (l + 5.f) * (1.f / 3.f);
+        f[1] = pr[0] > 0.f ? log10f(pr[0]) + 2.f : -2.f;
+        float musp = pr[1] * (1.f - pr[2]);
+        f[2] = musp > 0.f ? log10f(musp) : -3.f;
+        f[3] = (log_photons[n] - 5.5f) * 2.f;
+        for (int e = 4; e < 8; ++e) f[e] = 0.f;
+        for (int e = 0; e < 8; ++e) z[e] = 0.f;
+        store8(x0 + v * 16, f);
+        store8(x0 + v * 16 + 8, z);
+        xres[v] = l;
+    }
+}
+
+// AdamW on fp32 master weights (decoupled weight decay), gradient cleared after use.  Writes the
+// bf16 weights and, for a convolution (taps > 0), the flipped transposed copy the data gradient
+// runs on: wt[ci][taps-1-t][co] = w[co][t][ci].
+__global__ void adamw_kernel(float* __restrict__ master, float* __restrict__ grad, float* __restrict__ m1,
+                             float* __restrict__ m2, bf16* __restrict__ w16, bf16* __restrict__ wt16, long long n,
+                             int cout, int taps, int cin, float lr, float b1, float b2, float eps, float wd,
+                             float bc1, float bc2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float gr = grad[i];
+        float a = b1 * m1[i] + (1.f - b1) * gr;
+        float s = b2 * m2[i] + (1.f - b2) * gr * gr;
+        m1[i] = a;
+        m2[i] = s;
+        float p = master[i];
+        p -= lr * (wd * p + (a / bc1) / (sqrtf(s / bc2) + eps));
+        master[i] = p;
+        grad[i] = 0.f;
+        bf16 pb = __float2bfloat16_rn(p);
+        if (w16) w16[i] = pb;
+        if (wt16 && taps > 0) {
+            int ci = (int)(i % cin);
+            int t = (int)((i / cin) % taps);
+            int co = (int)(i / ((long long)cin * taps));
+            wt16[((long long)ci * taps + (taps - 1 - t)) * cout + co] = pb;
+        }
+    }
+}
+
+thread_local char g_err[256];
+
+int fail(const char* msg) {
+    snprintf(g_err, sizeof(g_err), "%s", msg);
+    return -1;
+}
+
+int launched() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof(g_err), "denoiser kernel launch: %s", cudaGetErrorString(e));
+        return -(int)e;
+    }
+    return 0;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int grid_for(long long work, int block) {
+    long long g = (work + block - 1) / block;
+    return (int)(g < 1 ? 1 : (g > 152 * 32 ? 152 * 32 : g));
+}
+
+template <int BN, int BK>
+int conv_fwd_launch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
+                    int cout, int taps, int relu, cudaStream_t st) {
+    constexpr int STAGES = 4, BM = 128;
+    constexpr int stage_bytes = (BM + BN) * BK * 2;
+    constexpr int epi_bytes = BM * (BN + 8) * 2;
+    constexpr int smem = STAGES * stage_bytes > epi_bytes ? STAGES * stage_bytes : epi_bytes;
+    auto kern = conv_fwd_kernel<BN, BK, STAGES>;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    dim3 grid((unsigned)((g.m + BM - 1) / BM), (unsigned)(cout / BN));
+    kern<<<grid, 256, smem, st>>>(x, w, bias, mask, y, g, cin, cout, taps, relu);
+    return launched();
+}
+
+template <int BK>
+int conv_fwd_bn(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin, int cout,
+                int taps, int relu, cudaStream_t st) {
+    if (cout % 128 == 0) return conv_fwd_launch<128, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    if (cout % 64 == 0) return conv_fwd_launch<64, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    if (cout % 32 == 0) return conv_fwd_launch<32, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    return conv_fwd_launch<16, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+}
+
+template <int BM>
+int wgrad_launch(const bf16* dy, const bf16* x, float* dw, Geo g, int cin, int taps, cudaStream_t st) {
+    constexpr int STAGES = 4;
+    constexpr int smem = STAGES * (32 * BM + 32 * 64) * 2;
+    auto kern = conv_wgrad_kernel<BM, STAGES>;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    const int ntiles = (taps * cin + 63) / 64;
+    // about 4 CTAs per SM over the (column tile, voxel slice) grid, slices a multiple of 32 voxels
+    long long want = 152 * 4 / ntiles;
+    if (want < 1) want = 1;
+    long long kslice = (g.m + want - 1) / want;
+    kslice = ((kslice + 31) / 32) * 32;
+    if (kslice < 256) kslice = 256;
+    unsigned nsl = (unsigned)((g.m + kslice - 1) / kslice);
+    kern<<<dim3((unsigned)ntiles, nsl), 128, smem, st>>>(dy, x, dw, g, cin, taps, kslice);
+    return launched();
+}
+
+Geo make_geo(int nvol, int d, int h, int w) {
+    Geo g;
+    g.nvol = nvol;
+    g.d = d;
+    g.h = h;
+    g.w = w;
+    g.m = (long long)nvol * d * h * w;
+    return g;
+}
+
+bool dims_ok(int nvol, int d, int h, int w) { return nvol > 0 && d > 0 && h > 0 && w > 0; }
+
+}  // namespace
+
+extern "C" {
+
+const char* mcxg_dn_last_error(void) { return g_err; }
+
+int mcxg_dn_conv_fwd(const void* x, const void* w, const float* bias, const void* mask, void* y, int nvol, int d,
+                     int h, int wd, int cin, int cout, int taps, int relu, void* stream) {
+    if (!x || !w || !y || !dims_ok(nvol, d, h, wd)) return fail("conv: null tensor or empty volume");
+    if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0) return fail("conv: channel counts must be multiples of 16");
+    if (taps != 1 && taps != 27) return fail("conv: taps must be 1 or 27");
+    if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
+        return fail("conv: tensors must be 16-byte aligned");
+    Geo g = make_geo(nvol, d, h, wd);
+    auto st = static_cast<cudaStream_t>(stream);
+    auto X = static_cast<const bf16*>(x);
+    auto W = static_cast<const bf16*>(w);
+    auto M = static_cast<const bf16*>(mask);
+    auto Y = static_cast<bf16*>(y);
+    if (cin % 32 == 0) return conv_fwd_bn<32>(X, W, bias, M, Y, g, cin, cout, taps, relu, st);
+    return conv_fwd_bn<16>(X, W, bias, M, Y, g, cin, cout, taps, relu, st);
+}
+
+int mcxg_dn_conv_wgrad(const void* dy, const void* x, float* dw, int nvol, int d, int h, int wd, int cin, int cout,
+                       int taps, void* stream) {
+    if (!dy || !x || !dw || !dims_ok(nvol, d, h, wd)) return fail("wgrad: null tensor or empty volume");
+    if (cin % 16 || cin <= 0) return fail("wgrad: input channels must be a multiple of 16");
+    if (taps != 1 && taps != 27) return fail("wgrad: taps must be 1 or 27");
+    if (!aligned16(dy) || !aligned16(x)) return fail("wgrad: tensors must be 16-byte aligned");
+    Geo g = make_geo(nvol, d, h, wd);
+    auto st = static_cast<cudaStream_t>(stream);
+    auto DY = static_cast<const bf16*>(dy);
+    auto X = static_cast<const bf16*>(x);
+    switch (cout) {
+        case 16: return wgrad_launch<16>(DY, X, dw, g, cin, taps, st);
+        case 32: return wgrad_launch<32>(DY, X, dw, g, cin, taps, st);
+        case 64: return wgrad_launch<64>(DY, X, dw, g, cin, taps, st);
+        case 128: return wgrad_launch<128>(DY, X, dw, g, cin, taps, st);
+        default: return fail("wgrad: output channels must be 16, 32, 64 or 128");
+    }
+}
+
+int mcxg_dn_bias_grad(const void* dy, float* db, long long m, int c, void* stream) {
+    if (!dy || !db || m <= 0) return fail("bias grad: null tensor or no voxels");
+    if (c <= 0 || 256 % c) return fail("bias grad: channels must divide 256");
+    long long rows = 4096;
+    unsigned blocks = (unsigned)((m + rows - 1) / rows);
+    bias_grad_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(dy), db, m, c, rows);
+    return launched();
+}
+
+int mcxg_dn_pool(const void* x, void* y, int nvol, int d, int h, int w, int c, void* stream) {
+    if (!x || !y || !dims_ok(nvol, d, h, w) || (d | h | w) & 1 || c % 8) return fail("pool: bad shape");
+    long long work = (long long)nvol * (d / 2) * (h / 2) * (w / 2) * (c / 8);
+    pool_kernel<<<grid_for(work, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(x), static_cast<bf16*>(y), nvol, d, h, w, c);
+    return launched();
+}
+
+int mcxg_dn_upcat(const void* low, const void* skip, void* cat, int nvol, int d, int h, int w, int c1, int c2,
+                  void* stream) {
+    if (!low || !skip || !cat || !dims_ok(nvol, d, h, w) || (d | h | w) & 1 || c1 % 8 || c2 % 8)
+        return fail("upcat: bad shape");
+    long long work = (long long)nvol * d * h * w * ((c1 + c2) / 8);
+    upcat_kernel<<<grid_for(work, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(low), static_cast<const bf16*>(skip), static_cast<bf16*>(cat), nvol, d, h, w, c1, c2);
+    return launched();
+}
+
+int mcxg_dn_upcat_bwd(const void* dcat, const void* low, void* dlow, int nvol, int d, int h, int w, int c1, int c2,
+                      void* stream) {
+    if (!dcat || !low || !dlow || !dims_ok(nvol, d, h, w) || (d | h | w) & 1 || c1 % 8 || c2 % 8)
+        return fail("upcat backward: bad shape");
+    long long work = (long long)nvol * (d / 2) * (h / 2) * (w / 2) * (c1 / 8);
+    upcat_bwd_kernel<<<grid_for(work, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dcat), static_cast<const bf16*>(low), static_cast<bf16*>(dlow), nvol, d, h, w, c1, c2);
+    return launched();
+}
+
+int mcxg_dn_unpool_add(const void* dpool, const void* dcat, const void* enc, void* denc, int nvol, int d, int h, int w,
+                       int c1, int c, void* stream) {
+    if (!dpool || !enc || !denc || !dims_ok(nvol, d, h, w) || (d | h | w) & 1 || c % 8 || c1 % 8)
+        return fail("unpool: bad shape");
+    long long work = (long long)nvol * d * h * w * (c / 8);
+    unpool_add_kernel<<<grid_for(work, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dpool), static_cast<const bf16*>(dcat), static_cast<const bf16*>(enc),
+        static_cast<bf16*>(denc), nvol, d, h, w, c1, c);
+    return launched();
+}
+
+int mcxg_dn_head(const void* act, const float* xres, const float* w, const float* b, const float* target,
+                 const float* valid, float* out, void* dact, float* dw, float* db, float* loss, long long m, float inv,
+                 void* stream) {
+    if (!act || !xres || !w || !b || m <= 0) return fail("head: null tensor or no voxels");
+    if (target && (!valid || !dact || !dw || !db || !loss)) return fail("head: training needs valid/dact/dw/db/loss");
+    if (!target && !out) return fail("head: nothing to write");
+    head_kernel<<<grid_for(m, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(act), xres, w, b, target, valid, out, static_cast<bf16*>(dact), dw, db, loss, m, inv);
+    return launched();
+}
+
+int mcxg_dn_pack(const float* flux, const uint8_t* label, const float* props, const float* log_photons, void* x0,
+                 float* xres, int nvol, long long vox, int nprop, void* stream) {
+    if (!flux || !label || !props || !log_photons || !x0 || !xres || nvol <= 0 || vox <= 0 || nprop <= 0)
+        return fail("pack: bad arguments");
+    pack_kernel<<<grid_for((long long)nvol * vox, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        flux, label, props, log_photons, static_cast<bf16*>(x0), xres, nvol, vox, nprop);
+    return launched();
+}
+
+int mcxg_dn_adamw(float* master, float* grad, float* m1, float* m2, void* w16, void* wt16, long long n, int cout,
+                  int taps, int cin, float lr, float b1, float b2, float eps, float wd, int step, void* stream) {
+    if (!master || !grad || !m1 || !m2 || n <= 0 || step < 1) return fail("adamw: bad arguments");
+    if (wt16 && (taps <= 0 || (long long)cout * taps * cin != n)) return fail("adamw: transposed copy needs the shape");
+    float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
+    adamw_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        master, grad, m1, m2, static_cast<bf16*>(w16), static_cast<bf16*>(wt16), n, cout, taps, cin, lr, b1, b2, eps,
+        wd, bc1, bc2);
+    return launched();
+}
+
+}  // extern "C"

@@ -1,0 +1,510 @@
+"""MC + learned denoiser: a 4-level 3D U-Net that maps low-photon fluence to high-photon fluence.
+
+The network works on log10 fluence: its input features are the noisy map, the voxel's absorption
+and reduced scattering coefficients and the photon count (``mcxg_dn_pack``); 3x3x3 convolutions
+with ReLU at 16/32/64/128 channels, 2x2x2 average pooling, nearest upsampling with skip
+concatenation, and a 1x1x1 head whose output is added to the input log-fluence (the network
+learns a correction; at initialisation it is nearly the identity).
+
+Everything on the device runs on this engine's own kernels (include/mcxg_denoise.h): BF16
+tensor-core implicit-GEMM convolutions forward, data and weight gradient, pooling, upsampling,
+the fused head + masked-L1 loss, and AdamW on fp32 master weights.  PyTorch only owns device
+memory and the stream.  Training pairs come from the engine itself (``make_pairs``): the same
+volume simulated at 1e5 / 1e6 photons (inputs) and at a high photon count (target).
+
+The MC stays the judge: ``time_to_error`` reports how long plain MC needs to reach a given median
+relative fluence error against a high-photon run, and how long MC + denoiser needs, with plain MC
+as the fallback wherever the denoised map does not reach it.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from pathlib import Path
+from typing import Any
+
+import numpy as np
+import torch
+
+from . import problems
+from ._lib import lib
+
+# (name, input channels, output channels, level): level l runs at 1/2^l of the input grid
+LAYERS = [
+    ("enc1a", 16, 16, 0), ("enc1b", 16, 16, 0),
+    ("enc2a", 16, 32, 1), ("enc2b", 32, 32, 1),
+    ("enc3a", 32, 64, 2), ("enc3b", 64, 64, 2),
+    ("bota", 64, 128, 3), ("botb", 128, 128, 3),
+    ("dec3a", 192, 64, 2), ("dec3b", 64, 64, 2),
+    ("dec2a", 96, 32, 1), ("dec2b", 32, 32, 1),
+    ("dec1a", 48, 16, 0), ("dec1b", 16, 16, 0),
+]
+SPEC = {name: (cin, cout, lvl) for name, cin, cout, lvl in LAYERS}
+IN_CH = 16
+TAPS = 27
+FLUX_FLOOR = 1e-10          # log10(F + FLUX_FLOOR) is the network's fluence coordinate
+VALID_FRAC = 1e-4           # voxels at or above this fraction of the reference map's maximum are scored
+DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "denoiser_unet64.npz"
+
+
+def init_params(seed: int = 0) -> dict[str, np.ndarray]:
+    """He-normal convolution weights [cout, 27, cin], zero biases, a small random head."""
+    rng = np.random.default_rng(seed)
+    p = {}
+    for name, cin, cout, _ in LAYERS:
+        p[name + ".w"] = (rng.standard_normal((cout, TAPS, cin)) * math.sqrt(2.0 / (TAPS * cin))).astype(np.float32)
+        p[name + ".b"] = np.zeros(cout, np.float32)
+    p["head.w"] = (rng.standard_normal(16) * 0.01).astype(np.float32)
+    p["head.b"] = np.zeros(1, np.float32)
+    return p
+
+
+def load_params(path: str | Path = DEFAULT_WEIGHTS) -> dict[str, np.ndarray]:
+    with np.load(path) as z:
+        return {k: z[k].astype(np.float32) for k in z.files}
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _ok(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what}: {lib.mcxg_dn_last_error().decode()} ({rc})")
+
+
+class UNet:
+    """The denoiser on one GPU: fp32 master weights, bf16 copies (and the flipped transposed copies
+    the data gradient runs on), Adam moments, gradients and cached activation buffers."""
+
+    def __init__(self, params: dict[str, np.ndarray] | None = None, seed: int = 0, device: str = "cuda"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the denoiser runs on the GPU only")
+        self.dev = torch.device(device)
+        params = params if params is not None else init_params(seed)
+        self.t: dict[str, dict[str, torch.Tensor]] = {}
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        for name, cin, cout, _ in LAYERS:
+            w = torch.from_numpy(np.ascontiguousarray(params[name + ".w"], np.float32).reshape(-1)).to(self.dev)
+            b = torch.from_numpy(np.ascontiguousarray(params[name + ".b"], np.float32)).to(self.dev)
+            self.t[name] = {
+                "w": w, "b": b, "gw": torch.zeros_like(w), "gb": torch.zeros_like(b),
+                "mw": torch.zeros_like(w), "vw": torch.zeros_like(w), "mb": torch.zeros_like(b), "vb": torch.zeros_like(b),
+                "w16": torch.empty(w.numel(), dtype=torch.bfloat16, device=self.dev),
+                "wt16": torch.empty(w.numel(), dtype=torch.bfloat16, device=self.dev),
+            }
+        hw = torch.from_numpy(np.ascontiguousarray(params["head.w"], np.float32)).to(self.dev)
+        hb = torch.from_numpy(np.ascontiguousarray(params["head.b"], np.float32)).to(self.dev)
+        self.t["head"] = {"w": hw, "b": hb, "gw": torch.zeros_like(hw), "gb": torch.zeros_like(hb),
+                          "mw": torch.zeros_like(hw), "vw": torch.zeros_like(hw), "mb": torch.zeros_like(hb),
+                          "vb": torch.zeros_like(hb)}
+        self.loss_acc = torch.zeros(1, **f32)
+        self.step_count = 0
+        self._bufs: dict[tuple, torch.Tensor] = {}
+        self.refresh_bf16()
+
+    # -- parameters ---------------------------------------------------------------------------
+    def refresh_bf16(self) -> None:
+        """bf16 weights and transposed copies from the masters (an AdamW step with lr 0 and the
+        gradient left untouched would do the same; this keeps the moments as they are)."""
+        s = self._stream()
+        for name, cin, cout, _ in LAYERS:
+            t = self.t[name]
+            g = t["gw"].clone()
+            m1, m2 = t["mw"].clone(), t["vw"].clone()
+            _ok(lib.mcxg_dn_adamw(_ptr(t["w"]), _ptr(g), _ptr(m1), _ptr(m2), _ptr(t["w16"]), _ptr(t["wt16"]),
+                                  t["w"].numel(), cout, TAPS, cin, 0.0, 0.9, 0.999, 1e-8, 0.0, 1, s), "weights")
+
+    def params(self) -> dict[str, np.ndarray]:
+        p = {}
+        for name, cin, cout, _ in LAYERS:
+            p[name + ".w"] = self.t[name]["w"].cpu().numpy().reshape(cout, TAPS, cin)
+            p[name + ".b"] = self.t[name]["b"].cpu().numpy()
+        p["head.w"] = self.t["head"]["w"].cpu().numpy()
+        p["head.b"] = self.t["head"]["b"].cpu().numpy()
+        return p
+
+    def grads(self) -> dict[str, np.ndarray]:
+        g = {}
+        for name, cin, cout, _ in LAYERS:
+            g[name + ".w"] = self.t[name]["gw"].cpu().numpy().reshape(cout, TAPS, cin)
+            g[name + ".b"] = self.t[name]["gb"].cpu().numpy()
+        g["head.w"] = self.t["head"]["gw"].cpu().numpy()
+        g["head.b"] = self.t["head"]["gb"].cpu().numpy()
+        return g
+
+    def zero_grad(self) -> None:
+        for t in self.t.values():
+            t["gw"].zero_()
+            t["gb"].zero_()
+
+    def save(self, path: str | Path) -> None:
+        np.savez_compressed(path, **self.params())
+
+    # -- plumbing -----------------------------------------------------------------------------
+    @staticmethod
+    def _stream() -> int:
+        return torch.cuda.current_stream().cuda_stream
+
+    def _buf(self, key: str, n: int, dtype=torch.bfloat16) -> torch.Tensor:
+        k = (key, n, dtype)
+        b = self._bufs.get(k)
+        if b is None:
+            b = torch.empty(n, dtype=dtype, device=self.dev)
+            self._bufs[k] = b
+        return b
+
+    def _conv(self, name: str, x: torch.Tensor, y: torch.Tensor, geo: tuple, mask=None, transposed=False) -> None:
+        cin, cout, _ = SPEC[name]
+        t = self.t[name]
+        if transposed:   # data gradient: channels swap, no bias, no ReLU, times the mask
+            _ok(lib.mcxg_dn_conv_fwd(_ptr(x), _ptr(t["wt16"]), None, _ptr(mask), _ptr(y), *geo, cout, cin, TAPS, 0,
+                                     self._stream()), name + " data gradient")
+        else:
+            _ok(lib.mcxg_dn_conv_fwd(_ptr(x), _ptr(t["w16"]), _ptr(t["b"]), None, _ptr(y), *geo, cin, cout, TAPS, 1,
+                                     self._stream()), name)
+
+    # -- forward / backward -------------------------------------------------------------------
+    def pack(self, flux: torch.Tensor, labels: torch.Tensor, props: torch.Tensor, log_photons: torch.Tensor):
+        """Input features and residual base of nvol volumes: flux fp32 [nvol, vox], labels uint8
+        [nvol, vox], props fp32 [nvol, nprop, 4], log_photons fp32 [nvol]."""
+        nvol, vox = flux.shape
+        x0 = self._buf("x0", nvol * vox * IN_CH)
+        xres = self._buf("xres", nvol * vox, torch.float32)
+        _ok(lib.mcxg_dn_pack(_ptr(flux), _ptr(labels), _ptr(props), _ptr(log_photons), _ptr(x0), _ptr(xres), nvol, vox,
+                             props.shape[1], self._stream()), "pack")
+        return x0, xres
+
+    def forward(self, x0: torch.Tensor, xres: torch.Tensor, nvol: int, d: int, h: int, w: int,
+                out: torch.Tensor | None = None) -> dict[str, torch.Tensor]:
+        """Runs the network; returns the activations (kept for ``backward``) and, when `out` is
+        given, writes the predicted log10 fluence there."""
+        if d % 8 or h % 8 or w % 8:
+            raise ValueError("the U-Net needs grid sizes divisible by 8")
+        geo = [(nvol, d >> l, h >> l, w >> l) for l in range(4)]
+        vox = [nvol * (d >> l) * (h >> l) * (w >> l) for l in range(4)]
+        s = self._stream()
+        A: dict[str, torch.Tensor] = {"x0": x0, "xres": xres}
+
+        def conv(name, src, dst):
+            cin, cout, lvl = SPEC[name]
+            A[dst] = self._buf(dst, vox[lvl] * cout)
+            self._conv(name, A[src], A[dst], geo[lvl])
+
+        def pool(src, dst, lvl, c):
+            A[dst] = self._buf(dst, vox[lvl + 1] * c)
+            _ok(lib.mcxg_dn_pool(_ptr(A[src]), _ptr(A[dst]), *geo[lvl], c, s), "pool")
+
+        def upcat(low, skip, dst, lvl, c1, c2):
+            A[dst] = self._buf(dst, vox[lvl] * (c1 + c2))
+            _ok(lib.mcxg_dn_upcat(_ptr(A[low]), _ptr(A[skip]), _ptr(A[dst]), *geo[lvl], c1, c2, s), "upcat")
+
+        conv("enc1a", "x0", "e1a"); conv("enc1b", "e1a", "e1"); pool("e1", "p1", 0, 16)
+        conv("enc2a", "p1", "e2a"); conv("enc2b", "e2a", "e2"); pool("e2", "p2", 1, 32)
+        conv("enc3a", "p2", "e3a"); conv("enc3b", "e3a", "e3"); pool("e3", "p3", 2, 64)
+        conv("bota", "p3", "e4a"); conv("botb", "e4a", "e4")
+        upcat("e4", "e3", "c3", 2, 128, 64)
+        conv("dec3a", "c3", "d3a"); conv("dec3b", "d3a", "d3")
+        upcat("d3", "e2", "c2", 1, 64, 32)
+        conv("dec2a", "c2", "d2a"); conv("dec2b", "d2a", "d2")
+        upcat("d2", "e1", "c1", 0, 32, 16)
+        conv("dec1a", "c1", "d1a"); conv("dec1b", "d1a", "d1")
+        if out is not None:
+            hd = self.t["head"]
+            _ok(lib.mcxg_dn_head(_ptr(A["d1"]), _ptr(xres), _ptr(hd["w"]), _ptr(hd["b"]), None, None, _ptr(out), None,
+                                 None, None, None, vox[0], 0.0, s), "head")
+        A["_geo"] = geo
+        A["_vox"] = vox
+        return A
+
+    def backward(self, A: dict, target: torch.Tensor, valid: torch.Tensor, inv_count: float) -> None:
+        """Masked L1 loss of the predicted log-fluence against `target` (weights `valid`, scaled by
+        inv_count) and the gradients of every parameter, accumulated into the fp32 gradients."""
+        geo, vox = A["_geo"], A["_vox"]
+        s = self._stream()
+        hd = self.t["head"]
+        G: dict[str, torch.Tensor] = {}
+        G["d1"] = self._buf("g_d1", vox[0] * 16)
+        _ok(lib.mcxg_dn_head(_ptr(A["d1"]), _ptr(A["xres"]), _ptr(hd["w"]), _ptr(hd["b"]), _ptr(target), _ptr(valid),
+                             None, _ptr(G["d1"]), _ptr(hd["gw"]), _ptr(hd["gb"]), _ptr(self.loss_acc), vox[0],
+                             float(inv_count), s), "head backward")
+
+        def layer(name, gout, inp, gin=None, mask=None):
+            cin, cout, lvl = SPEC[name]
+            t = self.t[name]
+            _ok(lib.mcxg_dn_conv_wgrad(_ptr(G[gout]), _ptr(A[inp]), _ptr(t["gw"]), *geo[lvl], cin, cout, TAPS, s),
+                name + " weight gradient")
+            _ok(lib.mcxg_dn_bias_grad(_ptr(G[gout]), _ptr(t["gb"]), vox[lvl], cout, s), name + " bias gradient")
+            if gin is not None:
+                G[gin] = self._buf("g_" + gin, vox[lvl] * cin)
+                self._conv(name, G[gout], G[gin], geo[lvl], mask=None if mask is None else A[mask], transposed=True)
+
+        def upcat_bwd(gcat, low, glow, lvl, c1, c2):
+            G[glow] = self._buf("g_" + glow, vox[lvl + 1] * c1)
+            _ok(lib.mcxg_dn_upcat_bwd(_ptr(G[gcat]), _ptr(A[low]), _ptr(G[glow]), *geo[lvl], c1, c2, s), "upcat backward")
+
+        def unpool(gpool, gcat, enc, genc, lvl, c1, c):
+            G[genc] = self._buf("g_" + genc, vox[lvl] * c)
+            _ok(lib.mcxg_dn_unpool_add(_ptr(G[gpool]), _ptr(G[gcat]), _ptr(A[enc]), _ptr(G[genc]), *geo[lvl], c1, c, s),
+                "unpool")
+
+        layer("dec1b", "d1", "d1a", "d1a", "d1a")
+        layer("dec1a", "d1a", "c1", "c1", "c1")
+        upcat_bwd("c1", "d2", "d2", 0, 32, 16)
+        layer("dec2b", "d2", "d2a", "d2a", "d2a")
+        layer("dec2a", "d2a", "c2", "c2", "c2")
+        upcat_bwd("c2", "d3", "d3", 1, 64, 32)
+        layer("dec3b", "d3", "d3a", "d3a", "d3a")
+        layer("dec3a", "d3a", "c3", "c3", "c3")
+        upcat_bwd("c3", "e4", "e4", 2, 128, 64)
+        layer("botb", "e4", "e4a", "e4a", "e4a")
+        layer("bota", "e4a", "p3", "p3", None)
+        unpool("p3", "c3", "e3", "e3", 2, 128, 64)
+        layer("enc3b", "e3", "e3a", "e3a", "e3a")
+        layer("enc3a", "e3a", "p2", "p2", None)
+        unpool("p2", "c2", "e2", "e2", 1, 64, 32)
+        layer("enc2b", "e2", "e2a", "e2a", "e2a")
+        layer("enc2a", "e2a", "p1", "p1", None)
+        unpool("p1", "c1", "e1", "e1", 0, 32, 16)
+        layer("enc1b", "e1", "e1a", "e1a", "e1a")
+        layer("enc1a", "e1a", "x0")
+
+    def step(self, lr: float, weight_decay: float = 1e-4, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        """AdamW on every parameter (no decay on biases and the head); clears the gradients."""
+        self.step_count += 1
+        s = self._stream()
+        k = self.step_count
+        for name, cin, cout, _ in LAYERS:
+            t = self.t[name]
+            _ok(lib.mcxg_dn_adamw(_ptr(t["w"]), _ptr(t["gw"]), _ptr(t["mw"]), _ptr(t["vw"]), _ptr(t["w16"]),
+                                  _ptr(t["wt16"]), t["w"].numel(), cout, TAPS, cin, lr, b1, b2, eps, weight_decay, k, s),
+                name + " AdamW")
+            _ok(lib.mcxg_dn_adamw(_ptr(t["b"]), _ptr(t["gb"]), _ptr(t["mb"]), _ptr(t["vb"]), None, None, cout, 0, 0, 0,
+                                  lr, b1, b2, eps, 0.0, k, s), name + " bias AdamW")
+        hd = self.t["head"]
+        _ok(lib.mcxg_dn_adamw(_ptr(hd["w"]), _ptr(hd["gw"]), _ptr(hd["mw"]), _ptr(hd["vw"]), None, None, 16, 0, 0, 0, lr,
+                              b1, b2, eps, 0.0, k, s), "head AdamW")
+        _ok(lib.mcxg_dn_adamw(_ptr(hd["b"]), _ptr(hd["gb"]), _ptr(hd["mb"]), _ptr(hd["vb"]), None, None, 1, 0, 0, 0, lr,
+                              b1, b2, eps, 0.0, k, s), "head AdamW")
+
+    # -- inference ----------------------------------------------------------------------------
+    def denoise(self, flux: np.ndarray | torch.Tensor, vol: np.ndarray, prop: np.ndarray, nphoton: float) -> np.ndarray:
+        """Denoised fluence of one MC result: `flux` and `vol` in MCX's [x, y, z] order (first time
+        gate of a [x, y, z, t] map is used), `prop` the media table.  Returns fp32 [x, y, z]."""
+        f = np.asarray(flux, np.float32)
+        if f.ndim == 4:
+            f = f[..., 0]
+        nx, ny, nz = f.shape
+        fl = torch.from_numpy(np.ascontiguousarray(f.reshape(-1, order="F"))).to(self.dev).view(1, -1)
+        lab = torch.from_numpy(np.ascontiguousarray(np.asarray(vol, np.uint8).reshape(-1, order="F"))).to(self.dev).view(1, -1)
+        pr = torch.from_numpy(np.ascontiguousarray(prop, np.float32)).to(self.dev).view(1, -1, 4)
+        lp = torch.tensor([math.log10(nphoton)], dtype=torch.float32, device=self.dev)
+        x0, xres = self.pack(fl, lab, pr, lp)
+        out = self._buf("out", nx * ny * nz, torch.float32)
+        self.forward(x0, xres, 1, nz, ny, nx, out=out)
+        lf = out.cpu().numpy()
+        return np.clip(10.0 ** lf.astype(np.float64) - FLUX_FLOOR, 0.0, None).astype(np.float32).reshape((nx, ny, nz), order="F")
+
+
+# -- data -------------------------------------------------------------------------------------
+def median_rel_error(est: np.ndarray, ref: np.ndarray, frac: float = VALID_FRAC) -> float:
+    """Median over voxels with ref >= frac * max(ref) of |est - ref| / ref."""
+    est = np.asarray(est, np.float64).reshape(-1)
+    ref = np.asarray(ref, np.float64).reshape(-1)
+    m = ref >= frac * ref.max()
+    return float(np.median(np.abs(est[m] - ref[m]) / ref[m]))
+
+
+def _flat(f: np.ndarray) -> np.ndarray:
+    f = np.asarray(f, np.float32)
+    if f.ndim == 4:
+        f = f[..., 0]
+    return f.reshape(-1, order="F")
+
+
+def simulate(cfgs: list[dict[str, Any]], chunk: int = 96) -> list[np.ndarray]:
+    """Fluence maps (first gate, voxel order x fastest) of many simulations through the batched
+    CUDA-graph runner."""
+    from .api import run_batch
+
+    out = []
+    for i in range(0, len(cfgs), chunk):
+        res, _ = run_batch(cfgs[i:i + chunk])
+        out += [_flat(r["flux"]) for r in res]
+    return out
+
+
+def make_pairs(count: int, edge: int = 64, seed: int = 1, target_photons: float = 1e7,
+               input_photons: tuple[float, ...] = (1e5, 1e6)) -> dict[str, Any]:
+    """Training pairs: `count` random volumes (the batched workload's property ranges), each
+    simulated at every input photon count and once at `target_photons` with independent seeds.
+    Returns device tensors: inputs [len(input_photons), count, vox], target log10 fluence and
+    score weights [count, vox], labels, media tables, and the photon counts."""
+    base = problems.denoise_instances(count, edge, seed)
+    nprop = max(c["prop"].shape[0] for c in base)
+    cfgs = []
+    for k, n in enumerate((target_photons,) + tuple(input_photons)):
+        for i, c in enumerate(base):
+            cc = dict(c)
+            cc["nphoton"] = int(n)
+            cc["seed"] = int((c["seed"] + 7919 * (k + 1)) % (2**31 - 1)) or 1
+            cfgs.append(cc)
+    maps = simulate(cfgs)
+    dev = torch.device("cuda")
+    tgt = torch.from_numpy(np.stack(maps[:count])).to(dev)
+    inputs = torch.from_numpy(np.stack(maps[count:]).reshape(len(input_photons), count, -1)).to(dev)
+    props = np.zeros((count, nprop, 4), np.float32)
+    for i, c in enumerate(base):
+        props[i, :c["prop"].shape[0]] = c["prop"]
+        props[i, c["prop"].shape[0]:] = c["prop"][-1]
+    labels = torch.from_numpy(np.stack([c["vol"].reshape(-1, order="F") for c in base])).to(dev)
+    ltgt = torch.log10(tgt + FLUX_FLOOR)
+    valid = (tgt >= VALID_FRAC * tgt.amax(dim=1, keepdim=True)).float()
+    return {"inputs": inputs, "target": ltgt, "valid": valid, "labels": labels,
+            "props": torch.from_numpy(props).to(dev), "photons": tuple(float(n) for n in input_photons),
+            "edge": edge, "count": count, "target_photons": float(target_photons), "seed": seed}
+
+
+def _augment(t: torch.Tensor, edge: int, flips: tuple[bool, bool, bool]) -> torch.Tensor:
+    """Mirror in x and/or y and swap x with y ([count, vox] tensors, voxel order x fastest); the
+    pencil enters along +z, so these leave the physics unchanged."""
+    v = t.view(t.shape[0], edge, edge, edge)     # [n, z, y, x]
+    if flips[0]:
+        v = v.flip(3)
+    if flips[1]:
+        v = v.flip(2)
+    if flips[2]:
+        v = v.transpose(2, 3)
+    return v.reshape(t.shape[0], -1).contiguous()
+
+
+def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr: float = 2e-3,
+          seed: int = 0, log_every: int = 100, verbose: bool = True) -> list[float]:
+    """AdamW with a short warm-up and cosine decay over `steps` batches of `batch` volumes, each
+    with a random input photon count and a random mirror/swap.  Returns the loss per log point
+    (mean absolute log10 error over scored voxels)."""
+    rng = np.random.default_rng(seed)
+    edge, count = data["edge"], data["count"]
+    vox = edge ** 3
+    lp_all = torch.tensor([math.log10(n) for n in data["photons"]], dtype=torch.float32, device=net.dev)
+    losses, acc, nacc = [], 0.0, 0
+    warm = max(1, steps // 20)
+    for it in range(steps):
+        idx = rng.choice(count, size=batch, replace=count < batch)
+        lvl = rng.integers(0, len(data["photons"]), size=batch)
+        flips = tuple(bool(v) for v in rng.integers(0, 2, 3))
+        ii = torch.from_numpy(idx).to(net.dev)
+        ll = torch.from_numpy(lvl).to(net.dev)
+        flux = _augment(data["inputs"][ll, ii], edge, flips)
+        labels = _augment(data["labels"][ii], edge, flips)
+        target = _augment(data["target"][ii], edge, flips)
+        valid = _augment(data["valid"][ii], edge, flips)
+        x0, xres = net.pack(flux, labels, data["props"][ii].contiguous(), lp_all[ll].contiguous())
+        A = net.forward(x0, xres, batch, edge, edge, edge)
+        nval = float(valid.sum().item())
+        net.loss_acc.zero_()
+        net.backward(A, target.reshape(-1), valid.reshape(-1), 1.0 / max(nval, 1.0))
+        f = min(1.0, (it + 1) / warm) * 0.5 * (1.0 + math.cos(math.pi * it / steps))
+        net.step(lr * max(f, 0.02))
+        acc += float(net.loss_acc.item()) / max(nval, 1.0)
+        nacc += 1
+        if (it + 1) % log_every == 0 or it + 1 == steps:
+            losses.append(acc / nacc)
+            if verbose:
+                print(f"step {it + 1}: loss {acc / nacc:.4f}", flush=True)
+            acc, nacc = 0.0, 0
+    return losses
+
+
+# -- the metric -------------------------------------------------------------------------------
+def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, target: float = 0.05,
+                  ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
+                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6)) -> dict[str, Any]:
+    """Wall time to reach a median relative fluence error of `target` against a
+    `judge_photons` run, for plain MC and for MC + denoiser, on one volume.
+
+    Plain MC runs each budget of `ladder` end to end through the engine's API; its time to the
+    target is interpolated in log(error)-log(photons) between the bracketing budgets (or
+    extrapolated with the 1/sqrt(N) law beyond the last one) and priced at the measured photon
+    rate.  MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the
+    target, timed end to end (simulation, upload, network, download); where none does, plain MC
+    is the fallback and its time is the pipeline's."""
+    from .api import run
+
+    t0 = time.perf_counter()
+    judge = _flat(run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))["flux"])
+    judge_s = time.perf_counter() - t0
+    plain = []
+    for n in ladder:
+        t0 = time.perf_counter()
+        f = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))["flux"]
+        dt = time.perf_counter() - t0
+        plain.append((n, median_rel_error(_flat(f), judge), dt))
+    rate = sum(p[0] for p in plain) / sum(p[2] for p in plain)  # photons per second over the ladder
+    t_plain = None
+    for (n0, e0, _), (n1, e1, _) in zip(plain, plain[1:]):
+        if e0 > target >= e1:
+            a = math.log(e1 / e0) / math.log(n1 / n0)
+            t_plain = n0 * (target / e0) ** (1.0 / a) / rate
+            break
+    if t_plain is None:
+        n_last, e_last, _ = plain[-1]
+        n_star = n_last * (e_last / target) ** 2 if e_last > target else plain[0][0]
+        t_plain = n_star / rate
+    dn = []
+    t_dn = None
+    vol, prop = cfg["vol"], cfg["prop"]
+    net.denoise(np.ones(vol.shape, np.float32), vol, prop, 1e5)       # buffers for this grid
+    torch.cuda.synchronize()
+    for n in dn_ladder:
+        t0 = time.perf_counter()
+        f = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 100 + int(math.log10(n) * 10)))["flux"]
+        t_mc = time.perf_counter() - t0
+        d = net.denoise(f, vol, prop, n)
+        dt = time.perf_counter() - t0
+        e_raw = median_rel_error(_flat(f), judge)
+        e = median_rel_error(_flat(d), judge)
+        dn.append({"photons": n, "error": e, "error_plain": e_raw, "s": dt, "mc_s": t_mc})
+        if t_dn is None and e <= target:
+            t_dn = dt
+    fallback = t_dn is None
+    if fallback:
+        t_dn = t_plain
+    return {"plain": [{"photons": n, "error": e, "s": s} for n, e, s in plain], "denoised": dn,
+            "t_plain_s": t_plain, "t_denoised_s": t_dn, "speedup": t_plain / t_dn, "fallback": fallback,
+            "judge_photons": judge_photons, "judge_s": judge_s, "photons_per_s": rate}
+
+
+def main(argv: list[str] | None = None) -> None:
+    """``python -m mcx_gb300.denoise train ...``: simulate training pairs, train, save the weights."""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(prog="python -m mcx_gb300.denoise")
+    ap.add_argument("command", choices=["train"])
+    ap.add_argument("--count", type=int, default=192, help="training volumes")
+    ap.add_argument("--edge", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--target-photons", type=float, default=1e7)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    a = ap.parse_args(argv)
+    t0 = time.perf_counter()
+    data = make_pairs(a.count, a.edge, a.seed, a.target_photons)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net = UNet(seed=a.seed)
+    losses = train(net, data, steps=a.steps, batch=a.batch, lr=a.lr)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    net.save(a.out)
+    print(json.dumps({"volumes": a.count, "edge": a.edge, "target_photons": a.target_photons, "steps": a.steps,
+                      "batch": a.batch, "simulate_s": t1 - t0, "train_s": t2 - t1,
+                      "ms_per_step": 1e3 * (t2 - t1) / a.steps, "losses": losses, "out": a.out}))
+
+
+if __name__ == "__main__":
+    main()

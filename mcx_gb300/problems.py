@@ -200,3 +200,37 @@ def batch_instances(count: int = 256, seed: int = 20251204, budget_scale: float 
             "maxdetphoton": max(1000, int(budget * 0.005)),
         })
     return out
+
+
+def denoise_instances(count: int, edge: int, seed: int, nphoton: float = 1e6) -> list[dict]:
+    """Volumes for the fluence denoiser, drawn from the batched workload's property ranges: a cube
+    of `edge` voxels (1 mm) of medium 1 with 1-4 random axis-aligned ellipsoids (labels 2..5),
+    every medium with mua log-uniform in [1e-3, 5e-2]/mm, mus uniform in [0.5, 20]/mm, g uniform
+    in [0.7, 0.95], n = 1.37 (background n = 1, Fresnel reflection on); a pencil source entering
+    the z = 0 face along +z at a random point of its central half; one 0-5 ns gate; no detectors.
+    The same (count, edge, seed) gives the same volumes; `nphoton` and the per-run seed are the
+    caller's to change (the training pairs reuse one volume at several photon counts)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    idx = np.arange(edge, dtype=np.float32) + 0.5
+    for i in range(count):
+        vol = np.ones((edge, edge, edge), dtype=np.uint8)
+        nell = int(rng.integers(1, 5))
+        for e in range(nell):
+            c = rng.uniform(0.2 * edge, 0.8 * edge, 3)
+            r = rng.uniform(0.08 * edge, 0.3 * edge, 3)
+            X, Y, Z = np.meshgrid((idx - c[0]) / r[0], (idx - c[1]) / r[1], (idx - c[2]) / r[2], indexing="ij")
+            vol[X * X + Y * Y + Z * Z <= 1.0] = 2 + e
+        prop = np.zeros((nell + 2, 4), np.float32)
+        prop[0] = [0.0, 0.0, 1.0, 1.0]
+        for m in range(1, nell + 2):
+            prop[m] = [np.exp(rng.uniform(np.log(1e-3), np.log(5e-2))), rng.uniform(0.5, 20.0),
+                       rng.uniform(0.7, 0.95), 1.37]
+        sx, sy = (float(np.floor(v)) for v in rng.uniform(0.25 * edge, 0.75 * edge, 2))
+        out.append({
+            "nphoton": int(nphoton), "seed": int(rng.integers(1, 2**31 - 1)), "vol": vol, "prop": prop,
+            "tstart": 0.0, "tend": 5e-9, "tstep": 5e-9,
+            "srcpos": [sx, sy, 0.0], "srcdir": [0.0, 0.0, 1.0], "issrcfrom0": 1,
+            "isreflect": 1, "issavedet": 0,
+        })
+    return out
