@@ -58,11 +58,13 @@ int mcxg_dn_head(const void* act, const float* xres, const float* w, const float
                  const float* valid, float* out, void* dact, float* dw, float* db, float* loss, long long m, float inv,
                  void* stream);
 
-/* Input features of nvol volumes of vox voxels: fluence (fp32, normalised as MCX writes it),
- * labels (uint8) with per-volume media tables props[nvol][nprop][4] (mua, mus, g, n), and
- * log10(photons) per volume -> x0 (bf16, 16 channels) and xres = log10(fluence + 1e-10). */
+/* Input features of nvol volumes of d x h x w voxels: fluence (fp32, normalised as MCX writes
+ * it, x fastest), labels (uint8) with per-volume media tables props[nvol][nprop][4] (mua, mus, g,
+ * n), and log10(photons) per volume -> x0 (bf16, 16 channels: log10 of the fluence and of its
+ * 3x3x3 and 5x5x5 in-bounds means, log10 mua, log10 reduced scattering, photon-count code) and
+ * xres = log10(3x3x3 mean + 1e-10). */
 int mcxg_dn_pack(const float* flux, const uint8_t* label, const float* props, const float* log_photons, void* x0,
-                 float* xres, int nvol, long long vox, int nprop, void* stream);
+                 float* xres, int nvol, int d, int h, int w, int nprop, void* stream);
 
 /* One AdamW step (decoupled weight decay) over n fp32 parameters; clears grad.  Writes bf16
  * weights to w16 (may be NULL) and, for a convolution, the flipped transposed copy

@@ -95,7 +95,7 @@ _DN = {
     "mcxg_dn_upcat_bwd": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P],
     "mcxg_dn_unpool_add": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P],
     "mcxg_dn_head": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _LL, _F, _P],
-    "mcxg_dn_pack": [_P, _P, _P, _P, _P, _P, _I, _LL, _I, _P],
+    "mcxg_dn_pack": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
     "mcxg_dn_adamw": [_P, _P, _P, _P, _P, _P, _LL, _I, _I, _I, _F, _F, _F, _F, _F, _I, _P],
 }
 for _name, _args in _DN.items():

@@ -555,31 +555,64 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16* __restrict__ act,
     }
 }
 
-// Input features of one voxel (16 channels, 0..4 used):
-//   0: (log10(F + 1e-10) + 5) / 3 of the noisy fluence F
-//   1: log10(mua) + 2        2: log10(mus * (1 - g))        3: (log10(photons) - 5.5) * 2
-// and xres[v] = log10(F + 1e-10), the residual base the head adds its correction to.
+// Input features of one voxel (16 channels, 0..5 used):
+//   0, 1, 2: (log10(m + 1e-10) + 5) / 3 for m = the noisy fluence F, the mean of F over the
+//            in-bounds voxels of its 3x3x3 neighbourhood, and over its 5x5x5 neighbourhood
+//   3: log10(mua) + 2        4: log10(mus * (1 - g))        5: (log10(photons) - 5.5) * 2
+// and xres[v] = log10(3x3x3 mean + 1e-10), the residual base the head adds its correction to.
+// The means are taken in linear fluence, where a voxel no photon reached is a zero among its
+// neighbours rather than a -10 outlier as it is in log space.
 __global__ void pack_kernel(const float* __restrict__ flux, const uint8_t* __restrict__ label,
                             const float* __restrict__ props, const float* __restrict__ log_photons,
-                            bf16* __restrict__ x0, float* __restrict__ xres, int nvol, long long vox, int nprop) {
-    long long total = (long long)nvol * vox;
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < total; v += (long long)gridDim.x * blockDim.x) {
-        int n = (int)(v / vox);
+                            bf16* __restrict__ x0, float* __restrict__ xres, Geo g, int nprop) {
+    const long long vvol = (long long)g.d * g.h * g.w;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < g.m; v += (long long)gridDim.x * blockDim.x) {
+        int n = (int)(v / vvol);
+        long long r = v % vvol;
+        int x = (int)(r % g.w), y = (int)((r / g.w) % g.h), z = (int)(r / ((long long)g.w * g.h));
+        float s3 = 0.f, s5 = 0.f;
+        int c3 = 0, c5 = 0;
+        for (int dz = -2; dz <= 2; ++dz) {
+            int zz = z + dz;
+            if (zz < 0 || zz >= g.d) continue;
+            for (int dy = -2; dy <= 2; ++dy) {
+                int yy = y + dy;
+                if (yy < 0 || yy >= g.h) continue;
+                const float* row = flux + ((long long)n * vvol + ((long long)zz * g.h + yy) * g.w);
+                bool inner = dz >= -1 && dz <= 1 && dy >= -1 && dy <= 1;
+                for (int dx = -2; dx <= 2; ++dx) {
+                    int xx = x + dx;
+                    if (xx < 0 || xx >= g.w) continue;
+                    float f = fmaxf(row[xx], 0.f);
+                    s5 += f;
+                    ++c5;
+                    if (inner && dx >= -1 && dx <= 1) {
+                        s3 += f;
+                        ++c3;
+                    }
+                }
+            }
+        }
         int lab = label[v];
         if (lab >= nprop) lab = nprop - 1;
         const float* pr = props + ((long long)n * nprop + lab) * 4;
-        float l = log10f(fmaxf(flux[v], 0.f) + 1e-10f);
-        float f[8], z[8];
-        f[0] = (l + 5.f) * (1.f / 3.f);
-        f[1] = pr[0] > 0.f ? log10f(pr[0]) + 2.f : -2.f;
+        float l0 = log10f(fmaxf(flux[v], 0.f) + 1e-10f);
+        float l3 = log10f(s3 / (float)c3 + 1e-10f);
+        float l5 = log10f(s5 / (float)c5 + 1e-10f);
+        float f[8], zz8[8];
+        f[0] = (l0 + 5.f) * (1.f / 3.f);
+        f[1] = (l3 + 5.f) * (1.f / 3.f);
+        f[2] = (l5 + 5.f) * (1.f / 3.f);
+        f[3] = pr[0] > 0.f ? log10f(pr[0]) + 2.f : -2.f;
         float musp = pr[1] * (1.f - pr[2]);
-        f[2] = musp > 0.f ? log10f(musp) : -3.f;
-        f[3] = (log_photons[n] - 5.5f) * 2.f;
-        for (int e = 4; e < 8; ++e) f[e] = 0.f;
-        for (int e = 0; e < 8; ++e) z[e] = 0.f;
+        f[4] = musp > 0.f ? log10f(musp) : -3.f;
+        f[5] = (log_photons[n] - 5.5f) * 2.f;
+        f[6] = 0.f;
+        f[7] = 0.f;
+        for (int e = 0; e < 8; ++e) zz8[e] = 0.f;
         store8(x0 + v * 16, f);
-        store8(x0 + v * 16 + 8, z);
-        xres[v] = l;
+        store8(x0 + v * 16 + 8, zz8);
+        xres[v] = l3;
     }
 }
 
@@ -797,11 +830,12 @@ int mcxg_dn_head(const void* act, const float* xres, const float* w, const float
 }
 
 int mcxg_dn_pack(const float* flux, const uint8_t* label, const float* props, const float* log_photons, void* x0,
-                 float* xres, int nvol, long long vox, int nprop, void* stream) {
-    if (!flux || !label || !props || !log_photons || !x0 || !xres || nvol <= 0 || vox <= 0 || nprop <= 0)
+                 float* xres, int nvol, int d, int h, int w, int nprop, void* stream) {
+    if (!flux || !label || !props || !log_photons || !x0 || !xres || !dims_ok(nvol, d, h, w) || nprop <= 0)
         return fail("pack: bad arguments");
-    pack_kernel<<<grid_for((long long)nvol * vox, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        flux, label, props, log_photons, static_cast<bf16*>(x0), xres, nvol, vox, nprop);
+    Geo g = make_geo(nvol, d, h, w);
+    pack_kernel<<<grid_for(g.m, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        flux, label, props, log_photons, static_cast<bf16*>(x0), xres, g, nprop);
     return launched();
 }
 

@@ -1,10 +1,12 @@
 """MC + learned denoiser: a 4-level 3D U-Net that maps low-photon fluence to high-photon fluence.
 
-The network works on log10 fluence: its input features are the noisy map, the voxel's absorption
-and reduced scattering coefficients and the photon count (``mcxg_dn_pack``); 3x3x3 convolutions
-with ReLU at 16/32/64/128 channels, 2x2x2 average pooling, nearest upsampling with skip
-concatenation, and a 1x1x1 head whose output is added to the input log-fluence (the network
-learns a correction; at initialisation it is nearly the identity).
+The network works on log10 fluence: its input features are the noisy map and its 3x3x3 and 5x5x5
+neighbourhood means (taken in linear fluence, so that voxels no photon reached do not become
+log-space outliers), the voxel's absorption and reduced scattering coefficients and the photon
+count (``mcxg_dn_pack``); 3x3x3 convolutions with ReLU at 16/32/64/128 channels, 2x2x2 average
+pooling, nearest upsampling with skip concatenation, and a 1x1x1 head whose output is added to
+the log of the 3x3x3 mean (the network learns a correction to a box filter; at initialisation it
+is nearly that filter).
 
 Everything on the device runs on this engine's own kernels (include/mcxg_denoise.h): BF16
 tensor-core implicit-GEMM convolutions forward, data and weight gradient, pooling, upsampling,
@@ -166,14 +168,18 @@ class UNet:
                                      self._stream()), name)
 
     # -- forward / backward -------------------------------------------------------------------
-    def pack(self, flux: torch.Tensor, labels: torch.Tensor, props: torch.Tensor, log_photons: torch.Tensor):
-        """Input features and residual base of nvol volumes: flux fp32 [nvol, vox], labels uint8
-        [nvol, vox], props fp32 [nvol, nprop, 4], log_photons fp32 [nvol]."""
+    def pack(self, flux: torch.Tensor, labels: torch.Tensor, props: torch.Tensor, log_photons: torch.Tensor,
+             d: int, h: int, w: int):
+        """Input features and residual base of nvol volumes of d x h x w voxels: flux fp32
+        [nvol, vox], labels uint8 [nvol, vox], props fp32 [nvol, nprop, 4], log_photons fp32
+        [nvol]."""
         nvol, vox = flux.shape
+        if vox != d * h * w:
+            raise ValueError("flux does not hold d * h * w voxels per volume")
         x0 = self._buf("x0", nvol * vox * IN_CH)
         xres = self._buf("xres", nvol * vox, torch.float32)
-        _ok(lib.mcxg_dn_pack(_ptr(flux), _ptr(labels), _ptr(props), _ptr(log_photons), _ptr(x0), _ptr(xres), nvol, vox,
-                             props.shape[1], self._stream()), "pack")
+        _ok(lib.mcxg_dn_pack(_ptr(flux), _ptr(labels), _ptr(props), _ptr(log_photons), _ptr(x0), _ptr(xres), nvol, d, h,
+                             w, props.shape[1], self._stream()), "pack")
         return x0, xres
 
     def forward(self, x0: torch.Tensor, xres: torch.Tensor, nvol: int, d: int, h: int, w: int,
@@ -300,7 +306,7 @@ class UNet:
         lab = torch.from_numpy(np.ascontiguousarray(np.asarray(vol, np.uint8).reshape(-1, order="F"))).to(self.dev).view(1, -1)
         pr = torch.from_numpy(np.ascontiguousarray(prop, np.float32)).to(self.dev).view(1, -1, 4)
         lp = torch.tensor([math.log10(nphoton)], dtype=torch.float32, device=self.dev)
-        x0, xres = self.pack(fl, lab, pr, lp)
+        x0, xres = self.pack(fl, lab, pr, lp, nz, ny, nx)
         out = self._buf("out", nx * ny * nz, torch.float32)
         self.forward(x0, xres, 1, nz, ny, nx, out=out)
         lf = out.cpu().numpy()
@@ -400,7 +406,7 @@ def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr
         labels = _augment(data["labels"][ii], edge, flips)
         target = _augment(data["target"][ii], edge, flips)
         valid = _augment(data["valid"][ii], edge, flips)
-        x0, xres = net.pack(flux, labels, data["props"][ii].contiguous(), lp_all[ll].contiguous())
+        x0, xres = net.pack(flux, labels, data["props"][ii].contiguous(), lp_all[ll].contiguous(), edge, edge, edge)
         A = net.forward(x0, xres, batch, edge, edge, edge)
         nval = float(valid.sum().item())
         net.loss_acc.zero_()
@@ -415,6 +421,28 @@ def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr
                 print(f"step {it + 1}: loss {acc / nacc:.4f}", flush=True)
             acc, nacc = 0.0, 0
     return losses
+
+
+def evaluate_loss(net: UNet, data: dict[str, Any], batch: int = 4) -> list[float]:
+    """Mean absolute log10 error over scored voxels of the whole training set, per input photon
+    count, without augmentation."""
+    edge, count = data["edge"], data["count"]
+    out = []
+    for k, n in enumerate(data["photons"]):
+        num, den = 0.0, 0.0
+        for i in range(0, count, batch):
+            ii = torch.arange(i, min(count, i + batch), device=net.dev)
+            b = ii.numel()
+            lp = torch.full((b,), math.log10(n), dtype=torch.float32, device=net.dev)
+            x0, xres = net.pack(data["inputs"][k][ii].contiguous(), data["labels"][ii].contiguous(),
+                                data["props"][ii].contiguous(), lp, edge, edge, edge)
+            o = net._buf("eval_out", b * edge ** 3, torch.float32)
+            net.forward(x0, xres, b, edge, edge, edge, out=o)
+            v = data["valid"][ii].reshape(-1)
+            num += float(((o - data["target"][ii].reshape(-1)).abs() * v).sum())
+            den += float(v.sum())
+        out.append(num / max(den, 1.0))
+    return out
 
 
 # -- the metric -------------------------------------------------------------------------------

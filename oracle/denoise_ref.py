@@ -48,21 +48,47 @@ def conv(x: torch.Tensor, w: torch.Tensor, b: torch.Tensor | None, relu: bool = 
     return F.relu(y) if relu else y
 
 
-def features(flux: np.ndarray, labels: np.ndarray, props: np.ndarray, log_photons: np.ndarray) -> tuple:
-    """The 16 input channels (4 used) and residual base, restating mcxg_dn_pack on [nvol, vox]
-    arrays: log10(F + 1e-10) scaled, log10(mua) + 2, log10(mus (1 - g)), photon-count code."""
+def box_means(flux: np.ndarray, edge: tuple[int, int, int]) -> tuple[np.ndarray, np.ndarray]:
+    """Means of the fluence over the in-bounds voxels of each voxel's 3x3x3 and 5x5x5
+    neighbourhoods; flux [nvol, vox] in voxel order x fastest over a (d, h, w) = edge grid."""
+    d, h, w = edge
+    f = np.maximum(np.asarray(flux, np.float64), 0).reshape(-1, d, h, w)
+    out = []
+    for r in (1, 2):
+        s = np.zeros_like(f)
+        cnt = np.zeros((d, h, w))
+        pad = np.pad(f, ((0, 0), (r, r), (r, r), (r, r)))
+        one = np.pad(np.ones((d, h, w)), r)
+        for dz in range(2 * r + 1):
+            for dy in range(2 * r + 1):
+                for dx in range(2 * r + 1):
+                    s += pad[:, dz:dz + d, dy:dy + h, dx:dx + w]
+                    cnt += one[dz:dz + d, dy:dy + h, dx:dx + w]
+        out.append((s / cnt).reshape(f.shape[0], -1))
+    return out[0], out[1]
+
+
+def features(flux: np.ndarray, labels: np.ndarray, props: np.ndarray, log_photons: np.ndarray,
+             edge: tuple[int, int, int]) -> tuple:
+    """The 16 input channels (6 used) and residual base, restating mcxg_dn_pack on [nvol, vox]
+    arrays over a (d, h, w) grid: log10 of the fluence, of its 3x3x3 and of its 5x5x5 in-bounds
+    means (each + 1e-10, scaled (l + 5) / 3), log10(mua) + 2, log10(mus (1 - g)), the photon-count
+    code (log10(photons) - 5.5) * 2; the residual base is log10(3x3x3 mean + 1e-10)."""
     nvol, vox = flux.shape
     lab = np.minimum(labels.astype(np.int64), props.shape[1] - 1)
     pr = np.take_along_axis(props, lab[..., None].repeat(4, -1), axis=1)        # [nvol, vox, 4]
-    l = np.log10(np.maximum(flux, 0).astype(np.float32) + np.float32(1e-10)).astype(np.float32)
+    b3, b5 = box_means(flux, edge)
+    lg = lambda a: np.log10(np.maximum(a, 0).astype(np.float32) + np.float32(1e-10)).astype(np.float32)  # noqa: E731
     x = np.zeros((nvol, vox, 16), np.float32)
-    x[..., 0] = (l + 5.0) / 3.0
+    x[..., 0] = (lg(flux) + 5.0) / 3.0
+    x[..., 1] = (lg(b3) + 5.0) / 3.0
+    x[..., 2] = (lg(b5) + 5.0) / 3.0
     with np.errstate(divide="ignore"):
-        x[..., 1] = np.where(pr[..., 0] > 0, np.log10(np.where(pr[..., 0] > 0, pr[..., 0], 1.0)) + 2.0, -2.0)
+        x[..., 3] = np.where(pr[..., 0] > 0, np.log10(np.where(pr[..., 0] > 0, pr[..., 0], 1.0)) + 2.0, -2.0)
         musp = pr[..., 1] * (1.0 - pr[..., 2])
-        x[..., 2] = np.where(musp > 0, np.log10(np.where(musp > 0, musp, 1.0)), -3.0)
-    x[..., 3] = ((log_photons - 5.5) * 2.0)[:, None]
-    return x, l
+        x[..., 4] = np.where(musp > 0, np.log10(np.where(musp > 0, musp, 1.0)), -3.0)
+    x[..., 5] = ((log_photons - 5.5) * 2.0)[:, None]
+    return x, lg(b3)
 
 
 def forward(params: dict, x0: torch.Tensor, xres: torch.Tensor, nvol: int, d: int, h: int, w: int) -> torch.Tensor:

@@ -90,16 +90,35 @@ def test_reference_gradients_match_finite_differences(dn):
 
 
 def test_features():
-    flux = np.array([[0.0, 1.0, 1e-3, -1.0]], np.float32)
+    flux = np.array([[0.0, 1.0, 1e-3, -1.0]], np.float32)            # a 1 x 1 x 4 grid
     labels = np.array([[0, 1, 2, 9]], np.uint8)
     props = np.array([[[0, 0, 1, 1], [0.01, 10.0, 0.9, 1.37], [0.001, 2.0, 0.5, 1.37]]], np.float32)
-    x, l = R.features(flux, labels, props, np.array([5.0], np.float32))
-    np.testing.assert_allclose(l, np.log10(np.maximum(flux, 0) + 1e-10), rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 0], (l[0] + 5) / 3, rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 1], [-2.0, 0.0, -1.0, -1.0], atol=1e-6)      # label 9 clamps to the last row
-    np.testing.assert_allclose(x[0, :, 2], [-3.0, 0.0, 0.0, 0.0], atol=1e-6)
-    np.testing.assert_allclose(x[0, :, 3], -1.0)
-    assert not x[..., 4:].any()
+    x, l = R.features(flux, labels, props, np.array([5.0], np.float32), (1, 1, 4))
+    f = np.maximum(flux[0], 0)
+    b3 = np.array([f[:2].mean(), f[:3].mean(), f[1:].mean(), f[2:].mean()])
+    b5 = np.array([f[:3].mean(), f.mean(), f.mean(), f[1:].mean()])
+    lg = lambda a: np.log10(a + 1e-10)  # noqa: E731
+    np.testing.assert_allclose(l[0], lg(b3), rtol=1e-6)
+    np.testing.assert_allclose(x[0, :, 0], (lg(f) + 5) / 3, rtol=1e-6)
+    np.testing.assert_allclose(x[0, :, 1], (lg(b3) + 5) / 3, rtol=1e-6)
+    np.testing.assert_allclose(x[0, :, 2], (lg(b5) + 5) / 3, rtol=1e-6)
+    np.testing.assert_allclose(x[0, :, 3], [-2.0, 0.0, -1.0, -1.0], atol=1e-6)      # label 9 clamps to the last row
+    np.testing.assert_allclose(x[0, :, 4], [-3.0, 0.0, 0.0, 0.0], atol=1e-6)
+    np.testing.assert_allclose(x[0, :, 5], -1.0)
+    assert not x[..., 6:].any()
+
+
+def test_box_means_against_scipy():
+    from scipy.ndimage import uniform_filter
+
+    rng = np.random.default_rng(2)
+    f = rng.random((2, 5 * 6 * 7)).astype(np.float32)
+    b3, b5 = R.box_means(f, (5, 6, 7))
+    for r, b in ((3, b3), (5, b5)):
+        g = f.reshape(2, 5, 6, 7).astype(np.float64)
+        s = np.stack([uniform_filter(v, r, mode="constant") for v in g])
+        c = uniform_filter(np.ones((5, 6, 7)), r, mode="constant")
+        np.testing.assert_allclose(b, (s / c).reshape(2, -1), rtol=1e-9)
 
 
 def test_median_rel_error(dn):

@@ -238,7 +238,8 @@ def test_head_and_loss(lib):
 
 def test_pack(lib):
     rng = np.random.default_rng(8)
-    nvol, vox, nprop = 3, 4096, 5
+    nvol, d, h, w, nprop = 3, 12, 10, 14, 5
+    vox = d * h * w
     flux = (10.0 ** rng.uniform(-9, 0, (nvol, vox))).astype(np.float32) * (rng.random((nvol, vox)) < 0.9)
     labels = rng.integers(0, nprop + 2, (nvol, vox)).astype(np.uint8)
     props = np.stack([np.c_[rng.uniform(1e-3, 5e-2, nprop), rng.uniform(0.5, 20, nprop), rng.uniform(0.7, 0.95, nprop),
@@ -249,9 +250,9 @@ def test_pack(lib):
     x0 = torch.empty(nvol * vox * 16, dtype=BF, device="cuda")
     xres = torch.empty(nvol * vox, device="cuda")
     _call(lib, "mcxg_dn_pack", F.data_ptr(), Lb.data_ptr(), P.data_ptr(), LP.data_ptr(), x0.data_ptr(), xres.data_ptr(), nvol,
-          vox, nprop, _st())
-    rx, rl = R.features(flux, labels, props, lp)
-    np.testing.assert_allclose(xres.cpu().numpy().reshape(nvol, vox), rl, rtol=1e-5, atol=1e-5)
+          d, h, w, nprop, _st())
+    rx, rl = R.features(flux, labels, props, lp, (d, h, w))
+    np.testing.assert_allclose(xres.cpu().numpy().reshape(nvol, vox), rl, rtol=1e-5, atol=1e-4)
     _close_bf16(x0.float().cpu().numpy().reshape(nvol, vox, 16), R.bf16(rx), extra=1e-3)
 
 
@@ -325,28 +326,38 @@ def test_network_forward_and_gradients(dn):
 
 
 def test_training_lowers_the_loss(dn):
+    """Engine-made pairs (eight 32^3 volumes, 1e4 / 1e5 photons against 2e6): 400 AdamW steps
+    lower the loss over the training set, at both photon counts, below the network's starting
+    point (about the 3x3x3 box filter its head corrects)."""
     data = dn.make_pairs(8, edge=32, seed=77, target_photons=2e6, input_photons=(1e4, 1e5))
     net = dn.UNet(seed=1)
-    losses = dn.train(net, data, steps=240, batch=2, lr=2e-3, log_every=40, verbose=False)
-    print("losses", losses)
-    assert np.isfinite(losses).all()
-    assert losses[-1] <= 0.8 * losses[0], losses
+    before = dn.evaluate_loss(net, data)
+    dn.train(net, data, steps=400, batch=2, lr=1e-3, log_every=100, verbose=False)
+    after = dn.evaluate_loss(net, data)
+    print("loss before", before, "after", after)
+    assert np.isfinite(after).all()
+    assert all(a <= 0.93 * b for a, b in zip(after, before)), (before, after)
 
 
 def test_checkpoint_beats_raw_low_photon_maps(dn):
-    """Held-out 64^3 volumes (a seed the checkpoint never saw): the denoised 1e5-photon map is
-    closer to a 1e7-photon run than the raw 1e5-photon map is."""
+    """Held-out 64^3 volumes (a seed the checkpoint never saw): against a 1e7-photon run, the
+    denoised 1e5-photon map has a smaller median relative error than the raw 1e5-photon map
+    (what the network gains over plain MC) and than its 3x3x3 box filter (the network's
+    starting point, so the gain is learned)."""
     from mcx_gb300.api import run
 
     if not dn.DEFAULT_WEIGHTS.exists():
         pytest.skip("no trained checkpoint in the package")
     net = dn.UNet(dn.load_params())
-    raw, den = [], []
+    raw, box, den = [], [], []
     for cfg in dn.problems.denoise_instances(3, 64, seed=424242):
         judge = run(dict(cfg, nphoton=1e7))["flux"][..., 0]
         f = run(dict(cfg, nphoton=1e5, seed=cfg["seed"] + 5))["flux"][..., 0]
         d = net.denoise(f, cfg["vol"], cfg["prop"], 1e5)
+        b3 = R.box_means(f.reshape(1, -1, order="F"), (64, 64, 64))[0].reshape(f.shape, order="F")
         raw.append(dn.median_rel_error(f, judge))
+        box.append(dn.median_rel_error(b3, judge))
         den.append(dn.median_rel_error(d, judge))
-    print("raw", raw, "denoised", den)
+    print("raw", raw, "box", box, "denoised", den)
     assert np.median(den) <= 0.7 * np.median(raw), (raw, den)
+    assert np.median(den) < np.median(box), (box, den)
