@@ -16,7 +16,8 @@ detectors saving id / scattering counts / partial paths) at 1e8 photons.
 Other workloads (--workload): workload0 (homogeneous cube), workload2 (256^3 layered volume),
 cube60planar (planar source), batch (256 simulations in one CUDA graph), contest (MCX's speed
 contest: cube60 + cube60b + cube60planar at 1e8 photons, the score being the sum of the three
-photons/ms).
+photons/ms), denoise (MC + learned denoiser against plain MC: seconds to a 5% median relative
+fluence error on 128^3 volumes; --steps volumes, --judge-photons for the judge runs).
 
 Multi-GPU (torchrun, one rank per GPU): every rank simulates its own photon range of the same
 size (weak scaling, no collective in the data path); rank 0 prints.
@@ -40,10 +41,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "photons/ms (plain MC)"
 WORKLOAD_PHOTONS = {"workload0": 1_000_000, "workload1": 100_000_000, "workload2": 1_000_000_000,
-                    "cube60planar": 100_000_000, "batch": 0, "contest": 100_000_000}
+                    "cube60planar": 100_000_000, "batch": 0, "contest": 100_000_000, "denoise": 0}
 # photons of the CPU-oracle sample per workload: about 10 s on 16 cores
 CPU_SAMPLE = {"workload0": 8_000_000, "workload1": 4_000_000, "workload2": 1_000_000, "cube60planar": 6_000_000,
-              "batch": 20_000, "contest": 4_000_000}
+              "batch": 20_000, "contest": 4_000_000, "denoise": 200_000}
 # MCX's speed contest (manpage/mcxcontest.1:13, mcxlab/examples/mcx_gpu_benchmarks.m:124-130): the
 # built-in cube60, cube60b and cube60planar decks at 1e8 photons; the score is the sum of the three
 # photons/ms figures.
@@ -244,6 +245,112 @@ def batch_main(args, world, rank) -> None:
     print(json.dumps(line))
 
 
+DN_METRIC = "time to 5% median rel. fluence error on 128^3 volumes, MC+denoiser vs plain MC"
+
+
+def _dn_flops(d: int, h: int, w: int, nvol: int = 1) -> float:
+    """Multiply-add FLOPs (2 per MAC) of one U-Net forward pass over nvol d x h x w volumes."""
+    from mcx_gb300 import denoise as dn
+
+    return sum(2.0 * nvol * (d >> l) * (h >> l) * (w >> l) * ci * co * dn.TAPS for _, ci, co, l in dn.LAYERS)
+
+
+def denoise_main(args, world, rank) -> None:
+    """MC + learned denoiser against plain MC on held-out 128^3 volumes of the batched workload's
+    property ranges: per volume, the time to a median relative fluence error of 5% against a
+    `--judge-photons` run (mcx_gb300.denoise.time_to_error).  value = summed device time of
+    MC + denoiser (transport kernel + network); e2e = summed wall time through the public calls
+    (mcx_gb300.run, UNet.denoise) from host buffers; plain-MC times and the speed-up ride along.
+    One step = one volume; warm-up = full denoise pipelines at 1e5 photons on the first volume."""
+    import torch
+
+    from mcx_gb300 import denoise as dn
+    from mcx_gb300 import problems
+
+    torch.cuda.set_device(0)
+    if dn.DEFAULT_WEIGHTS.exists():
+        net, weights = dn.UNet(dn.load_params()), "checkpoint " + dn.DEFAULT_WEIGHTS.name
+    else:
+        data = dn.make_pairs(64, 64, 1, 1e7)
+        net = dn.UNet(seed=1)
+        dn.train(net, data, steps=800, batch=4, lr=1e-3, verbose=False)
+        weights = "trained in this run (64 volumes, 800 steps)"
+    cfgs = problems.denoise_instances(args.steps, 128, seed=31337)
+    import mcx_gb300
+
+    for i in range(args.warmup):
+        r = mcx_gb300.run(dict(cfgs[0], nphoton=int(1e5), seed=1000 + i))
+        net.denoise(r["flux"], cfgs[0]["vol"], cfgs[0]["prop"], 1e5)
+    # the network alone at 128^3: CUDA events around repeated forward passes on resident inputs
+    n = 128
+    x0 = torch.zeros(n ** 3 * dn.IN_CH, dtype=torch.bfloat16, device="cuda")
+    xr = torch.zeros(n ** 3, device="cuda")
+    out = torch.empty(n ** 3, device="cuda")
+    for _ in range(3):
+        net.forward(x0, xr, 1, n, n, n, out=out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(10):
+        net.forward(x0, xr, 1, n, n, n, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / 10
+    res = []
+    with Clocks(0) as clk:
+        for c in cfgs:
+            res.append(dn.time_to_error(net, c, judge_photons=args.judge_photons))
+    if rank != 0:
+        return
+    pk = peaks()
+    flops = _dn_flops(n, n, n)
+    tflops = flops / (fwd_ms * 1e-3) / 1e12
+    dev = sum(r["t_denoised_device_s"] for r in res)
+    wall = sum(r["t_denoised_s"] for r in res)
+    h2d = sum(c["vol"].size * 4 + np.asarray(c["prop"]).nbytes + 4 * c["vol"].size for c in cfgs)  # MC inputs + map up
+    d2h = sum(8 * c["vol"].size for c in cfgs)                                                        # map down twice
+    launches = sum(1 + 22 * len(r["denoised"]) for r in res)
+    line = {
+        "metric": DN_METRIC, "value": dev, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev / args.steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 transport, bf16 network (fp32 accumulate)", "data": "synthetic",
+        "config": {"workload": "denoise", "volumes": args.steps, "edge": n, "judge_photons": args.judge_photons,
+                   "target_error": 0.05, "weights": weights,
+                   "l2": "inputs (128^3 fields and activations) larger than L2"},
+        "plain_mc_s": sum(r["t_plain_device_s"] for r in res),
+        "speedup": sum(r["t_plain_device_s"] for r in res) / dev,
+        "e2e": {"value": wall, "unit": "s", "plain_mc_s": sum(r["t_plain_s"] for r in res),
+                "speedup": sum(r["t_plain_s"] for r in res) / wall, "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "per_volume": [{k: r[k] for k in ("photons_plain", "photons_denoised", "t_plain_device_s", "t_denoised_device_s",
+                                          "t_plain_s", "t_denoised_s", "fallback")} |
+                       {"ladder": [(p["photons"], round(p["error"], 4)) for p in r["plain"]],
+                        "denoised": [(p["photons"], round(p["error"], 4), round(p["error_plain"], 4)) for p in r["denoised"]]}
+                       for r in res],
+        "roofline": {"bound": "tensor", "kernel": "U-Net forward at 128^3 (14 implicit-GEMM convolutions)",
+                     "achieved": tflops, "peak": pk.get("bf16_tflops"), "unit": "TFLOP/s",
+                     "frac": tflops / pk["bf16_tflops"] if pk.get("bf16_tflops") else None, "traffic": None,
+                     "flops_per_launch": flops, "forward_ms": fwd_ms, "peak_source": pk["_source"]},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        # the CPU oracle's plain MC on a bounded sample of the first volume, priced at the photon
+        # count plain MC needs for 5%
+        import mcx_gb300
+        from oracle import oracle
+
+        sample = args.cpu_sample or 200_000
+        r = oracle.run(mcx_gb300.prepare(dict(cfgs[0], nphoton=sample)), nphoton=sample, seed=77,
+                       threads=os.cpu_count() or 1)
+        rate = sample / r["stat"]["seconds"]
+        line["cpu_baseline"] = {"value": sum(x["photons_plain"] for x in res) / rate, "unit": "s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{sample} photons of the first volume ({r['stat']['seconds']:.1f} s), "
+                                          "plain MC priced at the photon counts that reach 5%"}
+    print(json.dumps(line))
+
+
 def cpu_baseline(name: str, sample: int) -> dict:
     """The CPU oracle (a C++/OpenMP restatement of MCX's loop; MCX itself has no CPU path) on a
     bounded sample of the same workload, on every host core."""
@@ -288,6 +395,49 @@ def reference_arm(args, world, rank) -> None:
                     e2e={"value": sum(e2e.values()), "unit": "photons/ms", "per_deck": e2e, "h2d_bytes_per_step": 0,
                          "d2h_bytes_per_step": 0},
                     cpu_baseline={"value": v, "unit": "photons/ms", "cores": os.cpu_count(), "kind": "reference",
+                                  "sample": "the reference MCX CUDA build itself on this GPU"})
+        print(json.dumps(line))
+        return
+    if name == "denoise" and ref_mcx.available():
+        # MCX has no denoiser: its pipeline is plain MC.  The same held-out volumes, its own judge
+        # run and its own photon ladder give the photon count its fluence needs for a 5% median
+        # relative error, priced at its own photon rate (kernel-only and up to normalised output).
+        from mcx_gb300 import problems
+        from mcx_gb300.denoise import median_rel_error
+
+        ref_mcx.build()
+        cfgs = problems.denoise_instances(args.steps, 128, seed=31337)
+        for i in range(args.warmup):
+            ref_mcx.run(dict(cfgs[0], nphoton=100_000, seed=500 + i), keep_field=False)
+        per, t_kern, t_norm = [], 0.0, 0.0
+        for c in cfgs:
+            judge = ref_mcx.run(dict(c, nphoton=int(args.judge_photons), seed=c["seed"] + 1))["flux"][..., 0]
+            lad = []
+            for k, n in enumerate((1e5, 3e5, 1e6, 3e6, 1e7, 3e7)):
+                r = ref_mcx.run(dict(c, nphoton=int(n), seed=c["seed"] + 2 + k))
+                lad.append((n, median_rel_error(r["flux"][..., 0], judge), r["speed"], r["normalized_ms"]))
+            n_star = None
+            for a, b in zip(lad, lad[1:]):
+                if a[1] > 0.05 >= b[1]:
+                    n_star = a[0] * (0.05 / a[1]) ** (np.log(b[0] / a[0]) / np.log(b[1] / a[1]))
+                    break
+            if n_star is None:
+                n_star = lad[-1][0] * (lad[-1][1] / 0.05) ** 2 if lad[-1][1] > 0.05 else lad[0][0]
+            big = [x for x in lad if x[0] >= 1e6 and x[2]]
+            rate_k = sum(x[0] for x in big) / sum(x[0] / x[2] for x in big)           # photons per kernel ms
+            rate_n = sum(x[0] for x in big) / max(1, sum(x[3] for x in big))          # photons per normalised ms
+            t_kern += n_star / rate_k / 1e3
+            t_norm += n_star / rate_n / 1e3
+            per.append({"photons_plain": n_star, "ladder": [(x[0], round(x[1], 4)) for x in lad],
+                        "photons_per_ms": rate_k})
+        line = dict(base, metric=DN_METRIC, value=t_kern, unit="s", higher_is_better=False,
+                    ms_per_step=1e3 * t_kern / args.steps,
+                    config={"workload": "denoise", "volumes": args.steps, "edge": 128,
+                            "judge_photons": args.judge_photons, "target_error": 0.05,
+                            "note": "MCX has no denoiser: plain MC on the reference build"},
+                    per_volume=per,
+                    e2e={"value": t_norm, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    cpu_baseline={"value": t_kern, "unit": "s", "cores": os.cpu_count(), "kind": "reference",
                                   "sample": "the reference MCX CUDA build itself on this GPU"})
         print(json.dumps(line))
         return
@@ -395,8 +545,12 @@ def main() -> None:
     ap.add_argument("--ref-sample", type=int, default=16, help="batch instances the reference arm runs")
     ap.add_argument("--no-detectors", action="store_true",
                     help="drop the deck's detectors (measures the cost of detected-photon bookkeeping)")
+    ap.add_argument("--judge-photons", type=float, default=1e9, help="photons of the denoise workload's judge runs")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.workload == "denoise" and args.impl != "reference":
+        denoise_main(args, world, rank)
+        return
     if args.workload == "batch" and args.impl != "reference":
         batch_main(args, world, rank)
         return

@@ -46,7 +46,7 @@ SPEC = {name: (cin, cout, lvl) for name, cin, cout, lvl in LAYERS}
 IN_CH = 16
 TAPS = 27
 FLUX_FLOOR = 1e-10          # log10(F + FLUX_FLOOR) is the network's fluence coordinate
-VALID_FRAC = 1e-4           # voxels at or above this fraction of the reference map's maximum are scored
+VALID_FRAC = 1e-6           # voxels at or above this fraction of the reference map's maximum are scored
 DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "denoiser_unet64.npz"
 
 
@@ -306,10 +306,14 @@ class UNet:
         lab = torch.from_numpy(np.ascontiguousarray(np.asarray(vol, np.uint8).reshape(-1, order="F"))).to(self.dev).view(1, -1)
         pr = torch.from_numpy(np.ascontiguousarray(prop, np.float32)).to(self.dev).view(1, -1, 4)
         lp = torch.tensor([math.log10(nphoton)], dtype=torch.float32, device=self.dev)
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev[0].record()
         x0, xres = self.pack(fl, lab, pr, lp, nz, ny, nx)
         out = self._buf("out", nx * ny * nz, torch.float32)
         self.forward(x0, xres, 1, nz, ny, nx, out=out)
+        ev[1].record()
         lf = out.cpu().numpy()
+        self.last_gpu_ms = ev[0].elapsed_time(ev[1])     # pack + network on the device
         return np.clip(10.0 ** lf.astype(np.float64) - FLUX_FLOOR, 0.0, None).astype(np.float32).reshape((nx, ny, nz), order="F")
 
 
@@ -341,12 +345,13 @@ def simulate(cfgs: list[dict[str, Any]], chunk: int = 96) -> list[np.ndarray]:
     return out
 
 
-def make_pairs(count: int, edge: int = 64, seed: int = 1, target_photons: float = 1e7,
-               input_photons: tuple[float, ...] = (1e5, 1e6)) -> dict[str, Any]:
+def make_pairs(count: int, edge: int = 64, seed: int = 1, target_photons: float = 1e8,
+               input_photons: tuple[float, ...] = (1e5, 1e6, 1e7), valid_frac: float = VALID_FRAC) -> dict[str, Any]:
     """Training pairs: `count` random volumes (the batched workload's property ranges), each
-    simulated at every input photon count and once at `target_photons` with independent seeds.
-    Returns device tensors: inputs [len(input_photons), count, vox], target log10 fluence and
-    score weights [count, vox], labels, media tables, and the photon counts."""
+    simulated at every input photon count and once at `target_photons` with independent seeds;
+    voxels at or above `valid_frac` of a target's maximum are scored.  Returns device tensors:
+    inputs [len(input_photons), count, vox], target log10 fluence and score weights [count, vox],
+    labels, media tables, and the photon counts."""
     base = problems.denoise_instances(count, edge, seed)
     nprop = max(c["prop"].shape[0] for c in base)
     cfgs = []
@@ -366,7 +371,7 @@ def make_pairs(count: int, edge: int = 64, seed: int = 1, target_photons: float 
         props[i, c["prop"].shape[0]:] = c["prop"][-1]
     labels = torch.from_numpy(np.stack([c["vol"].reshape(-1, order="F") for c in base])).to(dev)
     ltgt = torch.log10(tgt + FLUX_FLOOR)
-    valid = (tgt >= VALID_FRAC * tgt.amax(dim=1, keepdim=True)).float()
+    valid = (tgt >= valid_frac * tgt.amax(dim=1, keepdim=True)).float()
     return {"inputs": inputs, "target": ltgt, "valid": valid, "labels": labels,
             "props": torch.from_numpy(props).to(dev), "photons": tuple(float(n) for n in input_photons),
             "edge": edge, "count": count, "target_photons": float(target_photons), "seed": seed}
@@ -448,60 +453,76 @@ def evaluate_loss(net: UNet, data: dict[str, Any], batch: int = 4) -> list[float
 # -- the metric -------------------------------------------------------------------------------
 def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, target: float = 0.05,
                   ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
-                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6)) -> dict[str, Any]:
-    """Wall time to reach a median relative fluence error of `target` against a
-    `judge_photons` run, for plain MC and for MC + denoiser, on one volume.
+                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7), judge_check: bool = True) -> dict[str, Any]:
+    """Time to reach a median relative fluence error of `target` against a `judge_photons` run,
+    for plain MC and for MC + denoiser, on one volume.
 
-    Plain MC runs each budget of `ladder` end to end through the engine's API; its time to the
-    target is interpolated in log(error)-log(photons) between the bracketing budgets (or
-    extrapolated with the 1/sqrt(N) law beyond the last one) and priced at the measured photon
-    rate.  MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the
-    target, timed end to end (simulation, upload, network, download); where none does, plain MC
-    is the fallback and its time is the pipeline's."""
+    Plain MC runs each budget of `ladder` end to end through the engine's API; the photon count
+    that reaches the target is interpolated in log(error)-log(photons) between the bracketing
+    budgets (extrapolated with the 1/sqrt(N) law past the last one) and priced at the ladder's
+    photon rate -- on the device (transport kernel time) and end to end (wall time of the calls).
+    MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the
+    target: on the device its transport time plus the network's, end to end the wall time of the
+    simulation call plus upload, network and download.  Where no budget reaches the target,
+    plain MC is the fallback and its times are the pipeline's.  With `judge_check`, a second,
+    independent run of a quarter of the judge's photons estimates the judge's own median error
+    (their difference has sqrt(5) times the judge's standard error)."""
     from .api import run
 
     t0 = time.perf_counter()
-    judge = _flat(run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))["flux"])
+    jr = run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))
+    judge = _flat(jr["flux"])
     judge_s = time.perf_counter() - t0
+    judge_err = None
+    if judge_check:
+        j4 = _flat(run(dict(cfg, nphoton=judge_photons / 4, seed=int(cfg["seed"]) + 99))["flux"])
+        judge_err = median_rel_error(j4, judge) / math.sqrt(5.0)
     plain = []
     for n in ladder:
         t0 = time.perf_counter()
-        f = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))["flux"]
+        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))
         dt = time.perf_counter() - t0
-        plain.append((n, median_rel_error(_flat(f), judge), dt))
-    rate = sum(p[0] for p in plain) / sum(p[2] for p in plain)  # photons per second over the ladder
-    t_plain = None
-    for (n0, e0, _), (n1, e1, _) in zip(plain, plain[1:]):
-        if e0 > target >= e1:
-            a = math.log(e1 / e0) / math.log(n1 / n0)
-            t_plain = n0 * (target / e0) ** (1.0 / a) / rate
+        plain.append({"photons": n, "error": median_rel_error(_flat(r["flux"]), judge), "s": dt,
+                      "kernel_s": r["stat"]["kernel_ms"] * 1e-3})
+    rate_wall = sum(p["photons"] for p in plain) / sum(p["s"] for p in plain)
+    rate_dev = sum(p["photons"] for p in plain) / sum(p["kernel_s"] for p in plain)
+    n_star = None
+    for a, b in zip(plain, plain[1:]):
+        if a["error"] > target >= b["error"]:
+            slope = math.log(b["error"] / a["error"]) / math.log(b["photons"] / a["photons"])
+            n_star = a["photons"] * (target / a["error"]) ** (1.0 / slope)
             break
-    if t_plain is None:
-        n_last, e_last, _ = plain[-1]
-        n_star = n_last * (e_last / target) ** 2 if e_last > target else plain[0][0]
-        t_plain = n_star / rate
+    if n_star is None:
+        last = plain[-1]
+        n_star = last["photons"] * (last["error"] / target) ** 2 if last["error"] > target else plain[0]["photons"]
     dn = []
-    t_dn = None
+    chosen = None
     vol, prop = cfg["vol"], cfg["prop"]
     net.denoise(np.ones(vol.shape, np.float32), vol, prop, 1e5)       # buffers for this grid
     torch.cuda.synchronize()
     for n in dn_ladder:
         t0 = time.perf_counter()
-        f = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 100 + int(math.log10(n) * 10)))["flux"]
-        t_mc = time.perf_counter() - t0
-        d = net.denoise(f, vol, prop, n)
+        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 100 + int(math.log10(n) * 10)))
+        d = net.denoise(r["flux"], vol, prop, n)
         dt = time.perf_counter() - t0
-        e_raw = median_rel_error(_flat(f), judge)
-        e = median_rel_error(_flat(d), judge)
-        dn.append({"photons": n, "error": e, "error_plain": e_raw, "s": dt, "mc_s": t_mc})
-        if t_dn is None and e <= target:
-            t_dn = dt
-    fallback = t_dn is None
-    if fallback:
-        t_dn = t_plain
-    return {"plain": [{"photons": n, "error": e, "s": s} for n, e, s in plain], "denoised": dn,
-            "t_plain_s": t_plain, "t_denoised_s": t_dn, "speedup": t_plain / t_dn, "fallback": fallback,
-            "judge_photons": judge_photons, "judge_s": judge_s, "photons_per_s": rate}
+        rec = {"photons": n, "error": median_rel_error(_flat(d), judge),
+               "error_plain": median_rel_error(_flat(r["flux"]), judge), "s": dt,
+               "kernel_s": r["stat"]["kernel_ms"] * 1e-3, "network_s": net.last_gpu_ms * 1e-3}
+        dn.append(rec)
+        if chosen is None and rec["error"] <= target:
+            chosen = rec
+    out = {"plain": plain, "denoised": dn, "photons_plain": n_star, "t_plain_s": n_star / rate_wall,
+           "t_plain_device_s": n_star / rate_dev, "judge_photons": judge_photons, "judge_s": judge_s,
+           "judge_error_est": judge_err,
+           "photons_per_s": rate_wall, "photons_per_s_device": rate_dev, "fallback": chosen is None}
+    if chosen is None:
+        out.update(t_denoised_s=out["t_plain_s"], t_denoised_device_s=out["t_plain_device_s"], photons_denoised=n_star)
+    else:
+        out.update(t_denoised_s=chosen["s"], t_denoised_device_s=chosen["kernel_s"] + chosen["network_s"],
+                   photons_denoised=chosen["photons"])
+    out["speedup"] = out["t_plain_s"] / out["t_denoised_s"]
+    out["speedup_device"] = out["t_plain_device_s"] / out["t_denoised_device_s"]
+    return out
 
 
 def main(argv: list[str] | None = None) -> None:
@@ -511,17 +532,18 @@ def main(argv: list[str] | None = None) -> None:
 
     ap = argparse.ArgumentParser(prog="python -m mcx_gb300.denoise")
     ap.add_argument("command", choices=["train"])
-    ap.add_argument("--count", type=int, default=192, help="training volumes")
+    ap.add_argument("--count", type=int, default=128, help="training volumes")
     ap.add_argument("--edge", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--target-photons", type=float, default=1e7)
-    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--target-photons", type=float, default=1e8)
+    ap.add_argument("--input-photons", default="1e5,1e6,1e7")
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     a = ap.parse_args(argv)
     t0 = time.perf_counter()
-    data = make_pairs(a.count, a.edge, a.seed, a.target_photons)
+    data = make_pairs(a.count, a.edge, a.seed, a.target_photons, tuple(float(v) for v in a.input_photons.split(",")))
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     net = UNet(seed=a.seed)
@@ -529,7 +551,8 @@ def main(argv: list[str] | None = None) -> None:
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     net.save(a.out)
-    print(json.dumps({"volumes": a.count, "edge": a.edge, "target_photons": a.target_photons, "steps": a.steps,
+    print(json.dumps({"volumes": a.count, "edge": a.edge, "target_photons": a.target_photons,
+                      "input_photons": data["photons"], "final_loss": evaluate_loss(net, data), "steps": a.steps,
                       "batch": a.batch, "simulate_s": t1 - t0, "train_s": t2 - t1,
                       "ms_per_step": 1e3 * (t2 - t1) / a.steps, "losses": losses, "out": a.out}))
 
