@@ -122,10 +122,12 @@ def test_box_means_against_scipy():
 
 
 def test_median_rel_error(dn):
-    ref = np.array([1.0, 0.5, 1e-6, 0.2])
+    ref = np.array([1.0, 0.5, 1e-7, 0.2])
     est = np.array([1.1, 0.5, 5.0, 0.1])
-    # scored: ref >= 1e-4 * 1.0 -> voxels 0, 1, 3 with errors 0.1, 0, 0.5
+    # scored: ref >= 1e-6 * 1.0 -> voxels 0, 1, 3 with errors 0.1, 0, 0.5
+    assert dn.VALID_FRAC == 1e-6
     assert dn.median_rel_error(est, ref) == pytest.approx(0.1)
+    assert dn.median_rel_error(est, ref, frac=1e-8) == pytest.approx(0.3)
 
 
 def test_denoise_instances(engine):
