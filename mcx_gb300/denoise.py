@@ -377,6 +377,15 @@ def make_pairs(count: int, edge: int = 64, seed: int = 1, target_photons: float 
             "edge": edge, "count": count, "target_photons": float(target_photons), "seed": seed}
 
 
+def _crop(t: torch.Tensor, edge: int, crop: int, offs: list[tuple[int, int, int]]) -> torch.Tensor:
+    """Per-sample crop^3 windows at offsets (z, y, x) of [n, edge^3] tensors (voxel order x
+    fastest), flattened back to [n, crop^3]."""
+    v = t.view(t.shape[0], edge, edge, edge)
+    if crop == edge:
+        return t
+    return torch.stack([v[i, z:z + crop, y:y + crop, x:x + crop] for i, (z, y, x) in enumerate(offs)]).reshape(t.shape[0], -1)
+
+
 def _augment(t: torch.Tensor, edge: int, flips: tuple[bool, bool, bool]) -> torch.Tensor:
     """Mirror in x and/or y and swap x with y ([count, vox] tensors, voxel order x fastest); the
     pencil enters along +z, so these leave the physics unchanged."""
@@ -390,14 +399,17 @@ def _augment(t: torch.Tensor, edge: int, flips: tuple[bool, bool, bool]) -> torc
     return v.reshape(t.shape[0], -1).contiguous()
 
 
-def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr: float = 2e-3,
-          seed: int = 0, log_every: int = 100, verbose: bool = True) -> list[float]:
-    """AdamW with a short warm-up and cosine decay over `steps` batches of `batch` volumes, each
-    with a random input photon count and a random mirror/swap.  Returns the loss per log point
-    (mean absolute log10 error over scored voxels)."""
+def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr: float = 1e-3,
+          seed: int = 0, log_every: int = 100, verbose: bool = True, crop: int | None = None) -> list[float]:
+    """AdamW with a short warm-up and cosine decay over `steps` batches of `batch` samples, each
+    a random crop^3 window (the whole volume by default) of a random volume at a random input
+    photon count, randomly mirrored / swapped.  Returns the loss per log point (mean absolute
+    log10 error over scored voxels)."""
     rng = np.random.default_rng(seed)
     edge, count = data["edge"], data["count"]
-    vox = edge ** 3
+    crop = crop or edge
+    if crop % 8 or crop > edge:
+        raise ValueError("crop must be a multiple of 8 no larger than the volumes")
     lp_all = torch.tensor([math.log10(n) for n in data["photons"]], dtype=torch.float32, device=net.dev)
     losses, acc, nacc = [], 0.0, 0
     warm = max(1, steps // 20)
@@ -405,14 +417,19 @@ def train(net: UNet, data: dict[str, Any], steps: int = 1000, batch: int = 4, lr
         idx = rng.choice(count, size=batch, replace=count < batch)
         lvl = rng.integers(0, len(data["photons"]), size=batch)
         flips = tuple(bool(v) for v in rng.integers(0, 2, 3))
+        offs = [tuple(int(o) for o in rng.integers(0, edge - crop + 1, 3)) for _ in range(batch)]
         ii = torch.from_numpy(idx).to(net.dev)
         ll = torch.from_numpy(lvl).to(net.dev)
-        flux = _augment(data["inputs"][ll, ii], edge, flips)
-        labels = _augment(data["labels"][ii], edge, flips)
-        target = _augment(data["target"][ii], edge, flips)
-        valid = _augment(data["valid"][ii], edge, flips)
-        x0, xres = net.pack(flux, labels, data["props"][ii].contiguous(), lp_all[ll].contiguous(), edge, edge, edge)
-        A = net.forward(x0, xres, batch, edge, edge, edge)
+
+        def prep(t):
+            return _augment(_crop(t, edge, crop, offs), crop, flips)
+
+        flux = prep(data["inputs"][ll, ii])
+        labels = prep(data["labels"][ii])
+        target = prep(data["target"][ii])
+        valid = prep(data["valid"][ii])
+        x0, xres = net.pack(flux, labels, data["props"][ii].contiguous(), lp_all[ll].contiguous(), crop, crop, crop)
+        A = net.forward(x0, xres, batch, crop, crop, crop)
         nval = float(valid.sum().item())
         net.loss_acc.zero_()
         net.backward(A, target.reshape(-1), valid.reshape(-1), 1.0 / max(nval, 1.0))
@@ -486,15 +503,27 @@ def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, ta
                       "kernel_s": r["stat"]["kernel_ms"] * 1e-3})
     rate_wall = sum(p["photons"] for p in plain) / sum(p["s"] for p in plain)
     rate_dev = sum(p["photons"] for p in plain) / sum(p["kernel_s"] for p in plain)
-    n_star = None
+    # photon count that reaches the target: log-log interpolation between the bracketing budgets
+    # (the 1/sqrt(N) law past the last one); its time: the measured times interpolated linearly
+    # in photons between the same budgets (so plain MC pays the same per-call costs and
+    # long-photon latency the denoised pipeline pays), extrapolated at the last segment's rate
+    n_star, seg = None, None
     for a, b in zip(plain, plain[1:]):
         if a["error"] > target >= b["error"]:
             slope = math.log(b["error"] / a["error"]) / math.log(b["photons"] / a["photons"])
-            n_star = a["photons"] * (target / a["error"]) ** (1.0 / slope)
+            n_star, seg = a["photons"] * (target / a["error"]) ** (1.0 / slope), (a, b)
             break
     if n_star is None:
         last = plain[-1]
-        n_star = last["photons"] * (last["error"] / target) ** 2 if last["error"] > target else plain[0]["photons"]
+        if last["error"] > target:
+            n_star, seg = last["photons"] * (last["error"] / target) ** 2, (plain[-2], plain[-1])
+        else:
+            n_star, seg = plain[0]["photons"], (plain[0], plain[1])
+
+    def at(key):
+        a, b = seg
+        return a[key] + (n_star - a["photons"]) * (b[key] - a[key]) / (b["photons"] - a["photons"])
+
     dn = []
     chosen = None
     vol, prop = cfg["vol"], cfg["prop"]
@@ -511,8 +540,8 @@ def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, ta
         dn.append(rec)
         if chosen is None and rec["error"] <= target:
             chosen = rec
-    out = {"plain": plain, "denoised": dn, "photons_plain": n_star, "t_plain_s": n_star / rate_wall,
-           "t_plain_device_s": n_star / rate_dev, "judge_photons": judge_photons, "judge_s": judge_s,
+    out = {"plain": plain, "denoised": dn, "photons_plain": n_star, "t_plain_s": max(at("s"), plain[0]["s"]),
+           "t_plain_device_s": max(at("kernel_s"), plain[0]["kernel_s"]), "judge_photons": judge_photons, "judge_s": judge_s,
            "judge_error_est": judge_err,
            "photons_per_s": rate_wall, "photons_per_s_device": rate_dev, "fallback": chosen is None}
     if chosen is None:
@@ -532,8 +561,9 @@ def main(argv: list[str] | None = None) -> None:
 
     ap = argparse.ArgumentParser(prog="python -m mcx_gb300.denoise")
     ap.add_argument("command", choices=["train"])
-    ap.add_argument("--count", type=int, default=128, help="training volumes")
-    ap.add_argument("--edge", type=int, default=64)
+    ap.add_argument("--count", type=int, default=64, help="training volumes")
+    ap.add_argument("--edge", type=int, default=128, help="edge of the simulated training volumes")
+    ap.add_argument("--crop", type=int, default=64, help="edge of the training windows")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--target-photons", type=float, default=1e8)
     ap.add_argument("--input-photons", default="1e5,1e6,1e7")
@@ -547,11 +577,11 @@ def main(argv: list[str] | None = None) -> None:
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     net = UNet(seed=a.seed)
-    losses = train(net, data, steps=a.steps, batch=a.batch, lr=a.lr)
+    losses = train(net, data, steps=a.steps, batch=a.batch, lr=a.lr, crop=a.crop)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     net.save(a.out)
-    print(json.dumps({"volumes": a.count, "edge": a.edge, "target_photons": a.target_photons,
+    print(json.dumps({"volumes": a.count, "edge": a.edge, "crop": a.crop, "target_photons": a.target_photons,
                       "input_photons": data["photons"], "final_loss": evaluate_loss(net, data), "steps": a.steps,
                       "batch": a.batch, "simulate_s": t1 - t0, "train_s": t2 - t1,
                       "ms_per_step": 1e3 * (t2 - t1) / a.steps, "losses": losses, "out": a.out}))
