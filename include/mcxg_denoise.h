@@ -60,9 +60,9 @@ int mcxg_dn_head(const void* act, const float* xres, const float* w, const float
 
 /* Input features of nvol volumes of d x h x w voxels: fluence (fp32, normalised as MCX writes
  * it, x fastest), labels (uint8) with per-volume media tables props[nvol][nprop][4] (mua, mus, g,
- * n), and log10(photons) per volume -> x0 (bf16, 16 channels: log10 of the fluence and of its
- * 3x3x3 and 5x5x5 in-bounds means, log10 mua, log10 reduced scattering, photon-count code) and
- * xres = log10(3x3x3 mean + 1e-10). */
+ * n), and log10(photons) per volume -> x0 (bf16, 16 channels: with l0, l3, l5 the log10 of the
+ * fluence and of its 3x3x3 and 5x5x5 in-bounds means, the scaled l3, 4 (l0 - l3), 4 (l5 - l3),
+ * an empty-voxel flag, log10 mua, log10 reduced scattering, a photon-count code) and xres = l3. */
 int mcxg_dn_pack(const float* flux, const uint8_t* label, const float* props, const float* log_photons, void* x0,
                  float* xres, int nvol, int d, int h, int w, int nprop, void* stream);
 

@@ -85,23 +85,23 @@ __device__ __forceinline__ long long tap_voxel(const Geo& g, long long v, int z,
 }
 
 // ---------------------------------------------------------------------------------------------
-// Forward convolution (and data gradient): Y[v, n0:n0+BN] over a tile of BM = 128 voxels.
-// 256 threads; warps tile the BM x BN output as WARPS_M x WARPS_N.
-template <int BN, int BK, int STAGES>
-__global__ void __launch_bounds__(256) conv_fwd_kernel(const bf16* __restrict__ x, const bf16* __restrict__ wt,
-                                                       const float* __restrict__ bias, const bf16* __restrict__ mask,
-                                                       bf16* __restrict__ y, Geo g, int cin, int cout, int taps,
-                                                       int relu) {
-    constexpr int BM = 128;
+// Forward convolution (and data gradient): Y[v, n0:n0+BN] over a tile of BM voxels.  K runs over
+// (tap, input channel) flattened, k = tap*cin + ci, in stages of BK: with few input channels one
+// stage spans several taps (4 taps of 16 channels at BK = 64), so small layers still feed the
+// tensor cores several k16 steps per barrier.  A chunk of 8 channels never straddles two taps
+// (cin % 8 == 0); chunks past the last tap are zero-filled, as are the halo's out-of-volume rows.
+template <int BM, int BN, int BK, int WARPS_M, int WARPS_N, int STAGES>
+__global__ void __launch_bounds__(32 * WARPS_M * WARPS_N) conv_fwd_kernel(
+    const bf16* __restrict__ x, const bf16* __restrict__ wt, const float* __restrict__ bias,
+    const bf16* __restrict__ mask, bf16* __restrict__ y, Geo g, int cin, int cout, int taps, int relu) {
+    constexpr int THREADS = 32 * WARPS_M * WARPS_N;
     constexpr int CPR = BK / 8;
-    constexpr int WARPS_N = BN >= 64 ? BN / 32 : 1;
-    constexpr int WARPS_M = 8 / WARPS_N;
     constexpr int WM = BM / WARPS_M, WN = BN / WARPS_N;
     constexpr int MI = WM / 16, NI = WN / 8;
     constexpr int A_ELEMS = BM * BK, B_ELEMS = BN * BK;
     constexpr int STAGE = A_ELEMS + B_ELEMS;
-    constexpr int A_IT = BM * CPR / 256;
-    static_assert(NI % 2 == 0 && MI >= 1 && A_IT >= 1, "tile shape");
+    constexpr int A_IT = BM * CPR / THREADS;
+    static_assert(NI % 2 == 0 && MI >= 1 && A_IT >= 1 && (BM * CPR) % THREADS == 0 && THREADS % CPR == 0, "tile shape");
 
     extern __shared__ __align__(128) unsigned char dyn_smem[];
     bf16* sm = reinterpret_cast<bf16*>(dyn_smem);
@@ -110,38 +110,55 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(const bf16* __restrict__ 
     const int wm0 = (warp / WARPS_N) * WM, wn0 = (warp % WARPS_N) * WN;
     const long long m0 = (long long)blockIdx.x * BM;
     const int n0 = blockIdx.y * BN;
-    const int kc = cin / BK;
-    const int ktiles = taps * kc;
+    const int ktot = taps * cin;
+    const int ktiles = (ktot + BK - 1) / BK;
+    const int ac = tid % CPR;                      // the A chunk column this thread loads
+    const int hw = g.h * g.w;
 
-    // voxel coordinates of the A rows this thread loads (fixed over the K loop)
-    long long av[A_IT];
-    int az[A_IT], ay[A_IT], ax[A_IT];
+    // voxel index and packed (z, y, x) of the A rows this thread loads (fixed over the K loop);
+    // a row past the last voxel has index -1
+    int av[A_IT], azyx[A_IT];
 #pragma unroll
     for (int i = 0; i < A_IT; ++i) {
-        int row = (tid + i * 256) / CPR;
+        int row = tid / CPR + i * (THREADS / CPR);
         long long v = m0 + row;
-        av[i] = v < g.m ? v : -1;
-        long long r = v % ((long long)g.d * g.h * g.w);
-        ax[i] = (int)(r % g.w);
-        ay[i] = (int)((r / g.w) % g.h);
-        az[i] = (int)(r / ((long long)g.w * g.h));
+        long long r = v % ((long long)g.d * hw);
+        int xx = (int)(r % g.w), yy = (int)((r / g.w) % g.h), zz = (int)(r / hw);
+        av[i] = v < g.m ? (int)v : -1;
+        azyx[i] = (zz << 20) | (yy << 10) | xx;
     }
 
     auto load_stage = [&](int stage, int kt) {
         bf16* sa = sm + stage * STAGE;
         bf16* sb = sa + A_ELEMS;
-        const int t = kt / kc, c0 = (kt % kc) * BK;
+        const int k = kt * BK + ac * 8;
+        const int t = k / cin, ch = k - t * cin;
+        int dz = 0, dy = 0, dx = 0;
+        if (taps == 27) {
+            dz = t / 9 - 1;
+            dy = (t / 3) % 3 - 1;
+            dx = t % 3 - 1;
+        }
+        const bool kin = t < taps;
+        const int delta = dz * hw + dy * g.w + dx;
 #pragma unroll
         for (int i = 0; i < A_IT; ++i) {
-            int q = tid + i * 256, row = q / CPR, c = q % CPR;
-            long long src = av[i] >= 0 ? tap_voxel(g, av[i], az[i], ay[i], ax[i], t, taps) : -1;
-            const bf16* p = src >= 0 ? x + src * cin + c0 + c * 8 : x;
-            cp_async16(smem_addr(sa + row * BK + ((c ^ swz<CPR>(row)) << 3)), p, src >= 0);
+            int row = tid / CPR + i * (THREADS / CPR);
+            int zz = (azyx[i] >> 20) + dz, yy = ((azyx[i] >> 10) & 1023) + dy, xx = (azyx[i] & 1023) + dx;
+            bool ok = kin && av[i] >= 0 && zz >= 0 && zz < g.d && yy >= 0 && yy < g.h && xx >= 0 && xx < g.w;
+            const bf16* p = ok ? x + (long long)(av[i] + delta) * cin + ch : x;
+            cp_async16(smem_addr(sa + row * BK + ((ac ^ swz<CPR>(row)) << 3)), p, ok);
         }
-        for (int q = tid; q < BN * CPR; q += 256) {
-            int row = q / CPR, c = q % CPR;
-            const bf16* p = wt + ((long long)(n0 + row) * taps + t) * cin + c0 + c * 8;
-            cp_async16(smem_addr(sb + row * BK + ((c ^ swz<CPR>(row)) << 3)), p, true);
+#pragma unroll
+        for (int i = 0; i < (BN * CPR + THREADS - 1) / THREADS; ++i) {
+            int q = tid + i * THREADS;
+            if (q < BN * CPR) {
+                int row = q / CPR, c = q % CPR;
+                int kb = kt * BK + c * 8;
+                bool ok = kb < ktot;
+                const bf16* p = ok ? wt + (long long)(n0 + row) * ktot + kb : wt;
+                cp_async16(smem_addr(sb + row * BK + ((c ^ swz<CPR>(row)) << 3)), p, ok);
+            }
         }
     };
 
@@ -208,7 +225,7 @@ __global__ void __launch_bounds__(256) conv_fwd_kernel(const bf16* __restrict__ 
         }
     __syncthreads();
     constexpr int CH = BN / 8;
-    for (int q = tid; q < BM * CH; q += 256) {
+    for (int q = tid; q < BM * CH; q += THREADS) {
         int row = q / CH, c = q % CH;
         long long v = m0 + row;
         if (v >= g.m) continue;
@@ -555,13 +572,15 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16* __restrict__ act,
     }
 }
 
-// Input features of one voxel (16 channels, 0..5 used):
-//   0, 1, 2: (log10(m + 1e-10) + 5) / 3 for m = the noisy fluence F, the mean of F over the
-//            in-bounds voxels of its 3x3x3 neighbourhood, and over its 5x5x5 neighbourhood
-//   3: log10(mua) + 2        4: log10(mus * (1 - g))        5: (log10(photons) - 5.5) * 2
-// and xres[v] = log10(3x3x3 mean + 1e-10), the residual base the head adds its correction to.
-// The means are taken in linear fluence, where a voxel no photon reached is a zero among its
-// neighbours rather than a -10 outlier as it is in log space.
+// Input features of one voxel (16 channels, 0..6 used), with l0, l3, l5 = log10(m + 1e-10) of the
+// noisy fluence F and of its means over the in-bounds voxels of the 3x3x3 and 5x5x5
+// neighbourhoods:
+//   0: (l3 + 5) / 3      1: clamp(4 (l0 - l3), -4, 4)      2: clamp(4 (l5 - l3), -4, 4)
+//   3: 1 where F is 0    4: log10(mua) + 2    5: log10(mus (1 - g))    6: (log10(photons) - 5.5) * 2
+// and xres[v] = l3, the residual base the head adds its correction to.  The means are taken in
+// linear fluence, where a voxel no photon reached is a zero among its neighbours rather than a
+// -10 outlier as in log space; channels 1 and 2 hand the network the noise and the curvature at
+// the scale of its correction instead of as small differences of large inputs.
 __global__ void pack_kernel(const float* __restrict__ flux, const uint8_t* __restrict__ label,
                             const float* __restrict__ props, const float* __restrict__ log_photons,
                             bf16* __restrict__ x0, float* __restrict__ xres, Geo g, int nprop) {
@@ -596,18 +615,19 @@ __global__ void pack_kernel(const float* __restrict__ flux, const uint8_t* __res
         int lab = label[v];
         if (lab >= nprop) lab = nprop - 1;
         const float* pr = props + ((long long)n * nprop + lab) * 4;
-        float l0 = log10f(fmaxf(flux[v], 0.f) + 1e-10f);
+        const float fv = flux[v];
+        float l0 = log10f(fmaxf(fv, 0.f) + 1e-10f);
         float l3 = log10f(s3 / (float)c3 + 1e-10f);
         float l5 = log10f(s5 / (float)c5 + 1e-10f);
         float f[8], zz8[8];
-        f[0] = (l0 + 5.f) * (1.f / 3.f);
-        f[1] = (l3 + 5.f) * (1.f / 3.f);
-        f[2] = (l5 + 5.f) * (1.f / 3.f);
-        f[3] = pr[0] > 0.f ? log10f(pr[0]) + 2.f : -2.f;
+        f[0] = (l3 + 5.f) * (1.f / 3.f);
+        f[1] = fminf(fmaxf(4.f * (l0 - l3), -4.f), 4.f);
+        f[2] = fminf(fmaxf(4.f * (l5 - l3), -4.f), 4.f);
+        f[3] = fv <= 0.f ? 1.f : 0.f;
+        f[4] = pr[0] > 0.f ? log10f(pr[0]) + 2.f : -2.f;
         float musp = pr[1] * (1.f - pr[2]);
-        f[4] = musp > 0.f ? log10f(musp) : -3.f;
-        f[5] = (log_photons[n] - 5.5f) * 2.f;
-        f[6] = 0.f;
+        f[5] = musp > 0.f ? log10f(musp) : -3.f;
+        f[6] = (log_photons[n] - 5.5f) * 2.f;
         f[7] = 0.f;
         for (int e = 0; e < 8; ++e) zz8[e] = 0.f;
         store8(x0 + v * 16, f);
@@ -667,31 +687,32 @@ int grid_for(long long work, int block) {
     return (int)(g < 1 ? 1 : (g > 152 * 32 ? 152 * 32 : g));
 }
 
-template <int BN, int BK>
+template <int BM, int BN, int BK, int WARPS_M, int WARPS_N, int STAGES>
 int conv_fwd_launch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
                     int cout, int taps, int relu, cudaStream_t st) {
-    constexpr int STAGES = 4, BM = 128;
     constexpr int stage_bytes = (BM + BN) * BK * 2;
     constexpr int epi_bytes = BM * (BN + 8) * 2;
     constexpr int smem = STAGES * stage_bytes > epi_bytes ? STAGES * stage_bytes : epi_bytes;
-    auto kern = conv_fwd_kernel<BN, BK, STAGES>;
+    auto kern = conv_fwd_kernel<BM, BN, BK, WARPS_M, WARPS_N, STAGES>;
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         attr = true;
     }
     dim3 grid((unsigned)((g.m + BM - 1) / BM), (unsigned)(cout / BN));
-    kern<<<grid, 256, smem, st>>>(x, w, bias, mask, y, g, cin, cout, taps, relu);
+    kern<<<grid, 32 * WARPS_M * WARPS_N, smem, st>>>(x, w, bias, mask, y, g, cin, cout, taps, relu);
     return launched();
 }
 
-template <int BK>
-int conv_fwd_bn(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin, int cout,
-                int taps, int relu, cudaStream_t st) {
-    if (cout % 128 == 0) return conv_fwd_launch<128, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
-    if (cout % 64 == 0) return conv_fwd_launch<64, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
-    if (cout % 32 == 0) return conv_fwd_launch<32, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
-    return conv_fwd_launch<16, BK>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+// Tile per output width: 128 voxels x (128 | 64 | 32 | 16) channels; narrow outputs take deeper
+// K stages and fewer, taller warp tiles (two 16-row fragments per warp) so that each B fragment
+// feeds more MMAs.
+int conv_fwd_dispatch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
+                      int cout, int taps, int relu, cudaStream_t st) {
+    if (cout % 128 == 0) return conv_fwd_launch<128, 128, 32, 2, 4, 4>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    if (cout % 64 == 0) return conv_fwd_launch<128, 64, 32, 4, 2, 4>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    if (cout % 32 == 0) return conv_fwd_launch<128, 32, 64, 4, 1, 3>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
+    return conv_fwd_launch<128, 16, 64, 4, 1, 3>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
 }
 
 template <int BM>
@@ -737,18 +758,15 @@ const char* mcxg_dn_last_error(void) { return g_err; }
 int mcxg_dn_conv_fwd(const void* x, const void* w, const float* bias, const void* mask, void* y, int nvol, int d,
                      int h, int wd, int cin, int cout, int taps, int relu, void* stream) {
     if (!x || !w || !y || !dims_ok(nvol, d, h, wd)) return fail("conv: null tensor or empty volume");
-    if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0) return fail("conv: channel counts must be multiples of 16");
+    if (cin % 8 || cout % 16 || cin <= 0 || cout <= 0) return fail("conv: cin must be a multiple of 8, cout of 16");
     if (taps != 1 && taps != 27) return fail("conv: taps must be 1 or 27");
     if (!aligned16(x) || !aligned16(w) || !aligned16(y) || (mask && !aligned16(mask)))
         return fail("conv: tensors must be 16-byte aligned");
     Geo g = make_geo(nvol, d, h, wd);
-    auto st = static_cast<cudaStream_t>(stream);
-    auto X = static_cast<const bf16*>(x);
-    auto W = static_cast<const bf16*>(w);
-    auto M = static_cast<const bf16*>(mask);
-    auto Y = static_cast<bf16*>(y);
-    if (cin % 32 == 0) return conv_fwd_bn<32>(X, W, bias, M, Y, g, cin, cout, taps, relu, st);
-    return conv_fwd_bn<16>(X, W, bias, M, Y, g, cin, cout, taps, relu, st);
+    if (g.m >= (1LL << 31) || d >= 1024 || h >= 1024 || wd >= 1024) return fail("conv: volume too large");
+    return conv_fwd_dispatch(static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias,
+                             static_cast<const bf16*>(mask), static_cast<bf16*>(y), g, cin, cout, taps, relu,
+                             static_cast<cudaStream_t>(stream));
 }
 
 int mcxg_dn_conv_wgrad(const void* dy, const void* x, float* dw, int nvol, int d, int h, int wd, int cin, int cout,

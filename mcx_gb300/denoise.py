@@ -1,9 +1,10 @@
 """MC + learned denoiser: a 4-level 3D U-Net that maps low-photon fluence to high-photon fluence.
 
-The network works on log10 fluence: its input features are the noisy map and its 3x3x3 and 5x5x5
-neighbourhood means (taken in linear fluence, so that voxels no photon reached do not become
-log-space outliers), the voxel's absorption and reduced scattering coefficients and the photon
-count (``mcxg_dn_pack``); 3x3x3 convolutions with ReLU at 16/32/64/128 channels, 2x2x2 average
+The network works on log10 fluence: its input features are the 3x3x3 neighbourhood mean of the
+noisy map and the deviations of the map and of its 5x5x5 mean from it (means taken in linear
+fluence, so that voxels no photon reached do not become log-space outliers), an empty-voxel flag,
+the voxel's absorption and reduced scattering coefficients and the photon count
+(``mcxg_dn_pack``); 3x3x3 convolutions with ReLU at 16/32/64/128 channels, 2x2x2 average
 pooling, nearest upsampling with skip concatenation, and a 1x1x1 head whose output is added to
 the log of the 3x3x3 mean (the network learns a correction to a box filter; at initialisation it
 is nearly that filter).

@@ -70,25 +70,30 @@ def box_means(flux: np.ndarray, edge: tuple[int, int, int]) -> tuple[np.ndarray,
 
 def features(flux: np.ndarray, labels: np.ndarray, props: np.ndarray, log_photons: np.ndarray,
              edge: tuple[int, int, int]) -> tuple:
-    """The 16 input channels (6 used) and residual base, restating mcxg_dn_pack on [nvol, vox]
-    arrays over a (d, h, w) grid: log10 of the fluence, of its 3x3x3 and of its 5x5x5 in-bounds
-    means (each + 1e-10, scaled (l + 5) / 3), log10(mua) + 2, log10(mus (1 - g)), the photon-count
-    code (log10(photons) - 5.5) * 2; the residual base is log10(3x3x3 mean + 1e-10)."""
+    """The 16 input channels (7 used) and residual base, restating mcxg_dn_pack on [nvol, vox]
+    arrays over a (d, h, w) grid, with l0, l3, l5 = log10(m + 1e-10) of the fluence and of its
+    3x3x3 and 5x5x5 in-bounds means:
+      0: (l3 + 5) / 3          1: clamp(4 (l0 - l3), -4, 4)       2: clamp(4 (l5 - l3), -4, 4)
+      3: 1 where the fluence is 0, else 0
+      4: log10(mua) + 2        5: log10(mus (1 - g))              6: (log10(photons) - 5.5) * 2
+    and the residual base l3."""
     nvol, vox = flux.shape
     lab = np.minimum(labels.astype(np.int64), props.shape[1] - 1)
     pr = np.take_along_axis(props, lab[..., None].repeat(4, -1), axis=1)        # [nvol, vox, 4]
     b3, b5 = box_means(flux, edge)
     lg = lambda a: np.log10(np.maximum(a, 0).astype(np.float32) + np.float32(1e-10)).astype(np.float32)  # noqa: E731
+    l0, l3, l5 = lg(flux), lg(b3), lg(b5)
     x = np.zeros((nvol, vox, 16), np.float32)
-    x[..., 0] = (lg(flux) + 5.0) / 3.0
-    x[..., 1] = (lg(b3) + 5.0) / 3.0
-    x[..., 2] = (lg(b5) + 5.0) / 3.0
+    x[..., 0] = (l3 + 5.0) / 3.0
+    x[..., 1] = np.clip(4.0 * (l0 - l3), -4.0, 4.0)
+    x[..., 2] = np.clip(4.0 * (l5 - l3), -4.0, 4.0)
+    x[..., 3] = (np.asarray(flux) <= 0).astype(np.float32)
     with np.errstate(divide="ignore"):
-        x[..., 3] = np.where(pr[..., 0] > 0, np.log10(np.where(pr[..., 0] > 0, pr[..., 0], 1.0)) + 2.0, -2.0)
+        x[..., 4] = np.where(pr[..., 0] > 0, np.log10(np.where(pr[..., 0] > 0, pr[..., 0], 1.0)) + 2.0, -2.0)
         musp = pr[..., 1] * (1.0 - pr[..., 2])
-        x[..., 4] = np.where(musp > 0, np.log10(np.where(musp > 0, musp, 1.0)), -3.0)
-    x[..., 5] = ((log_photons - 5.5) * 2.0)[:, None]
-    return x, lg(b3)
+        x[..., 5] = np.where(musp > 0, np.log10(np.where(musp > 0, musp, 1.0)), -3.0)
+    x[..., 6] = ((log_photons - 5.5) * 2.0)[:, None]
+    return x, l3
 
 
 def forward(params: dict, x0: torch.Tensor, xres: torch.Tensor, nvol: int, d: int, h: int, w: int) -> torch.Tensor:

@@ -99,13 +99,14 @@ def test_features():
     b5 = np.array([f[:3].mean(), f.mean(), f.mean(), f[1:].mean()])
     lg = lambda a: np.log10(a + 1e-10)  # noqa: E731
     np.testing.assert_allclose(l[0], lg(b3), rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 0], (lg(f) + 5) / 3, rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 1], (lg(b3) + 5) / 3, rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 2], (lg(b5) + 5) / 3, rtol=1e-6)
-    np.testing.assert_allclose(x[0, :, 3], [-2.0, 0.0, -1.0, -1.0], atol=1e-6)      # label 9 clamps to the last row
-    np.testing.assert_allclose(x[0, :, 4], [-3.0, 0.0, 0.0, 0.0], atol=1e-6)
-    np.testing.assert_allclose(x[0, :, 5], -1.0)
-    assert not x[..., 6:].any()
+    np.testing.assert_allclose(x[0, :, 0], (lg(b3) + 5) / 3, rtol=1e-6)
+    np.testing.assert_allclose(x[0, :, 1], np.clip(4 * (lg(f) - lg(b3)), -4, 4), rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(x[0, :, 2], np.clip(4 * (lg(b5) - lg(b3)), -4, 4), rtol=1e-5, atol=1e-5)
+    np.testing.assert_array_equal(x[0, :, 3], [1, 0, 0, 1])
+    np.testing.assert_allclose(x[0, :, 4], [-2.0, 0.0, -1.0, -1.0], atol=1e-6)      # label 9 clamps to the last row
+    np.testing.assert_allclose(x[0, :, 5], [-3.0, 0.0, 0.0, 0.0], atol=1e-6)
+    np.testing.assert_allclose(x[0, :, 6], -1.0)
+    assert not x[..., 7:].any()
 
 
 def test_box_means_against_scipy():
