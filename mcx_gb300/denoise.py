@@ -469,45 +469,12 @@ def evaluate_loss(net: UNet, data: dict[str, Any], batch: int = 4) -> list[float
 
 
 # -- the metric -------------------------------------------------------------------------------
-def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, target: float = 0.05,
-                  ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
-                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7), judge_check: bool = True) -> dict[str, Any]:
-    """Time to reach a median relative fluence error of `target` against a `judge_photons` run,
-    for plain MC and for MC + denoiser, on one volume.
-
-    Plain MC runs each budget of `ladder` end to end through the engine's API; the photon count
-    that reaches the target is interpolated in log(error)-log(photons) between the bracketing
-    budgets (extrapolated with the 1/sqrt(N) law past the last one) and priced at the ladder's
-    photon rate -- on the device (transport kernel time) and end to end (wall time of the calls).
-    MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the
-    target: on the device its transport time plus the network's, end to end the wall time of the
-    simulation call plus upload, network and download.  Where no budget reaches the target,
-    plain MC is the fallback and its times are the pipeline's.  With `judge_check`, a second,
-    independent run of a quarter of the judge's photons estimates the judge's own median error
-    (their difference has sqrt(5) times the judge's standard error)."""
-    from .api import run
-
-    t0 = time.perf_counter()
-    jr = run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))
-    judge = _flat(jr["flux"])
-    judge_s = time.perf_counter() - t0
-    judge_err = None
-    if judge_check:
-        j4 = _flat(run(dict(cfg, nphoton=judge_photons / 4, seed=int(cfg["seed"]) + 99))["flux"])
-        judge_err = median_rel_error(j4, judge) / math.sqrt(5.0)
-    plain = []
-    for n in ladder:
-        t0 = time.perf_counter()
-        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))
-        dt = time.perf_counter() - t0
-        plain.append({"photons": n, "error": median_rel_error(_flat(r["flux"]), judge), "s": dt,
-                      "kernel_s": r["stat"]["kernel_ms"] * 1e-3})
-    rate_wall = sum(p["photons"] for p in plain) / sum(p["s"] for p in plain)
-    rate_dev = sum(p["photons"] for p in plain) / sum(p["kernel_s"] for p in plain)
-    # photon count that reaches the target: log-log interpolation between the bracketing budgets
-    # (the 1/sqrt(N) law past the last one); its time: the measured times interpolated linearly
-    # in photons between the same budgets (so plain MC pays the same per-call costs and
-    # long-photon latency the denoised pipeline pays), extrapolated at the last segment's rate
+def _time_at(plain: list[dict], target: float) -> tuple[float, float, float]:
+    """(photons, wall s, device s) plain MC needs for a median error of `target`: photons by
+    log-log interpolation between the bracketing budgets of the ladder (the 1/sqrt(N) law past
+    the last one), times interpolated linearly in photons between the same budgets -- so plain MC
+    pays the per-call costs and long-photon latency its measured runs paid -- and extrapolated at
+    the last segment's rate."""
     n_star, seg = None, None
     for a, b in zip(plain, plain[1:]):
         if a["error"] > target >= b["error"]:
@@ -523,35 +490,71 @@ def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, ta
 
     def at(key):
         a, b = seg
-        return a[key] + (n_star - a["photons"]) * (b[key] - a[key]) / (b["photons"] - a["photons"])
+        return max(plain[0][key], a[key] + (n_star - a["photons"]) * (b[key] - a[key]) / (b["photons"] - a["photons"]))
 
-    dn = []
-    chosen = None
+    return n_star, at("s"), at("kernel_s")
+
+
+def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, targets: tuple[float, ...] = (0.05, 0.02),
+                  ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
+                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7), judge_check: bool = True) -> dict[str, Any]:
+    """Time to reach a median relative fluence error of each of `targets` against a
+    `judge_photons` run, for plain MC and for MC + denoiser, on one volume.
+
+    Plain MC runs each budget of `ladder` end to end through the engine's API and is priced by
+    ``_time_at``, on the device (transport kernel time) and end to end (wall time of the calls).
+    MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the target:
+    on the device its transport time plus the network's, end to end the wall time of the
+    simulation call plus upload, network and download.  Where no budget reaches a target, plain
+    MC is the fallback and its times are the pipeline's.  With `judge_check`, a second,
+    independent run of a quarter of the judge's photons estimates the judge's own median error
+    (their difference has sqrt(5) times the judge's standard error).  The first target's figures
+    are also returned at the top level."""
+    from .api import run
+
+    t0 = time.perf_counter()
+    judge = _flat(run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))["flux"])
+    judge_s = time.perf_counter() - t0
+    judge_err = None
+    if judge_check:
+        j4 = _flat(run(dict(cfg, nphoton=judge_photons / 4, seed=int(cfg["seed"]) + 99))["flux"])
+        judge_err = median_rel_error(j4, judge) / math.sqrt(5.0)
+    plain = []
+    for n in ladder:
+        t0 = time.perf_counter()
+        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))
+        dt = time.perf_counter() - t0
+        plain.append({"photons": n, "error": median_rel_error(_flat(r["flux"]), judge), "s": dt,
+                      "kernel_s": r["stat"]["kernel_ms"] * 1e-3})
     vol, prop = cfg["vol"], cfg["prop"]
     net.denoise(np.ones(vol.shape, np.float32), vol, prop, 1e5)       # buffers for this grid
     torch.cuda.synchronize()
+    dn = []
     for n in dn_ladder:
         t0 = time.perf_counter()
         r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 100 + int(math.log10(n) * 10)))
         d = net.denoise(r["flux"], vol, prop, n)
         dt = time.perf_counter() - t0
-        rec = {"photons": n, "error": median_rel_error(_flat(d), judge),
-               "error_plain": median_rel_error(_flat(r["flux"]), judge), "s": dt,
-               "kernel_s": r["stat"]["kernel_ms"] * 1e-3, "network_s": net.last_gpu_ms * 1e-3}
-        dn.append(rec)
-        if chosen is None and rec["error"] <= target:
-            chosen = rec
-    out = {"plain": plain, "denoised": dn, "photons_plain": n_star, "t_plain_s": max(at("s"), plain[0]["s"]),
-           "t_plain_device_s": max(at("kernel_s"), plain[0]["kernel_s"]), "judge_photons": judge_photons, "judge_s": judge_s,
-           "judge_error_est": judge_err,
-           "photons_per_s": rate_wall, "photons_per_s_device": rate_dev, "fallback": chosen is None}
-    if chosen is None:
-        out.update(t_denoised_s=out["t_plain_s"], t_denoised_device_s=out["t_plain_device_s"], photons_denoised=n_star)
-    else:
-        out.update(t_denoised_s=chosen["s"], t_denoised_device_s=chosen["kernel_s"] + chosen["network_s"],
-                   photons_denoised=chosen["photons"])
-    out["speedup"] = out["t_plain_s"] / out["t_denoised_s"]
-    out["speedup_device"] = out["t_plain_device_s"] / out["t_denoised_device_s"]
+        dn.append({"photons": n, "error": median_rel_error(_flat(d), judge),
+                   "error_plain": median_rel_error(_flat(r["flux"]), judge), "s": dt,
+                   "kernel_s": r["stat"]["kernel_ms"] * 1e-3, "network_s": net.last_gpu_ms * 1e-3})
+    per = []
+    for tgt in targets:
+        n_plain, t_wall, t_dev = _time_at(plain, tgt)
+        chosen = next((rec for rec in dn if rec["error"] <= tgt), None)
+        rec = {"target": tgt, "photons_plain": n_plain, "t_plain_s": t_wall, "t_plain_device_s": t_dev,
+               "fallback": chosen is None}
+        if chosen is None:
+            rec.update(photons_denoised=n_plain, t_denoised_s=t_wall, t_denoised_device_s=t_dev)
+        else:
+            rec.update(photons_denoised=chosen["photons"], t_denoised_s=chosen["s"],
+                       t_denoised_device_s=chosen["kernel_s"] + chosen["network_s"])
+        rec["speedup"] = rec["t_plain_s"] / rec["t_denoised_s"]
+        rec["speedup_device"] = rec["t_plain_device_s"] / rec["t_denoised_device_s"]
+        per.append(rec)
+    out = {"plain": plain, "denoised": dn, "targets": per, "judge_photons": judge_photons, "judge_s": judge_s,
+           "judge_error_est": judge_err}
+    out.update({k: v for k, v in per[0].items() if k != "target"})
     return out
 
 
@@ -561,7 +564,9 @@ def main(argv: list[str] | None = None) -> None:
     import json
 
     ap = argparse.ArgumentParser(prog="python -m mcx_gb300.denoise")
-    ap.add_argument("command", choices=["train"])
+    ap.add_argument("command", choices=["train", "forward"],
+                    help="train: simulate pairs, train, save; forward: time the network on one volume")
+    ap.add_argument("--repeat", type=int, default=10, help="forward: timed passes")
     ap.add_argument("--count", type=int, default=64, help="training volumes")
     ap.add_argument("--edge", type=int, default=128, help="edge of the simulated training volumes")
     ap.add_argument("--crop", type=int, default=64, help="edge of the training windows")
@@ -573,6 +578,26 @@ def main(argv: list[str] | None = None) -> None:
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     a = ap.parse_args(argv)
+    if a.command == "forward":
+        net = UNet(load_params() if DEFAULT_WEIGHTS.exists() else None, seed=a.seed)
+        n = a.edge
+        g = torch.Generator(device="cuda").manual_seed(a.seed)
+        x0 = torch.randn(n ** 3 * IN_CH, generator=g, device="cuda").to(torch.bfloat16)
+        xr = torch.zeros(n ** 3, device="cuda")
+        out = torch.empty(n ** 3, device="cuda")
+        for _ in range(3):
+            net.forward(x0, xr, 1, n, n, n, out=out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.repeat):
+            net.forward(x0, xr, 1, n, n, n, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / a.repeat
+        flops = sum(2.0 * (n >> l) ** 3 * ci * co * TAPS for _, ci, co, l in LAYERS)
+        print(json.dumps({"edge": n, "forward_ms": ms, "gflop": flops / 1e9, "tflops": flops / ms / 1e9}))
+        return
     t0 = time.perf_counter()
     data = make_pairs(a.count, a.edge, a.seed, a.target_photons, tuple(float(v) for v in a.input_photons.split(",")))
     torch.cuda.synchronize()
