@@ -115,17 +115,25 @@ __global__ void __launch_bounds__(32 * WARPS_M * WARPS_N) conv_fwd_kernel(
     const int ac = tid % CPR;                      // the A chunk column this thread loads
     const int hw = g.h * g.w;
 
-    // voxel index and packed (z, y, x) of the A rows this thread loads (fixed over the K loop);
-    // a row past the last voxel has index -1
+    // packed (z, y, x) of the tile's rows, one 32-bit decomposition per row shared through shared
+    // memory (-1 past the last voxel); each thread keeps those of the A rows it loads
+    __shared__ int s_zyx[BM];
+    {
+        const int vvol = g.d * hw;
+        for (int r = tid; r < BM; r += THREADS) {
+            long long v = m0 + r;
+            int rr = (int)(v % vvol);
+            int xx = rr % g.w, q = rr / g.w;
+            s_zyx[r] = v < g.m ? (((q / g.h) << 20) | ((q % g.h) << 10) | xx) : -1;
+        }
+    }
+    __syncthreads();
     int av[A_IT], azyx[A_IT];
 #pragma unroll
     for (int i = 0; i < A_IT; ++i) {
         int row = tid / CPR + i * (THREADS / CPR);
-        long long v = m0 + row;
-        long long r = v % ((long long)g.d * hw);
-        int xx = (int)(r % g.w), yy = (int)((r / g.w) % g.h), zz = (int)(r / hw);
-        av[i] = v < g.m ? (int)v : -1;
-        azyx[i] = (zz << 20) | (yy << 10) | xx;
+        azyx[i] = s_zyx[row];
+        av[i] = azyx[i] >= 0 ? (int)(m0 + row) : -1;
     }
 
     auto load_stage = [&](int stage, int kt) {
@@ -279,6 +287,33 @@ __global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict_
     const int ktiles = (int)((kend - kbeg + BK - 1) / BK);
     const long long vvol = (long long)g.d * g.h * g.w;
 
+    // the B (input) chunks this thread loads: one fixed column chunk (tap, 8 channels) and rows
+    // tid / CPB + 16 i, whose voxel coordinates advance by BK voxels per stage (stages are
+    // loaded in order), so no division runs inside the K loop
+    constexpr int B_IT = BK * CPB / 128;
+    static_assert(B_IT * 128 == BK * CPB && 128 % CPB == 0, "B loader shape");
+    const int bc = tid % CPB;
+    const int ncol = nt0 + bc * 8;
+    const bool col_ok = ncol < ntot;
+    const int tap = col_ok ? ncol / cin : 0, ci = col_ok ? ncol - tap * cin : 0;
+    int tz = 0, ty = 0, tx = 0;
+    if (taps == 27) {
+        tz = tap / 9 - 1;
+        ty = (tap / 3) % 3 - 1;
+        tx = tap % 3 - 1;
+    }
+    const long long delta = (long long)tz * g.h * g.w + ty * g.w + tx;
+    long long bv[B_IT];
+    int bz[B_IT], by[B_IT], bx[B_IT];
+#pragma unroll
+    for (int i = 0; i < B_IT; ++i) {
+        bv[i] = kbeg + tid / CPB + i * (128 / CPB);
+        long long r = bv[i] % vvol;
+        bx[i] = (int)(r % g.w);
+        by[i] = (int)((r / g.w) % g.h);
+        bz[i] = (int)(r / ((long long)g.w * g.h));
+    }
+
     auto load_stage = [&](int stage, int kt) {
         bf16* sa = sm + stage * STAGE;
         bf16* sb = sa + A_ELEMS;
@@ -291,19 +326,22 @@ __global__ void __launch_bounds__(128) conv_wgrad_kernel(const bf16* __restrict_
             cp_async16(smem_addr(sa + row * BM + ((c ^ swz<CPA>(row)) << 3)), p, ok);
         }
 #pragma unroll
-        for (int i = 0; i < BK * CPB / 128; ++i) {
-            int q = tid + i * 128, row = q / CPB, c = q % CPB;
-            long long v = vb + row;
-            int n = nt0 + c * 8;
-            long long src = -1;
-            if (v < kend && n < ntot) {
-                int t = n / cin;
-                long long r = v % vvol;
-                int xx = (int)(r % g.w), yy = (int)((r / g.w) % g.h), zz = (int)(r / ((long long)g.w * g.h));
-                src = tap_voxel(g, v, zz, yy, xx, t, taps);
+        for (int i = 0; i < B_IT; ++i) {
+            int row = tid / CPB + i * (128 / CPB);
+            int zz = bz[i] + tz, yy = by[i] + ty, xx = bx[i] + tx;
+            bool ok = col_ok && bv[i] < kend && zz >= 0 && zz < g.d && yy >= 0 && yy < g.h && xx >= 0 && xx < g.w;
+            const bf16* p = ok ? x + (bv[i] + delta) * cin + ci : x;
+            cp_async16(smem_addr(sb + row * BN + ((bc ^ swz<CPB>(row)) << 3)), p, ok);
+            // next stage: BK voxels further on
+            bv[i] += BK;
+            bx[i] += BK;
+            while (bx[i] >= g.w) {
+                bx[i] -= g.w;
+                if (++by[i] >= g.h) {
+                    by[i] = 0;
+                    if (++bz[i] >= g.d) bz[i] = 0;
+                }
             }
-            const bf16* p = src >= 0 ? x + src * cin + (n % cin) : x;
-            cp_async16(smem_addr(sb + row * BN + ((c ^ swz<CPB>(row)) << 3)), p, src >= 0);
         }
     };
 
