@@ -29,7 +29,8 @@ _SRC_TYPES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "f
 _SAVEDET_CHARS = "dspmxvwi"      # detid, nscat, ppath, momentum, exit pos, exit dir, w0, iquv (src/mcx_utils.c)
 
 _SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "printnum", "maxvoidstep",
-                "maxjumpdebug", "gscatter", "srcnum", "srcid", "replaydet", "gpuid", "voidtime", "debuglevel"]
+                "maxjumpdebug", "gscatter", "srcnum", "srcid", "replaydet", "gpuid", "voidtime"]
+_DEBUG_CHARS = "RMPT"            # -D letters: RNG test, trajectories, progress, trajectories only (src/mcx_utils.c:159)
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "sradius", "minenergy", "unitinmm", "omega"]
 _SCALARS_CHAR = ["isreflect", "isref3", "isrefint", "isnormalized", "issrcfrom0", "autopilot", "issaveref",
                  "issaveexit", "ismomentum", "isspecular", "issave2pt", "issavedet", "isgpuinfo", "isrowmajor",
@@ -122,6 +123,13 @@ class PreparedConfig:
         for k in _SCALARS_INT:
             if k in cfg:
                 setattr(c, k, int(float(cfg[k])))
+        if "debuglevel" in cfg:
+            # pmcx takes the -D letters (mcx_parsedebugopt, src/mcx_utils.c:5333-5348); a number is the bit mask
+            d = cfg["debuglevel"]
+            if isinstance(d, str) and not d.strip().isdigit():
+                c.debuglevel = sum(1 << _DEBUG_CHARS.index(ch) for ch in set(d.upper()) if ch in _DEBUG_CHARS)
+            else:
+                c.debuglevel = int(d)
         for k in _SCALARS_FLOAT:
             if k in cfg:
                 setattr(c, k, float(cfg[k]))
@@ -309,6 +317,23 @@ def _take_seeds(pc: PreparedConfig):
     return seeds
 
 
+def _take_traj(pc: PreparedConfig):
+    """Trajectory records (-D M / T) as pmcx's `traj`: float32 [6, n], rows id (uint32 bits), x, y, z,
+    weight, source id."""
+    c = pc.c
+    ptr, n = c.exportdebugdata, int(c.debugdatalen)
+    traj = None
+    if ptr:
+        buf = (C.c_float * (6 * n)).from_address(ptr) if n else None
+        traj = np.frombuffer(buf, dtype=np.float32).copy().reshape((6, n), order="F") if n else np.zeros((6, 0), np.float32)
+        libc.free(C.c_void_p(ptr))
+        c.exportdebugdata = None
+        c.debugdatalen = 0
+    elif int(c.debuglevel) & 10:
+        traj = np.zeros((6, 0), np.float32)
+    return traj
+
+
 def _take_detected(pc: PreparedConfig):
     c = pc.c
     det_ptr = c.exportdetected
@@ -369,11 +394,14 @@ def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]
         libc.free(info)
         seeds = _take_seeds(pc)
         detp = _take_detected(pc)
+        traj = _take_traj(pc)
     st = abi.Stats()
     lib.mcxg_get_stats(C.byref(st))
     out = _result(pc, flux, maxgate, detp, st)
     if seeds is not None:
         out["seeds"] = seeds
+    if traj is not None:
+        out["traj"] = traj
     return out
 
 
@@ -399,7 +427,11 @@ def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[s
         for pc in pcs:
             _take_seeds(pc)
         dets = [_take_detected(pc) for pc in pcs]
+        trajs = [_take_traj(pc) for pc in pcs]
     out = [_result(pc, f, g, d, stats[i]) for i, (pc, (f, g), d) in enumerate(zip(pcs, fields, dets))]
+    for o, t in zip(out, trajs):
+        if t is not None:
+            o["traj"] = t
     return out, float(ms.value)
 
 

@@ -290,7 +290,7 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
-    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords;
+    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, traj, trajcount;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
     double kernel_ms = 0.0;
@@ -309,7 +309,7 @@ struct Session {
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
         pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
-        seeddata.release(); voxwords.release();
+        seeddata.release(); voxwords.release(); traj.release(); trajcount.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -465,6 +465,14 @@ struct Session {
         if (k.saveseed) {
             seeddata.alloc((size_t)k.maxdet * kSeedBytes, stream);
             k.seeddata = seeddata.as<unsigned long long>();
+        }
+        if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly)) {
+            // trajectory records (src/mcx_core.cu:3158-3160): maxjumpdebug x 6 floats
+            k.traj_max = cfg->maxjumpdebug;
+            traj.alloc((size_t)std::max(1u, k.traj_max) * kTrajRecLen * sizeof(float), stream);
+            trajcount.alloc(sizeof(unsigned), stream);
+            k.traj = traj.as<float>();
+            k.traj_count = trajcount.as<unsigned>();
         }
         energy.alloc(sizeof(double) * kNumEnergy, stream);
         counters.alloc(sizeof(unsigned long long) * kNumCounters, stream);
@@ -885,6 +893,27 @@ void append_detected(Config* cfg, Session& S) {
     }
 }
 
+// Trajectory records of the last launch appended to exportdebugdata (src/mcx_core.cu:3594-3614).
+void append_trajectory(Config* cfg, Session& S) {
+    if (!S.kp.traj) return;
+    unsigned rec = 0;
+    CK(cudaMemcpyAsync(&rec, S.trajcount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    if (rec > S.kp.traj_max && cfg->flog)
+        fprintf(cfg->flog, "WARNING: the saved trajectory positions are more than what your have specified (%u > %u), please use the --maxjumpdebug option to specify a greater number\n",
+                rec, S.kp.traj_max);
+    rec = std::min(rec, S.kp.traj_max);
+    if (rec) {
+        cfg->exportdebugdata = (float*)realloc(cfg->exportdebugdata,
+                                               ((size_t)cfg->debugdatalen + rec) * kTrajRecLen * sizeof(float));
+        if (!cfg->exportdebugdata) MCXG_RAISE(-4, "out of host memory for the trajectory records");
+        CK(cudaMemcpyAsync(cfg->exportdebugdata + (size_t)cfg->debugdatalen * kTrajRecLen, S.traj.p,
+                           (size_t)rec * kTrajRecLen * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        cfg->debugdatalen += rec;
+    }
+}
+
 // End of one gate window: statistics, energies, normalised field added to exportfield
 // (src/mcx_core.cu:3716-3770, 3823-3925).
 void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg_stats& total) {
@@ -1028,9 +1057,11 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
         S.reset();
         for (int it = 0; it < reps; it++) {
             if (S.savedet) CK(cudaMemsetAsync(S.detcount.p, 0, sizeof(unsigned), S.stream));
+            if (S.kp.traj) CK(cudaMemsetAsync(S.trajcount.p, 0, sizeof(unsigned), S.stream));
             S.run(run_index * nper, nper, seed);
             run_index++;
             append_detected(cfg, S);
+            append_trajectory(cfg, S);
         }
         finish_window(cfg, S, host_field, total);
     }
@@ -1063,6 +1094,7 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
         S[i]->set_window(cfg->tstart, cfg->tstart + cfg->tstep * S[i]->kp.maxgate);
         if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
         begin_outputs(cfg, *S[i]);
+        if (S[i]->kp.traj) CK(cudaMemsetAsync(S[i]->trajcount.p, 0, sizeof(unsigned), S[i]->stream));
     }
     for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
 
@@ -1120,6 +1152,7 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
             std::vector<float> host_field;
             mcxg_stats total{};
             append_detected(cfgs[i], *S[i]);
+            append_trajectory(cfgs[i], *S[i]);
             finish_window(cfgs[i], *S[i], host_field, total);
             total.kernel_ms = ms;
             if (stats) stats[i] = total;

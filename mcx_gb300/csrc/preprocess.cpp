@@ -175,6 +175,10 @@ void validate(Config* cfg) {
     if (len < FLT_EPSILON) MCXG_RAISE(-4, "source initial direction vector can not have a length of 0");
     const float inv = (float)(1.0 / len);
     cfg->srcdir.x *= inv; cfg->srcdir.y *= inv; cfg->srcdir.z *= inv;
+    if (cfg->debuglevel & kDebugMoveOnly) {     // trajectories only (src/mcx_utils.c:1539-1542)
+        cfg->issave2pt = 0;
+        cfg->issavedet = 0;
+    }
 
     int isbcdet = 0;
     for (int i = 0; i < 6; i++)

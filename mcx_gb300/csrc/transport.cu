@@ -507,6 +507,22 @@ __device__ __forceinline__ void field_add_small(const KParams& P, size_t addr, f
 }
 
 // Shared-memory carve-up of one CTA.
+// One trajectory record (savedebugdata, src/mcx_core.cu:427-442): photon id as uint bits, the
+// position in grid units, the weight and the source id (0: one source).  Records past traj_max
+// are counted but not written.
+__device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x, float y, float z, float w) {
+    const unsigned pos = atomicAdd(P.traj_count, 1u);
+    if (pos < P.traj_max) {
+        float* r = P.traj + (size_t)pos * 6;
+        r[0] = __uint_as_float(id);
+        r[1] = x;
+        r[2] = y;
+        r[3] = z;
+        r[4] = w;
+        r[5] = 0.f;
+    }
+}
+
 struct Smem {
     float4* prop;                 // medianum x (mua, mus, g, n)
     unsigned long long* pool;     // per warp: next, end of its photon-index pool
@@ -523,6 +539,7 @@ struct Smem {
     float* rtof;                  // per thread, replay: its time of flight
     float* rcos;                  // per thread, RF replay: cos and sin of omega x time of flight
     int* rbin;                    // per thread, replay: its field block (gate + detector offset), -1 none
+    unsigned* pid;                // per thread, trajectories: the photon's id
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
@@ -548,7 +565,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
         s.rtof = s.rw + blockDim.x;
         s.rcos = s.rtof + blockDim.x;                 // cos, then sin, blockDim.x each
         s.rbin = reinterpret_cast<int*>(s.rcos + 2 * blockDim.x);
-        end = reinterpret_cast<float*>(s.rbin + blockDim.x);
+        s.pid = reinterpret_cast<unsigned*>(s.rbin + blockDim.x);
+        end = reinterpret_cast<float*>(s.pid + blockDim.x);
     }
     s.tile = reinterpret_cast<unsigned*>(end);
     return s;
@@ -653,6 +671,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (left > 0u) {
                     S.left[tid] = left - 1u;
                     start = true;
+                    if (FULL && P.traj) S.pid[tid] += 1u;       // the stream's next photon
                 }
             }
             const unsigned want = __ballot_sync(kFull, !alive && !start);
@@ -714,11 +733,15 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                             r1 = ((unsigned long long)sw.z << 32) | sw.w;
                             S.left[tid] = cnt - 1u;
                             start = true;
+                            // MCX's id: the thread's first photon index plus its 1-based count
+                            if (FULL && P.traj)
+                                S.pid[tid] = (unsigned)mine * P.mcx_per + min((unsigned)mine, P.mcx_odd) + 1u;
                         }
                     } else {
                         seed_photon(P.seed, P.photon_offset + mine, r0, r1);
                         start = true;
                     }
+                    if (FULL && P.traj && (P.seed_mode != 1 || P.replay)) S.pid[tid] = (unsigned)(P.photon_offset + mine) + 1u;
                 }
             }
             if (FULL && start && P.saveseed) {      // state at launch (src/mcx_core.cu:1213-1215)
@@ -762,6 +785,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 pr = props_of<WORDS>(P, S.prop, (unsigned)med);
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 1681-1687
                 alive = true;
             }
             const unsigned attempted = __ballot_sync(kFull, start), ran = __ballot_sync(kFull, entered);
@@ -835,6 +859,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 nscat++;
                 rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                 c_scat++;
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 2068-2074
             } else {
                 nscat = 0;
             }
@@ -1011,6 +1036,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != prn.w)) {
+                    if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 2435-2441
                     float Rtotal = 1.f;
                     const float a2 = n1 * n1, b2 = prn.w * prn.w;
                     const float va = (axis == 0) ? vx : ((axis == 1) ? vy : vz);
@@ -1066,6 +1092,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
+            if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);         // 1116-1122
             bool detected = false;
             if (SAVEDET && (detflag & kDET_MASK) && med == 0) {
                 const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
@@ -1202,7 +1229,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 5 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 6 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1219,7 +1246,7 @@ bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 
 int transport_mode(const KParams& p) {
     if (media_words(p.mediaformat)) return 3;
-    if (p.replay || p.saveseed || p.outputtype > kOutEnergy) return 2;
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 

@@ -39,6 +39,10 @@ __host__ __device__ constexpr bool src_is_point(int t) {
 // Indices into the device FP64 energy array.
 enum Energy : int { kELaunch = 0, kEEscape, kEDetect, kEAbsDep, kEAbsOther, kNumEnergy };
 // Bits of the device error word.
+// debuglevel bits (src/mcx_const.h:67-70) and the trajectory record length (MCX_DEBUG_REC_LEN, :82)
+enum DebugBits : unsigned { kDebugRNG = 1u, kDebugMove = 2u, kDebugProgress = 4u, kDebugMoveOnly = 8u };
+constexpr unsigned kTrajRecLen = 6;
+
 enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow = 4u, kErrIndex = 8u };
 
 // Everything one transport launch needs.  Passed as a __grid_constant__ kernel parameter, so
@@ -80,6 +84,12 @@ struct KParams {
     int src_focus;                  // kFocus*: what srcdir.w asks of the area sources
     const float* srcpattern;        // pattern (param1.w x param2.w) or pattern3d intensities
     int isspecular, voidtime;
+
+    // --- photon trajectories, MCX's -D M (savedebugdata, src/mcx_core.cu:427-442; records at launch
+    //     1681-1687, scattering 2068-2074, mismatched faces 2435-2441, termination 1116-1122)
+    float* traj;                    // traj_max x 6 floats: id (uint bits), x, y, z, weight, source id; null: off
+    unsigned* traj_count;           // records written (may exceed traj_max; the rest is dropped)
+    unsigned traj_max;
 
     // --- seed saving and photon replay (src/mcx_core.cu:375-377, 1203-1215, 2018-2066, 2207-2226)
     int saveseed;                   // store each detected photon's generator state at launch

@@ -139,6 +139,8 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
         session_keys["MaxDetPhoton"] = int(cfg["maxdetphoton"])
     if cfg.get("issaveseed"):
         session_keys["DoSaveSeed"] = 1
+    if cfg.get("debuglevel"):
+        session_keys["DebugFlag"] = str(cfg["debuglevel"])       # -D letters, e.g. "M" for trajectories
     out = {
         "Session": session_keys,
         "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0, "LengthUnit": 1,
@@ -199,6 +201,12 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
         ng = max(1, int((cfg["tend"] - cfg["tstart"]) / cfg["tstep"] + 0.5))
         f = np.fromfile(tmp / f"{session}.mc2", dtype=np.float32)
         res["flux"] = f.reshape(vol.shape + (ng,), order="F")
+    mct = tmp / f"{session}.mct"
+    if mct.exists():
+        # trajectory records after a History header (src/mcx_utils.c:982-1017): 6 floats each
+        raw = mct.read_bytes()
+        n = struct.unpack("<4s7If1I", raw[:40])[7]
+        res["traj"] = np.frombuffer(raw[64:64 + 24 * n], dtype=np.float32).reshape((6, n), order="F").copy()
     mch = tmp / f"{session}.mch"
     if mch.exists():
         raw = mch.read_bytes()

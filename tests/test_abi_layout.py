@@ -184,3 +184,16 @@ def test_pack_media_layouts():
     assert f == 2 and w.dtype == np.uint32
     with pytest.raises(Exception):
         pack_media(np.ones((3, 3, 3, 3), np.float32))
+
+
+def test_debug_flags_and_trajectory_only(engine):
+    """-D letters as pmcx parses them (src/mcx_utils.c:5333-5348); -D T turns the fluence and
+    detector outputs off as mcx_preprocess does (src/mcx_utils.c:1539-1542)."""
+    from mcx_gb300 import problems
+
+    for flag, bits in (("M", 2), ("mp", 6), ("T", 8), ("RMPT", 15), (2, 2), ("10", 10)):
+        pc = engine.prepare(problems.cube60(100) | {"debuglevel": flag})
+        assert pc.c.debuglevel == bits, (flag, pc.c.debuglevel)
+    pc = engine.prepare(problems.cube60(100) | {"debuglevel": "T", "issavedet": 1,
+                                                  "detpos": np.array([[29, 34, 0, 2]], np.float32)})
+    assert pc.c.issave2pt == b"\x00" and pc.c.issavedet == b"\x00"
