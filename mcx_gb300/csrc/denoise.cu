@@ -257,6 +257,149 @@ __global__ void __launch_bounds__(32 * WARPS_M * WARPS_N) conv_fwd_kernel(
 }
 
 // ---------------------------------------------------------------------------------------------
+// 3x3x3 convolution over a halo tile, for narrow outputs (BN = 16 or 32 channels): the CTA's 128
+// output voxels are a 2 x 8 x 8 (z, y, x) block; for each 16-channel slice of the input it loads
+// the 4 x 10 x 10 halo around that block once, and the slice's weights for all 27 taps, and forms
+// every tap's A fragments by ldmatrix addressing into the halo (the 8 rows of one 8 x 8 matrix
+// are 8 consecutive x of one line, i.e. 8 consecutive halo voxels).  The input is read once per
+// tile instead of once per tap.  Halo and weight rows are 32 bytes (16 channels), their two
+// 16-byte chunks swapped on every other group of 4 rows so the 8 rows of an ldmatrix phase fall
+// in 8 different bank groups.
+template <int BN>
+__global__ void __launch_bounds__(128) conv3_halo_kernel(const bf16* __restrict__ x, const bf16* __restrict__ wt,
+                                                         const float* __restrict__ bias,
+                                                         const bf16* __restrict__ mask, bf16* __restrict__ y, Geo g,
+                                                         int cin, int cout, int relu, int tiles_x, int tiles_y,
+                                                         int tiles_z) {
+    constexpr int TZ = 2, TY = 8, TX = 8, BM = TZ * TY * TX;
+    constexpr int HZ = TZ + 2, HY = TY + 2, HX = TX + 2, HV = HZ * HY * HX;   // 400 halo voxels
+    constexpr int WARPS_M = 4, WM = BM / WARPS_M, MI = WM / 16, NI = BN / 8;
+    static_assert(NI % 2 == 0 && MI == 2, "tile shape");
+    constexpr int ROWB = 32;                     // bytes per halo / weight row (16 channels)
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    unsigned char* sh = dyn_smem;                // [HV][32 B]
+    unsigned char* sw = dyn_smem + HV * ROWB;    // [27][BN][32 B]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm0 = warp * WM;
+    int tile = blockIdx.x;
+    const int txi = tile % tiles_x;
+    tile /= tiles_x;
+    const int tyi = tile % tiles_y;
+    tile /= tiles_y;
+    const int tzi = tile % tiles_z;
+    const int n = tile / tiles_z;
+    const int x0 = txi * TX, y0 = tyi * TY, z0 = tzi * TZ;
+    const int n0 = blockIdx.y * BN;
+    const long long vol0 = (long long)n * g.d * g.h * g.w;
+
+    // halo-voxel index of this lane's A rows (tap offset added per tap)
+    int hbase[MI];
+#pragma unroll
+    for (int i = 0; i < MI; ++i) {
+        int r = wm0 + i * 16 + (lane & 15);
+        int tx = r & 7, ty = (r >> 3) & 7, tz = r >> 6;
+        hbase[i] = ((tz + 1) * HY + (ty + 1)) * HX + (tx + 1);
+    }
+    const int achunk = lane >> 4;                // A: lanes 16-31 read the second 8 channels
+
+    float acc[MI][NI][4];
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+
+    const int slices = cin / 16;
+    for (int sl = 0; sl < slices; ++sl) {
+        const int c0 = sl * 16;
+        // halo: HV rows x 2 chunks, zero outside the volume
+        for (int q = tid; q < HV * 2; q += 128) {
+            int hv = q >> 1, c = q & 1;
+            int hx = hv % HX, hy = (hv / HX) % HY, hz = hv / (HX * HY);
+            int zz = z0 + hz - 1, yy = y0 + hy - 1, xx = x0 + hx - 1;
+            bool ok = zz >= 0 && zz < g.d && yy >= 0 && yy < g.h && xx >= 0 && xx < g.w;
+            const bf16* p = ok ? x + (vol0 + ((long long)zz * g.h + yy) * g.w + xx) * cin + c0 + c * 8 : x;
+            cp_async16(smem_addr(sh + hv * ROWB + ((c ^ ((hv >> 2) & 1)) << 4)), p, ok);
+        }
+        // weights of this slice for all taps: row (t, co), 16 channels
+        for (int q = tid; q < 27 * BN * 2; q += 128) {
+            int row = q >> 1, c = q & 1;
+            int t = row / BN, co = row - t * BN;
+            const bf16* p = wt + ((long long)(n0 + co) * 27 + t) * cin + c0 + c * 8;
+            cp_async16(smem_addr(sw + row * ROWB + ((c ^ ((row >> 2) & 1)) << 4)), p, true);
+        }
+        cp_commit();
+        cp_wait<0>();
+        __syncthreads();
+#pragma unroll 3
+        for (int t = 0; t < 27; ++t) {
+            const int off = (t / 9 - 1) * (HY * HX) + ((t / 3) % 3 - 1) * HX + (t % 3 - 1);
+            uint32_t af[MI][4];
+#pragma unroll
+            for (int i = 0; i < MI; ++i) {
+                int hv = hbase[i] + off;
+                ldsm_x4(smem_addr(sh + hv * ROWB + ((achunk ^ ((hv >> 2) & 1)) << 4)), af[i]);
+            }
+#pragma unroll
+            for (int jj = 0; jj < NI / 2; ++jj) {
+                uint32_t bfr[4];
+                int row = t * BN + jj * 16 + (lane & 7) + ((lane >> 4) << 3);
+                int c = (lane >> 3) & 1;
+                ldsm_x4(smem_addr(sw + row * ROWB + ((c ^ ((row >> 2) & 1)) << 4)), bfr);
+#pragma unroll
+                for (int i = 0; i < MI; ++i) {
+                    mma_bf16(acc[i][2 * jj], af[i], bfr[0], bfr[1]);
+                    mma_bf16(acc[i][2 * jj + 1], af[i], bfr[2], bfr[3]);
+                }
+            }
+        }
+        __syncthreads();                 // the next slice overwrites the halo and the weights
+    }
+
+    // epilogue: bias + ReLU into a padded shared tile, then 16-byte rows to global (times the mask)
+    constexpr int EP = BN + 8;
+    bf16* se = reinterpret_cast<bf16*>(dyn_smem);
+#pragma unroll
+    for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NI; ++j) {
+            int row = wm0 + i * 16 + (lane >> 2), col = j * 8 + (lane & 3) * 2;
+            float b0 = bias ? bias[n0 + col] : 0.f, b1 = bias ? bias[n0 + col + 1] : 0.f;
+            float v0 = acc[i][j][0] + b0, v1 = acc[i][j][1] + b1, v2 = acc[i][j][2] + b0, v3 = acc[i][j][3] + b1;
+            if (relu) {
+                v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f);
+            }
+            *reinterpret_cast<__nv_bfloat162*>(se + row * EP + col) = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162*>(se + (row + 8) * EP + col) = __floats2bfloat162_rn(v2, v3);
+        }
+    __syncthreads();
+    constexpr int CH = BN / 8;
+    for (int q = tid; q < BM * CH; q += 128) {
+        int r = q / CH, c = q % CH;
+        int xx = x0 + (r & 7), yy = y0 + ((r >> 3) & 7), zz = z0 + (r >> 6);
+        if (xx >= g.w || yy >= g.h || zz >= g.d) continue;
+        long long v = vol0 + ((long long)zz * g.h + yy) * g.w + xx;
+        uint4 val = *reinterpret_cast<const uint4*>(se + r * EP + c * 8);
+        long long o = v * cout + n0 + c * 8;
+        if (mask) {
+            uint4 mk = *reinterpret_cast<const uint4*>(mask + o);
+            uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
+            const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
+                uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
+                                ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
+                pv[e] &= keep;
+            }
+        }
+        *reinterpret_cast<uint4*>(y + o) = val;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // Weight gradient: dW[co, n] += sum_v dY[v, co] * X[v + off(t), ci], n = t*Cin + ci, over the
 // voxel slice [blockIdx.y*kslice, +kslice).  BM = Cout (the whole output-channel range), BN = 64
 // columns of (tap, ci); 128 threads; K staged 32 voxels at a time.
@@ -745,8 +888,33 @@ int conv_fwd_launch(const bf16* x, const bf16* w, const float* bias, const bf16*
 // Tile per output width: 128 voxels x (128 | 64 | 32 | 16) channels; narrow outputs take deeper
 // K stages and fewer, taller warp tiles (two 16-row fragments per warp) so that each B fragment
 // feeds more MMAs.
+template <int BN>
+int conv3_halo_launch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
+                      int cout, int relu, cudaStream_t st) {
+    constexpr int smem_in = 400 * 32 + 27 * BN * 32;
+    constexpr int smem_epi = 128 * (BN + 8) * 2;
+    constexpr int smem = smem_in > smem_epi ? smem_in : smem_epi;
+    auto kern = conv3_halo_kernel<BN>;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    const int tx = (g.w + 7) / 8, ty = (g.h + 7) / 8, tz = (g.d + 1) / 2;
+    const long long tiles = (long long)g.nvol * tx * ty * tz;
+    if (tiles >= (1LL << 31)) return fail("conv: too many tiles");
+    kern<<<dim3((unsigned)tiles, (unsigned)(cout / BN)), 128, smem, st>>>(x, w, bias, mask, y, g, cin, cout, relu, tx, ty,
+                                                                          tz);
+    return launched();
+}
+
 int conv_fwd_dispatch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
                       int cout, int taps, int relu, cudaStream_t st) {
+    // narrow 3x3x3 layers: halo tiles (each input voxel loaded once per tile, not once per tap)
+    if (taps == 27 && cin % 16 == 0 && cout % 32 == 0 && cout / 32 <= 3 && cout % 64 != 0)
+        return conv3_halo_launch<32>(x, w, bias, mask, y, g, cin, cout, relu, st);
+    if (taps == 27 && cin % 16 == 0 && cout % 32 != 0)
+        return conv3_halo_launch<16>(x, w, bias, mask, y, g, cin, cout, relu, st);
     if (cout % 128 == 0) return conv_fwd_launch<128, 128, 32, 2, 4, 4>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
     if (cout % 64 == 0) return conv_fwd_launch<128, 64, 32, 4, 2, 4>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
     if (cout % 32 == 0) return conv_fwd_launch<128, 32, 64, 4, 1, 3>(x, w, bias, mask, y, g, cin, cout, taps, relu, st);
