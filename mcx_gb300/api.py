@@ -78,6 +78,8 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
       float   (nx, ny, nz)        mua per voxel, MEDIA_MUA_FLOAT (101): float bits of mua x unitinmm,
                                   0 -> FLT_EPSILON (not void), NaN -> 0 (void)
       float   (2, nx, ny, nz)     mua, mus per voxel, MEDIA_AS_F2H (100): two binary16 halves
+      float   (3, nx, ny, nz)     value, field (0-3: mua, mus, g, n) and label per voxel,
+                                  MEDIA_LABEL_HALF (99): the label's properties with one field replaced
       uint8   (4, nx, ny, nz)     interpolation bytes for mua, mus, g, n, MEDIA_ASGN_BYTE (103)
       uint16  (2, nx, ny, nz)     interpolation shorts for mua, mus, MEDIA_AS_SHORT (104)"""
     v = np.asarray(vol)
@@ -95,6 +97,16 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
         w = _f2h_mcx(mua) | (_f2h_mcx(mus) << 16)
         w[np.isnan(mua) | np.isnan(mus)] = 0
         return np.asfortranarray(w.astype(np.uint32)), 100
+    if v.ndim == 4 and v.dtype.kind == "f" and v.shape[0] == 3:
+        # src/pmcx.cpp:266-300: [binary16 value][2-bit field | 14-bit label]; fields 1 and 2 are
+        # scaled by unitinmm as pmcx scales them
+        val, fld, lab = (v[k].astype(np.float32) for k in range(3))
+        if (fld < 0).any() or (fld >= 4).any() or (lab < 0).any():
+            raise MCXError(-4, "the 2nd volume must have an integer value between 0 and 3")
+        val = np.where((fld >= 1) & (fld <= 2), val * np.float32(unitinmm), val).astype(np.float32)
+        lo = ((fld.astype(np.uint8).astype(np.uint32) & 3) << 14) | (lab.astype(np.uint32) & 0xFFFF)
+        w = (lo & 0xFFFF) | (_f2h_mcx(val).astype(np.uint32) << 16)
+        return np.asfortranarray(w.astype(np.uint32)), 99
     if v.ndim == 4 and v.dtype == np.uint8 and v.shape[0] == 4:
         b = v.astype(np.uint32)
         return np.asfortranarray(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24)), 103

@@ -836,11 +836,18 @@ void check_config(const Config* cfg) {
     if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
-        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 100-104");
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 99-104");
     if ((cfg->mediabyte == kMediaAsF2H || cfg->mediabyte == kMediaMuaFloat || cfg->mediabyte == kMediaAsHalf) && cfg->medianum < 2)
         MCXG_RAISE(-4, "the per-voxel media format needs the 2nd row of prop for the properties it does not store");
     if ((cfg->mediabyte == kMediaAsgnByte || cfg->mediabyte == kMediaAsShort) && cfg->medianum < 3)
         MCXG_RAISE(-4, "the interpolating media formats need prop rows 2 and 3 as their end points");
+    if (cfg->mediabyte == kMediaLabelHalf && cfg->vol) {
+        // the word's 14-bit label indexes the property table
+        const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        for (size_t i = 0; i < nv; i++)
+            if ((cfg->vol[i] & 0x3FFFu) >= cfg->medianum)
+                MCXG_RAISE(-6, "a MEDIA_LABEL_HALF voxel's label exceeds the number of media");
+    }
     if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
     check_source(cfg);
 }

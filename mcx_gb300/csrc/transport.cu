@@ -168,12 +168,23 @@ __device__ __forceinline__ float half_bits(unsigned h) { return __half2float(__u
 
 // Optical properties (mua, mus, g, n) of a voxel's medium value m (src/mcx_core.cu:582-730):
 // the table row for labels; decoded from the word for the per-voxel formats, whose missing
-// fields come from table rows 1 and 2.  A void or outside voxel (m = 0) takes row 0 in every
+// fields come from table rows 1 and 2 (MEDIA_LABEL_HALF: from the row of the word's label).  A void or outside voxel (m = 0) takes row 0 in every
 // format; MCX decodes it like any word, which for MEDIA_ASGN_BYTE gives the outside row 2's n
 // and mus, so photons there scatter outside the volume.
 template <bool WORDS>
 __device__ __forceinline__ float4 props_of(const KParams& P, const float4* tab, unsigned m) {
     if (!WORDS || m == 0u) return tab[m];     // void and outside: row 1 of prop, as for labels
+    if (P.mediaformat == kMediaLabelHalf) {
+        // [half value][2-bit field | 14-bit label]: the label's row with one field replaced
+        float4 r = tab[m & 0x3FFFu];
+        const float v = fabsf(half_bits(m >> 16));
+        const unsigned f = (m >> 14) & 3u;
+        if (f == 0u) r.x = v;
+        else if (f == 1u) r.y = v;
+        else if (f == 2u) r.z = v;
+        else r.w = v;
+        return r;
+    }
     const float4 r1 = tab[1];
     const float n = r1.w;
     if (P.mediaformat == kMediaMuaFloat) return make_float4(__uint_as_float(m), r1.y, r1.z, n);

@@ -21,9 +21,10 @@ enum SrcType : int {
 };
 // Per-voxel media formats (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730 does).
 enum MediaFormat : int {
-    kMediaAsF2H = 100, kMediaMuaFloat = 101, kMediaAsHalf = 102, kMediaAsgnByte = 103, kMediaAsShort = 104
+    kMediaLabelHalf = 99, kMediaAsF2H = 100, kMediaMuaFloat = 101, kMediaAsHalf = 102, kMediaAsgnByte = 103,
+    kMediaAsShort = 104
 };
-__host__ __device__ constexpr bool media_words(int f) { return f >= kMediaAsF2H && f <= kMediaAsShort; }
+__host__ __device__ constexpr bool media_words(int f) { return f >= kMediaLabelHalf && f <= kMediaAsShort; }
 
 // Launch-direction options of area sources, from srcdir.w (src/mcx_core.cu:1672-1710): 0 =
 // along srcdir, a finite value = focal length, NaN = isotropic, -inf = Lambertian.

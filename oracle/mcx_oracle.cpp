@@ -108,6 +108,16 @@ struct Ctx {
     Prop prop_of(uint32_t m) const {
         const int f = P->mediaformat;
         if (f <= 4 || m == 0) return prop[m];
+        if (f == 99) {      // src/mcx_core.cu:597-613: the label's row with one field replaced
+            Prop r = prop[m & 0x3FFF];
+            const float v = std::fabs(half_to_float(m >> 16));
+            const uint32_t fld = (m >> 14) & 3;
+            if (fld == 0) r.mua = v;
+            else if (fld == 1) r.mus = v;
+            else if (fld == 2) r.g = v;
+            else r.n = v;
+            return r;
+        }
         const Prop r1 = prop[1];
         const float n = r1.n;
         if (f == 101) {

@@ -182,8 +182,19 @@ def test_pack_media_layouts():
     assert w[0, 0, 1] == np.array(0.5, np.float32).view(np.uint32) and w[0, 0, 2] == 0  # scaled; NaN void
     w, f = pack_media(np.ones((3, 3, 3), np.uint16))
     assert f == 2 and w.dtype == np.uint32
+    lh = np.zeros((3, 1, 1, 2), np.float32)
+    lh[:, 0, 0, 0] = [0.25, 1, 5]           # mus of label 5 replaced by 0.25 (x unitinmm)
+    lh[:, 0, 0, 1] = [1.5, 3, 2]            # n of label 2 replaced by 1.5
+    w, f = pack_media(lh, unitinmm=2.0)
+    assert f == 99
+    assert w[0, 0, 0] == (0x3800 << 16) | (1 << 14) | 5     # binary16 0.5 = 0x3800
+    assert w[0, 0, 1] == (0x3E00 << 16) | (3 << 14) | 2     # binary16 1.5 = 0x3E00
     with pytest.raises(Exception):
-        pack_media(np.ones((3, 3, 3, 3), np.float32))
+        pack_media(np.ones((5, 3, 3, 3), np.float32))
+    bad = np.ones((3, 2, 2, 2), np.float32)
+    bad[1] = 4
+    with pytest.raises(Exception):
+        pack_media(bad)
 
 
 def test_debug_flags_and_trajectory_only(engine):

@@ -1,8 +1,9 @@
 """Per-voxel media formats (src/mcx_core.cu:582-730) on the GPU.
 
 MCX's 32-bit voxel words encode the properties of every voxel: mua as a float (MEDIA_MUA_FLOAT),
-mua and mus as binary16 (MEDIA_AS_F2H), or interpolation fractions between prop rows 2 and 3
-(MEDIA_ASGN_BYTE, MEDIA_AS_SHORT); the fields a format does not store come from row 2.  Checked:
+mua and mus as binary16 (MEDIA_AS_F2H), interpolation fractions between prop rows 2 and 3
+(MEDIA_ASGN_BYTE, MEDIA_AS_SHORT), or a label with one property replaced by a binary16 value
+(MEDIA_LABEL_HALF); the fields a format does not store come from row 2 (the label's row).  Checked:
 a label volume rewritten per voxel gives the label run's result; each format against the oracle's
 decode (absorbed fraction, launched weight, detected count within 5 standard errors); detectors
 keep only format-independent record columns.
@@ -39,6 +40,12 @@ def deck(fmt: str, n: int, nphoton: int) -> dict:
         cfg["vol"] = np.stack([(255 * k / n), (255 * i / n), (255 * j / n), (127 * (k > n / 2))]).astype(np.uint8)
     elif fmt == "as_short":
         cfg["vol"] = np.stack([(65535 * k / n), (32767 * i / n)]).astype(np.uint16)
+    elif fmt == "label_half":
+        # labels 1 / 2 by x; deeper than n/2 the mus of the label is replaced by 4, elsewhere its g by 0.5
+        lab = np.where(i < n / 2, 1.0, 2.0)
+        fld = np.where(k > n / 2, 1.0, 2.0)
+        val = np.where(k > n / 2, 4.0, 0.5)
+        cfg["vol"] = np.stack([val, fld, lab]).astype(np.float32)
     return cfg
 
 
@@ -55,7 +62,27 @@ def test_label_volume_rewritten_per_voxel(engine):
     assert abs(a["n_steps"] - b["n_steps"]) <= 1e-4 * a["n_steps"]
 
 
-@pytest.mark.parametrize("fmt,code", [("mua_float", 101), ("f2h", 100), ("asgn_byte", 103), ("as_short", 104)])
+def test_label_half_equals_label_volume(engine):
+    """MEDIA_LABEL_HALF (src/mcx_core.cu:597-613): a cube of label 1 whose inclusion voxels replace
+    mua by 0.0625 (exact in binary16) runs as the label volume with that inclusion as label 2."""
+    base = problems.cube60(1_000_000)
+    base.update(issavedet=0, seed=99)
+    base.pop("detpos")
+    inc = np.zeros((60, 60, 60), bool)
+    inc[20:40, 20:40, 5:25] = True
+    prop = np.vstack([np.asarray(base["prop"], np.float32), np.asarray(base["prop"], np.float32)[1:2]])
+    prop[2, 0] = 0.0625
+    a = engine.run(dict(base, vol=np.where(inc, 2, 1).astype(np.uint8), prop=prop))["stat"]
+    # inside: field 0 (mua) := 0.0625; outside: field 1 (mus) := 1.0, label 1's own value (exact in binary16)
+    vol = np.stack([np.where(inc, 0.0625, 1.0), np.where(inc, 0.0, 1.0), np.ones((60, 60, 60))]).astype(np.float32)
+    b = engine.run(dict(base, vol=vol))["stat"]
+    assert b["error_flags"] == 0
+    assert abs(a["energyabs"] / a["energytot"] - b["energyabs"] / b["energytot"]) < 1e-4
+    assert abs(a["n_steps"] - b["n_steps"]) <= 1e-4 * a["n_steps"]
+
+
+@pytest.mark.parametrize("fmt,code", [("mua_float", 101), ("f2h", 100), ("asgn_byte", 103), ("as_short", 104),
+                                      ("label_half", 99)])
 def test_media_format_matches_oracle(engine, oracle, fmt, code):
     ng, no = 1_000_000, 200_000
     g = engine.run(deck(fmt, 40, ng))
