@@ -80,8 +80,14 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
       float   (2, nx, ny, nz)     mua, mus per voxel, MEDIA_AS_F2H (100): two binary16 halves
       float   (3, nx, ny, nz)     value, field (0-3: mua, mus, g, n) and label per voxel,
                                   MEDIA_LABEL_HALF (99): the label's properties with one field replaced
+      float   (4, nx, ny, nz)     mua, mus, g, n per voxel, MEDIA_ASGN_F2H (96): four binary16 halves in
+                                  two words per voxel (the second words follow all the first ones)
       uint8   (4, nx, ny, nz)     interpolation bytes for mua, mus, g, n, MEDIA_ASGN_BYTE (103)
-      uint16  (2, nx, ny, nz)     interpolation shorts for mua, mus, MEDIA_AS_SHORT (104)"""
+      [u]int16 (2, nx, ny, nz)    interpolation shorts for mua, mus, MEDIA_AS_SHORT (104)
+      [u]int16 (3, nx, ny, nz)    label 0, label 1 and the fraction (0-32767) of label 1 per voxel,
+                                  MEDIA_2LABEL_MIX (98)
+
+    The words come back as an (nx, ny, nz) array, or (nx, ny, nz, 2) for MEDIA_ASGN_F2H."""
     v = np.asarray(vol)
     if v.ndim == 3 and v.dtype.kind in "iub":
         return np.asfortranarray(v.astype(np.uint32, copy=False)), {1: 1, 2: 2, 4: 4, 8: 4}[v.dtype.itemsize]
@@ -107,6 +113,24 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
         lo = ((fld.astype(np.uint8).astype(np.uint32) & 3) << 14) | (lab.astype(np.uint32) & 0xFFFF)
         w = (lo & 0xFFFF) | (_f2h_mcx(val).astype(np.uint32) << 16)
         return np.asfortranarray(w.astype(np.uint32)), 99
+    if v.ndim == 4 and v.dtype.kind == "f" and v.shape[0] == 4:
+        # src/pmcx.cpp:305-336: [mus][mua] halves (x unitinmm), then [n][g]; NaN mua / mus is void
+        mua = (v[0].astype(np.float32) * np.float32(unitinmm)).astype(np.float32)
+        mus = (v[1].astype(np.float32) * np.float32(unitinmm)).astype(np.float32)
+        w0 = (_f2h_mcx(mua) | (_f2h_mcx(mus) << 16)).astype(np.uint32)
+        w1 = (_f2h_mcx(v[2].astype(np.float32)) | (_f2h_mcx(v[3].astype(np.float32)) << 16)).astype(np.uint32)
+        void = np.isnan(mua) | np.isnan(mus)
+        w0[void] = 0
+        w1[void] = 0
+        return np.asfortranarray(np.stack([w0, w1], axis=-1)), 96
+    if v.ndim == 4 and v.dtype in (np.int16, np.uint16) and v.shape[0] == 3:
+        # src/pmcx.cpp:156-170: [15-bit fraction of label 1][label 1][label 0]
+        b = v.astype(np.int64)
+        w = (b[0] & 0xFF) | ((b[1] & 0xFF) << 8) | ((b[2] & 0x7FFF) << 16)
+        return np.asfortranarray(w.astype(np.uint32)), 98
+    if v.ndim == 4 and v.dtype == np.int16 and v.shape[0] == 2:
+        b = v.astype(np.uint16).astype(np.uint32)
+        return np.asfortranarray(b[0] | (b[1] << 16)), 104
     if v.ndim == 4 and v.dtype == np.uint8 and v.shape[0] == 4:
         b = v.astype(np.uint32)
         return np.asfortranarray(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24)), 103
@@ -194,7 +218,7 @@ class PreparedConfig:
         vol = np.asarray(cfg["vol"])
         words, mediabyte = pack_media(vol, float(cfg.get("unitinmm", 1.0)))
         vol32 = words.ravel(order="F").copy()
-        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in words.shape)
+        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in words.shape[:3])
         c.mediabyte = mediabyte
         self.vol = vol32
         c.vol = vol32.ctypes.data

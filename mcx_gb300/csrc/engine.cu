@@ -114,6 +114,28 @@ struct DevBuf {
 
 float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 
+// IEEE 754 binary16 bits to float (normals, subnormals, zero)
+float half_to_float(uint32_t h) {
+    const uint32_t sign = (h >> 15) & 1u, e = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+    const float v = e ? std::ldexp((float)(man | 0x400u), (int)e - 25) : std::ldexp((float)man, -24);
+    return sign ? -v : v;
+}
+
+// Refractive index of voxel `id` as the kernel decodes it (props_of in transport.cu)
+float host_n(const Config* cfg, long id) {
+    const uint32_t w = cfg->vol[id] & kMED_MASK;
+    const int f = (int)cfg->mediabyte;
+    if (!media_words(f) || w == 0) return cfg->prop[w].n;
+    if (f == kMediaLabelHalf) return ((w >> 14) & 3u) == 3u ? std::fabs(half_to_float(w >> 16)) : cfg->prop[w & 0x3FFFu].n;
+    if (f == kMedia2LabelMix) return cfg->prop[w & 0xFFu].n;     // the first tissue's, as the kernel's void search
+    if (f == kMediaAsgnF2H) {
+        const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        return std::fabs(half_to_float(cfg->vol[nv + id] >> 16));
+    }
+    if (f == kMediaAsgnByte) return (w >> 24) * (1.f / 127.f) * (cfg->prop[2].n - cfg->prop[1].n) + cfg->prop[1].n;
+    return cfg->prop[1].n;
+}
+
 }  // namespace
 
 // Void skipping of a pencil source launched outside the volume or in a 0 voxel
@@ -152,10 +174,10 @@ int host_skipvoid(const Config* cfg, float4& p, float3& v, float& t, int fd[3]) 
             if (!inside(f)) return -1;
             t = cfg->voidtime ? t : 0.f;
             const long id = index(f);
-            const Medium& np = cfg->prop[cfg->vol[id] & kMED_MASK];
-            if (cfg->isspecular && axis >= 0 && np.n != cfg->prop[0].n) {
+            const float n2 = host_n(cfg, id);
+            if (cfg->isspecular && axis >= 0 && n2 != cfg->prop[0].n) {
                 // specular loss at the entry face (reflectcoeff, src/mcx_core.cu:552-570) and refraction
-                const float n1 = cfg->prop[0].n, n2 = np.n;
+                const float n1 = cfg->prop[0].n;
                 const float vv[3] = {v.x, v.y, v.z};
                 const float Icos = std::fabs(vv[axis]);
                 const float a = n1 * n1, b = n2 * n2;
@@ -290,7 +312,7 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
-    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, traj, trajcount;
+    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
     double kernel_ms = 0.0;
@@ -309,7 +331,7 @@ struct Session {
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
         pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
-        seeddata.release(); voxwords.release(); traj.release(); trajcount.release();
+        seeddata.release(); voxwords.release(); voxwords2.release(); traj.release(); trajcount.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -365,6 +387,10 @@ struct Session {
             voxwords.alloc(nvox * sizeof(uint32_t), stream);
             err.alloc(sizeof(unsigned), stream);
             CK(cudaMemcpyAsync(voxwords.p, cfg->vol, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+            if (cfg->mediabyte == kMediaAsgnF2H) {      // the second word of every voxel follows the first nvox
+                voxwords2.alloc(nvox * sizeof(uint32_t), stream);
+                CK(cudaMemcpyAsync(voxwords2.p, cfg->vol + nvox, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+            }
         } else {
             DevBuf vol32;
             vol32.alloc(nvox * sizeof(uint32_t), stream);
@@ -383,6 +409,7 @@ struct Session {
         std::memset(&k, 0, sizeof(k));
         k.mediaformat = cfg->mediabyte;
         k.words = voxwords.as<uint32_t>();
+        k.words2 = voxwords2.as<uint32_t>();
         k.nx = (int)cfg->dim.x; k.ny = (int)cfg->dim.y; k.nz = (int)cfg->dim.z;
         k.dimxy = cfg->dim.x * cfg->dim.y;
         k.nvox = (unsigned)nvox;
@@ -836,11 +863,18 @@ void check_config(const Config* cfg) {
     if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
-        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 99-104");
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96 and 98-104");
     if ((cfg->mediabyte == kMediaAsF2H || cfg->mediabyte == kMediaMuaFloat || cfg->mediabyte == kMediaAsHalf) && cfg->medianum < 2)
         MCXG_RAISE(-4, "the per-voxel media format needs the 2nd row of prop for the properties it does not store");
     if ((cfg->mediabyte == kMediaAsgnByte || cfg->mediabyte == kMediaAsShort) && cfg->medianum < 3)
         MCXG_RAISE(-4, "the interpolating media formats need prop rows 2 and 3 as their end points");
+    if (cfg->mediabyte == kMedia2LabelMix && cfg->vol) {
+        // both tissue labels of every word index the property table
+        const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        for (size_t i = 0; i < nv; i++)
+            if ((cfg->vol[i] & 0xFFu) >= cfg->medianum || ((cfg->vol[i] >> 8) & 0xFFu) >= cfg->medianum)
+                MCXG_RAISE(-6, "a MEDIA_2LABEL_MIX voxel's label exceeds the number of media");
+    }
     if (cfg->mediabyte == kMediaLabelHalf && cfg->vol) {
         // the word's 14-bit label indexes the property table
         const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;

@@ -190,7 +190,7 @@ void validate(Config* cfg) {
     if (cfg->medianum == 0) MCXG_RAISE(-4, "you must define the 'prop' field in the input structure");
     if (cfg->dim.x == 0 || cfg->dim.y == 0 || cfg->dim.z == 0) MCXG_RAISE(-4, "the 'vol' field in the input structure can not be empty");
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
-        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 99-104");
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96 and 98-104");
     check_source(cfg);
 
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) cfg->unitinmm = cfg->steps.x;
@@ -256,9 +256,9 @@ void validate(Config* cfg) {
     if (cfg->issavedet && cfg->savedetflag == 0) cfg->savedetflag = 0x5;
     // per-voxel media have no labels: no per-medium record columns (src/mcx_utils.c:1801-1806)
     // per-voxel formats carry no per-medium slots (src/mcx_utils.c:1801-1803, mediabyte >= 100); for
-    // MEDIA_LABEL_HALF MCX keeps the flags and indexes the slots by the whole voxel word, past the
-    // end of the record, so the engine clears them there too
-    if (cfg->mediabyte >= kMediaLabelHalf && cfg->savedetflag) cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u | 0x80u);
+    // mediabyte 96, 98 and 99 MCX keeps the flags and indexes the slots by the voxel word, past the
+    // end of the record, so the engine clears them for every non-label format
+    if (cfg->mediabyte > 4 && cfg->savedetflag) cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u | 0x80u);
     if (cfg->issaveref) MCXG_RAISE(-6, "diffuse-reflectance output (issaveref) is not supported by the GB300 engine");
 
     // history header bookkeeping done at the end of mcx_validatecfg (src/mcx_utils.c:3853-3857)

@@ -166,14 +166,36 @@ __device__ __forceinline__ bool voxel_det(unsigned v) { return WORDS ? (v >> 31)
 
 __device__ __forceinline__ float half_bits(unsigned h) { return __half2float(__ushort_as_half((unsigned short)h)); }
 
+// MEDIA_2LABEL_MIX (src/mcx_core.cu:649-666): a voxel word [fraction (15 bits)][label 1][label 0]
+// is tissue 1 with probability fraction / 32767, else tissue 0, drawn once when the photon enters
+// the voxel (MCX draws at its first step there and keeps the choice for the voxel).  Returns the
+// word with the chosen label in place and the detector bit kept; other formats pass through.
+template <bool WORDS>
+__device__ __forceinline__ unsigned voxel_pick(const KParams& P, unsigned lab, unsigned long long& r0,
+                                               unsigned long long& r1) {
+    if (!WORDS || P.mediaformat != kMedia2LabelMix) return lab;
+    const unsigned frac = (lab >> 16) & 0x7FFFu;
+    unsigned c = lab & 0xFFu;
+    if (frac > 0u && rng_next(r0, r1) * 32767.f < (float)frac) c = (lab >> 8) & 0xFFu;
+    return (lab & kDET_MASK) | c;
+}
+
 // Optical properties (mua, mus, g, n) of a voxel's medium value m (src/mcx_core.cu:582-730):
 // the table row for labels; decoded from the word for the per-voxel formats, whose missing
-// fields come from table rows 1 and 2 (MEDIA_LABEL_HALF: from the row of the word's label).  A void or outside voxel (m = 0) takes row 0 in every
+// fields come from table rows 1 and 2 (MEDIA_LABEL_HALF: from the row of the word's label;
+// MEDIA_ASGN_F2H stores all four, two in a second word per voxel).  `idx` is the voxel's index.  A void or outside voxel (m = 0) takes row 0 in every
 // format; MCX decodes it like any word, which for MEDIA_ASGN_BYTE gives the outside row 2's n
 // and mus, so photons there scatter outside the volume.
 template <bool WORDS>
-__device__ __forceinline__ float4 props_of(const KParams& P, const float4* tab, unsigned m) {
+__device__ __forceinline__ float4 props_of(const KParams& P, const float4* tab, unsigned m, unsigned idx) {
     if (!WORDS || m == 0u) return tab[m];     // void and outside: row 1 of prop, as for labels
+    if (P.mediaformat == kMedia2LabelMix) return tab[m & 0xFFu];     // resolved to one label (voxel_pick)
+    if (P.mediaformat == kMediaAsgnF2H) {
+        // [n][g] halves in the voxel's second word, [mus][mua] in the first (src/mcx_core.cu:628-647)
+        const unsigned m2 = __ldg(P.words2 + idx);
+        return make_float4(fabsf(half_bits(m & 0xFFFFu)), fabsf(half_bits(m >> 16)), fabsf(half_bits(m2 & 0xFFFFu)),
+                           fabsf(half_bits(m2 >> 16)));
+    }
     if (P.mediaformat == kMediaLabelHalf) {
         // [half value][2-bit field | 14-bit label]: the label's row with one field replaced
         float4 r = tab[m & 0x3FFFu];
@@ -239,7 +261,8 @@ __device__ int skip_void(const KParams& P, Launch& L) {
             if (!in_grid(P, fx, fy, fz)) return -1;
             if (!P.voidtime) L.t = 0.f;
             const unsigned lab = at(fx, fy, fz);
-            const float n2 = props_of<WORDS>(P, P.prop, voxel_med<WORDS>(lab)).w, n0 = P.prop[0].w;
+            const unsigned eidx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
+            const float n2 = props_of<WORDS>(P, P.prop, voxel_med<WORDS>(lab), eidx).w, n0 = P.prop[0].w;
             if (P.isspecular && axis >= 0 && n2 != n0) {
                 L.w *= 1.f - reflect_coeff(L.vx, L.vy, L.vz, n0, n2, axis);
                 if (L.w > kEPS) transmit(L.vx, L.vy, L.vz, n0, n2, axis);
@@ -767,8 +790,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 vx = P.src_v.x; vy = P.src_v.y; vz = P.src_v.z;
                 t = P.src_t * inv_c0;
                 idx = P.src_idx;
-                med = (int)voxel_med<WORDS>(P.src_label);
-                det = voxel_det<WORDS>(P.src_label);
+                const unsigned lab = voxel_pick<WORDS>(P, P.src_label, r0, r1);
+                med = (int)voxel_med<WORDS>(lab);
+                det = voxel_det<WORDS>(lab);
                 fx = (float)P.src_fx; fy = (float)P.src_fy; fz = (float)P.src_fz;
                 entered = true;
             } else if (AREA && start) {
@@ -779,8 +803,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     vx = L.vx; vy = L.vy; vz = L.vz;
                     t = L.t;
                     idx = L.idx;
-                    med = (int)voxel_med<WORDS>(L.label);
-                    det = voxel_det<WORDS>(L.label);
+                    const unsigned lab = voxel_pick<WORDS>(P, L.label, r0, r1);
+                    med = (int)voxel_med<WORDS>(lab);
+                    det = voxel_det<WORDS>(lab);
                     fx = (float)L.ix; fy = (float)L.iy; fz = (float)L.iz;
                 }
             }
@@ -793,7 +818,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (SAVEDET) S.nscat0[tid] = 0;
                 w0 = w; eabs = 0.f;
                 S.step0[tid] = c_step;
-                pr = props_of<WORDS>(P, S.prop, (unsigned)med);
+                pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
                 if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 1681-1687
@@ -877,7 +902,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
 
         const float n1 = pr.w;
-        pr = props_of<WORDS>(P, S.prop, (unsigned)med);
+        pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
 
         // distance to the nearest voxel face (hitgrid, src/mcx_core.cu:493-507)
         const float hx = fabsf((fx + (vx > 0.f ? 1.f : 0.f) - px) * rvx);
@@ -933,7 +958,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 }
             }
             if (inside) {
-                const unsigned lab = voxel_load<WORDS>(P, idx);
+                const unsigned lab = voxel_pick<WORDS>(P, voxel_load<WORDS>(P, idx), r0, r1);
                 med = (int)voxel_med<WORDS>(lab);
                 det = voxel_det<WORDS>(lab);
             } else {
@@ -1020,7 +1045,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             else { pz = nextafter_mcx(roundf(pz + shift), (vz > 0.f) - (vz < 0.f), P.maxvoidstep); fz = floorf(pz); }
             if (fx >= 0.f && fx < fnx && fy >= 0.f && fy < fny && fz >= 0.f && fz < fnz) {
                 idx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
-                const unsigned lab = voxel_load<WORDS>(P, idx);
+                const unsigned lab = voxel_pick<WORDS>(P, voxel_load<WORDS>(P, idx), r0, r1);
                 med = (int)voxel_med<WORDS>(lab);
                 det = voxel_det<WORDS>(lab);
                 carry = det;
@@ -1042,7 +1067,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             }
             // Fresnel reflection / refraction on crossing (2381-2503)
             if (REFLECT && !kill && !stay) {
-                const float4 prn = props_of<WORDS>(P, S.prop, (unsigned)med);
+                const float4 prn = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
                 pr = prn;
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
@@ -1086,13 +1111,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         }
                         rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                         idx = idxold;
-                        const unsigned lab = voxel_load<WORDS>(P, idx);
+                        const unsigned lab = voxel_pick<WORDS>(P, voxel_load<WORDS>(P, idx), r0, r1);
                         med = (int)voxel_med<WORDS>(lab);
                         det = voxel_det<WORDS>(lab);     // carry keeps the bounced-off value
-                        pr = props_of<WORDS>(P, S.prop, (unsigned)med);
+                        pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
                     }
                 } else {
-                    pr = props_of<WORDS>(P, S.prop, (unsigned)medold);
+                    pr = props_of<WORDS>(P, S.prop, (unsigned)medold, idxold);
                 }
             }
         }

@@ -105,9 +105,15 @@ struct Ctx {
     // starts from row 1 and never overwrites them), n from row 1 (src/mcx_core.cu:614-695).  A
     // void or outside voxel (m = 0) takes row 0 in every format, unlike MCX's decode of a zero
     // MEDIA_ASGN_BYTE word (the engine's rule, restated here).
-    Prop prop_of(uint32_t m) const {
+    Prop prop_of(uint32_t m, uint32_t idx) const {
         const int f = P->mediaformat;
         if (f <= 4 || m == 0) return prop[m];
+        if (f == 98) return prop[m & 0xFF];        // a mixed voxel resolved to one label (pick)
+        if (f == 96) {      // src/mcx_core.cu:628-647: [mus][mua] halves, [n][g] in the second word
+            const uint32_t m2 = P->vol[(size_t)dimxy * nz + idx];
+            return {std::fabs(half_to_float(m & 0xFFFF)), std::fabs(half_to_float(m >> 16)),
+                    std::fabs(half_to_float(m2 & 0xFFFF)), std::fabs(half_to_float(m2 >> 16))};
+        }
         if (f == 99) {      // src/mcx_core.cu:597-613: the label's row with one field replaced
             Prop r = prop[m & 0x3FFF];
             const float v = std::fabs(half_to_float(m >> 16));
@@ -132,6 +138,18 @@ struct Ctx {
                     ((m >> 16) & 0xFF) * (1.f / 255.f) * (r2.g - r1.g) + r1.g, (m >> 24) * (1.f / 127.f) * (r2.n - r1.n) + r1.n};
         return {(m & 0xFFFF) * (1.f / 65535.f) * (r2.mua - r1.mua) + r1.mua, (m >> 16) * (1.f / 65535.f) * (r2.mus - r1.mus) + r1.mus,
                 r1.g, n};
+    }
+
+    // MEDIA_2LABEL_MIX (src/mcx_core.cu:649-666): a word [15-bit fraction][label 1][label 0] is
+    // label 1 with probability fraction / 32767, else label 0, drawn when the photon enters the
+    // voxel; the detector bit is kept.  Other formats pass through.
+    template <class R>
+    uint32_t pick(uint32_t w, R& rng) const {
+        if (P->mediaformat != 98) return w;
+        const uint32_t frac = (w >> 16) & 0x7FFF;
+        uint32_t c = w & 0xFF;
+        if (frac > 0 && rng.next() * 32767.f < (float)frac) c = (w >> 8) & 0xFF;
+        return (w & kDET_MASK) | c;
     }
 
     // IEEE 754 binary16 bits to float (normals, subnormals, zero; the formats store no inf/NaN)
@@ -264,7 +282,7 @@ int skipvoid(const Ctx& C, Photon& ph) {
                     if (count++ > 3) break;
                 }
                 ph.t = P->voidtime ? ph.t : 0.f;
-                const Prop np = C.prop_of(P->vol[id] & kMED_MASK);
+                const Prop np = C.prop_of(P->vol[id] & kMED_MASK, (uint32_t)id);
                 if (P->isspecular && np.n != C.prop[0].n) {
                     ph.w *= 1.f - reflectcoeff(ph.v, C.prop[0].n, np.n, fd[3]);
                     if (ph.w > kEPS) transmit(ph.v, C.prop[0].n, np.n, fd[3]);
@@ -564,7 +582,8 @@ struct Runner {
             attempts += 1.f;
             if (attempts > (float)P->maxvoidstep) return false;
         } while ((ph.mediaid & kMED_MASK) == 0 || std::fabs(ph.w) <= P->minenergy);
-        ph.prop = C.prop_of(ph.mediaid & kMED_MASK);
+        ph.mediaid = C.pick(ph.mediaid, rng);
+        ph.prop = C.prop_of(ph.mediaid & kMED_MASK, ph.idx1d);
         T.e_launch += ph.w;
         T.launches++;
         ph.w0 = ph.w;
@@ -633,7 +652,7 @@ struct Runner {
             }
 
             float n1 = ph.prop.n;
-            ph.prop = C.prop_of(ph.mediaid);
+            ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
 
             float len = hitgrid(ph.p, ph.v, ph.rv, ph.fd);
             float musp = ph.prop.mus * ((ph.nscat + 1.f > (float)P->gscatter) ? (1.f - ph.prop.g) : 1.f);
@@ -662,7 +681,7 @@ struct Runner {
                 ph.idx1d = (ph.fd[0] < 0 || ph.fd[1] < 0 || ph.fd[2] < 0) ? kOUT_MIN : kOUT_MAX;
                 isdet = (uint8_t)P->bc[(ph.idx1d == kOUT_MAX) * 3 + ph.fd[3]];
             } else {
-                uint32_t m = P->vol[ph.idx1d];
+                uint32_t m = C.pick(P->vol[ph.idx1d], rng);
                 isdet = m & kDET_MASK;
                 ph.mediaid = m & kMED_MASK;
             }
@@ -707,7 +726,7 @@ struct Runner {
                     ph.fd[a] = (short)std::floor(pp[a]);
                     if (inside(C, ph.fd)) {
                         ph.idx1d = vidx(C, ph.fd);
-                        uint32_t m = P->vol[ph.idx1d];
+                        uint32_t m = C.pick(P->vol[ph.idx1d], rng);
                         ph.isdet = (int)(m & kDET_MASK);
                         ph.mediaid = m & kMED_MASK;
                         continue;
@@ -734,7 +753,7 @@ struct Runner {
             }
 
             if (C.isreflect) {
-                ph.prop = C.prop_of(med);
+                ph.prop = C.prop_of(med, ph.idx1d);
                 if (((med && P->isreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P->isreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != ph.prop.n)) {
@@ -768,11 +787,11 @@ struct Runner {
                         ph.p[a] = nextafter_mcx(std::nearbyint(ph.p[a]), (ph.v[a] > 0.f) - (ph.v[a] < 0.f), (float)P->maxvoidstep);
                         ph.fd[a] = (short)std::floor(ph.p[a]);
                         ph.idx1d = idx1dold;
-                        ph.mediaid = P->vol[ph.idx1d] & kMED_MASK;
-                        ph.prop = C.prop_of(ph.mediaid);
+                        ph.mediaid = C.pick(P->vol[ph.idx1d], rng) & kMED_MASK;
+                        ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
                     }
                 } else {
-                    ph.prop = C.prop_of(mediaidold & kMED_MASK);
+                    ph.prop = C.prop_of(mediaidold & kMED_MASK, idx1dold);
                 }
             }
         }

@@ -189,6 +189,21 @@ def test_pack_media_layouts():
     assert f == 99
     assert w[0, 0, 0] == (0x3800 << 16) | (1 << 14) | 5     # binary16 0.5 = 0x3800
     assert w[0, 0, 1] == (0x3E00 << 16) | (3 << 14) | 2     # binary16 1.5 = 0x3E00
+    a4 = np.zeros((4, 1, 1, 2), np.float32)
+    a4[:, 0, 0, 0] = [0.25, 2.0, 0.5, 1.5]
+    a4[:, 0, 0, 1] = [np.nan, 1.0, 0.5, 1.5]
+    w, f = pack_media(a4)
+    assert f == 96 and w.shape == (1, 1, 2, 2)
+    assert w[0, 0, 0, 0] == (0x4000 << 16) | 0x3400 and w[0, 0, 0, 1] == (0x3E00 << 16) | 0x3800   # halves
+    assert w[0, 0, 1, 0] == 0 and w[0, 0, 1, 1] == 0                                          # NaN: void
+    mx = np.zeros((3, 1, 1, 1), np.int16)
+    mx[:, 0, 0, 0] = [3, 7, 16384]
+    w, f = pack_media(mx)
+    assert f == 98 and w[0, 0, 0] == (16384 << 16) | (7 << 8) | 3
+    sh = np.zeros((2, 1, 1, 1), np.int16)
+    sh[:, 0, 0, 0] = [-1, 5]
+    w, f = pack_media(sh)
+    assert f == 104 and w[0, 0, 0] == (5 << 16) | 0xFFFF
     with pytest.raises(Exception):
         pack_media(np.ones((5, 3, 3, 3), np.float32))
     bad = np.ones((3, 2, 2, 2), np.float32)
