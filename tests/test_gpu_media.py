@@ -78,12 +78,11 @@ def test_label_half_equals_label_volume(engine):
     base.pop("detpos")
     inc = np.zeros((60, 60, 60), bool)
     inc[20:40, 20:40, 5:25] = True
-    prop = np.vstack([np.asarray(base["prop"], np.float32), np.asarray(base["prop"], np.float32)[1:2]])
-    prop[2, 0] = 0.0625
+    prop = np.array([[0, 0, 1, 1], [0.005, 1.0, 0.01, 1.37], [0.0625, 1.0, 0.01, 1.37]], np.float32)
     a = engine.run(dict(base, vol=np.where(inc, 2, 1).astype(np.uint8), prop=prop))["stat"]
     # inside: field 0 (mua) := 0.0625; outside: field 1 (mus) := 1.0, label 1's own value (exact in binary16)
     vol = np.stack([np.where(inc, 0.0625, 1.0), np.where(inc, 0.0, 1.0), np.ones((60, 60, 60))]).astype(np.float32)
-    b = engine.run(dict(base, vol=vol))["stat"]
+    b = engine.run(dict(base, vol=vol, prop=prop[:2]))["stat"]
     assert b["error_flags"] == 0
     assert abs(a["energyabs"] / a["energytot"] - b["energyabs"] / b["energytot"]) < 1e-4
     assert abs(a["n_steps"] - b["n_steps"]) <= 1e-4 * a["n_steps"]
