@@ -140,9 +140,9 @@ void mcxg_run_simulation_fp64(Config* cfg, GPUInfo* gpu);
  * (1..32), largest photon budget first; the block scheduler fills the SMs a finishing launch
  * frees with the CTAs of launches queued behind it.  Every Config receives exactly the outputs
  * mcx_run_simulation gives it (exportfield accumulated, exportdetected, energies, normaliser,
- * detected count); its `runtime` is the whole graph's time.  Each Config must run one repetition
- * (respin 1) with all its time gates on the device.  `stats` (count entries) and `graph_ms` may
- * be NULL.  Returns 0 or a negative MCX error id (message via mcxg_last_error). */
+ * detected count); its `runtime` is the whole batch's graph time.  Repetitions (respin) and gate
+ * groups run in waves, one graph per wave holding every Config's next (group, repetition).
+ * `stats` (count entries) and `graph_ms` may be NULL.  Returns 0 or a negative MCX error id (message via mcxg_last_error). */
 int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms);
 
 /* ---- Allocation-free transport ----------------------------------------------------------- */

@@ -445,7 +445,7 @@ def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[s
     """Run many independent simulations in one CUDA graph on one GPU (``mcxg_run_batch``).
 
     Returns the per-simulation results -- the same dicts ``run`` gives -- and the graph time in
-    ms.  Each input runs one repetition with all its time gates on the device."""
+    ms (all waves: repetitions and gate groups run as further graphs)."""
     pcs = [prepare(cfg) for cfg in cfgs]
     for pc in pcs:
         nact, info = _active_devices(pc.c)

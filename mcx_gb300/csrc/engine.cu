@@ -683,7 +683,9 @@ struct Session {
 
     // Queue a cleared-buffer launch over photons [offset, offset + n) on stream `s` without
     // waiting (the batch captures these into one graph).  MCX seeding words must be in place.
-    void enqueue(cudaStream_t s, uint64_t offset, uint64_t n, uint64_t seed) {
+    // One repetition enqueued on `s` (for graph capture).  `fresh` starts a gate window: field,
+    // energies and counters cleared; later repetitions of the window add to them.
+    void enqueue(cudaStream_t s, uint64_t offset, uint64_t n, uint64_t seed, bool fresh = true) {
         kp.photon_offset = offset;
         kp.nphoton = n;
         kp.seed = seed;
@@ -691,13 +693,16 @@ struct Session {
             kp.mcx_per = (unsigned)(n / mcx_streams);
             kp.mcx_odd = (unsigned)(n - (uint64_t)kp.mcx_per * mcx_streams);
         }
-        CK(cudaMemsetAsync(field.p, 0, field.bytes, s));
-        if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, s));
-        if (field64.p) CK(cudaMemsetAsync(field64.p, 0, field64.bytes, s));
+        if (fresh) {
+            CK(cudaMemsetAsync(field.p, 0, field.bytes, s));
+            if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, s));
+            if (field64.p) CK(cudaMemsetAsync(field64.p, 0, field64.bytes, s));
+            CK(cudaMemsetAsync(energy.p, 0, energy.bytes, s));
+            CK(cudaMemsetAsync(counters.p, 0, counters.bytes, s));
+            CK(cudaMemsetAsync(err.p, 0, err.bytes, s));
+        }
         if (detcount.p) CK(cudaMemsetAsync(detcount.p, 0, detcount.bytes, s));
-        CK(cudaMemsetAsync(energy.p, 0, energy.bytes, s));
-        CK(cudaMemsetAsync(counters.p, 0, counters.bytes, s));
-        CK(cudaMemsetAsync(err.p, 0, err.bytes, s));
+        if (trajcount.p) CK(cudaMemsetAsync(trajcount.p, 0, trajcount.bytes, s));
         CK(cudaMemsetAsync(work.p, 0, sizeof(unsigned long long), s));
         CK(launch_transport(kp, reflect, savedet, grid, block, smem, s));
         launches = 1;
@@ -1124,18 +1129,25 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
     nstreams = std::max(1, std::min(nstreams, 32));
     const int gpuid = cfgs[0]->deviceid[0] - 1;
     if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
+    // Each simulation runs |respin| repetitions in each of its gate groups, as mcx_run_simulation
+    // does; the batch runs them in waves, wave w holding every simulation's w-th (group,
+    // repetition), each wave one CUDA graph over all its simulations.
     std::vector<std::unique_ptr<Session>> S(count);
+    std::vector<int> reps(count), groups(count);
+    std::vector<uint64_t> nper(count);
+    std::vector<mcxg_stats> totals(count);
+    int waves = 0;
     for (int i = 0; i < count; i++) {
         Config* cfg = cfgs[i];
         check_config(cfg);
-        if (std::abs(cfg->respin) != 1) MCXG_RAISE(-6, "batched simulations run one repetition (respin 1) each");
         S[i] = std::make_unique<Session>();
         S[i]->create(cfg, gpuid, false);
-        if (S[i]->totalgates > S[i]->kp.maxgate) MCXG_RAISE(-6, "batched simulations must hold all their time gates on the device");
-        S[i]->set_window(cfg->tstart, cfg->tstart + cfg->tstep * S[i]->kp.maxgate);
-        if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
+        reps[i] = std::abs(cfg->respin);
+        groups[i] = (S[i]->totalgates + S[i]->kp.maxgate - 1) / S[i]->kp.maxgate;
+        nper[i] = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps[i];
+        waves = std::max(waves, reps[i] * groups[i]);
         begin_outputs(cfg, *S[i]);
-        if (S[i]->kp.traj) CK(cudaMemsetAsync(S[i]->trajcount.p, 0, sizeof(unsigned), S[i]->stream));
+        std::memset(&totals[i], 0, sizeof(mcxg_stats));
     }
     for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
 
@@ -1149,9 +1161,14 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
     cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    auto cleanup = [&]() {
+    auto drop_graph = [&]() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    };
+    auto cleanup = [&]() {
+        drop_graph();
         for (auto e : joins) if (e) cudaEventDestroy(e);
         for (auto x : st) if (x) cudaStreamDestroy(x);
         if (fork) cudaEventDestroy(fork);
@@ -1159,6 +1176,8 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
         if (t1) cudaEventDestroy(t1);
         if (origin) cudaStreamDestroy(origin);
     };
+    double total_ms = 0.0;
+    std::vector<float> host_field;
     try {
         CK(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
@@ -1168,36 +1187,56 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
             CK(cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&joins[k], cudaEventDisableTiming));
         }
-        CK(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
-        CK(cudaEventRecord(fork, origin));
-        for (int k = 0; k < nstreams; k++) CK(cudaStreamWaitEvent(st[k], fork, 0));
-        for (int j = 0; j < count; j++) {
-            Session& s = *S[order[j]];
-            const Config* cfg = cfgs[order[j]];
-            s.enqueue(st[j % nstreams], 0, (uint64_t)cfg->nphoton, (uint64_t)(uint32_t)cfg->seed);
+        for (int w = 0; w < waves; w++) {
+            // host-side set-up of this wave: gate window and MCX seed words per simulation
+            for (int i = 0; i < count; i++) {
+                if (w >= reps[i] * groups[i]) continue;
+                const Config* cfg = cfgs[i];
+                const int g = w / reps[i];
+                if (w % reps[i] == 0) {
+                    const float twin0 = cfg->tstart + cfg->tstep * g * S[i]->kp.maxgate;
+                    S[i]->set_window(twin0, twin0 + cfg->tstep * S[i]->kp.maxgate);
+                }
+                if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
+            }
+            for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
+            CK(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
+            CK(cudaEventRecord(fork, origin));
+            for (int k = 0; k < nstreams; k++) CK(cudaStreamWaitEvent(st[k], fork, 0));
+            int slot = 0;
+            for (int j = 0; j < count; j++) {
+                const int i = order[j];
+                if (w >= reps[i] * groups[i]) continue;
+                const Config* cfg = cfgs[i];
+                S[i]->enqueue(st[slot++ % nstreams], (uint64_t)w * nper[i], nper[i], (uint64_t)(uint32_t)cfg->seed,
+                              w % reps[i] == 0);
+            }
+            for (int k = 0; k < nstreams; k++) {
+                CK(cudaEventRecord(joins[k], st[k]));
+                CK(cudaStreamWaitEvent(origin, joins[k], 0));
+            }
+            CK(cudaStreamEndCapture(origin, &graph));
+            CK(cudaGraphInstantiate(&exec, graph, 0));
+            CK(cudaEventRecord(t0, origin));
+            CK(cudaGraphLaunch(exec, origin));
+            CK(cudaEventRecord(t1, origin));
+            CK(cudaEventSynchronize(t1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, t0, t1));
+            total_ms += ms;
+            drop_graph();
+            for (int i = 0; i < count; i++) {
+                if (w >= reps[i] * groups[i]) continue;
+                append_detected(cfgs[i], *S[i]);
+                append_trajectory(cfgs[i], *S[i]);
+                if (w % reps[i] == reps[i] - 1) finish_window(cfgs[i], *S[i], host_field, totals[i]);
+            }
         }
-        for (int k = 0; k < nstreams; k++) {
-            CK(cudaEventRecord(joins[k], st[k]));
-            CK(cudaStreamWaitEvent(origin, joins[k], 0));
-        }
-        CK(cudaStreamEndCapture(origin, &graph));
-        CK(cudaGraphInstantiate(&exec, graph, 0));
-        CK(cudaEventRecord(t0, origin));
-        CK(cudaGraphLaunch(exec, origin));
-        CK(cudaEventRecord(t1, origin));
-        CK(cudaEventSynchronize(t1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, t0, t1));
-        if (graph_ms) *graph_ms = ms;
+        if (graph_ms) *graph_ms = total_ms;
         for (int i = 0; i < count; i++) {
-            std::vector<float> host_field;
-            mcxg_stats total{};
-            append_detected(cfgs[i], *S[i]);
-            append_trajectory(cfgs[i], *S[i]);
-            finish_window(cfgs[i], *S[i], host_field, total);
-            total.kernel_ms = ms;
-            if (stats) stats[i] = total;
-            end_outputs(cfgs[i], *S[i], ms, 1);
+            totals[i].kernel_ms = total_ms;
+            if (stats) stats[i] = totals[i];
+            end_outputs(cfgs[i], *S[i], total_ms, reps[i]);
         }
     } catch (...) {
         cudaStreamEndCapture(origin, &graph);      // leaves capture mode if an error came mid-capture

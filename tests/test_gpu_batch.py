@@ -3,6 +3,7 @@
 Photons are seeded by (seed, photon index), so a simulation run inside the batch follows the same
 photon histories as the same Config run alone: counters and detected records are identical, the
 field differs only by FP32 summation order (the batch also uses the smallest deposit tile).
+Repetitions and gate groups run in waves of graphs, with the same photon ranges as a single run.
 """
 
 from __future__ import annotations
@@ -62,8 +63,24 @@ def test_batch_energy_balance_and_normalisation(engine):
         assert abs(deposited - s["e_absdep"] / s["e_launch"]) <= 1e-3 * deposited
 
 
-def test_batch_rejects_repetitions(engine):
-    insts = _small_batch()[:2]
-    insts[1]["respin"] = 2
-    with pytest.raises(engine.MCXError, match="respin"):
-        engine.run_batch(insts)
+def test_batch_repetitions_and_gate_groups(engine):
+    """Repetitions (respin) and gate groups (maxgate below the gate count) run in waves of
+    graphs; each simulation gets what mcx_run_simulation gives it: the same photons (counters and
+    detected count identical), energies and the field accumulated over repetitions and groups."""
+    insts = _small_batch()[:4]
+    insts[1]["respin"] = 3
+    insts[2].update(tstep=1e-9, maxgate=2)          # 5 gates in groups of 2: 3 windows
+    insts[3].update(respin=-2, tstep=2.5e-9, maxgate=1)
+    res, ms = engine.run_batch([dict(c) for c in insts], streams=3)
+    assert ms > 0
+    for cfg, rb in zip(insts, res):
+        ra = engine.run(dict(cfg))
+        sa, sb = ra["stat"], rb["stat"]
+        assert sb["error_flags"] == 0
+        for key in ("n_steps", "n_scatter", "n_photon", "detected", "nphoton"):
+            assert sa[key] == sb[key], (key, sa[key], sb[key])
+        for key in ("energytot", "energyabs"):
+            assert abs(sa[key] - sb[key]) <= 1e-6 * max(1.0, sa[key]), key
+        fa, fb = ra["flux"], rb["flux"]
+        assert fa.shape == fb.shape
+        assert np.abs(fa - fb).max() <= 1e-4 * np.abs(fa).max() + 1e-12
