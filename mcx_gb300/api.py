@@ -83,11 +83,14 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
       float   (4, nx, ny, nz)     mua, mus, g, n per voxel, MEDIA_ASGN_F2H (96): four binary16 halves in
                                   two words per voxel (the second words follow all the first ones)
       uint8   (4, nx, ny, nz)     interpolation bytes for mua, mus, g, n, MEDIA_ASGN_BYTE (103)
+      uint8   (8, nx, ny, nz)     split voxels, MEDIA_2LABEL_SPLIT (97): lower label, upper label, plane
+                                  point x, y, z (0-255 across the voxel), plane normal x, y, z
+                                  (0-255 for -1..1); two words per voxel as mcx_preprocess lays them out
       [u]int16 (2, nx, ny, nz)    interpolation shorts for mua, mus, MEDIA_AS_SHORT (104)
       [u]int16 (3, nx, ny, nz)    label 0, label 1 and the fraction (0-32767) of label 1 per voxel,
                                   MEDIA_2LABEL_MIX (98)
 
-    The words come back as an (nx, ny, nz) array, or (nx, ny, nz, 2) for MEDIA_ASGN_F2H."""
+    The words come back as an (nx, ny, nz) array, or (nx, ny, nz, 2) for the two-word formats."""
     v = np.asarray(vol)
     if v.ndim == 3 and v.dtype.kind in "iub":
         return np.asfortranarray(v.astype(np.uint32, copy=False)), {1: 1, 2: 2, 4: 4, 8: 4}[v.dtype.itemsize]
@@ -131,6 +134,12 @@ def pack_media(vol: np.ndarray, unitinmm: float = 1.0) -> tuple[np.ndarray, int]
     if v.ndim == 4 and v.dtype == np.int16 and v.shape[0] == 2:
         b = v.astype(np.uint16).astype(np.uint32)
         return np.asfortranarray(b[0] | (b[1] << 16)), 104
+    if v.ndim == 4 and v.dtype == np.uint8 and v.shape[0] == 8:
+        # src/mcx_utils.c:1708-1731: [lower][upper][point x][point y], then [point z][normal x, y, z]
+        b = v.astype(np.uint32)
+        w0 = (b[0] << 24) | (b[1] << 16) | (b[2] << 8) | b[3]
+        w1 = (b[4] << 24) | (b[5] << 16) | (b[6] << 8) | b[7]
+        return np.asfortranarray(np.stack([w0, w1], axis=-1).astype(np.uint32)), 97
     if v.ndim == 4 and v.dtype == np.uint8 and v.shape[0] == 4:
         b = v.astype(np.uint32)
         return np.asfortranarray(b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24)), 103

@@ -121,11 +121,23 @@ float half_to_float(uint32_t h) {
     return sign ? -v : v;
 }
 
-// Refractive index of voxel `id` as the kernel decodes it (props_of in transport.cu)
-float host_n(const Config* cfg, long id) {
+// Refractive index of voxel `id` (at grid coordinates f[3]) for a photon at p, as the kernel
+// decodes it (props_of and split_voxel_at in transport.cu)
+float host_n(const Config* cfg, long id, const int f3[3], const float4& p) {
     const uint32_t w = cfg->vol[id] & kMED_MASK;
     const int f = (int)cfg->mediabyte;
     if (!media_words(f) || w == 0) return cfg->prop[w].n;
+    if (f == kMedia2LabelSplit) {
+        const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        const uint32_t wb = cfg->vol[nv + id];
+        const uint32_t lo = w >> 24, up = (w >> 16) & 0xFFu;
+        float nx = ((wb >> 16) & 0xFFu) * (2.f / 255.f) - 1.f, ny = ((wb >> 8) & 0xFFu) * (2.f / 255.f) - 1.f,
+              nz = (wb & 0xFFu) * (2.f / 255.f) - 1.f;
+        if (up == 0 || nx * nx + ny * ny + nz * nz <= 0.f) return cfg->prop[lo].n;
+        const float rx = ((w >> 8) & 0xFFu) * (1.f / 255.f) + f3[0], ry = (w & 0xFFu) * (1.f / 255.f) + f3[1],
+                    rz = (wb >> 24) * (1.f / 255.f) + f3[2];
+        return ((rx - p.x) * nx + (ry - p.y) * ny + (rz - p.z) * nz < 0.f) ? cfg->prop[up].n : cfg->prop[lo].n;
+    }
     if (f == kMediaLabelHalf) return ((w >> 14) & 3u) == 3u ? std::fabs(half_to_float(w >> 16)) : cfg->prop[w & 0x3FFFu].n;
     if (f == kMedia2LabelMix) return cfg->prop[w & 0xFFu].n;     // the first tissue's, as the kernel's void search
     if (f == kMediaAsgnF2H) {
@@ -174,7 +186,7 @@ int host_skipvoid(const Config* cfg, float4& p, float3& v, float& t, int fd[3]) 
             if (!inside(f)) return -1;
             t = cfg->voidtime ? t : 0.f;
             const long id = index(f);
-            const float n2 = host_n(cfg, id);
+            const float n2 = host_n(cfg, id, f, p);
             if (cfg->isspecular && axis >= 0 && n2 != cfg->prop[0].n) {
                 // specular loss at the entry face (reflectcoeff, src/mcx_core.cu:552-570) and refraction
                 const float n1 = cfg->prop[0].n;
@@ -387,7 +399,8 @@ struct Session {
             voxwords.alloc(nvox * sizeof(uint32_t), stream);
             err.alloc(sizeof(unsigned), stream);
             CK(cudaMemcpyAsync(voxwords.p, cfg->vol, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
-            if (cfg->mediabyte == kMediaAsgnF2H) {      // the second word of every voxel follows the first nvox
+            if (cfg->mediabyte == kMediaAsgnF2H || cfg->mediabyte == kMedia2LabelSplit) {
+                // the second word of every voxel follows the first nvox
                 voxwords2.alloc(nvox * sizeof(uint32_t), stream);
                 CK(cudaMemcpyAsync(voxwords2.p, cfg->vol + nvox, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
             }
@@ -868,11 +881,18 @@ void check_config(const Config* cfg) {
     if (ot < otFlux || ot > otWPTOF) MCXG_RAISE(-6, "unknown output type");
     if (cfg->respin == 0) MCXG_RAISE(-1, "respin number can not be 0, check your -r/--repeat input or cfg.respin value");
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
-        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96 and 98-104");
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96-104");
     if ((cfg->mediabyte == kMediaAsF2H || cfg->mediabyte == kMediaMuaFloat || cfg->mediabyte == kMediaAsHalf) && cfg->medianum < 2)
         MCXG_RAISE(-4, "the per-voxel media format needs the 2nd row of prop for the properties it does not store");
     if ((cfg->mediabyte == kMediaAsgnByte || cfg->mediabyte == kMediaAsShort) && cfg->medianum < 3)
         MCXG_RAISE(-4, "the interpolating media formats need prop rows 2 and 3 as their end points");
+    if (cfg->mediabyte == kMedia2LabelSplit && cfg->vol) {
+        // both labels of every split voxel index the property table
+        const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        for (size_t i = 0; i < nv; i++)
+            if (((cfg->vol[i] & kMED_MASK) >> 24) >= cfg->medianum || ((cfg->vol[i] >> 16) & 0xFFu) >= cfg->medianum)
+                MCXG_RAISE(-6, "a split voxel's label exceeds the number of media");
+    }
     if (cfg->mediabyte == kMedia2LabelMix && cfg->vol) {
         // both tissue labels of every word index the property table
         const size_t nv = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;

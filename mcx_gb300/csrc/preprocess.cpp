@@ -190,7 +190,7 @@ void validate(Config* cfg) {
     if (cfg->medianum == 0) MCXG_RAISE(-4, "you must define the 'prop' field in the input structure");
     if (cfg->dim.x == 0 || cfg->dim.y == 0 || cfg->dim.z == 0) MCXG_RAISE(-4, "the 'vol' field in the input structure can not be empty");
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
-        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96 and 98-104");
+        MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96-104");
     check_source(cfg);
 
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) cfg->unitinmm = cfg->steps.x;

@@ -190,6 +190,7 @@ template <bool WORDS>
 __device__ __forceinline__ float4 props_of(const KParams& P, const float4* tab, unsigned m, unsigned idx) {
     if (!WORDS || m == 0u) return tab[m];     // void and outside: row 1 of prop, as for labels
     if (P.mediaformat == kMedia2LabelMix) return tab[m & 0xFFu];     // resolved to one label (voxel_pick)
+    if (P.mediaformat == kMedia2LabelSplit) return tab[m >> 24];     // the lower label (split_voxel_at decides)
     if (P.mediaformat == kMediaAsgnF2H) {
         // [n][g] halves in the voxel's second word, [mus][mua] in the first (src/mcx_core.cu:628-647)
         const unsigned m2 = __ldg(P.words2 + idx);
@@ -228,6 +229,43 @@ __device__ __forceinline__ bool in_grid(const KParams& P, int x, int y, int z) {
     return (unsigned)x < (unsigned)P.nx && (unsigned)y < (unsigned)P.ny && (unsigned)z < (unsigned)P.nz;
 }
 
+// Split voxel (MEDIA_2LABEL_SPLIT, SVMC; updateproperty, src/mcx_core.cu:688-730).  Two words per
+// voxel: the first [lower label][upper label][plane point x][plane point y], the second [plane
+// point z][normal x][normal y][normal z], bytes scaled to [0, 1] (point, within the voxel) and
+// [-1, 1] (normal).  A voxel with upper label 0 is plain (its lower label); in a split one the
+// photon is in the upper tissue when it lies on the side the normal points away from, and the
+// stored normal then points to the other side (outward from the photon's tissue).
+struct SplitVoxel {
+    int lo, up;
+    bool split, isup;
+    float rx, ry, rz, nx, ny, nz;
+    __device__ __forceinline__ int tissue() const { return isup ? up : lo; }
+};
+
+__device__ __forceinline__ void split_voxel_at(const KParams& P, unsigned vidx, float fx, float fy, float fz, float px,
+                                               float py, float pz, SplitVoxel& sv) {
+    const unsigned wa = __ldg(P.words + vidx) & kMED_MASK, wb = __ldg(P.words2 + vidx);
+    sv.lo = (int)(wa >> 24);
+    sv.up = (int)((wa >> 16) & 0xFFu);
+    sv.isup = false;
+    float nx = ((wb >> 16) & 0xFFu) * (2.f / 255.f) - 1.f, ny = ((wb >> 8) & 0xFFu) * (2.f / 255.f) - 1.f,
+          nz = (wb & 0xFFu) * (2.f / 255.f) - 1.f;
+    const float nn = nx * nx + ny * ny + nz * nz;
+    sv.split = sv.up != 0 && nn > 0.f;
+    if (sv.split) {
+        sv.rx = ((wa >> 8) & 0xFFu) * (1.f / 255.f) + fx;
+        sv.ry = (wa & 0xFFu) * (1.f / 255.f) + fy;
+        sv.rz = (wb >> 24) * (1.f / 255.f) + fz;
+        const float inv = rsqrtf(nn);
+        nx *= inv; ny *= inv; nz *= inv;
+        if ((sv.rx - px) * nx + (sv.ry - py) * ny + (sv.rz - pz) * nz < 0.f) {
+            sv.isup = true;
+            nx = -nx; ny = -ny; nz = -nz;
+        }
+        sv.nx = nx; sv.ny = ny; sv.nz = nz;
+    }
+}
+
 // src/mcx_core.cu:866-956 (skipvoid): march a photon launched outside the volume or in a 0 voxel
 // in unit steps until it is inside a non-zero voxel, back up one step and find the exact entry
 // face with voxel-to-voxel steps; optional specular loss and refraction there.  Returns the
@@ -262,7 +300,13 @@ __device__ int skip_void(const KParams& P, Launch& L) {
             if (!P.voidtime) L.t = 0.f;
             const unsigned lab = at(fx, fy, fz);
             const unsigned eidx = (unsigned)fz * P.dimxy + (unsigned)fy * (unsigned)P.nx + (unsigned)fx;
-            const float n2 = props_of<WORDS>(P, P.prop, voxel_med<WORDS>(lab), eidx).w, n0 = P.prop[0].w;
+            float n2 = props_of<WORDS>(P, P.prop, voxel_med<WORDS>(lab), eidx).w;
+            if (P.mediaformat == kMedia2LabelSplit) {
+                SplitVoxel sv;
+                split_voxel_at(P, eidx, (float)fx, (float)fy, (float)fz, L.px, L.py, L.pz, sv);
+                n2 = P.prop[sv.tissue()].w;
+            }
+            const float n0 = P.prop[0].w;
             if (P.isspecular && axis >= 0 && n2 != n0) {
                 L.w *= 1.f - reflect_coeff(L.vx, L.vy, L.vz, n0, n2, axis);
                 if (L.w > kEPS) transmit(L.vx, L.vy, L.vz, n0, n2, axis);
@@ -628,7 +672,8 @@ template <bool REFLECT, bool SAVEDET, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_constant__ KParams P) {
     constexpr bool AREA = MODE >= 1;
     constexpr bool FULL = MODE >= 2;
-    constexpr bool WORDS = MODE == 3;
+    constexpr bool WORDS = MODE >= 3;
+    constexpr bool SVMC = MODE == 4;       // split voxels (MEDIA_2LABEL_SPLIT)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Smem S = carve<SAVEDET, FULL>(P, smem_raw);
     const int tid = threadIdx.x;
@@ -690,6 +735,8 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
     bool det = false, carry = false;
     int med = 0;
     float4 pr = make_float4(0.f, 0.f, 0.f, 1.f);
+    SplitVoxel sv{0, 0, false, false, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool sv_test = false;           // test the plane on the next flight (off right after crossing it)
     unsigned long long r0 = 0ull, r1 = 0ull;
     unsigned c_step = 0u, c_scat = 0u, c_dep = 0u;
     S.left[tid] = 0u;
@@ -819,6 +866,11 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 w0 = w; eabs = 0.f;
                 S.step0[tid] = c_step;
                 pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
+                if constexpr (SVMC) {           // src/mcx_core.cu:1246-1251, 1679
+                    split_voxel_at(P, idx, fx, fy, fz, px, py, pz, sv);
+                    pr = S.prop[sv.tissue()];
+                    sv_test = true;
+                }
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
                 if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 1681-1687
@@ -902,7 +954,8 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
 
         const float n1 = pr.w;
-        pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
+        if constexpr (SVMC) pr = S.prop[med ? sv.tissue() : 0];
+        else pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
 
         // distance to the nearest voxel face (hitgrid, src/mcx_core.cu:493-507)
         const float hx = fabsf((fx + (vx > 0.f ? 1.f : 0.f) - px) * rvx);
@@ -915,8 +968,23 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         const float musp = (nscat >= gscat) ? pr.y * (1.f - pr.z) : pr.y;
         const float sdist = dist * musp;
         const bool stay = !(sdist < pscat);                 // flight ends inside this voxel
-        const float slen = stay ? pscat : sdist;
-        const float len = stay ? __fdividef(pscat, musp) : dist;
+        float slen = stay ? pscat : sdist;
+        float len = stay ? __fdividef(pscat, musp) : dist;
+        bool hit = false;                                   // split voxel: the flight stops on its plane
+        if constexpr (SVMC) {
+            // ray_plane_intersect (src/mcx_core.cu:747-772)
+            const float vn = vx * sv.nx + vy * sv.ny + vz * sv.nz;
+            if (sv.split && sv_test && vn > 0.f) {
+                const float d0 = (px - sv.rx) * sv.nx + (py - sv.ry) * sv.ny + (pz - sv.rz) * sv.nz;
+                const float d1 = d0 + len * vn;
+                if (d0 * d1 <= 0.f) {
+                    const float l0 = len * __fdividef(d0, d0 - d1);
+                    if (l0 > 0.f) len = l0;
+                    slen = len * musp;
+                    hit = true;
+                }
+            }
+        }
 
         px = fmaf(len, vx, px);
         py = fmaf(len, vy, py);
@@ -938,9 +1006,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         const unsigned idxold = idx;
         const float ox = fx, oy = fy, oz = fz;
 
-        if (stay) {
+        if (stay && !hit) {
             carry = det;
-        } else {
+        } else if (hit) {
+            carry = det;                    // same voxel: the segment up to the plane is deposited below
+        }
+        if (!stay || hit) {
+          if (!hit) {
             // cross the face: only the crossed axis can leave the volume (2169-2186)
             float c, lim, sg;
             unsigned stride;
@@ -968,8 +1040,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 det = false;                // a boundary code, never the detector bit
             }
             carry = det;
+          }
 
-            // deposit into the voxel just left, time bin taken at exit (2191-2292)
+            // deposit into the voxel just left (or the split voxel's tissue just left), time bin
+            // taken at exit (2191-2292)
             bool rec = false;
             if (P.save2pt && t >= tw0 && t < tw1) {
                 int tshift = (P.maxgate > 1) ? min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b))) : 0;
@@ -1030,10 +1104,25 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             segp += pathlen;
             pathlen = 0.f;
 
+            if constexpr (SVMC) {
+                // a new voxel: its tissue at the photon's position; the plane: the other tissue
+                // (src/mcx_core.cu:2295-2303)
+                if (!hit) {
+                    if (inside && med) split_voxel_at(P, idx, fx, fy, fz, px, py, pz, sv);
+                    sv_test = true;
+                } else {
+                    sv.nx = -sv.nx; sv.ny = -sv.ny; sv.nz = -sv.nz;
+                    sv.isup = !sv.isup;
+                    sv_test = false;
+                }
+            }
+
             // leaving into a 0 voxel or the outside without reflection (2307-2354)
             if (med == 0 && ((!REFLECT || n1 == n0) || (bcf == BC_UNKNOWN && !P.doreflect) || bcf == BC_ABSORB ||
                              bcf == BC_CYCLIC) && bcf != BC_MIRROR)
                 kill = true;
+            // entering a split voxel's tissue 0 (its background) without reflection
+            if (SVMC && inside && med && !sv.isup && sv.lo == 0 && (!REFLECT || n1 == n0)) kill = true;
         }
         if (t > tw1) kill = true;
 
@@ -1049,6 +1138,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 med = (int)voxel_med<WORDS>(lab);
                 det = voxel_det<WORDS>(lab);
                 carry = det;
+                if constexpr (SVMC) {
+                    if (med) split_voxel_at(P, idx, fx, fy, fz, px, py, pz, sv);
+                    sv_test = true;
+                }
                 if (SAVEDET && !WORDS && med != medold) flush_segment(P, S, tid, B, medold, segp, nscat);
                 continue;
             }
@@ -1065,9 +1158,50 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     detflag = detold & kDET_MASK;
                 }
             }
+            // Fresnel reflection / refraction at the split voxel's plane (reflectray,
+            // src/mcx_core.cu:784-830, 2386-2404): the normal turned back to point along the flight
+            if (SVMC && REFLECT && !kill && hit) {
+                const float nlo = S.prop[sv.lo].w, nup = S.prop[sv.up].w;
+                if (nlo != nup) {
+                    sv.nx = -sv.nx; sv.ny = -sv.ny; sv.nz = -sv.nz;
+                    const float n2 = S.prop[sv.tissue()].w;           // the tissue entered
+                    const float ic = fabsf(vx * sv.nx + vy * sv.ny + vz * sv.nz);
+                    const float a2 = n1 * n1, b2 = n2 * n2;
+                    const float c2 = 1.f - __fdividef(a2, b2) * (1.f - ic * ic);
+                    bool refl = true;
+                    float ct = 0.f;
+                    if (c2 > 0.f) {
+                        ct = sqrtf(c2);
+                        float re = a2 * ic * ic + b2 * c2;
+                        const float im = 2.f * n1 * n2 * ic * ct;
+                        float R = __fdividef(re - im, re + im);
+                        re = b2 * ic * ic + a2 * c2;
+                        R = (R + __fdividef(re - im, re + im)) * 0.5f;
+                        refl = rng_next(r0, r1) <= R;
+                    }
+                    if (refl) {                     // back into the tissue it came from
+                        vx -= 2.f * ic * sv.nx; vy -= 2.f * ic * sv.ny; vz -= 2.f * ic * sv.nz;
+                        sv.isup = !sv.isup;
+                    } else {                        // refracted into the other tissue
+                        const float q = __fdividef(n1, n2);
+                        vx = ct * sv.nx + q * (vx - ic * sv.nx);
+                        vy = ct * sv.ny + q * (vy - ic * sv.ny);
+                        vz = ct * sv.nz + q * (vz - ic * sv.nz);
+                        sv.nx = -sv.nx; sv.ny = -sv.ny; sv.nz = -sv.nz;
+                        if (sv.tissue() == 0) {     // out into the background: the photon leaves
+                            kill = true;
+                            detflag = detold & kDET_MASK;
+                        }
+                    }
+                    const float vi = rsqrtf(vx * vx + vy * vy + vz * vz);
+                    vx *= vi; vy *= vi; vz *= vi;
+                    rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
+                }
+                pr = S.prop[sv.tissue()];
+            }
             // Fresnel reflection / refraction on crossing (2381-2503)
-            if (REFLECT && !kill && !stay) {
-                const float4 prn = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
+            if (REFLECT && !kill && !stay && !hit) {
+                const float4 prn = SVMC ? S.prop[med ? sv.tissue() : 0] : props_of<WORDS>(P, S.prop, (unsigned)med, idx);
                 pr = prn;
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
@@ -1115,9 +1249,20 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         med = (int)voxel_med<WORDS>(lab);
                         det = voxel_det<WORDS>(lab);     // carry keeps the bounced-off value
                         pr = props_of<WORDS>(P, S.prop, (unsigned)med, idx);
+                        if constexpr (SVMC) {
+                            // the voxel left, at the reflection point; its background ends the
+                            // photon (src/mcx_core.cu:2478-2497)
+                            split_voxel_at(P, idx, fx, fy, fz, px, py, pz, sv);
+                            pr = S.prop[sv.tissue()];
+                            sv_test = true;
+                            if (sv.tissue() == 0) {
+                                kill = true;
+                                detflag = detold & kDET_MASK;
+                            }
+                        }
                     }
                 } else {
-                    pr = props_of<WORDS>(P, S.prop, (unsigned)medold, idxold);
+                    pr = SVMC ? S.prop[med ? sv.tissue() : 0] : props_of<WORDS>(P, S.prop, (unsigned)medold, idxold);
                 }
             }
         }
@@ -1130,7 +1275,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
             if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);         // 1116-1122
             bool detected = false;
-            if (SAVEDET && (detflag & kDET_MASK) && med == 0) {
+            if (SAVEDET && (detflag & kDET_MASK) && (med == 0 || (SVMC && sv.tissue() == 0))) {
                 const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
                 if (detid) {
                     detected = true;
@@ -1281,6 +1426,7 @@ int transport_variant() { return g_minb; }
 bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 
 int transport_mode(const KParams& p) {
+    if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
     if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
@@ -1295,6 +1441,7 @@ static const void* pick_flags(bool reflect, bool savedet) {
 // The pencil variants run at 4 CTAs of 256 per SM (64 registers) unless the tuner asks for 3;
 // the variants with the general launch need more registers and run at 3 (80 registers).
 static const void* pick(bool reflect, bool savedet, int mode) {
+    if (mode == 4) return pick_flags<3, 4>(reflect, savedet);
     if (mode == 3) return pick_flags<3, 3>(reflect, savedet);
     if (mode == 2) return pick_flags<3, 2>(reflect, savedet);
     if (mode == 1) return pick_flags<3, 1>(reflect, savedet);

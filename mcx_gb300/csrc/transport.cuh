@@ -21,11 +21,11 @@ enum SrcType : int {
 };
 // Per-voxel media formats (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730 does).
 enum MediaFormat : int {
-    kMediaAsgnF2H = 96, kMedia2LabelMix = 98, kMediaLabelHalf = 99, kMediaAsF2H = 100, kMediaMuaFloat = 101,
+    kMediaAsgnF2H = 96, kMedia2LabelSplit = 97, kMedia2LabelMix = 98, kMediaLabelHalf = 99, kMediaAsF2H = 100, kMediaMuaFloat = 101,
     kMediaAsHalf = 102, kMediaAsgnByte = 103, kMediaAsShort = 104
 };
 __host__ __device__ constexpr bool media_words(int f) {
-    return f == kMediaAsgnF2H || f == kMedia2LabelMix || (f >= kMediaLabelHalf && f <= kMediaAsShort);
+    return (f >= kMediaAsgnF2H && f <= kMedia2LabelMix) || (f >= kMediaLabelHalf && f <= kMediaAsShort);
 }
 
 // Launch-direction options of area sources, from srcdir.w (src/mcx_core.cu:1672-1710): 0 =
@@ -56,7 +56,7 @@ struct KParams {
     const uint8_t* labels;          // Nvox bytes: bit 7 detector mask, bits 0-6 medium label
     const uint32_t* words;          // per-voxel media formats: MCX's 32-bit voxel words instead
     int mediaformat;                // MCX mediabyte: 1/2/4 labels, kMedia* per-voxel formats
-    const uint32_t* words2;         // MEDIA_ASGN_F2H: each voxel's second word (g, n halves)
+    const uint32_t* words2;         // MEDIA_ASGN_F2H / MEDIA_2LABEL_SPLIT: each voxel's second word
     float* field;                   // maxgate x Nvox raw flux accumulator
     float* shadow;                  // maxgate x Nvox spill copy (values moved out past kMaxAccum)
     double* field64;                // FP64 accumulator (reference-accuracy runs only), else null

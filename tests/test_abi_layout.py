@@ -204,6 +204,11 @@ def test_pack_media_layouts():
     sh[:, 0, 0, 0] = [-1, 5]
     w, f = pack_media(sh)
     assert f == 104 and w[0, 0, 0] == (5 << 16) | 0xFFFF
+    sp = np.zeros((8, 1, 1, 1), np.uint8)
+    sp[:, 0, 0, 0] = [1, 2, 10, 20, 30, 40, 50, 60]
+    w, f = pack_media(sp)
+    assert f == 97 and w.shape == (1, 1, 1, 2)
+    assert w[0, 0, 0, 0] == 0x0102_0A14 and w[0, 0, 0, 1] == 0x1E28_323C     # mcx_preprocess's two words
     with pytest.raises(Exception):
         pack_media(np.ones((5, 3, 3, 3), np.float32))
     bad = np.ones((3, 2, 2, 2), np.float32)
