@@ -45,7 +45,8 @@ typedef struct MCXMedium {
     float n;
 } Medium;
 
-/* Particle description for polarised media (carried, not used by this engine). */
+/* Sphere population of a polarised medium: absorption (1/mm), radius (um), number density
+ * (1/um^3), sphere and background refractive indices. */
 typedef struct MCXPolarizeMedium {
     float mua;
     float r;

@@ -53,6 +53,9 @@ class uint3(C.Structure):
 
 Medium = _layout("Medium", [("mua", C.c_float, 4), ("mus", C.c_float, 4), ("g", C.c_float, 4), ("n", C.c_float, 4)])
 
+POLMedium = _layout("POLMedium", [("mua", C.c_float, 4), ("r", C.c_float, 4), ("rho", C.c_float, 4),
+                                  ("nsph", C.c_float, 4), ("nmed", C.c_float, 4)])
+
 History = _layout("History", [
     ("magic", C.c_char * 4, 1), ("version", C.c_uint, 4), ("maxmedia", C.c_uint, 4), ("detnum", C.c_uint, 4),
     ("colcount", C.c_uint, 4), ("totalphoton", C.c_uint, 4), ("detected", C.c_uint, 4), ("savedphoton", C.c_uint, 4),

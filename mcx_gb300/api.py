@@ -31,7 +31,7 @@ _SAVEDET_CHARS = "dspmxvwi"      # detid, nscat, ppath, momentum, exit pos, exit
 _SCALARS_INT = ["nphoton", "nblocksize", "nthread", "maxdetphoton", "maxgate", "respin", "printnum", "maxvoidstep",
                 "maxjumpdebug", "gscatter", "srcnum", "srcid", "replaydet", "gpuid", "voidtime"]
 _DEBUG_CHARS = "RMPT"            # -D letters: RNG test, trajectories, progress, trajectories only (src/mcx_utils.c:159)
-_SCALARS_FLOAT = ["tstart", "tstep", "tend", "sradius", "minenergy", "unitinmm", "omega"]
+_SCALARS_FLOAT = ["tstart", "tstep", "tend", "sradius", "minenergy", "unitinmm", "omega", "lambda"]
 _SCALARS_CHAR = ["isreflect", "isref3", "isrefint", "isnormalized", "issrcfrom0", "autopilot", "issaveref",
                  "issaveexit", "ismomentum", "isspecular", "issave2pt", "issavedet", "isgpuinfo", "isrowmajor",
                  "issaveseed", "faststep"]
@@ -177,7 +177,7 @@ class PreparedConfig:
                 c.debuglevel = int(d)
         for k in _SCALARS_FLOAT:
             if k in cfg:
-                setattr(c, k, float(cfg[k]))
+                setattr(c, "lambda_" if k == "lambda" else k, float(cfg[k]))
         for k in _SCALARS_CHAR:
             if k in cfg:
                 setattr(c, k, bytes([int(cfg[k]) & 0xFF]))
@@ -216,6 +216,13 @@ class PreparedConfig:
                 _set_vec(getattr(c, key), cfg[key], n)
         if "steps" in cfg:
             _set_vec(c.steps, cfg["steps"], 3)
+        if "polprop" in cfg and cfg["polprop"] is not None and np.asarray(cfg["polprop"]).size:
+            # sphere populations of the polarised media, one row per medium after the background:
+            # mua, radius (um), number density (1/um^3), sphere and background indices (src/pmcx.cpp:689-725)
+            pp = np.asarray(cfg["polprop"], dtype=np.float32).reshape(-1, 5)
+            self.polprop = (abi.POLMedium * len(pp))(*[abi.POLMedium(*map(float, r)) for r in pp])
+            c.polprop = C.addressof(self.polprop)
+            c.polmedianum = len(pp)
         if "srcpattern" in cfg and cfg["srcpattern"] is not None:
             # x fastest, as pmcx passes a (param1.w, param2.w) or (nx, ny, nz) array (src/pmcx.cpp)
             pat = np.asarray(cfg["srcpattern"], dtype=np.float32).ravel(order="F").copy()
@@ -232,7 +239,8 @@ class PreparedConfig:
         self.vol = vol32
         c.vol = vol32.ctypes.data
 
-        prop = np.ascontiguousarray(np.asarray(cfg["prop"], dtype=np.float32).reshape(-1, 4))
+        # a private copy: preparation rewrites the rows of polarised media in place
+        prop = np.array(cfg["prop"], dtype=np.float32).reshape(-1, 4)
         self.prop = prop
         c.prop = prop.ctypes.data
         c.medianum = prop.shape[0]
@@ -273,6 +281,10 @@ class PreparedConfig:
                 if ptr:
                     libc.free(C.c_void_p(ptr))
                     setattr(c.replay, name, None)
+        # the Mueller tables the polarised-media preparation allocated with malloc
+        if c is not None and c.smatrix:
+            libc.free(C.c_void_p(c.smatrix))
+            c.smatrix = None
 
     @property
     def dims(self) -> tuple[int, int, int]:

@@ -324,7 +324,7 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
-    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount;
+    DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount, smat;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
     double kernel_ms = 0.0;
@@ -343,7 +343,7 @@ struct Session {
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
         pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
-        seeddata.release(); voxwords.release(); voxwords2.release(); traj.release(); trajcount.release();
+        seeddata.release(); voxwords.release(); voxwords2.release(); traj.release(); trajcount.release(); smat.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
         if (ev0) cudaEventDestroy(ev0);
@@ -449,7 +449,8 @@ struct Session {
         k.savedetflag = f;
         k.nmedia_det = (int)cfg->medianum - 1;
         k.partialdata = (cfg->medianum - 1) * (((f >> 1) & 1u) + ((f >> 2) & 1u) + ((f >> 3) & 1u));
-        k.reclen = k.partialdata + (f & 1u) + 3u * (((f >> 4) & 1u) + ((f >> 5) & 1u)) + ((f >> 6) & 1u);
+        k.reclen = k.partialdata + (f & 1u) + 3u * (((f >> 4) & 1u) + ((f >> 5) & 1u)) + ((f >> 6) & 1u) +
+                   (cfg->polmedianum ? 4u * ((f >> 7) & 1u) : 0u);
         k.maxdet = cfg->maxdetphoton;
         k.ndet = (int)cfg->detnum;
         if (cfg->detnum) {
@@ -505,6 +506,15 @@ struct Session {
         if (k.saveseed) {
             seeddata.alloc((size_t)k.maxdet * kSeedBytes, stream);
             k.seeddata = seeddata.as<unsigned long long>();
+        }
+        if (cfg->polmedianum) {
+            // polarised media: the Mueller tables of every medium after the background
+            const size_t n = (size_t)cfg->polmedianum * kNAngles;
+            smat.alloc(n * sizeof(float4), stream);
+            CK(cudaMemcpyAsync(smat.p, cfg->smatrix, n * sizeof(float4), cudaMemcpyHostToDevice, stream));
+            k.polarized = 1;
+            k.smatrix = smat.as<float4>();
+            k.srciquv = cfg->srciquv;
         }
         if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly)) {
             // trajectory records (src/mcx_core.cu:3158-3160): maxjumpdebug x 6 floats
@@ -907,7 +917,8 @@ void check_config(const Config* cfg) {
             if ((cfg->vol[i] & 0x3FFFu) >= cfg->medianum)
                 MCXG_RAISE(-6, "a MEDIA_LABEL_HALF voxel's label exceeds the number of media");
     }
-    if (cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
+    if (cfg->polmedianum && (cfg->mediabyte > 4 || !cfg->smatrix || cfg->medianum != cfg->polmedianum + 1))
+        MCXG_RAISE(-6, "polarized media need label volumes and the Mueller tables of mcx_prep_polarized");
     check_source(cfg);
 }
 

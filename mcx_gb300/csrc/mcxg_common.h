@@ -15,6 +15,8 @@ constexpr uint32_t kOUT_MIN   = 0xFFFFFFFFu;              // photon left through
 constexpr uint32_t kOUT_MAX   = 0x7FFFFFFFu;              // photon left through a far face
 constexpr float    kR_C0      = 3.335640951981520e-12f;   // 1/c in s/mm
 constexpr float    kTWO_PI    = 6.28318530717959f;
+constexpr float    kPI        = 3.1415926535897932f;
+constexpr float    kR_PI      = 0.318309886183791f;         // 1/pi
 constexpr int      kSEED_FROM_FILE = -999;
 constexpr int      kFILL_MAXDETPHOTON = 3;
 constexpr size_t   kSeedBytes = 16;                      // saved generator state per photon: RAND_BUF_LEN x 8 B

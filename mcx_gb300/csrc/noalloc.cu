@@ -84,6 +84,8 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
         MCXG_RAISE(-6, "the allocation-free entry point takes byte labels: no per-voxel media formats");
     if (cfg->seed == kSEED_FROM_FILE || cfg->issaveseed)
         MCXG_RAISE(-6, "the allocation-free entry point runs no replay and saves no seeds");
+    if (cfg->polmedianum)
+        MCXG_RAISE(-6, "the allocation-free entry point runs no polarised media (they need a Mueller table buffer)");
     if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly))
         MCXG_RAISE(-6, "the allocation-free entry point saves no trajectories (they need a record buffer)");
     k.minenergy = cfg->minenergy;

@@ -9,10 +9,13 @@
 //   mcxg_validatecfg  <- mcx_validatecfg    src/mcx_utils.c:3748-3857 (origin shift, time gates)
 //                        mcx_preprocess     src/mcx_utils.c:1525-1820 (direction, media, launch voxel)
 //   mcxg_maskdet      <- mcx_maskdet        src/mcx_utils.c:4214-4340 (label-media branch)
-// Out of this restatement (and rejected by the engine): seed files, polarised and
-// split-voxel media, extra sources, shapes/JSON parsing.
+//                        mcx_prep_polarized src/mcx_utils.c:1831-1871 (Mie tables), with the Mie
+//                        series of src/mcx_mie.cpp:91-216 restated
+// Out of this restatement (and rejected by the engine): seed files, extra sources, shapes/JSON
+// parsing.
 
 #include <cmath>
+#include <complex>
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
@@ -143,6 +146,140 @@ extern "C" void mcxg_maskdet(Config* cfg) {
 
 namespace {
 
+constexpr int kNAngles = 1000;      // NANGLES, src/mcx_const.h:59
+
+typedef std::complex<double> cplx;
+
+void put_mueller(float4& out, cplx s1, cplx s2) {
+    const double a1 = std::abs(s1), a2 = std::abs(s2);
+    const cplx c = std::conj(s1) * s2;
+    out = make_float4((float)(0.5 * a2 * a2 + 0.5 * a1 * a1), (float)(0.5 * a2 * a2 - 0.5 * a1 * a1),
+                      (float)std::real(c), (float)std::imag(c));
+}
+
+// Small spheres (m x < 0.1): the dipole/quadrupole expansion of Wiscombe (1980) in the form MCX
+// evaluates it (src/mcx_mie.cpp:232-312), for a real relative index m.  The coefficients a1, b1
+// and a2 follow Wiscombe's series in x^2; S1 = a1 + (b1 + a2) mu and S2 = b1 + (a1 + a2)(2 mu^2 - 1)
+// after scaling by 3/2 x^3 (a2 also by 5/3), which is how MCX combines them.
+void small_mie(double x, double m, const std::vector<double>& mu, float4* sm, double& qsca, double& g) {
+    const double m2 = m * m, m4 = m2 * m2, x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
+    const cplx z0(0.0, m2 - 1.0);          // i (m^2 - 1)
+    const cplx z1 = 2.0 / 3.0 * z0;
+    const cplx z3 = z1 * cplx(1.0 - 0.1 * x2 + (4.0 * m2 + 5.0) * x4 / 1400.0, 0.0);
+    const cplx z4 = x3 * (1.0 - 0.1 * x2) * z1;
+    const cplx den(2.0 + m2 + (1 - 0.7 * m2) * x2 + (8 * m4 - 385 * m2 + 350.0) / 1400 * x4 + std::real(z4), std::imag(z4));
+    cplx a1 = z3 / den;
+    cplx b1 = (x2 / 45.0 * z0) * (cplx(1.0 + (2.0 * m2 - 5.0) * x2 / 70.0, 0.0) / cplx(1.0 - (2.0 * m2 - 5.0) * x2 / 30.0, 0.0));
+    cplx a2 = ((1.0 - x2 / 14) * x2 / 15.0 * z0) / cplx(2.0 * m2 + 3.0 - (m2 / 7.0 - 0.5) * x2, 0.0);
+    const double aa1 = std::abs(a1), ab1 = std::abs(b1), aa2 = std::abs(a2);
+    const double t = aa1 * aa1 + ab1 * ab1 + 5.0 / 3.0 * aa2 * aa2;
+    qsca = 6.0 * x4 * t;
+    g = (std::real(a1) * (std::real(a2) + std::real(b1)) + std::imag(a1) * (std::imag(a2) + std::imag(b1))) / t;
+    const double sc = x3 * 1.5;
+    a1 *= sc;
+    b1 *= sc;
+    a2 *= sc * 5.0 / 3.0;
+    for (size_t k = 0; k < mu.size(); k++) {
+        const double c2 = 2 * mu[k] * mu[k] - 1;
+        put_mueller(sm[k], a1 + (b1 + a2) * mu[k], b1 + (a1 + a2) * c2);
+    }
+}
+
+// Lorenz-Mie scattering by a homogeneous sphere of size parameter x and real relative refractive
+// index m, in the series form of Wiscombe (1980) as MCX evaluates it (src/mcx_mie.cpp:91-216):
+// the logarithmic derivative D_n(mx) by upward recurrence (MCX fills D_0..D_{nstop-1} and the
+// last term of the series sees D_nstop = 0), Riccati-Bessel psi_n and xi_n = psi_n + i chi_n by
+// upward recurrence, the coefficients a_n and b_n, the amplitudes S1 and S2 at cos(theta) = mu[k],
+// the scattering efficiency and the asymmetry g.  Writes the Mueller elements per angle as
+// (S11, S12, S33, S34).
+void mie(double x, double m, const std::vector<double>& mu, float4* sm, double& qsca, double& g) {
+    if (x <= 0.0) MCXG_RAISE(-6, "sphere size must be positive");
+    if (x > 20000.0) MCXG_RAISE(-6, "spheres with x>20000 are not validated");
+    if (std::abs(m) * x < 0.1) {
+        small_mie(x, m, mu, sm, qsca, g);
+        return;
+    }
+    const int nk = (int)mu.size();
+    const long nstop = (long)std::floor(x + 4.05 * std::pow(x, 0.33333) + 2.0);
+    std::vector<cplx> s1(nk), s2(nk);
+    std::vector<double> pi1(nk, 1.0), pi0(nk, 0.0), tau(nk, 0.0);
+    const double z = m * x, zinv = 1.0 / z;
+    std::vector<double> D(nstop + 1, 0.0);
+    D[0] = 1.0 / std::tan(z);
+    for (long k = 1; k < nstop; k++) D[k] = 1.0 / (k * zinv - D[k - 1]) - k * zinv;
+    double psi0 = std::sin(x), psi1 = psi0 / x - std::cos(x);
+    cplx xi0(psi0, std::cos(x)), xi1(psi1, std::cos(x) / x + std::sin(x));
+    cplx anm1(0.0, 0.0), bnm1(0.0, 0.0);
+    qsca = 0.0;
+    g = 0.0;
+    for (long n = 1; n <= nstop; n++) {
+        const double da = D[n] / m + n / x, db = D[n] * m + n / x;
+        const cplx an = (da * psi1 - psi0) / (da * xi1 - xi0);
+        const cplx bn = (db * psi1 - psi0) / (db * xi1 - xi0);
+        const double f = (2.0 * n + 1.0) / (n + 1.0) / n;
+        for (int k = 0; k < nk; k++) {
+            tau[k] = n * mu[k] * pi1[k] - (n + 1) * pi0[k];
+            const double al = f * pi1[k], be = f * tau[k];
+            s1[k] += cplx(al * an.real() + be * bn.real(), al * an.imag() + be * bn.imag());
+            s2[k] += cplx(al * bn.real() + be * an.real(), al * bn.imag() + be * an.imag());
+        }
+        for (int k = 0; k < nk; k++) {
+            const double p = pi1[k];
+            pi1[k] = ((2.0 * n + 1.0) * mu[k] * pi1[k] - (n + 1.0) * pi0[k]) / n;
+            pi0[k] = p;
+        }
+        g += (n - 1.0 / n) * (anm1.real() * an.real() + anm1.imag() * an.imag() + bnm1.real() * bn.real() + bnm1.imag() * bn.imag());
+        g += (2.0 * n + 1.0) / n / (n + 1.0) * (an.real() * bn.real() + an.imag() * bn.imag());
+        const double aa = std::abs(an), ab = std::abs(bn);
+        qsca += (2.0 * n + 1.0) * (aa * aa + ab * ab);
+        const cplx xi = (2.0 * n + 1.0) / x * xi1 - xi0;
+        xi0 = xi1;
+        xi1 = xi;
+        psi0 = psi1;
+        psi1 = xi1.real();
+        anm1 = an;
+        bnm1 = bn;
+    }
+    qsca *= 2.0 / (x * x);
+    g *= 4.0 / qsca / (x * x);
+    for (int k = 0; k < nk; k++) put_mueller(sm[k], s1[k], s2[k]);
+}
+
+// mcx_prep_polarized (src/mcx_utils.c:1831-1871): each polarised medium's Mueller table and, from
+// its spheres (radius r um, number density rho per um^3, indices nsph in nmed at lambda nm), its
+// scattering coefficient; a medium whose prop row already holds mus (and g) gets the density
+// that reproduces that mus (or mus(1 - g)).  The angle grid, size parameter and cross-section use
+// single-precision pi and float products as MCX does, so the tables agree bit for bit.  The table
+// is malloc'ed into cfg->smatrix.
+void prep_polarized(Config* cfg) {
+    const float pi_f = 3.14159265358979f, two_pi_f = 6.28318530717959f;
+    std::vector<double> mu(kNAngles);
+    for (int i = 0; i < kNAngles; i++) mu[i] = std::cos((double)(pi_f * (float)i / (float)(kNAngles - 1)));
+    std::free(cfg->smatrix);
+    cfg->smatrix = (float4*)std::malloc(sizeof(float4) * kNAngles * cfg->polmedianum);
+    if (!cfg->smatrix) MCXG_RAISE(-4, "out of host memory for the scattering matrices");
+    for (uint32_t i = 0; i < cfg->polmedianum; i++) {
+        POLMedium& pm = cfg->polprop[i];
+        Medium& md = cfg->prop[i + 1];
+        md.mua = pm.mua;
+        md.n = pm.nmed;
+        const double x = (double)(two_pi_f * pm.r * pm.nmed) / (cfg->lambda * 1e-3);
+        const float area = pi_f * pm.r * pm.r;                   // um^2
+        double qsca = 0.0, g = 0.0;
+        mie(x, (double)(pm.nsph / pm.nmed), mu, cfg->smatrix + (size_t)i * kNAngles, qsca, g);
+        if (md.mus > kEPS) {
+            float target = md.mus;
+            if (md.g < 1.f - kEPS) {
+                const float musp = md.mus * (1.f - md.g);
+                target = (float)(musp / (1.0 - g));
+            }
+            pm.rho = (float)(target / qsca / area * 1e-3);
+        }
+        md.mus = (float)(qsca * area * pm.rho * 1e3);
+        md.g = (float)g;
+    }
+}
+
 void validate(Config* cfg) {
     // replay of saved photons (src/mcx_utils.c:1651-1664)
     if (cfg->seed == kSEED_FROM_FILE && (cfg->respin > 1 || cfg->respin < 0)) {
@@ -151,7 +288,7 @@ void validate(Config* cfg) {
     }
     if (cfg->replaydet > (int)cfg->detnum) MCXG_RAISE(-4, "replay detector ID exceeds the maximum detector number");
     if (cfg->replaydet == -1 && cfg->detnum == 1) cfg->replaydet = 1;
-    if (cfg->polprop || cfg->polmedianum) MCXG_RAISE(-6, "polarized media are not supported by the GB300 engine");
+
     if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
 
     // mcx_validatecfg: grid-origin shift, time gates (src/mcx_utils.c:3761-3795)
@@ -192,6 +329,19 @@ void validate(Config* cfg) {
     if (cfg->mediabyte > 4 && !media_words(cfg->mediabyte))
         MCXG_RAISE(-6, "the GB300 engine supports label media (mediabyte 1, 2, 4) and the per-voxel formats 96-104");
     check_source(cfg);
+
+    // polarised media (src/mcx_utils.c:1569-1591): label volumes only, one sphere population per
+    // medium after the background, a wavelength, and a Stokes vector of non-negative intensity
+    if (cfg->polprop && cfg->polmedianum) {
+        if (cfg->mediabyte > 4) MCXG_RAISE(-1, "Unsupported media format");
+        if (cfg->medianum != cfg->polmedianum + 1) MCXG_RAISE(-6, "number of particle types does not match number of media");
+        if (cfg->lambda == 0.f) MCXG_RAISE(-1, "you must specify light wavelength lambda to run polarized photon simulation");
+        if (cfg->srciquv.x < 0.f) MCXG_RAISE(-4, "initial total light intensity must not be negative");
+        if (cfg->srciquv.y < -1.f || cfg->srciquv.y > 1.f || cfg->srciquv.z < -1.f || cfg->srciquv.z > 1.f ||
+            cfg->srciquv.w < -1.f || cfg->srciquv.w > 1.f)
+            MCXG_RAISE(-4, "initial Q, U and V must be floating-point numbers between -1 and 1");
+        prep_polarized(cfg);
+    }
 
     if (cfg->steps.x != 1.f && cfg->unitinmm == 1.f) cfg->unitinmm = cfg->steps.x;
     if (cfg->unitinmm != 1.f) {
@@ -252,7 +402,10 @@ void validate(Config* cfg) {
         if (cfg->deviceid[i] == '0') cfg->deviceid[i] = '\0';
     if (cfg->ismomentum) cfg->savedetflag |= 0x8;
     if (cfg->issaveexit) cfg->savedetflag |= 0x30;
-    cfg->savedetflag &= ~0x80u;       // no Stokes vector without polarisation
+    if (cfg->polmedianum)             // src/mcx_utils.c:1788-1795: P, V, W0 and the Stokes vector
+        cfg->savedetflag |= 0x4u | 0x20u | 0x40u | 0x80u;
+    else
+        cfg->savedetflag &= ~0x80u;   // no Stokes vector without polarisation
     if (cfg->issavedet && cfg->savedetflag == 0) cfg->savedetflag = 0x5;
     // per-voxel media have no labels: no per-medium record columns (src/mcx_utils.c:1801-1806)
     // per-voxel formats carry no per-medium slots (src/mcx_utils.c:1801-1803, mediabyte >= 100); for

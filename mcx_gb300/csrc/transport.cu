@@ -618,6 +618,7 @@ struct Smem {
     float* rcos;                  // per thread, RF replay: cos and sin of omega x time of flight
     int* rbin;                    // per thread, replay: its field block (gate + detector offset), -1 none
     unsigned* pid;                // per thread, trajectories: the photon's id
+    float* stokes;                // 4 x blockDim, polarised light: the photon's Stokes vector (I, Q, U, V)
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
@@ -644,7 +645,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
         s.rcos = s.rtof + blockDim.x;                 // cos, then sin, blockDim.x each
         s.rbin = reinterpret_cast<int*>(s.rcos + 2 * blockDim.x);
         s.pid = reinterpret_cast<unsigned*>(s.rbin + blockDim.x);
-        end = reinterpret_cast<float*>(s.pid + blockDim.x);
+        s.stokes = reinterpret_cast<float*>(s.pid + blockDim.x);
+        end = s.stokes + 4 * blockDim.x;
     }
     s.tile = reinterpret_cast<unsigned*>(end);
     return s;
@@ -873,6 +875,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 }
                 if (SAVEDET)
                     for (unsigned k = 0; k < P.partialdata; k++) S.ppath[k * B + tid] = 0.f;
+                if (FULL && P.polarized) {      // src/mcx_core.cu:1254-1256
+                    S.stokes[tid] = P.srciquv.x;
+                    S.stokes[B + tid] = P.srciquv.y;
+                    S.stokes[2 * B + tid] = P.srciquv.z;
+                    S.stokes[3 * B + tid] = P.srciquv.w;
+                }
                 if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 1681-1687
                 alive = true;
             }
@@ -903,7 +911,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             }
             pscat = -__logf(u_len + kEPS);                               // src/mcx_rand_xorshift128p.cu:122
             if (nscat >= 0) {                                           // not the launch flight
-                if (P.seed_mode == 1) {
+                if (P.seed_mode == 1 && !(FULL && P.polarized)) {   // polarised: the rejection loop draws
                     u_phi = rng_next(r0, r1);
                     u_th = rng_next(r0, r1);
                 }
@@ -911,7 +919,26 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 __sincosf(kTWO_PI * u_phi, &sphi, &cphi);               // src/mcx_core.cu:1930-1933
                 const float g = (nscat > gscat) ? 0.f : pr.z;
                 float ct;
-                if (fabsf(g) > kEPS) {                                  // Henyey-Greenstein, 1946-1959
+                float pol_theta = 0.f, pol_phi = 0.f;
+                const float4* mrow = nullptr;
+                if (FULL && P.polarized) {
+                    // polarised: (theta, phi) from the medium's Mueller table by rejection against
+                    // the forward intensity for the photon's Stokes vector (src/mcx_core.cu:1909-1930)
+                    mrow = P.smatrix + (size_t)kNAngles * (unsigned)(med - 1);
+                    const float si = S.stokes[tid], sq = S.stokes[B + tid], su = S.stokes[2 * B + tid];
+                    const float4 m0 = __ldg(mrow);
+                    for (int tries = 0; tries < 100000; tries++) {
+                        pol_theta = acosf(2.f * rng_next(r0, r1) - 1.f);
+                        pol_phi = kTWO_PI * rng_next(r0, r1);
+                        float s2p, c2p;
+                        sincosf(2.f * pol_phi, &s2p, &c2p);
+                        const float lin = sq * c2p + su * s2p;
+                        const float4 mt = __ldg(mrow + (int)floorf(pol_theta * kNAngles * (kR_PI - kEPS)));
+                        if (rng_next(r0, r1) * (m0.x * si + m0.y * lin) < mt.x * si + mt.y * lin) break;
+                    }
+                    sincosf(pol_phi, &sphi, &cphi);
+                    ct = cosf(pol_theta);
+                } else if (fabsf(g) > kEPS) {                           // Henyey-Greenstein, 1946-1959
                     const float g2 = g * g;
                     float tmp = __fdividef(1.f - g2, 1.f - g + 2.f * g * u_th);
                     tmp *= tmp;
@@ -920,7 +947,8 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 } else {
                     ct = 2.f * u_th - 1.f;                              // isotropic, 1961-1963
                 }
-                const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+                const float st = (FULL && P.polarized) ? sinf(pol_theta) : sqrtf(fmaxf(0.f, 1.f - ct * ct));
+                const float ox0 = vx, oy0 = vy, oz0 = vz;               // direction before the event
                 if (SAVEDET && !WORDS && med > 0 && ((P.savedetflag >> 3) & 1u)) {   // momentum transfer, 1970-1993
                     const unsigned fS = (P.savedetflag >> 1) & 1u, fP = (P.savedetflag >> 2) & 1u;
                     S.ppath[((unsigned)P.nmedia_det * (fS + fP) + (unsigned)(med - 1)) * B + tid] += 1.f - ct;
@@ -944,6 +972,30 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     }
                 }
                 rotate(vx, vy, vz, st, ct, sphi, cphi);
+                if (FULL && P.polarized) {
+                    // updatestokes (src/mcx_core.cu:318-352): into the scattering plane, through the
+                    // Mueller matrix at theta, back to the new meridian plane, normalised to I = 1
+                    float si = S.stokes[tid], sq = S.stokes[B + tid], su = S.stokes[2 * B + tid], sv = S.stokes[3 * B + tid];
+                    float s2p, c2p;
+                    sincosf(2.f * pol_phi, &s2p, &c2p);
+                    const float q1 = sq * c2p + su * s2p, u1 = -sq * s2p + su * c2p;
+                    const float4 mt = __ldg(mrow + (int)floorf(pol_theta * kNAngles * (kR_PI - kEPS)));
+                    const float I = mt.x * si + mt.y * q1, Q = mt.y * si + mt.x * q1;
+                    const float U = mt.z * u1 + mt.w * sv, V = -mt.w * u1 + mt.z * sv;
+                    const float den = (vz > -1.f && vz < 1.f) ? (1.f - ct * ct) * (1.f - vz * vz) : 0.f;
+                    float ci = 0.f;
+                    if (den > 0.f) {
+                        ci = ((pol_phi > kPI && pol_phi < kTWO_PI) ? 1.f : -1.f) * (vz * ct - oz0) * rsqrtf(den);
+                        ci = fmaxf(-1.f, fminf(ci, 1.f));
+                    }
+                    const float sn = sqrtf(1.f - ci * ci), c22 = 2.f * ci * ci - 1.f, s22 = 2.f * sn * ci;
+                    const float inv = __fdividef(1.f, I);
+                    S.stokes[tid] = 1.f;
+                    S.stokes[B + tid] = (Q * c22 - U * s22) * inv;
+                    S.stokes[2 * B + tid] = (Q * s22 + U * c22) * inv;
+                    S.stokes[3 * B + tid] = V * inv;
+                    (void)ox0; (void)oy0;
+                }
                 nscat++;
                 rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                 c_scat++;
@@ -1292,6 +1344,12 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         if (P.savedetflag & 0x10u) { rec[k++] = px; rec[k++] = py; rec[k++] = pz; }
                         if (P.savedetflag & 0x20u) { rec[k++] = vx; rec[k++] = vy; rec[k++] = vz; }
                         if (P.savedetflag & 0x40u) rec[k++] = S.wlaunch[tid];
+                        if (FULL && P.polarized && (P.savedetflag & 0x80u)) {   // Stokes vector, 407-412
+                            rec[k++] = S.stokes[tid];
+                            rec[k++] = S.stokes[B + tid];
+                            rec[k++] = S.stokes[2 * B + tid];
+                            rec[k++] = S.stokes[3 * B + tid];
+                        }
                     }
                 }
             }
@@ -1410,7 +1468,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 6 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 10 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1428,7 +1486,7 @@ bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 int transport_mode(const KParams& p) {
     if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
-    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj) return 2;
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 

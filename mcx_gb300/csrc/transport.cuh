@@ -45,6 +45,7 @@ enum Energy : int { kELaunch = 0, kEEscape, kEDetect, kEAbsDep, kEAbsOther, kNum
 // debuglevel bits (src/mcx_const.h:67-70) and the trajectory record length (MCX_DEBUG_REC_LEN, :82)
 enum DebugBits : unsigned { kDebugRNG = 1u, kDebugMove = 2u, kDebugProgress = 4u, kDebugMoveOnly = 8u };
 constexpr unsigned kTrajRecLen = 6;
+constexpr int kNAngles = 1000;              // scattering-angle samples of a Mueller table (NANGLES)
 
 enum ErrBits : uint32_t { kErrStepCap = 1u, kErrBadLabel = 2u, kErrDetOverflow = 4u, kErrIndex = 8u };
 
@@ -88,6 +89,11 @@ struct KParams {
     int src_focus;                  // kFocus*: what srcdir.w asks of the area sources
     const float* srcpattern;        // pattern (param1.w x param2.w) or pattern3d intensities
     int isspecular, voidtime;
+
+    // --- polarised light (src/mcx_core.cu:298-352, 1909-1933): per-medium Mueller tables
+    int polarized;                  // label media with sphere populations (polmedianum > 0)
+    const float4* smatrix;          // (medianum - 1) x kNAngles (S11, S12, S33, S34)
+    float4 srciquv;                 // launch Stokes vector
 
     // --- photon trajectories, MCX's -D M (savedebugdata, src/mcx_core.cu:427-442; records at launch
     //     1681-1687, scattering 2068-2074, mismatched faces 2435-2441, termination 1116-1122)

@@ -57,6 +57,44 @@ def sphere60b(nphoton: float = 1e6) -> dict:
     return cfg
 
 
+def polarized_slab(nphoton: float = 1e6) -> dict:
+    """A 10 x 10 x 1.2 mm slab (100 x 100 x 12 voxels of 0.1 mm) of small polystyrene spheres in
+    water with a sphere of large ones at (6, 6, 0.6) mm, lit by a horizontally polarised planar
+    beam at 632.8 nm; photons leaving through z = 0 are detected with their Stokes vectors.  The
+    polarised-light deck of mcxlab/examples/demo_polarized_photon.m (sphere populations
+    mua (1/mm), radius (um), density (1/um^3), n_sphere, n_water)."""
+    dim = (100, 100, 12)
+    vol = np.ones(dim, dtype=np.uint8)
+    x, y, z = np.meshgrid(*(np.arange(n) + 0.5 for n in dim), indexing="ij")
+    vol[(x - 60) ** 2 + (y - 60) ** 2 + (z - 6) ** 2 < 25] = 2
+    return {
+        "nphoton": int(nphoton), "seed": 1648335518, "vol": vol, "unitinmm": 0.1,
+        "polprop": np.array([[0.005, 0.05, 19.1142, 1.59, 1.33], [0.005, 1.0, 1.11078e-3, 1.59, 1.33]], np.float32),
+        "prop": np.array([[0, 0, 1, 1], [0, 0, 1, 1], [0, 0, 1, 1]], np.float32),
+        "srctype": "planar", "srcpos": [0.0, 0.0, 0.0], "srcdir": [0.0, 0.0, 1.0],
+        "srcparam1": [100.0, 0.0, 0.0, 0.0], "srcparam2": [0.0, 100.0, 0.0, 0.0],
+        "srciquv": [1.0, 1.0, 0.0, 0.0], "lambda": 632.8, "issrcfrom0": 1,
+        "tstart": 0.0, "tend": 5e-8, "tstep": 5e-8, "isreflect": 0,
+        "savedetflag": "ixvw", "bc": "cc_cc_001000", "issavedet": 1, "maxdetphoton": int(nphoton),
+    }
+
+
+def rotated_stokes(detp: np.ndarray, nmedia: int, unitinmm: float, mua: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Stokes vectors of detected photons in the detector frame and their weights, from records of
+    (ppath x nmedia, exit position, exit direction, w0, I, Q, U, V) columns: Q and U are rotated by
+    twice the azimuth of the exit direction, and the weight is w0 exp(-sum mua ppath)
+    (mcxlab/examples/demo_polarized_photon.m, utils/mcxdetweight.m)."""
+    pp = detp[:nmedia]
+    v = detp[nmedia + 3:nmedia + 6]
+    w0 = detp[nmedia + 6]
+    s = detp[nmedia + 7:nmedia + 11]
+    phi = np.arctan2(v[1], v[0])
+    c2, s2 = np.cos(2 * phi), np.sin(2 * phi)
+    st = np.stack([s[0], s[1] * c2 + s[2] * s2, -s[1] * s2 + s[2] * c2, s[3]])
+    w = w0 * np.exp(-(np.asarray(mua, np.float64)[:, None] * pp).sum(0) * unitinmm)
+    return st, w
+
+
 def source_deck(g: dict, nphoton: float | None = None) -> dict:
     """The deck of a source-shape golden entry: its base deck with the entry's overrides."""
     cfg = {"cube60": cube60, "cube60planar": cube60planar}[g["deck"]](nphoton or g["nphoton"])

@@ -115,6 +115,36 @@ def build(force: bool = False) -> Path:
     return BIN
 
 
+MIE_LIB = REF / "lib" / "libmcxmie.so"
+
+# mcx_mie.cpp reports bad sizes through MCX's error handler; the library gets this one instead
+_MIE_STUB = r"""
+#include <stdio.h>
+#include <stdlib.h>
+extern "C" void mcx_error(const int id, const char* msg, const char* file, const int linenum) {
+    fprintf(stderr, "mcx_error %d: %s (%s:%d)\n", id, msg, file, linenum);
+    exit(1);
+}
+"""
+
+
+def build_mie(force: bool = False) -> Path:
+    """Compile the reference's Mie routines (src/mcx_mie.cpp, ``Mie`` and ``small_Mie``) into a
+    host shared library, so the Mueller tables of polarised media can be checked without a GPU."""
+    if MIE_LIB.exists() and not force:
+        return MIE_LIB
+    if not (SRC / "mcx_mie.cpp").exists():
+        raise RuntimeError("the reference sources are not staged in baseline/_ref/src")
+    obj = REF / "obj"
+    obj.mkdir(parents=True, exist_ok=True)
+    stub = obj / "mie_error_stub.cpp"
+    stub.write_text(_MIE_STUB)
+    MIE_LIB.parent.mkdir(parents=True, exist_ok=True)
+    _run(["g++", "-O2", "-shared", "-fPIC", f"-I{_cuda_home() / 'include'}", "-o", str(MIE_LIB), "mcx_mie.cpp",
+          str(stub)], SRC)
+    return MIE_LIB
+
+
 _SRC_NAMES = ["pencil", "isotropic", "cone", "gaussian", "planar", "pattern", "fourier", "arcsine", "disk",
               "fourierx", "fourierx2d", "zgaussian", "line", "slit", "pencilarray", "pattern3d", "hyperboloid", "ring"]
 
@@ -143,7 +173,8 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
         session_keys["DebugFlag"] = str(cfg["debuglevel"])       # -D letters, e.g. "M" for trajectories
     out = {
         "Session": session_keys,
-        "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0, "LengthUnit": 1,
+        "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0,
+                   "LengthUnit": float(cfg.get("unitinmm", 1.0)),
                    "MediaFormat": "byte", "VolumeFile": volfile,
                    "Media": [{"mua": float(r[0]), "mus": float(r[1]), "g": float(r[2]), "n": float(r[3])} for r in prop]},
         "Forward": {"T0": float(cfg["tstart"]), "T1": float(cfg["tend"]), "Dt": float(cfg["tstep"])},
@@ -159,6 +190,14 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
                                      for d in np.asarray(cfg["detpos"], float).reshape(-1, 4)]
     if "bc" in cfg:
         out["Session"]["BCFlags"] = cfg["bc"]
+    if "polprop" in cfg and np.asarray(cfg["polprop"]).size:
+        # polarised media: Domain.MieScatter, Optode.Source.WaveLength / IQUV (src/mcx_utils.c:2360-2400, 2731, 2873)
+        out["Domain"]["MieScatter"] = [{"mua": float(r[0]), "radius": float(r[1]), "rho": float(r[2]),
+                                        "nsph": float(r[3]), "nmed": float(r[4])}
+                                       for r in np.asarray(cfg["polprop"], float).reshape(-1, 5)]
+        out["Optode"]["Source"]["WaveLength"] = float(cfg["lambda"])
+        if "srciquv" in cfg:
+            out["Optode"]["Source"]["IQUV"] = [float(x) for x in cfg["srciquv"]]
     return out
 
 

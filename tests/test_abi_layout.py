@@ -24,6 +24,8 @@ def _probe_offsets(include_dir: Path, header: str, tmp_path: Path) -> dict[str, 
     lines.append('printf("sizeof_Config %zu\\n", sizeof(Config));')
     lines.append('printf("sizeof_GPUInfo %zu\\n", sizeof(GPUInfo));')
     lines.append('printf("sizeof_History %zu\\n", sizeof(History));')
+    lines.append('printf("sizeof_Medium %zu\\n", sizeof(Medium));')
+    lines.append('printf("sizeof_POLMedium %zu\\n", sizeof(POLMedium));')
     lines.append("return 0;}")
     src = tmp_path / "probe.c"
     src.write_text("\n".join(lines))
@@ -45,6 +47,8 @@ def test_ctypes_mirror_matches_header(engine, tmp_path):
     assert C.sizeof(abi.Config) == c["sizeof_Config"]
     assert C.sizeof(abi.GPUInfo) == c["sizeof_GPUInfo"]
     assert C.sizeof(abi.History) == c["sizeof_History"]
+    assert C.sizeof(abi.Medium) == c["sizeof_Medium"]
+    assert C.sizeof(abi.POLMedium) == c["sizeof_POLMedium"]
 
 
 @pytest.mark.skipif(not (REFERENCE_SRC / "mcx_utils.h").exists(), reason="reference headers not present")
