@@ -249,6 +249,7 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
     mch = tmp / f"{session}.mch"
     if mch.exists():
         raw = mch.read_bytes()
+        res["mch_header"] = raw[:64]
         # History header (src/mcx_utils.h:115-132): magic, version, maxmedia, detnum, colcount,
         # totalphoton, detected, savedphoton, unitinmm, seedbyte, ...
         hdr = struct.unpack("<4s7If1I", raw[:40])
