@@ -413,6 +413,14 @@ def _result(pc: PreparedConfig, flux, maxgate, detp, st) -> dict[str, Any]:
     if flux is not None:
         out["flux"] = flux.reshape((nx, ny, nz, maxgate), order="F")
         c.exportfield = None
+        if c.issaveref != b"\x00":
+            # diffuse reflectance as pmcx splits it off (src/pmcx.cpp:1268-1290): the negated field
+            # in void voxels, which the fluence then leaves at zero
+            void = (pc.vol[:nx * ny * nz] == 0).reshape((nx, ny, nz), order="F")
+            dref = np.zeros_like(out["flux"])
+            dref[void] = -out["flux"][void]
+            out["flux"][void] = 0.0
+            out["dref"] = dref
     if c.issavedet != b"\x00" and detp is not None:
         out["detp"] = detp
     out["stat"] = {

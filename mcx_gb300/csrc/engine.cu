@@ -434,6 +434,7 @@ struct Session {
         k.maxgate = maxgate;
         k.doreflect = cfg->isreflect ? 1 : 0;
         k.save2pt = cfg->issave2pt ? 1 : 0;
+        k.saveref = (cfg->issave2pt && cfg->issaveref == 1) ? 1 : 0;
         k.outputtype = cfg->outputtype;
         k.minenergy = cfg->minenergy;
         k.gscatter = (float)cfg->gscatter;

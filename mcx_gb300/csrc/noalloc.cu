@@ -77,6 +77,7 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     k.maxgate = (cfg->maxgate > 0) ? std::min<int>((int)cfg->maxgate, totalgates) : totalgates;
     k.doreflect = cfg->isreflect ? 1 : 0;
     k.save2pt = cfg->issave2pt ? 1 : 0;
+    k.saveref = (cfg->issave2pt && cfg->issaveref == 1) ? 1 : 0;
     k.outputtype = cfg->outputtype;
     if (k.outputtype != otFlux && k.outputtype != otFluence && k.outputtype != otEnergy)
         MCXG_RAISE(-6, "the allocation-free entry point supports flux, fluence and energy outputs");

@@ -412,7 +412,10 @@ void validate(Config* cfg) {
     // mediabyte 96, 98 and 99 MCX keeps the flags and indexes the slots by the voxel word, past the
     // end of the record, so the engine clears them for every non-label format
     if (cfg->mediabyte > 4 && cfg->savedetflag) cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u | 0x80u);
-    if (cfg->issaveref) MCXG_RAISE(-6, "diffuse-reflectance output (issaveref) is not supported by the GB300 engine");
+    // diffuse reflectance (src/mcx_utils.c:3757-3759, 1808-1818): needs the field; mode 2 (the exit
+    // path per voxel in the detected buffer) is not built
+    if (!cfg->issave2pt) cfg->issaveref = 0;
+    if (cfg->issaveref > 1) MCXG_RAISE(-6, "issaveref > 1 (exit path length per voxel) is not supported by the GB300 engine");
 
     // history header bookkeeping done at the end of mcx_validatecfg (src/mcx_utils.c:3853-3857)
     const uint32_t f = cfg->savedetflag;

@@ -1326,6 +1326,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
             if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);         // 1116-1122
+            if (FULL && P.saveref && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f) {
+                // diffuse reflectance (1124-1165): the weight leaving into a void voxel of the grid,
+                // negated, in that voxel at the photon's gate (a photon before the first gate, which
+                // MCX would write below the field, is left out)
+                const int ts = min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b)));
+                if (ts >= 0) field_add_large(P, (size_t)idx + (size_t)ts * P.nvox, -w);
+            }
             bool detected = false;
             if (SAVEDET && (detflag & kDET_MASK) && (med == 0 || (SVMC && sv.tissue() == 0))) {
                 const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
@@ -1486,7 +1493,7 @@ bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 int transport_mode(const KParams& p) {
     if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
-    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized) return 2;
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 

@@ -57,6 +57,21 @@ def sphere60b(nphoton: float = 1e6) -> dict:
     return cfg
 
 
+def reflectance_cube(nphoton: float = 1e6) -> dict:
+    """cube60's medium inside a one-voxel void shell (62^3 grid), a pencil beam entering at the
+    centre of the z = 1 face, no reflection, a 100 ns window: every photon that leaves the medium
+    ends in a void voxel of the grid, where the diffuse-reflectance output (issaveref) records it."""
+    vol = np.zeros((62, 62, 62), dtype=np.uint8)
+    vol[1:-1, 1:-1, 1:-1] = 1
+    return {
+        "nphoton": int(nphoton), "seed": CUBE60_SEED, "vol": vol,
+        "prop": np.array([[0.0, 0.0, 1.0, 1.0], [0.005, 1.0, 0.01, 1.37]], np.float32),
+        "tstart": 0.0, "tend": 1e-7, "tstep": 1e-7,
+        "srcpos": [31.0, 31.0, 1.0], "srcdir": [0.0, 0.0, 1.0], "issrcfrom0": 1,
+        "isreflect": 0, "issaveref": 1,
+    }
+
+
 def polarized_slab(nphoton: float = 1e6) -> dict:
     """A 10 x 10 x 1.2 mm slab (100 x 100 x 12 voxels of 0.1 mm) of small polystyrene spheres in
     water with a sphere of large ones at (6, 6, 0.6) mm, lit by a horizontally polarised planar
