@@ -34,6 +34,11 @@ def save_mch(fname: str | Path, pc, result: dict[str, Any]) -> Path:
     h = _header(pc)
     detp = result.get("detp")
     n = 0 if detp is None else int(detp.shape[1])
+    # the fields MCX's CLI sets just before it writes (src/mcx_core.cu:3948-3958)
+    h.unitinmm = pc.c.unitinmm
+    h.savedphoton = n
+    h.totalphoton = int(pc.c.nphoton)
+    h.detected = n
     if detp is not None and detp.shape[0] != h.colcount:
         raise ValueError(f"records have {detp.shape[0]} columns, the run's header says {h.colcount}")
     with open(fname, "wb") as f:

@@ -21,7 +21,7 @@ def _prepared(engine):
     cfg = problems.cube60(1000)
     pc = engine.prepare(cfg)
     h = pc.c.his
-    h.colcount, h.detected, h.savedphoton, h.totalphoton = 6, 3, 3, 1000
+    h.colcount, h.detected, h.savedphoton, h.totalphoton = 6, 0, 0, 0
     h.normalizer, h.seedbyte, h.respin = 2.5, 32, 1
     return pc
 
