@@ -343,6 +343,11 @@ def _active_devices(c) -> None:
     return nact, info
 
 
+def _srctype_code(c) -> int:
+    v = c.srctype
+    return v[0] if isinstance(v, bytes) else int(v)
+
+
 def _attach_field(pc: PreparedConfig):
     c = pc.c
     nx, ny, nz = pc.dims
@@ -351,9 +356,11 @@ def _attach_field(pc: PreparedConfig):
         maxgate *= max(1, int(c.detnum))     # one block of gates per detector
     if ord(c.outputtype) in (6, 8):
         maxgate *= 2                         # RF replay: real blocks, then imaginary blocks
+    # photon sharing: one channel per pattern, adjacent per voxel (src/mcx_core.cu:2782)
+    pc.chans = int(c.srcnum) if (_srctype_code(c) in (5, 15) and int(c.srcnum) > 1) else 1
     flux = None
     if c.issave2pt != b"\x00":
-        flux = np.zeros(nx * ny * nz * maxgate, dtype=np.float32)
+        flux = np.zeros(nx * ny * nz * maxgate * pc.chans, dtype=np.float32)
         c.exportfield = flux.ctypes.data
     return flux, maxgate
 
@@ -411,16 +418,20 @@ def _result(pc: PreparedConfig, flux, maxgate, detp, st) -> dict[str, Any]:
     nx, ny, nz = pc.dims
     out: dict[str, Any] = {}
     if flux is not None:
-        out["flux"] = flux.reshape((nx, ny, nz, maxgate), order="F")
+        ch = getattr(pc, "chans", 1)
+        # pmcx's shape: photon-sharing channels folded into the first axis, (srcnum * nx, ny, nz, nt)
+        out["flux"] = flux.reshape((ch * nx, ny, nz, maxgate), order="F")
         c.exportfield = None
         if c.issaveref != b"\x00":
             # diffuse reflectance as pmcx splits it off (src/pmcx.cpp:1268-1290): the negated field
             # in void voxels, which the fluence then leaves at zero
             void = (pc.vol[:nx * ny * nz] == 0).reshape((nx, ny, nz), order="F")
-            dref = np.zeros_like(out["flux"])
-            dref[void] = -out["flux"][void]
-            out["flux"][void] = 0.0
-            out["dref"] = dref
+            f5 = flux.reshape((ch, nx, ny, nz, maxgate), order="F")
+            d5 = np.zeros_like(f5)
+            d5[:, void] = -f5[:, void]
+            f5[:, void] = 0.0
+            out["dref"] = d5.reshape((ch * nx, ny, nz, maxgate), order="F")
+            out["flux"] = f5.reshape((ch * nx, ny, nz, maxgate), order="F")
     if c.issavedet != b"\x00" and detp is not None:
         out["detp"] = detp
     out["stat"] = {

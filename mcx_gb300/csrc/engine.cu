@@ -235,12 +235,19 @@ uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
 }  // namespace
 
 // Source settings the engine takes (src/mcx_core.cu:1261-1640): every MCX_SRC_* shape with one
-// source; not photon sharing (srcnum > 1), extra sources or a launch-angle table.
+// source, photon sharing (srcnum > 1 patterns of a pattern source); not extra sources or a
+// launch-angle table.
 void check_source(const Config* cfg) {
     if ((unsigned char)cfg->srctype >= kNumSrcTypes) MCXG_RAISE(-6, "unknown source type");
     if (std::isinf(cfg->srcdir.w) && cfg->srcdir.w > 0.f)
         MCXG_RAISE(-4, "a focal length of +inf is not a valid source setting (srcdir.w)");
-    if (cfg->srcnum > 1) MCXG_RAISE(-6, "photon sharing (srcnum > 1) is not supported by the GB300 engine");
+    if (cfg->srcnum > 1) {
+        const int t = (unsigned char)cfg->srctype;
+        if (t != kSrcPattern && t != kSrcPattern3D)
+            MCXG_RAISE(-6, "photon sharing (srcnum > 1) needs a pattern or pattern3d source");
+        if (cfg->seed == kSEED_FROM_FILE || (cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy))
+            MCXG_RAISE(-6, "photon sharing is supported with flux, fluence and energy outputs, without replay");
+    }
     if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
     if (cfg->nangle) MCXG_RAISE(-6, "launch-angle distributions (angleinvcdf) are not supported by the GB300 engine");
     const int st = (unsigned char)cfg->srctype;
@@ -256,10 +263,17 @@ void check_source(const Config* cfg) {
         MCXG_RAISE(-4, "a pencil-array source needs at least 2 beams along each side (srcparam1.w, srcparam2.w)");
 }
 
+// Field channels of a photon-sharing run: one per pattern (src/mcx_core.cu:2782); 1 otherwise.
+unsigned share_channels(const Config* cfg) {
+    const int t = (unsigned char)cfg->srctype;
+    return (cfg->srcnum > 1 && (t == kSrcPattern || t == kSrcPattern3D)) ? cfg->srcnum : 1u;
+}
+
 size_t source_pattern_len(const Config* cfg) {
     if (!cfg->srcpattern) return 0;
-    if ((unsigned char)cfg->srctype == kSrcPattern) return (size_t)cfg->srcparam1.w * (size_t)cfg->srcparam2.w;
-    if ((unsigned char)cfg->srctype == kSrcPattern3D) return (size_t)cfg->srcparam1.x * (size_t)cfg->srcparam1.y * (size_t)cfg->srcparam1.z;
+    const size_t ns = share_channels(cfg);
+    if ((unsigned char)cfg->srctype == kSrcPattern) return (size_t)cfg->srcparam1.w * (size_t)cfg->srcparam2.w * ns;
+    if ((unsigned char)cfg->srctype == kSrcPattern3D) return (size_t)cfg->srcparam1.x * (size_t)cfg->srcparam1.y * (size_t)cfg->srcparam1.z * ns;
     return 0;
 }
 
@@ -276,6 +290,7 @@ void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
                 : (f != 0.f) ? kFocusLength : kFocusNone;
     k.src_focal = std::isfinite(f) ? f : 0.f;
     k.srcpattern = d_pattern;
+    k.srcnum = (int)share_channels(cfg);
     k.isspecular = cfg->isspecular ? 1 : 0;
     k.voidtime = cfg->voidtime;
     k.src_ok = 1;
@@ -327,6 +342,7 @@ struct Session {
     DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount, smat;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
+    unsigned chans = 1;        // photon sharing: one channel per pattern, adjacent per voxel and gate
     double kernel_ms = 0.0;
     int launches = 0;
     // MCX per-thread seeding: stream count, host/device seed words and the glibc random_r state
@@ -380,7 +396,8 @@ struct Session {
         int maxgate = (cfg->maxgate > 0) ? std::min<int>((int)cfg->maxgate, totalgates) : totalgates;
         size_t freeb = 0, totalb = 0;
         cudaMemGetInfo(&freeb, &totalb);
-        const size_t per_gate = nvox * (use64 ? sizeof(double) : 2 * sizeof(float)) + nvox * sizeof(float);
+        chans = share_channels(cfg);
+        const size_t per_gate = (nvox * (use64 ? sizeof(double) : 2 * sizeof(float)) + nvox * sizeof(float)) * chans;
         const size_t budget = freeb > (size_t)(1u << 30) ? freeb - (size_t)(1u << 30) : freeb / 2;
         if ((size_t)maxgate * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / per_gate));
         // a replay of every detector at once keeps one block of gates per detector
@@ -390,7 +407,7 @@ struct Session {
         halves = (cfg->outputtype == otRF || cfg->outputtype == otRFmus) ? 2 : 1;
         if ((size_t)maxgate * blocks * halves * per_gate > budget)
             maxgate = std::max<int>(1, (int)(budget / (per_gate * blocks * halves)));
-        fieldlen = nvox * (size_t)maxgate * blocks * halves;
+        fieldlen = nvox * (size_t)maxgate * blocks * halves * chans;
 
         // labels: upload the uint32 volume, pack to one byte per voxel on the device; the
         // per-voxel media formats keep MCX's 32-bit words
@@ -1015,6 +1032,7 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
         // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
         float scale = 1.f;
         std::vector<float> block_scale;         // all-detector replay: one scale per detector block
+        std::vector<float> chan_scale;          // photon sharing: one scale per pattern
         const int ot = cfg->outputtype;
         const bool path_units = (ot == otJacobian || ot == otRF || ot == otWLTOF);
         if (cfg->isnormalized && st.e_launch > 0.0) {
@@ -1043,13 +1061,36 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
                 for (size_t i = 0; i < (size_t)cfg->nphoton; i++) sum += cfg->replay.weight[i];
                 scale = (sum > 0.0) ? (float)(cfg->unitinmm / sum) : 0.f;
             }
+            if (S.chans > 1) {
+                // photon sharing: each pattern's channel over its total intensity
+                // (src/mcx_core.cu:3778-3795, 3895-3906), Kahan-summed in float as MCX sums it
+                const bool p3 = (unsigned char)cfg->srctype == kSrcPattern3D;
+                const int psize = p3 ? (int)cfg->srcparam1.x * (int)cfg->srcparam1.y * (int)cfg->srcparam1.z
+                                     : (int)cfg->srcparam1.w * (int)cfg->srcparam2.w;
+                for (unsigned c = 0; c < S.chans; c++) {
+                    float sum = 0.f, comp = 0.f;
+                    for (int p = 0; p < psize; p++) {
+                        const float y = cfg->srcpattern[(size_t)p * S.chans + c] - comp;
+                        const float t = sum + y;
+                        comp = (t - sum) - y;
+                        sum = t;
+                    }
+                    chan_scale.push_back(psize / sum * scale);
+                }
+                scale = chan_scale[0];
+            }
             cfg->normalizer = scale;
             cfg->his.normalizer = scale;
         }
         host_field.resize(S.fieldlen);
-        S.read_field(host_field.data(), block_scale.empty() ? scale : 1.f, cfg->isnormalized == 2);
+        S.read_field(host_field.data(), (block_scale.empty() && chan_scale.empty()) ? scale : 1.f, cfg->isnormalized == 2);
         float* out = cfg->exportfield;
-        if (block_scale.empty()) {
+        if (!chan_scale.empty()) {
+            for (size_t i = 0; i < S.fieldlen; i++) {
+                const float v = host_field[i];
+                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * chan_scale[i % S.chans];
+            }
+        } else if (block_scale.empty()) {
             for (size_t i = 0; i < S.fieldlen; i++) out[i] += host_field[i];
         } else {
             const size_t per = S.fieldlen / (S.blocks * S.halves);     // one detector's gates

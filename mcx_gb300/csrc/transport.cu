@@ -134,6 +134,7 @@ __device__ int find_detector(const KParams& P, float px, float py, float pz) {
 struct Launch {
     float px, py, pz, w, vx, vy, vz, t;
     unsigned idx, label;
+    unsigned pix;               // photon sharing: the pattern pixel the photon started from
     int ix, iy, iz;             // integer coordinates of voxel idx (the position may sit on its face)
 };
 
@@ -363,13 +364,24 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                 const float rz = rng_next(r0, r1);
                 L.px += rx * p1.x; L.py += ry * p1.y; L.pz += rz * p1.z;
                 const int nx = (int)p1.x, ny = (int)p1.y;
-                L.w = P.src_p.w * __ldg(P.srcpattern + (int)(rz * kJustBelowOne * p1.z) * ny * nx +
-                                        (int)(ry * kJustBelowOne * p1.y) * nx + (int)(rx * kJustBelowOne * p1.x));
+                const unsigned pix = (int)(rz * kJustBelowOne * p1.z) * ny * nx + (int)(ry * kJustBelowOne * p1.y) * nx +
+                                     (int)(rx * kJustBelowOne * p1.x);
+                if (P.srcnum > 1) {         // photon sharing: unit weight, the patterns' weights per deposit
+                    L.pix = pix;
+                    L.w = 1.f;
+                } else {
+                    L.w = P.src_p.w * __ldg(P.srcpattern + pix);
+                }
             } else {
                 L.px += rx * p1.x + ry * p2.x; L.py += rx * p1.y + ry * p2.y; L.pz += rx * p1.z + ry * p2.z;
                 if (P.srctype == kSrcPattern) {
-                    L.w = P.src_p.w * __ldg(P.srcpattern + (int)(ry * kJustBelowOne * p2.w) * (int)p1.w +
-                                            (int)(rx * kJustBelowOne * p1.w));
+                    const unsigned pix = (int)(ry * kJustBelowOne * p2.w) * (int)p1.w + (int)(rx * kJustBelowOne * p1.w);
+                    if (P.srcnum > 1) {     // photon sharing (src/mcx_core.cu:1288-1296)
+                        L.pix = pix;
+                        L.w = 1.f;
+                    } else {
+                        L.w = P.src_p.w * __ldg(P.srcpattern + pix);
+                    }
                 } else if (P.srctype == kSrcFourier) {
                     L.w = P.src_p.w * (cosf((floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w)) * kTWO_PI) *
                                            (1.f - p2.w + floorf(p2.w)) + 1.f) * 0.5f;
@@ -584,6 +596,18 @@ __device__ __forceinline__ void field_add_small(const KParams& P, size_t addr, f
     else atomicAdd(P.field + addr, v);
 }
 
+// Photon sharing (src/mcx_core.cu:2259-2275): one deposit of a unit-weight photon feeds every
+// pattern's channel with that pattern's weight at the photon's starting pixel; the channels of
+// a voxel and gate are adjacent, (voxel + gate x nvox) x srcnum + pattern.
+__device__ __forceinline__ void share_deposit(const KParams& P, unsigned pix, size_t addr, float v) {
+    const float* pw = P.srcpattern + (size_t)pix * (unsigned)P.srcnum;
+    const size_t base = addr * (unsigned)P.srcnum;
+    for (int i = 0; i < P.srcnum; i++) {
+        const float f = __ldg(pw + i);
+        if (f != 0.f) field_add_small(P, base + i, v * f);
+    }
+}
+
 // Shared-memory carve-up of one CTA.
 // One trajectory record (savedebugdata, src/mcx_core.cu:427-442): photon id as uint bits, the
 // position in grid units, the weight and the source id (0: one source).  Records past traj_max
@@ -619,6 +643,7 @@ struct Smem {
     int* rbin;                    // per thread, replay: its field block (gate + detector offset), -1 none
     unsigned* pid;                // per thread, trajectories: the photon's id
     float* stokes;                // 4 x blockDim, polarised light: the photon's Stokes vector (I, Q, U, V)
+    unsigned* spix;               // per thread, photon sharing: the pattern pixel of its photon
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
@@ -646,7 +671,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
         s.rbin = reinterpret_cast<int*>(s.rcos + 2 * blockDim.x);
         s.pid = reinterpret_cast<unsigned*>(s.rbin + blockDim.x);
         s.stokes = reinterpret_cast<float*>(s.pid + blockDim.x);
-        end = s.stokes + 4 * blockDim.x;
+        s.spix = reinterpret_cast<unsigned*>(s.stokes + 4 * blockDim.x);
+        end = reinterpret_cast<float*>(s.spix + blockDim.x);
     }
     s.tile = reinterpret_cast<unsigned*>(end);
     return s;
@@ -856,6 +882,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     med = (int)voxel_med<WORDS>(lab);
                     det = voxel_det<WORDS>(lab);
                     fx = (float)L.ix; fy = (float)L.iy; fz = (float)L.iz;
+                    if (FULL && P.srcnum > 1) S.spix[tid] = L.pix;
                 }
             }
             if (entered) {
@@ -1129,7 +1156,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
                     // the index range of the tile box (empty without a tile) screens most deposits out
                     // with one compare before the box test
-                    if (idxold - P.d_tile_lo < P.d_tile_span && weight > 0.f && ox >= tx0 && ox < tx1 && oy >= ty0 &&
+                    if (FULL && P.srcnum > 1) {
+                        share_deposit(P, S.spix[tid], addr, weight);
+                    } else if (idxold - P.d_tile_lo < P.d_tile_span && weight > 0.f && ox >= tx0 && ox < tx1 && oy >= ty0 &&
                         oy < ty1 && oz >= tz0 && oz < tz1 && (unsigned)(tshift - P.tg0) < (unsigned)P.tng) {
                         const int ti = (((tshift - P.tg0) * P.tnz + (int)(oz - tz0)) * P.tny + (int)(oy - ty0)) * P.tnx +
                                        (int)(ox - tx0);
@@ -1331,7 +1360,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 // negated, in that voxel at the photon's gate (a photon before the first gate, which
                 // MCX would write below the field, is left out)
                 const int ts = min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b)));
-                if (ts >= 0) field_add_large(P, (size_t)idx + (size_t)ts * P.nvox, -w);
+                if (ts >= 0) {
+                    if (P.srcnum > 1) share_deposit(P, S.spix[tid], (size_t)idx + (size_t)ts * P.nvox, -w);
+                    else field_add_large(P, (size_t)idx + (size_t)ts * P.nvox, -w);
+                }
             }
             bool detected = false;
             if (SAVEDET && (detflag & kDET_MASK) && (med == 0 || (SVMC && sv.tissue() == 0))) {
@@ -1350,7 +1382,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                         for (unsigned i = 0; i < P.partialdata; i++) rec[k++] = S.ppath[i * B + tid];
                         if (P.savedetflag & 0x10u) { rec[k++] = px; rec[k++] = py; rec[k++] = pz; }
                         if (P.savedetflag & 0x20u) { rec[k++] = vx; rec[k++] = vy; rec[k++] = vz; }
-                        if (P.savedetflag & 0x40u) rec[k++] = S.wlaunch[tid];
+                        // launch weight; under photon sharing MCX's slot holds the pattern pixel's
+                        // index bits instead (src/mcx_core.cu:1290, 1697, 403)
+                        if (P.savedetflag & 0x40u) rec[k++] = (FULL && P.srcnum > 1) ? __uint_as_float(S.spix[tid]) : S.wlaunch[tid];
                         if (FULL && P.polarized && (P.savedetflag & 0x80u)) {   // Stokes vector, 407-412
                             rec[k++] = S.stokes[tid];
                             rec[k++] = S.stokes[B + tid];
@@ -1475,7 +1509,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 10 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 11 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1493,7 +1527,7 @@ bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 int transport_mode(const KParams& p) {
     if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
-    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref) return 2;
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref || p.srcnum > 1) return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 

@@ -126,6 +126,7 @@ struct KParams {
     int doreflect;                  // cfg->isreflect
     int save2pt;                    // record the field
     int saveref;                    // diffuse reflectance: -w into the void voxel a photon ends in
+    int srcnum;                     // photon sharing: patterns (field channels); 1 otherwise
     int outputtype;                 // 0 flux, 1 fluence, 2 energy
     float minenergy;                // Russian roulette threshold (0 = off)
     float gscatter;                 // scattering events after which mus' replaces mus

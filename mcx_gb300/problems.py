@@ -57,6 +57,21 @@ def sphere60b(nphoton: float = 1e6) -> dict:
     return cfg
 
 
+def shared_patterns(nphoton: float = 1e6) -> dict:
+    """cube60's medium lit by a 40 x 40 mm pattern source of 16 x 16 pixels carrying two
+    patterns at once (photon sharing, srcnum = 2): the left half of the field, and a linear ramp
+    along y.  ``srcpattern`` is (srcnum, 16, 16), patterns adjacent per pixel as MCX stores them."""
+    a = np.zeros((16, 16), np.float32)
+    a[:8, :] = 1.0
+    b = np.tile(np.linspace(0.1, 1.0, 16, dtype=np.float32)[None, :], (16, 1))
+    cfg = _cube60(nphoton, False, 1.37)
+    cfg.pop("detpos")
+    cfg.update(issavedet=0, srctype="pattern", srcpos=[10.0, 10.0, 0.0], srcdir=[0.0, 0.0, 1.0],
+               srcparam1=[40.0, 0.0, 0.0, 16.0], srcparam2=[0.0, 40.0, 0.0, 16.0], srcnum=2,
+               srcpattern=np.stack([a, b]))
+    return cfg
+
+
 def reflectance_cube(nphoton: float = 1e6) -> dict:
     """cube60's medium inside a one-voxel void shell (62^3 grid), a pencil beam entering at the
     centre of the z = 1 face, no reflection, a 100 ns window: every photon that leaves the medium

@@ -187,6 +187,16 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
     for key, name in (("srcparam1", "Param1"), ("srcparam2", "Param2")):
         if key in cfg:
             out["Optode"]["Source"][name] = [float(x) for x in cfg[key]]
+    if cfg.get("srcpattern") is not None:
+        # Optode.Source.Pattern {Nx, Ny, Nz, Data} with SrcNum patterns interleaved per pixel
+        # (src/mcx_utils.c:2878, 2906-2935)
+        pat = np.asarray(cfg["srcpattern"], np.float32)
+        ns = int(cfg.get("srcnum", 1))
+        shape = pat.shape[1:] if ns > 1 else pat.shape
+        dims = list(shape) + [1] * (3 - len(shape))
+        out["Optode"]["Source"]["SrcNum"] = ns
+        out["Optode"]["Source"]["Pattern"] = {"Nx": int(dims[0]), "Ny": int(dims[1]), "Nz": int(dims[2]),
+                                              "Data": [float(x) for x in pat.ravel(order="F")]}
     if "detpos" in cfg and np.asarray(cfg["detpos"]).size:
         out["Optode"]["Detector"] = [{"Pos": [float(d[0]), float(d[1]), float(d[2])], "R": float(d[3])}
                                      for d in np.asarray(cfg["detpos"], float).reshape(-1, 4)]
@@ -241,7 +251,8 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
     if keep_field:
         ng = max(1, int((cfg["tend"] - cfg["tstart"]) / cfg["tstep"] + 0.5))
         f = np.fromfile(tmp / f"{session}.mc2", dtype=np.float32)
-        res["flux"] = f.reshape(vol.shape + (ng,), order="F")
+        # photon-sharing channels fold into the first axis, (srcnum * nx, ny, nz, nt), as pmcx shapes it
+        res["flux"] = f.reshape((f.size // (vol.shape[1] * vol.shape[2] * ng),) + vol.shape[1:] + (ng,), order="F")
     mct = tmp / f"{session}.mct"
     if mct.exists():
         # trajectory records after a History header (src/mcx_utils.c:982-1017): 6 floats each
