@@ -223,6 +223,24 @@ class PreparedConfig:
             self.polprop = (abi.POLMedium * len(pp))(*[abi.POLMedium(*map(float, r)) for r in pp])
             c.polprop = C.addressof(self.polprop)
             c.polmedianum = len(pp)
+        if cfg.get("invcdf") is not None and np.asarray(cfg["invcdf"]).size:
+            # user phase function: the inverse CDF of cos(theta) between the ends -1 and 1 that
+            # pmcx adds (src/pmcx.cpp:843-866)
+            inv = np.asarray(cfg["invcdf"], np.float32).ravel(order="F")
+            if (inv < -1).any() or (inv > 1).any() or (np.diff(inv) < 0).any():
+                raise MCXError(-4, "cfg.invcdf contains invalid data; it must be a monotonically increasing vector with all values between -1 and 1")
+            tab = np.concatenate([[-1.0], inv, [1.0]]).astype(np.float32)
+            self.keep.append(tab)
+            c.invcdf = tab.ctypes.data
+            c.nphase = tab.size
+        if cfg.get("angleinvcdf") is not None and np.asarray(cfg["angleinvcdf"]).size:
+            # launch zenith angles / pi as an inverse CDF (src/pmcx.cpp:868-890)
+            ang = np.ascontiguousarray(np.asarray(cfg["angleinvcdf"], np.float32).ravel(order="F"))
+            if (ang < 0).any() or (ang > 1).any() or (np.diff(ang) < 0).any():
+                raise MCXError(-4, "cfg.angleinvcdf contains invalid data; it must be a monotonically increasing vector with all values between 0 and 1")
+            self.keep.append(ang)
+            c.angleinvcdf = ang.ctypes.data
+            c.nangle = ang.size
         if "srcpattern" in cfg and cfg["srcpattern"] is not None:
             # x fastest, as pmcx passes a (param1.w, param2.w) or (nx, ny, nz) array (src/pmcx.cpp)
             pat = np.asarray(cfg["srcpattern"], dtype=np.float32).ravel(order="F").copy()

@@ -235,8 +235,8 @@ uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
 }  // namespace
 
 // Source settings the engine takes (src/mcx_core.cu:1261-1640): every MCX_SRC_* shape with one
-// source, photon sharing (srcnum > 1 patterns of a pattern source); not extra sources or a
-// launch-angle table.
+// source, photon sharing (srcnum > 1 patterns of a pattern source) and launch-angle tables; not
+// extra sources.
 void check_source(const Config* cfg) {
     if ((unsigned char)cfg->srctype >= kNumSrcTypes) MCXG_RAISE(-6, "unknown source type");
     if (std::isinf(cfg->srcdir.w) && cfg->srcdir.w > 0.f)
@@ -249,7 +249,8 @@ void check_source(const Config* cfg) {
             MCXG_RAISE(-6, "photon sharing is supported with flux, fluence and energy outputs, without replay");
     }
     if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
-    if (cfg->nangle) MCXG_RAISE(-6, "launch-angle distributions (angleinvcdf) are not supported by the GB300 engine");
+    if (cfg->nangle && !cfg->angleinvcdf) MCXG_RAISE(-4, "nangle is set but the launch-angle table (angleinvcdf) is empty");
+    if (cfg->nphase > 2 && !cfg->invcdf) MCXG_RAISE(-4, "nphase is set but the phase-function table (invcdf) is empty");
     const int st = (unsigned char)cfg->srctype;
     if ((st == kSrcPattern || st == kSrcPattern3D) && !cfg->srcpattern)
         MCXG_RAISE(-4, "the 'srcpattern' field can not be empty when your 'srctype' is 'pattern'");
@@ -300,9 +301,10 @@ void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
         std::memcpy(&smed, &cfg->srcparam2.w, 4);
     }
     int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
-    if (k.srctype == kSrcPencil) {
+    if (k.srctype == kSrcPencil && cfg->nangle == 0) {
         // every pencil photon follows the same path through the void: traced once here, the
-        // photons start from its end (src/mcx_core.cu:1236-1243, 1652-1672)
+        // photons start from its end (src/mcx_core.cu:1236-1243, 1652-1672); with a launch-angle
+        // table each photon has its own direction and the kernel launches it (MCX's non-pencil path)
         if ((smed & kMED_MASK) == 0) {
             const int id = host_skipvoid(cfg, p, v, t, fd);
             if (id < 0) {
@@ -339,6 +341,7 @@ struct Session {
     size_t nvox = 0, fieldlen = 0;
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
+    DevBuf phase_tab, angle_tab;   // user phase function and launch-angle inverse CDFs
     DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount, smat;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
@@ -358,7 +361,7 @@ struct Session {
         labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
-        pattern.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
+        pattern.release(); phase_tab.release(); angle_tab.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
         seeddata.release(); voxwords.release(); voxwords2.release(); traj.release(); trajcount.release(); smat.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
@@ -484,6 +487,20 @@ struct Session {
             CK(cudaMemcpyAsync(pattern.p, cfg->srcpattern, npat * sizeof(float), cudaMemcpyHostToDevice, stream));
         }
         fill_source(k, cfg, pattern.as<float>());
+        // user phase function and launch-angle tables (src/mcx_core.cu:1804-1836 stage them in
+        // shared memory; here they are read through the read-only cache)
+        k.nphase = (cfg->nphase > 2) ? (int)cfg->nphase : 0;
+        k.nangle = (int)cfg->nangle;
+        if (k.nphase) {
+            phase_tab.alloc(k.nphase * sizeof(float), stream);
+            CK(cudaMemcpyAsync(phase_tab.p, cfg->invcdf, k.nphase * sizeof(float), cudaMemcpyHostToDevice, stream));
+            k.invcdf = phase_tab.as<float>();
+        }
+        if (k.nangle) {
+            angle_tab.alloc(k.nangle * sizeof(float), stream);
+            CK(cudaMemcpyAsync(angle_tab.p, cfg->angleinvcdf, k.nangle * sizeof(float), cudaMemcpyHostToDevice, stream));
+            k.angleinvcdf = angle_tab.as<float>();
+        }
         {
             std::lock_guard<std::mutex> g(g_override_mu);
             k.step_cap = g_step_cap;      // a photon longer than this is a fault: flagged and stopped

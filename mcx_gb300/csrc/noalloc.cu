@@ -89,6 +89,10 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
         MCXG_RAISE(-6, "the allocation-free entry point runs no polarised media (they need a Mueller table buffer)");
     if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly))
         MCXG_RAISE(-6, "the allocation-free entry point saves no trajectories (they need a record buffer)");
+    if (cfg->issaveref)
+        MCXG_RAISE(-6, "the allocation-free entry point records no diffuse reflectance");
+    if (cfg->nphase > 2 || cfg->nangle)
+        MCXG_RAISE(-6, "the allocation-free entry point takes no phase-function or launch-angle tables (they need device buffers)");
     k.minenergy = cfg->minenergy;
     k.gscatter = (float)cfg->gscatter;
     k.maxvoidstep = (float)cfg->maxvoidstep;

@@ -347,7 +347,7 @@ __device__ __forceinline__ void offset_normal(Launch& L, float r, float sphi, fl
 // maxvoidstep times; false when every attempt missed.
 // Inlined: a call here (tried) forced the loop's live state through the call's stack frame and
 // cost the planar deck 21% (143.7 K against 182.7 K photons/ms at 1e8 photons).
-template <bool WORDS>
+template <bool WORDS, bool FULL>
 __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long long& r0, unsigned long long& r1, Launch& L) {
     const float4 p1 = P.src_param1, p2 = P.src_param2;
     constexpr float kJustBelowOne = 0.9998f;                      // src/mcx_const.h:50
@@ -520,11 +520,36 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
             canfocus = (P.srctype == kSrcSlit);
             break;
         }
+        case kSrcPencil:            // only with a launch-angle table (MCX's non-pencil path then)
+            break;
         default:
             return false;
         }
         if (fabsf(L.w) <= P.minenergy) continue;
-        if (canfocus && P.src_focus != kFocusNone) {
+        if (FULL && P.nangle > 0) {
+            // launch zenith angle from the user's inverse CDF (src/mcx_core.cu:1581-1605): read
+            // directly with a positive focal length, else interpolated; the azimuth is uniform
+            const int na = P.nangle;
+            const float f = P.src_focal;
+            float ang = rng_next(r0, r1), c;
+            if (P.src_focus == kFocusLength && f > 0.f) {
+                ang = fminf(ang * na, na - kEPS);
+                c = __ldg(P.angleinvcdf + min((int)ang, na - 1));
+            } else {
+                ang = fminf(ang * (na - 1), na - 1 - kEPS);
+                const float fr = ang - (int)ang;
+                c = (1.f - fr) * __ldg(P.angleinvcdf + min((int)ang, na - 1)) +
+                    fr * __ldg(P.angleinvcdf + min((int)ang + 1, na - 1));
+            }
+            float st, ct, sphi, cphi;
+            sincosf(c * 3.14159265358979f, &st, &ct);
+            sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
+            // MCX resets the direction to srcdir for focal lengths in [0, 1.5)
+            if (P.src_focus == kFocusNone || (P.src_focus == kFocusLength && f >= 0.f && f < 1.5f)) {
+                L.vx = P.src_v.x; L.vy = P.src_v.y; L.vz = P.src_v.z;
+            }
+            rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
+        } else if (canfocus && P.src_focus != kFocusNone) {
             // the host classifies the focal length: fast-math code must not test for NaN or inf
             const float f = P.src_focal;
             float sphi, cphi, st, ct;
@@ -858,7 +883,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 S.seed0[2 * tid + 1] = r1;
             }
             bool entered = false;
-            if (start && P.srctype == kSrcPencil) {
+            if (start && P.srctype == kSrcPencil && !(FULL && P.nangle > 0)) {
                 // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
                 // skipping and specular loss of skipvoid() are folded into src_* by the host)
                 px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
@@ -872,7 +897,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 entered = true;
             } else if (AREA && start) {
                 Launch L;
-                entered = launch_source<WORDS>(P, r0, r1, L);
+                entered = launch_source<WORDS, FULL>(P, r0, r1, L);
                 if (entered) {
                     px = L.px; py = L.py; pz = L.pz; w = L.w;
                     vx = L.vx; vy = L.vy; vz = L.vz;
@@ -965,6 +990,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     }
                     sincosf(pol_phi, &sphi, &cphi);
                     ct = cosf(pol_theta);
+                } else if (FULL && P.nphase > 2) {
+                    // user phase function (src/mcx_core.cu:1937-1944): cos(theta) interpolated in
+                    // the inverse CDF, whose ends are -1 and 1
+                    const int np = P.nphase;
+                    const float a = u_th * (np - 1);
+                    const float fr = a - (int)a;
+                    ct = (1.f - fr) * __ldg(P.invcdf + min((int)a, np - 1)) + fr * __ldg(P.invcdf + min((int)a + 1, np - 1));
                 } else if (fabsf(g) > kEPS) {                           // Henyey-Greenstein, 1946-1959
                     const float g2 = g * g;
                     float tmp = __fdividef(1.f - g2, 1.f - g + 2.f * g * u_th);
@@ -1527,7 +1559,9 @@ bool transport_general(const KParams& p) { return transport_mode(p) != 0; }
 int transport_mode(const KParams& p) {
     if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
-    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref || p.srcnum > 1) return 2;
+    if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref || p.srcnum > 1 ||
+        p.nphase > 2 || p.nangle > 0)
+        return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
 

@@ -127,6 +127,10 @@ struct KParams {
     int save2pt;                    // record the field
     int saveref;                    // diffuse reflectance: -w into the void voxel a photon ends in
     int srcnum;                     // photon sharing: patterns (field channels); 1 otherwise
+    const float* invcdf;            // user phase function: inverse CDF of cos(theta), nphase values
+    int nphase;                     // > 2 replaces Henyey-Greenstein
+    const float* angleinvcdf;       // launch zenith angles / pi, inverse CDF, nangle values
+    int nangle;                     // > 0: launch directions from the table
     int outputtype;                 // 0 flux, 1 fluence, 2 energy
     float minenergy;                // Russian roulette threshold (0 = off)
     float gscatter;                 // scattering events after which mus' replaces mus

@@ -169,6 +169,8 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
         session_keys["MaxDetPhoton"] = int(cfg["maxdetphoton"])
     if cfg.get("issaveseed"):
         session_keys["DoSaveSeed"] = 1
+    if cfg.get("invcdf") is not None:
+        out["Domain"]["InverseCDF"] = [float(x) for x in np.asarray(cfg["invcdf"], float).ravel()]
     if cfg.get("issaveref"):
         session_keys["DoSaveRef"] = int(cfg["issaveref"])
     if cfg.get("debuglevel"):
