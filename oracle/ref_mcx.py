@@ -169,8 +169,6 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
         session_keys["MaxDetPhoton"] = int(cfg["maxdetphoton"])
     if cfg.get("issaveseed"):
         session_keys["DoSaveSeed"] = 1
-    if cfg.get("invcdf") is not None:
-        out["Domain"]["InverseCDF"] = [float(x) for x in np.asarray(cfg["invcdf"], float).ravel()]
     if cfg.get("issaveref"):
         session_keys["DoSaveRef"] = int(cfg["issaveref"])
     if cfg.get("debuglevel"):
@@ -204,6 +202,9 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
                                      for d in np.asarray(cfg["detpos"], float).reshape(-1, 4)]
     if "bc" in cfg:
         out["Session"]["BCFlags"] = cfg["bc"]
+    if cfg.get("invcdf") is not None:
+        # user phase function (src/mcx_utils.c:2456-2475; MCX adds the ends -1 and 1)
+        out["Domain"]["InverseCDF"] = [float(x) for x in np.asarray(cfg["invcdf"], float).ravel()]
     if "polprop" in cfg and np.asarray(cfg["polprop"]).size:
         # polarised media: Domain.MieScatter, Optode.Source.WaveLength / IQUV (src/mcx_utils.c:2360-2400, 2731, 2873)
         out["Domain"]["MieScatter"] = [{"mua": float(r[0]), "radius": float(r[1]), "rho": float(r[2]),
