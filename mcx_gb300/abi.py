@@ -53,6 +53,9 @@ class uint3(C.Structure):
 
 Medium = _layout("Medium", [("mua", C.c_float, 4), ("mus", C.c_float, 4), ("g", C.c_float, 4), ("n", C.c_float, 4)])
 
+ExtraSrc = _layout("ExtraSrc", [("srcpos", float4, 16), ("srcdir", float4, 16), ("srcparam1", float4, 16),
+                                ("srcparam2", float4, 16)])
+
 POLMedium = _layout("POLMedium", [("mua", C.c_float, 4), ("r", C.c_float, 4), ("rho", C.c_float, 4),
                                   ("nsph", C.c_float, 4), ("nmed", C.c_float, 4)])
 

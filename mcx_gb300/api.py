@@ -213,7 +213,20 @@ class PreparedConfig:
             c.bc = str(cfg["bc"]).encode()[:12]
         for key, n in (("srcpos", 4), ("srcdir", 4), ("srcparam1", 4), ("srcparam2", 4), ("srciquv", 4)):
             if key in cfg:
-                _set_vec(getattr(c, key), cfg[key], n)
+                _set_vec(getattr(c, key), np.asarray(cfg[key], np.float64).reshape(-1)[:4]
+                         if np.ndim(cfg[key]) < 2 else np.asarray(cfg[key])[0], n)
+        # several sources: rows 1.. of srcpos / srcdir / srcparam1 / srcparam2 (src/pmcx.cpp:470-600)
+        nsrc = max((len(cfg[k]) for k in ("srcpos", "srcdir", "srcparam1", "srcparam2")
+                    if k in cfg and np.ndim(cfg[k]) == 2), default=1)
+        if nsrc > 1:
+            self.srcdata = (abi.ExtraSrc * (nsrc - 1))()
+            for k, field in (("srcpos", "srcpos"), ("srcdir", "srcdir"), ("srcparam1", "srcparam1"), ("srcparam2", "srcparam2")):
+                if k in cfg and np.ndim(cfg[k]) == 2:
+                    rows = np.asarray(cfg[k], np.float64)
+                    for i in range(1, min(nsrc, len(rows))):
+                        _set_vec(getattr(self.srcdata[i - 1], field), rows[i], 4)
+            c.srcdata = C.addressof(self.srcdata)
+            c.extrasrclen = nsrc - 1
         if "steps" in cfg:
             _set_vec(c.steps, cfg["steps"], 3)
         if "polprop" in cfg and cfg["polprop"] is not None and np.asarray(cfg["polprop"]).size:
@@ -374,6 +387,8 @@ def _attach_field(pc: PreparedConfig):
         maxgate *= max(1, int(c.detnum))     # one block of gates per detector
     if ord(c.outputtype) in (6, 8):
         maxgate *= 2                         # RF replay: real blocks, then imaginary blocks
+    if int(c.extrasrclen) and int(c.srcid) < 0:
+        maxgate *= int(c.extrasrclen) + 1    # every source apart: one block of gates per source
     # photon sharing: one channel per pattern, adjacent per voxel (src/mcx_core.cu:2782)
     pc.chans = int(c.srcnum) if (_srctype_code(c) in (5, 15) and int(c.srcnum) > 1) else 1
     flux = None

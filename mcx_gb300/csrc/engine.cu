@@ -235,8 +235,8 @@ uint32_t host_label(const Config* cfg, long id) { return cfg->vol[id]; }
 }  // namespace
 
 // Source settings the engine takes (src/mcx_core.cu:1261-1640): every MCX_SRC_* shape with one
-// source, photon sharing (srcnum > 1 patterns of a pattern source) and launch-angle tables; not
-// extra sources.
+// source or several (extrasrclen), photon sharing (srcnum > 1 patterns of a pattern source) and
+// launch-angle tables.
 void check_source(const Config* cfg) {
     if ((unsigned char)cfg->srctype >= kNumSrcTypes) MCXG_RAISE(-6, "unknown source type");
     if (std::isinf(cfg->srcdir.w) && cfg->srcdir.w > 0.f)
@@ -248,7 +248,15 @@ void check_source(const Config* cfg) {
         if (cfg->seed == kSEED_FROM_FILE || (cfg->outputtype != otFlux && cfg->outputtype != otFluence && cfg->outputtype != otEnergy))
             MCXG_RAISE(-6, "photon sharing is supported with flux, fluence and energy outputs, without replay");
     }
-    if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
+    if (cfg->extrasrclen) {              // src/mcx_utils.c:1679-1692
+        if (!cfg->srcdata) MCXG_RAISE(-4, "extrasrclen is set but the extra sources (srcdata) are missing");
+        if (cfg->srcnum > 1) MCXG_RAISE(-4, "simulating multiple sources currently can not be used with photon-sharing");
+        if (cfg->srcid > (int)cfg->extrasrclen + 1) MCXG_RAISE(-4, "srcid exceeds total defined source count");
+        if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "replay with extra sources is not supported by the GB300 engine");
+        for (unsigned i = 0; i < cfg->extrasrclen; i++)
+            if (std::isinf(cfg->srcdata[i].srcdir.w) && cfg->srcdata[i].srcdir.w > 0.f)
+                MCXG_RAISE(-4, "a focal length of +inf is not a valid source setting (srcdir.w)");
+    }
     if (cfg->nangle && !cfg->angleinvcdf) MCXG_RAISE(-4, "nangle is set but the launch-angle table (angleinvcdf) is empty");
     if (cfg->nphase > 2 && !cfg->invcdf) MCXG_RAISE(-4, "nphase is set but the phase-function table (invcdf) is empty");
     const int st = (unsigned char)cfg->srctype;
@@ -301,7 +309,7 @@ void fill_source(KParams& k, const Config* cfg, const float* d_pattern) {
         std::memcpy(&smed, &cfg->srcparam2.w, 4);
     }
     int fd[3] = {(int)std::floor(p.x), (int)std::floor(p.y), (int)std::floor(p.z)};
-    if (k.srctype == kSrcPencil && cfg->nangle == 0) {
+    if (k.srctype == kSrcPencil && cfg->nangle == 0 && cfg->extrasrclen == 0) {
         // every pencil photon follows the same path through the void: traced once here, the
         // photons start from its end (src/mcx_core.cu:1236-1243, 1652-1672); with a launch-angle
         // table each photon has its own direction and the kernel launches it (MCX's non-pencil path)
@@ -342,6 +350,7 @@ struct Session {
     int totalgates = 1;
     DevBuf labels, field, shadow, field64, outbuf, detp, detcount, energy, counters, work, err, detpos, pattern;
     DevBuf phase_tab, angle_tab;   // user phase function and launch-angle inverse CDFs
+    DevBuf extra_src;              // extra sources, 5 float4 each
     DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount, smat;
     unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
@@ -361,7 +370,7 @@ struct Session {
         labels.release(); field.release(); shadow.release(); field64.release(); outbuf.release(); detp.release();
         words.release();
         detcount.release(); energy.release(); counters.release(); work.release(); err.release(); detpos.release();
-        pattern.release(); phase_tab.release(); angle_tab.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
+        pattern.release(); phase_tab.release(); angle_tab.release(); extra_src.release(); replay_seed.release(); replay_w.release(); replay_tof.release(); replay_detid.release();
         seeddata.release(); voxwords.release(); voxwords2.release(); traj.release(); trajcount.release(); smat.release();
         // every buffer above is freed on `stream`, which must outlive them
         if (stream) cudaStreamSynchronize(stream);
@@ -406,6 +415,8 @@ struct Session {
         // a replay of every detector at once keeps one block of gates per detector
         // (src/mcx_core.cu:2907-2913)
         blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
+        // every source kept apart (srcid -1): one block of gates per source (src/mcx_core.cu:3039)
+        if (cfg->extrasrclen && cfg->srcid < 0) blocks = cfg->extrasrclen + 1;
         // RF replay outputs carry a real and an imaginary field (src/mcx_core.cu:2908-2913)
         halves = (cfg->outputtype == otRF || cfg->outputtype == otRFmus) ? 2 : 1;
         if ((size_t)maxgate * blocks * halves * per_gate > budget)
@@ -489,6 +500,33 @@ struct Session {
         fill_source(k, cfg, pattern.as<float>());
         // user phase function and launch-angle tables (src/mcx_core.cu:1804-1836 stage them in
         // shared memory; here they are read through the read-only cache)
+        k.nextra = (int)cfg->extrasrclen;
+        k.srcid = cfg->srcid;
+        if (k.nextra) {
+            // position (weight 1 when 0), unit direction, param1, param2, and the focal length
+            // classified on the host as for the primary source (src/mcx_utils.c:1688-1692)
+            std::vector<float4> xs;
+            for (unsigned i = 0; i < cfg->extrasrclen; i++) {
+                const ExtraSrc& e = cfg->srcdata[i];
+                float4 p = e.srcpos;
+                if (p.w == 0.f) p.w = 1.f;
+                float3 v = f3(e.srcdir.x, e.srcdir.y, e.srcdir.z);
+                const float n = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+                if (n > 0.f) { v.x /= n; v.y /= n; v.z /= n; }
+                const float f = e.srcdir.w;
+                const int focus = std::isnan(f) ? kFocusIsotropic : std::isinf(f) ? kFocusLambertian
+                                : (f != 0.f) ? kFocusLength : kFocusNone;
+                xs.push_back(p);
+                xs.push_back(make_float4(v.x, v.y, v.z, 0.f));
+                xs.push_back(e.srcparam1);
+                xs.push_back(e.srcparam2);
+                xs.push_back(make_float4((float)focus, std::isfinite(f) ? f : 0.f, 0.f, 0.f));
+            }
+            extra_src.alloc(xs.size() * sizeof(float4), stream);
+            CK(cudaMemcpyAsync(extra_src.p, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));
+            k.extrasrc = extra_src.as<float4>();
+        }
         k.nphase = (cfg->nphase > 2) ? (int)cfg->nphase : 0;
         k.nangle = (int)cfg->nangle;
         if (k.nphase) {
@@ -1058,8 +1096,11 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
                 double sc = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
                 if (ot == otFluence) sc *= cfg->tstep;
                 scale = (float)sc;
+                // every source simulated apart: each got 1/(n+1) of the photons (3908-3910)
+                if (cfg->extrasrclen && cfg->srcid < 0) scale *= (float)(cfg->extrasrclen + 1);
             } else if (ot == otEnergy || ot == otL) {
                 scale = (float)(1.0 / cfg->energytot);
+                if (cfg->extrasrclen && cfg->srcid < 0) scale *= (float)(cfg->extrasrclen + 1);
             } else if (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) {
                 // each detector's block over its replayed weight; paths carry unitinmm
                 for (unsigned d = 1; d <= S.blocks; d++) {

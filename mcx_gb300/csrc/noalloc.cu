@@ -89,6 +89,8 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
         MCXG_RAISE(-6, "the allocation-free entry point runs no polarised media (they need a Mueller table buffer)");
     if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly))
         MCXG_RAISE(-6, "the allocation-free entry point saves no trajectories (they need a record buffer)");
+    if (cfg->extrasrclen)
+        MCXG_RAISE(-6, "the allocation-free entry point runs one source (extra sources need a device buffer)");
     if (cfg->issaveref)
         MCXG_RAISE(-6, "the allocation-free entry point records no diffuse reflectance");
     if (cfg->nphase > 2 || cfg->nangle)

@@ -289,11 +289,13 @@ void validate(Config* cfg) {
     if (cfg->replaydet > (int)cfg->detnum) MCXG_RAISE(-4, "replay detector ID exceeds the maximum detector number");
     if (cfg->replaydet == -1 && cfg->detnum == 1) cfg->replaydet = 1;
 
-    if (cfg->extrasrclen) MCXG_RAISE(-6, "multiple sources are not supported by the GB300 engine");
 
     // mcx_validatecfg: grid-origin shift, time gates (src/mcx_utils.c:3761-3795)
     if (!cfg->issrcfrom0) {
         cfg->srcpos.x -= 1.f; cfg->srcpos.y -= 1.f; cfg->srcpos.z -= 1.f;
+        for (uint32_t i = 0; cfg->srcdata && i < cfg->extrasrclen; i++) {      // 3766-3771
+            cfg->srcdata[i].srcpos.x -= 1.f; cfg->srcdata[i].srcpos.y -= 1.f; cfg->srcdata[i].srcpos.z -= 1.f;
+        }
         for (uint32_t i = 0; i < cfg->detnum; i++) {
             cfg->detpos[i].x -= 1.f; cfg->detpos[i].y -= 1.f; cfg->detpos[i].z -= 1.f;
         }

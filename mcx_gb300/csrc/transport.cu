@@ -348,14 +348,21 @@ __device__ __forceinline__ void offset_normal(Launch& L, float r, float sphi, fl
 // Inlined: a call here (tried) forced the loop's live state through the call's stack frame and
 // cost the planar deck 21% (143.7 K against 182.7 K photons/ms at 1e8 photons).
 template <bool WORDS, bool FULL>
-__device__ __forceinline__ bool launch_source(const KParams& P, unsigned long long& r0, unsigned long long& r1, Launch& L) {
-    const float4 p1 = P.src_param1, p2 = P.src_param2;
+__device__ __forceinline__ bool launch_source(const KParams& P, unsigned long long& r0, unsigned long long& r1, Launch& L,
+                                              const float4* __restrict__ alt = nullptr) {
+    // the source: the primary one from the parameters, or an extra source's five float4
+    // (position, direction, param1, param2, (focus class, focal length)) -- full kernel only
+    const bool ALT = FULL && alt != nullptr;
+    const float4 p1 = ALT ? alt[2] : P.src_param1, p2 = ALT ? alt[3] : P.src_param2;
+    const float4 sp = ALT ? alt[0] : P.src_p, sv = ALT ? alt[1] : P.src_v;
+    const int sfocus = ALT ? (int)alt[4].x : P.src_focus;
+    const float sfocal = ALT ? alt[4].y : P.src_focal;
     constexpr float kJustBelowOne = 0.9998f;                      // src/mcx_const.h:50
     for (int attempt = 1; attempt <= (int)P.maxvoidstep; attempt++) {
-        L.px = P.src_p.x; L.py = P.src_p.y; L.pz = P.src_p.z; L.w = P.src_p.w;
-        L.vx = P.src_v.x; L.vy = P.src_v.y; L.vz = P.src_v.z;
+        L.px = sp.x; L.py = sp.y; L.pz = sp.z; L.w = sp.w;
+        L.vx = sv.x; L.vy = sv.y; L.vz = sv.z;
         L.t = 0.f;
-        float ox = P.src_p.x, oy = P.src_p.y, oz = P.src_p.z;     // focus origin
+        float ox = sp.x, oy = sp.y, oz = sp.z;     // focus origin
         bool canfocus = true, located = false;
         switch (P.srctype) {
         case kSrcPlanar: case kSrcPattern: case kSrcPattern3D: case kSrcFourier: case kSrcPencilArray: {
@@ -370,7 +377,7 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                     L.pix = pix;
                     L.w = 1.f;
                 } else {
-                    L.w = P.src_p.w * __ldg(P.srcpattern + pix);
+                    L.w = sp.w * __ldg(P.srcpattern + pix);
                 }
             } else {
                 L.px += rx * p1.x + ry * p2.x; L.py += rx * p1.y + ry * p2.y; L.pz += rx * p1.z + ry * p2.z;
@@ -380,16 +387,16 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                         L.pix = pix;
                         L.w = 1.f;
                     } else {
-                        L.w = P.src_p.w * __ldg(P.srcpattern + pix);
+                        L.w = sp.w * __ldg(P.srcpattern + pix);
                     }
                 } else if (P.srctype == kSrcFourier) {
-                    L.w = P.src_p.w * (cosf((floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w)) * kTWO_PI) *
+                    L.w = sp.w * (cosf((floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w)) * kTWO_PI) *
                                            (1.f - p2.w + floorf(p2.w)) + 1.f) * 0.5f;
                 } else if (P.srctype == kSrcPencilArray) {
                     const float ix = floorf(rx * p1.w) / (p1.w - 1.f), iy = floorf(ry * p2.w) / (p2.w - 1.f);
-                    L.px = P.src_p.x + ix * p1.x + iy * p2.x;
-                    L.py = P.src_p.y + ix * p1.y + iy * p2.y;
-                    L.pz = P.src_p.z + ix * p1.z + iy * p2.z;
+                    L.px = sp.x + ix * p1.x + iy * p2.x;
+                    L.py = sp.y + ix * p1.y + iy * p2.y;
+                    L.pz = sp.z + ix * p1.z + iy * p2.z;
                 }
             }
             ox += (p1.x + p2.x) * 0.5f; oy += (p1.y + p2.y) * 0.5f; oz += (p1.z + p2.z) * 0.5f;
@@ -402,9 +409,9 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                         v2z = s * (L.vx * p1.y - L.vy * p1.x);
             L.px += rx * p1.x + ry * v2x; L.py += rx * p1.y + ry * v2y; L.pz += rx * p1.z + ry * v2z;
             if (P.srctype == kSrcFourierX2D)
-                L.w = P.src_p.w * (sinf((p2.x * rx + p2.z) * kTWO_PI) * sinf((p2.y * ry + p2.w) * kTWO_PI) + 1.f) * 0.5f;
+                L.w = sp.w * (sinf((p2.x * rx + p2.z) * kTWO_PI) * sinf((p2.y * ry + p2.w) * kTWO_PI) + 1.f) * 0.5f;
             else
-                L.w = P.src_p.w * (cosf((p2.x * rx + p2.y * ry + p2.z) * kTWO_PI) * (1.f - p2.w) + 1.f) * 0.5f;
+                L.w = sp.w * (cosf((p2.x * rx + p2.y * ry + p2.z) * kTWO_PI) * (1.f - p2.w) + 1.f) * 0.5f;
             ox += (p1.x + v2x) * 0.5f; oy += (p1.y + v2y) * 0.5f; oz += (p1.z + v2z) * 0.5f;
             break;
         }
@@ -419,11 +426,11 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
             float r;
             if (P.srctype != kSrcGaussian) {
                 r = sqrtf(rng_next(r0, r1) * fabsf(p1.x * p1.x - p1.y * p1.y) + p1.y * p1.y);
-            } else if (fabsf(P.src_focal) < 1e-5f || fabsf(p1.y) < 1e-5f) {
+            } else if (fabsf(sfocal) < 1e-5f || fabsf(p1.y) < 1e-5f) {
                 r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS)) * p1.x;
             } else {
                 const float zr = p1.x * p1.x * 3.14159265358979f / p1.y;        // Rayleigh range
-                r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS) * (1.f + P.src_focal * P.src_focal / (zr * zr))) * p1.x;
+                r = sqrtf(0.5f * -logf(rng_next(r0, r1) + kEPS) * (1.f + sfocal * sfocal / (zr * zr))) * p1.x;
             }
             offset_normal(L, r, sphi, cphi);
             break;
@@ -516,7 +523,7 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
                 r = rsqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
                 L.vx *= r; L.vy *= r; L.vz *= r;
             }
-            ox = P.src_p.x + p1.x * 0.5f; oy = P.src_p.y + p1.y * 0.5f; oz = P.src_p.z + p1.z * 0.5f;
+            ox = sp.x + p1.x * 0.5f; oy = sp.y + p1.y * 0.5f; oz = sp.z + p1.z * 0.5f;
             canfocus = (P.srctype == kSrcSlit);
             break;
         }
@@ -530,9 +537,9 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
             // launch zenith angle from the user's inverse CDF (src/mcx_core.cu:1581-1605): read
             // directly with a positive focal length, else interpolated; the azimuth is uniform
             const int na = P.nangle;
-            const float f = P.src_focal;
+            const float f = sfocal;
             float ang = rng_next(r0, r1), c;
-            if (P.src_focus == kFocusLength && f > 0.f) {
+            if (sfocus == kFocusLength && f > 0.f) {
                 ang = fminf(ang * na, na - kEPS);
                 c = __ldg(P.angleinvcdf + min((int)ang, na - 1));
             } else {
@@ -545,19 +552,19 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
             sincosf(c * 3.14159265358979f, &st, &ct);
             sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
             // MCX resets the direction to srcdir for focal lengths in [0, 1.5)
-            if (P.src_focus == kFocusNone || (P.src_focus == kFocusLength && f >= 0.f && f < 1.5f)) {
-                L.vx = P.src_v.x; L.vy = P.src_v.y; L.vz = P.src_v.z;
+            if (sfocus == kFocusNone || (sfocus == kFocusLength && f >= 0.f && f < 1.5f)) {
+                L.vx = sv.x; L.vy = sv.y; L.vz = sv.z;
             }
             rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
-        } else if (canfocus && P.src_focus != kFocusNone) {
+        } else if (canfocus && sfocus != kFocusNone) {
             // the host classifies the focal length: fast-math code must not test for NaN or inf
-            const float f = P.src_focal;
+            const float f = sfocal;
             float sphi, cphi, st, ct;
-            if (P.src_focus == kFocusIsotropic) {                       // NaN focal length
+            if (sfocus == kFocusIsotropic) {                       // NaN focal length
                 sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
                 sincosf(acosf(2.f * rng_next(r0, r1) - 1.f), &st, &ct);
                 rotate(L.vx, L.vy, L.vz, st, ct, sphi, cphi);
-            } else if (P.src_focus == kFocusLambertian) {               // -inf focal length
+            } else if (sfocus == kFocusLambertian) {               // -inf focal length
                 sincosf(kTWO_PI * rng_next(r0, r1), &sphi, &cphi);
                 st = sqrtf(rng_next(r0, r1));
                 ct = sqrtf(1.f - st * st);
@@ -572,7 +579,7 @@ __device__ __forceinline__ bool launch_source(const KParams& P, unsigned long lo
         }
         // launch voxel: the host's for point sources, else where the photon stands
         unsigned lab = 0u;
-        if (located) {
+        if (located && !ALT) {
             L.idx = P.src_idx;
             L.ix = P.src_fx; L.iy = P.src_fy; L.iz = P.src_fz;
             lab = P.src_label;
@@ -637,7 +644,7 @@ __device__ __forceinline__ void share_deposit(const KParams& P, unsigned pix, si
 // One trajectory record (savedebugdata, src/mcx_core.cu:427-442): photon id as uint bits, the
 // position in grid units, the weight and the source id (0: one source).  Records past traj_max
 // are counted but not written.
-__device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x, float y, float z, float w) {
+__device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x, float y, float z, float w, int src = 0) {
     const unsigned pos = atomicAdd(P.traj_count, 1u);
     if (pos < P.traj_max) {
         float* r = P.traj + (size_t)pos * 6;
@@ -646,7 +653,7 @@ __device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x
         r[2] = y;
         r[3] = z;
         r[4] = w;
-        r[5] = 0.f;
+        r[5] = (float)src;
     }
 }
 
@@ -669,6 +676,7 @@ struct Smem {
     unsigned* pid;                // per thread, trajectories: the photon's id
     float* stokes;                // 4 x blockDim, polarised light: the photon's Stokes vector (I, Q, U, V)
     unsigned* spix;               // per thread, photon sharing: the pattern pixel of its photon
+    int* ssrc;                    // per thread, extra sources: the source (1-based) of its photon
     unsigned* tile;               // deposit tile, fixed point (weight x d_tile_scale)
 };
 
@@ -697,7 +705,8 @@ __device__ __forceinline__ Smem carve(const KParams& P, unsigned char* raw) {
         s.pid = reinterpret_cast<unsigned*>(s.rbin + blockDim.x);
         s.stokes = reinterpret_cast<float*>(s.pid + blockDim.x);
         s.spix = reinterpret_cast<unsigned*>(s.stokes + 4 * blockDim.x);
-        end = reinterpret_cast<float*>(s.spix + blockDim.x);
+        s.ssrc = reinterpret_cast<int*>(s.spix + blockDim.x);
+        end = reinterpret_cast<float*>(s.ssrc + blockDim.x);
     }
     s.tile = reinterpret_cast<unsigned*>(end);
     return s;
@@ -882,8 +891,18 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 S.seed0[2 * tid] = r0;
                 S.seed0[2 * tid + 1] = r1;
             }
+            // extra sources (src/mcx_core.cu:1217-1227): the photon's source, drawn after the seed
+            // is saved when every source runs (srcid 0 or -1)
+            const float4* alt = nullptr;
+            if (FULL && start && P.nextra) {
+                int k = 1;
+                if (P.srcid > 1) k = P.srcid;
+                else if (P.srcid <= 0) k = (int)(rng_next(r0, r1) * 0.9998f * (P.nextra + 1)) + 1;
+                S.ssrc[tid] = k;
+                if (k > 1) alt = P.extrasrc + 5 * (k - 2);
+            }
             bool entered = false;
-            if (start && P.srctype == kSrcPencil && !(FULL && P.nangle > 0)) {
+            if (start && P.srctype == kSrcPencil && !(FULL && (P.nangle > 0 || P.nextra))) {
                 // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
                 // skipping and specular loss of skipvoid() are folded into src_* by the host)
                 px = P.src_p.x; py = P.src_p.y; pz = P.src_p.z; w = P.src_p.w;
@@ -897,7 +916,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 entered = true;
             } else if (AREA && start) {
                 Launch L;
-                entered = launch_source<WORDS, FULL>(P, r0, r1, L);
+                entered = launch_source<WORDS, FULL>(P, r0, r1, L, alt);
                 if (entered) {
                     px = L.px; py = L.py; pz = L.pz; w = L.w;
                     vx = L.vx; vy = L.vy; vz = L.vz;
@@ -933,7 +952,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.stokes[2 * B + tid] = P.srciquv.z;
                     S.stokes[3 * B + tid] = P.srciquv.w;
                 }
-                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 1681-1687
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 1681-1687
                 alive = true;
             }
             const unsigned attempted = __ballot_sync(kFull, start), ran = __ballot_sync(kFull, entered);
@@ -1058,7 +1077,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 nscat++;
                 rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                 c_scat++;
-                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 2068-2074
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 2068-2074
             } else {
                 nscat = 0;
             }
@@ -1185,7 +1204,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (weight != 0.f) {
                     rec = true;
                     c_dep++;
-                    const size_t addr = (size_t)idxold + (size_t)tshift * P.nvox;
+                    // all sources kept apart (srcid -1): one block of gates per source (2225-2227)
+                    const int sblk = (FULL && P.nextra && P.srcid < 0) ? (S.ssrc[tid] - 1) * P.maxgate : 0;
+                    const size_t addr = (size_t)idxold + (size_t)(tshift + sblk) * P.nvox;
                     // the index range of the tile box (empty without a tile) screens most deposits out
                     // with one compare before the box test
                     if (FULL && P.srcnum > 1) {
@@ -1319,7 +1340,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != prn.w)) {
-                    if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);     // 2435-2441
+                    if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 2435-2441
                     float Rtotal = 1.f;
                     const float a2 = n1 * n1, b2 = prn.w * prn.w;
                     const float va = (axis == 0) ? vx : ((axis == 1) ? vy : vz);
@@ -1386,12 +1407,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
-            if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w);         // 1116-1122
+            if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);         // 1116-1122
             if (FULL && P.saveref && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f) {
                 // diffuse reflectance (1124-1165): the weight leaving into a void voxel of the grid,
                 // negated, in that voxel at the photon's gate (a photon before the first gate, which
                 // MCX would write below the field, is left out)
-                const int ts = min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b)));
+                int ts = min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b)));
+                if (ts >= 0 && P.nextra && P.srcid < 0) ts += (S.ssrc[tid] - 1) * P.maxgate;
                 if (ts >= 0) {
                     if (P.srcnum > 1) share_deposit(P, S.spix[tid], (size_t)idx + (size_t)ts * P.nvox, -w);
                     else field_add_large(P, (size_t)idx + (size_t)ts * P.nvox, -w);
@@ -1410,7 +1432,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     if (slot < P.maxdet) {
                         float* rec = P.detp + (size_t)slot * P.reclen;
                         unsigned k = 0;
-                        if (P.savedetflag & 0x1u) rec[k++] = (float)detid;
+                        // with every source running, the source id sits above bit 16 (381-384)
+                        if (P.savedetflag & 0x1u)
+                            rec[k++] = (float)((FULL && P.nextra && P.srcid <= 0) ? (detid | (S.ssrc[tid] << 16)) : detid);
                         for (unsigned i = 0; i < P.partialdata; i++) rec[k++] = S.ppath[i * B + tid];
                         if (P.savedetflag & 0x10u) { rec[k++] = px; rec[k++] = py; rec[k++] = pz; }
                         if (P.savedetflag & 0x20u) { rec[k++] = vx; rec[k++] = vy; rec[k++] = vz; }
@@ -1541,7 +1565,7 @@ size_t transport_smem_bytes(const KParams& p, int block, bool savedet) {
     b += 4 * sizeof(unsigned) * (size_t)block;
     b += sizeof(float) * kNumEnergy * (size_t)block;
     if (savedet) b += sizeof(float) * (size_t)p.partialdata * block;
-    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 11 * sizeof(float)) * (size_t)block;
+    if (transport_mode(p) >= 2) b += 8 + (2 * sizeof(unsigned long long) + 12 * sizeof(float)) * (size_t)block;
     if (p.tile_on) b += sizeof(unsigned) * (size_t)p.tnx * p.tny * p.tnz * p.tng;
     return b;
 }
@@ -1560,7 +1584,7 @@ int transport_mode(const KParams& p) {
     if (p.mediaformat == kMedia2LabelSplit) return 4;
     if (media_words(p.mediaformat)) return 3;
     if (p.replay || p.saveseed || p.outputtype > kOutEnergy || p.traj || p.polarized || p.saveref || p.srcnum > 1 ||
-        p.nphase > 2 || p.nangle > 0)
+        p.nphase > 2 || p.nangle > 0 || p.nextra > 0)
         return 2;
     return (p.srctype != kSrcPencil) ? 1 : 0;
 }
@@ -1593,7 +1617,7 @@ void place_tile(KParams& k, int kb) {
     k.tile_on = 0;
     // area sources spread their deposits: only point sources get a tile; replay and path-length
     // outputs add other quantities than the absorbed weight the tile's scale is sized for
-    if (!k.save2pt || !k.src_ok || !src_is_point(k.srctype) || k.replay || k.outputtype > kOutEnergy) return;
+    if (!k.save2pt || !k.src_ok || !src_is_point(k.srctype) || k.replay || k.outputtype > kOutEnergy || k.nextra) return;
     const int elems = kb * 1024 / (int)sizeof(unsigned);
     int tg = std::min(k.maxgate, 4);
     int edge = 1;

@@ -26,6 +26,7 @@ def _probe_offsets(include_dir: Path, header: str, tmp_path: Path) -> dict[str, 
     lines.append('printf("sizeof_History %zu\\n", sizeof(History));')
     lines.append('printf("sizeof_Medium %zu\\n", sizeof(Medium));')
     lines.append('printf("sizeof_POLMedium %zu\\n", sizeof(POLMedium));')
+    lines.append('printf("sizeof_ExtraSrc %zu\\n", sizeof(ExtraSrc));')
     lines.append("return 0;}")
     src = tmp_path / "probe.c"
     src.write_text("\n".join(lines))
@@ -49,6 +50,7 @@ def test_ctypes_mirror_matches_header(engine, tmp_path):
     assert C.sizeof(abi.History) == c["sizeof_History"]
     assert C.sizeof(abi.Medium) == c["sizeof_Medium"]
     assert C.sizeof(abi.POLMedium) == c["sizeof_POLMedium"]
+    assert C.sizeof(abi.ExtraSrc) == c["sizeof_ExtraSrc"]
 
 
 @pytest.mark.skipif(not (REFERENCE_SRC / "mcx_utils.h").exists(), reason="reference headers not present")
