@@ -34,7 +34,7 @@ _DEBUG_CHARS = "RMPT"            # -D letters: RNG test, trajectories, progress,
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "sradius", "minenergy", "unitinmm", "omega", "lambda"]
 _SCALARS_CHAR = ["isreflect", "isref3", "isrefint", "isnormalized", "issrcfrom0", "autopilot", "issaveref",
                  "issaveexit", "ismomentum", "isspecular", "issave2pt", "issavedet", "isgpuinfo", "isrowmajor",
-                 "issaveseed", "faststep"]
+                 "issaveseed", "faststep", "istrajstokes"]
 
 
 class MCXError(RuntimeError):
@@ -421,8 +421,9 @@ def _take_traj(pc: PreparedConfig):
     ptr, n = c.exportdebugdata, int(c.debugdatalen)
     traj = None
     if ptr:
-        buf = (C.c_float * (6 * n)).from_address(ptr) if n else None
-        traj = np.frombuffer(buf, dtype=np.float32).copy().reshape((6, n), order="F") if n else np.zeros((6, 0), np.float32)
+        rl = 10 if c.istrajstokes != b"\x00" else 6          # with the Stokes vector: 10 floats
+        buf = (C.c_float * (rl * n)).from_address(ptr) if n else None
+        traj = np.frombuffer(buf, dtype=np.float32).copy().reshape((rl, n), order="F") if n else np.zeros((rl, 0), np.float32)
         libc.free(C.c_void_p(ptr))
         c.exportdebugdata = None
         c.debugdatalen = 0

@@ -592,7 +592,8 @@ struct Session {
         if (cfg->debuglevel & (kDebugMove | kDebugMoveOnly)) {
             // trajectory records (src/mcx_core.cu:3158-3160): maxjumpdebug x 6 floats
             k.traj_max = cfg->maxjumpdebug;
-            traj.alloc((size_t)std::max(1u, k.traj_max) * kTrajRecLen * sizeof(float), stream);
+            k.traj_reclen = (int)(kTrajRecLen + (cfg->istrajstokes ? 4u : 0u));
+            traj.alloc((size_t)std::max(1u, k.traj_max) * k.traj_reclen * sizeof(float), stream);
             trajcount.alloc(sizeof(unsigned), stream);
             k.traj = traj.as<float>();
             k.traj_count = trajcount.as<unsigned>();
@@ -1055,10 +1056,10 @@ void append_trajectory(Config* cfg, Session& S) {
     rec = std::min(rec, S.kp.traj_max);
     if (rec) {
         cfg->exportdebugdata = (float*)realloc(cfg->exportdebugdata,
-                                               ((size_t)cfg->debugdatalen + rec) * kTrajRecLen * sizeof(float));
+                                               ((size_t)cfg->debugdatalen + rec) * S.kp.traj_reclen * sizeof(float));
         if (!cfg->exportdebugdata) MCXG_RAISE(-4, "out of host memory for the trajectory records");
-        CK(cudaMemcpyAsync(cfg->exportdebugdata + (size_t)cfg->debugdatalen * kTrajRecLen, S.traj.p,
-                           (size_t)rec * kTrajRecLen * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaMemcpyAsync(cfg->exportdebugdata + (size_t)cfg->debugdatalen * S.kp.traj_reclen, S.traj.p,
+                           (size_t)rec * S.kp.traj_reclen * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
         CK(cudaStreamSynchronize(S.stream));
         cfg->debugdatalen += rec;
     }

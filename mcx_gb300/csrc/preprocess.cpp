@@ -334,6 +334,9 @@ void validate(Config* cfg) {
 
     // polarised media (src/mcx_utils.c:1569-1591): label volumes only, one sphere population per
     // medium after the background, a wavelength, and a Stokes vector of non-negative intensity
+    // Stokes vectors in trajectories only for trajectories of polarised runs (src/mcx_utils.c:1549-1552)
+    if (!(cfg->debuglevel & (kDebugMove | kDebugMoveOnly)) || !(cfg->mediabyte <= 4 && cfg->polmedianum > 0))
+        cfg->istrajstokes = 0;
     if (cfg->polprop && cfg->polmedianum) {
         if (cfg->mediabyte > 4) MCXG_RAISE(-1, "Unsupported media format");
         if (cfg->medianum != cfg->polmedianum + 1) MCXG_RAISE(-6, "number of particle types does not match number of media");

@@ -644,10 +644,18 @@ __device__ __forceinline__ void share_deposit(const KParams& P, unsigned pix, si
 // One trajectory record (savedebugdata, src/mcx_core.cu:427-442): photon id as uint bits, the
 // position in grid units, the weight and the source id (0: one source).  Records past traj_max
 // are counted but not written.
-__device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x, float y, float z, float w, int src = 0) {
+// With istrajstokes (polarised runs) the record continues with the Stokes vector (453-462).
+__device__ __forceinline__ void traj_save(const KParams& P, unsigned id, float x, float y, float z, float w, int src,
+                                          const float* stk, unsigned stride) {
     const unsigned pos = atomicAdd(P.traj_count, 1u);
     if (pos < P.traj_max) {
-        float* r = P.traj + (size_t)pos * 6;
+        float* r = P.traj + (size_t)pos * (unsigned)P.traj_reclen;
+        if (P.traj_reclen == 10) {
+            r[6] = stk[0];
+            r[7] = stk[stride];
+            r[8] = stk[2 * stride];
+            r[9] = stk[3 * stride];
+        }
         r[0] = __uint_as_float(id);
         r[1] = x;
         r[2] = y;
@@ -952,7 +960,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.stokes[2 * B + tid] = P.srciquv.z;
                     S.stokes[3 * B + tid] = P.srciquv.w;
                 }
-                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 1681-1687
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0, S.stokes + tid, B);     // 1681-1687
                 alive = true;
             }
             const unsigned attempted = __ballot_sync(kFull, start), ran = __ballot_sync(kFull, entered);
@@ -1077,7 +1085,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 nscat++;
                 rvx = __fdividef(1.f, vx); rvy = __fdividef(1.f, vy); rvz = __fdividef(1.f, vz);
                 c_scat++;
-                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 2068-2074
+                if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0, S.stokes + tid, B);     // 2068-2074
             } else {
                 nscat = 0;
             }
@@ -1340,7 +1348,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (((med && P.doreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P.doreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != prn.w)) {
-                    if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);     // 2435-2441
+                    if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0, S.stokes + tid, B);     // 2435-2441
                     float Rtotal = 1.f;
                     const float a2 = n1 * n1, b2 = prn.w * prn.w;
                     const float va = (axis == 0) ? vx : ((axis == 1) ? vy : vz);
@@ -1407,7 +1415,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         }
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
-            if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0);         // 1116-1122
+            if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0, S.stokes + tid, B);         // 1116-1122
             if (FULL && P.saveref && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f) {
                 // diffuse reflectance (1124-1165): the weight leaving into a void voxel of the grid,
                 // negated, in that voxel at the photon's gate (a photon before the first gate, which

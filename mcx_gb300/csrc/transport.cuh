@@ -133,6 +133,7 @@ struct KParams {
     int nangle;                     // > 0: launch directions from the table
     const float4* extrasrc;         // extra sources: 5 float4 each (pos, dir, param1, param2, focus)
     int nextra;                     // number of extra sources (extrasrclen)
+    int traj_reclen;                // trajectory record: 6 floats, 10 with the Stokes vector
     int srcid;                      // 1: primary only, > 1: that source, 0: all merged, -1: all, one block each
     int outputtype;                 // 0 flux, 1 fluence, 2 energy
     float minenergy;                // Russian roulette threshold (0 = off)

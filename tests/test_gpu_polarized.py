@@ -82,3 +82,15 @@ def test_against_reference_build(engine):
         b = np.zeros(n)
         b[:nr] = sr[k] * wr
         close(a, b, "R_" + what)
+
+
+def test_trajectories_with_stokes(engine):
+    # istrajstokes: trajectory records of polarised runs carry the Stokes vector (10 floats);
+    # without it, the plain 6-float records
+    cfg = problems.polarized_slab(2000) | {"debuglevel": "M", "maxjumpdebug": 200_000}
+    t = engine.run(cfg | {"istrajstokes": 1})["traj"]
+    assert t.shape[0] == 10 and t.shape[1] > 2000
+    s = t[6:10].astype(np.float64)
+    np.testing.assert_allclose(s[0], 1.0, atol=1e-5)
+    np.testing.assert_allclose((s[1:] ** 2).sum(0), 1.0, atol=2e-4)
+    assert engine.run(cfg)["traj"].shape[0] == 6
