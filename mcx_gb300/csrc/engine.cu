@@ -465,7 +465,7 @@ struct Session {
         k.maxgate = maxgate;
         k.doreflect = cfg->isreflect ? 1 : 0;
         k.save2pt = cfg->issave2pt ? 1 : 0;
-        k.saveref = (cfg->issave2pt && cfg->issaveref == 1) ? 1 : 0;
+        k.saveref = cfg->issave2pt ? (int)cfg->issaveref : 0;
         k.outputtype = cfg->outputtype;
         k.minenergy = cfg->minenergy;
         k.gscatter = (float)cfg->gscatter;
@@ -743,6 +743,7 @@ struct Session {
         if (shadow.p) CK(cudaMemsetAsync(shadow.p, 0, shadow.bytes, stream));
         if (field64.p) CK(cudaMemsetAsync(field64.p, 0, field64.bytes, stream));
         if (detcount.p) CK(cudaMemsetAsync(detcount.p, 0, detcount.bytes, stream));
+        if (kp.saveref > 1 && detp.p) CK(cudaMemsetAsync(detp.p, 0, detp.bytes, stream));     // per-voxel sums
         CK(cudaMemsetAsync(energy.p, 0, energy.bytes, stream));
         CK(cudaMemsetAsync(counters.p, 0, counters.bytes, stream));
         CK(cudaMemsetAsync(err.p, 0, err.bytes, stream));
@@ -799,6 +800,7 @@ struct Session {
             CK(cudaMemsetAsync(err.p, 0, err.bytes, s));
         }
         if (detcount.p) CK(cudaMemsetAsync(detcount.p, 0, detcount.bytes, s));
+        if (kp.saveref > 1 && detp.p) CK(cudaMemsetAsync(detp.p, 0, detp.bytes, s));
         if (trajcount.p) CK(cudaMemsetAsync(trajcount.p, 0, trajcount.bytes, s));
         CK(cudaMemsetAsync(work.p, 0, sizeof(unsigned long long), s));
         CK(launch_transport(kp, reflect, savedet, grid, block, smem, s));
@@ -815,6 +817,7 @@ struct Session {
 
     unsigned detected() {
         if (!detcount.p) return 0;
+        if (kp.saveref > 1) return kp.maxdet;      // one record per voxel (src/mcx_core.cu:2520-2522)
         unsigned d = 0;
         CK(cudaMemcpyAsync(&d, detcount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));

@@ -420,7 +420,15 @@ void validate(Config* cfg) {
     // diffuse reflectance (src/mcx_utils.c:3757-3759, 1808-1818): needs the field; mode 2 (the exit
     // path per voxel in the detected buffer) is not built
     if (!cfg->issave2pt) cfg->issaveref = 0;
-    if (cfg->issaveref > 1) MCXG_RAISE(-6, "issaveref > 1 (exit path length per voxel) is not supported by the GB300 engine");
+    if (cfg->issaveref > 1) {          // exit weight and paths per void voxel in the detected buffer
+        if (!cfg->issavedet) MCXG_RAISE(-4, "you must have at least two outputs if issaveref is greater than 1");
+        const uint32_t nv = cfg->dim.x * cfg->dim.y * cfg->dim.z;
+        if (nv > cfg->maxdetphoton) {
+            if (cfg->flog) fprintf(cfg->flog, "you must set --maxdetphoton larger than the total size of the voxels when --issaveref is greater than 1; autocorrecting ...\n");
+            cfg->maxdetphoton = nv;
+        }
+        cfg->savedetflag = 0x5;
+    }
 
     // history header bookkeeping done at the end of mcx_validatecfg (src/mcx_utils.c:3853-3857)
     const uint32_t f = cfg->savedetflag;

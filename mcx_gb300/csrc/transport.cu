@@ -1416,7 +1416,7 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         if (kill) {
             // terminate: detection and energy bookkeeping (src/mcx_core.cu:1113-1182, 365-417)
             if (FULL && P.traj) traj_save(P, S.pid[tid], px, py, pz, w, (P.nextra && P.srcid <= 0) ? S.ssrc[tid] : 0, S.stokes + tid, B);         // 1116-1122
-            if (FULL && P.saveref && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f) {
+            if (FULL && P.saveref == 1 && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f) {
                 // diffuse reflectance (1124-1165): the weight leaving into a void voxel of the grid,
                 // negated, in that voxel at the photon's gate (a photon before the first gate, which
                 // MCX would write below the field, is left out)
@@ -1427,8 +1427,17 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     else field_add_large(P, (size_t)idx + (size_t)ts * P.nvox, -w);
                 }
             }
+            if (SAVEDET && FULL && P.saveref > 1 && med == 0 && idx != kOUT_MIN && idx != kOUT_MAX && w > 0.f &&
+                idx < P.maxdet) {
+                // saveexitppath (src/mcx_core.cu:272-285): the exit weight and the weighted partial
+                // paths summed into the voxel's record, in MCX's slots (the path of medium 1 shares
+                // slot 0 with the weight; the last slot stays empty)
+                float* r = P.detp + (size_t)idx * P.reclen;
+                atomicAdd(r, w);
+                for (int i = 0; i < P.nmedia_det; i++) atomicAdd(r + i, S.ppath[i * B + tid] * w);
+            }
             bool detected = false;
-            if (SAVEDET && (detflag & kDET_MASK) && (med == 0 || (SVMC && sv.tissue() == 0))) {
+            if (SAVEDET && (detflag & kDET_MASK) && (med == 0 || (SVMC && sv.tissue() == 0)) && P.saveref < 2) {
                 const int detid = (detflag == kOUT_MIN) ? -1 : find_detector(P, px, py, pz);
                 if (detid) {
                     detected = true;

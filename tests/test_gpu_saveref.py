@@ -66,3 +66,30 @@ def test_against_reference_build(engine):
     po = np.bincount(ring.ravel(), ours[:, :, 0].ravel(), 11)
     pt = np.bincount(ring.ravel(), theirs[:, :, 0].ravel(), 11)
     np.testing.assert_allclose(po, pt, rtol=0.05, atol=0.002 * pt.sum())
+
+
+def test_exit_paths_against_reference_build(engine):
+    # issaveref = 2: one detected record per voxel holding the summed exit weight and weighted
+    # partial paths of the photons that ended there (MCX's slots), detection itself off
+    from oracle import ref_mcx
+
+    if not ref_mcx.available():
+        pytest.skip("reference sources are not staged in baseline/_ref/src")
+    ref_mcx.build()
+    n = 1_000_000
+    cfg = problems.reflectance_cube(n) | {"issaveref": 2, "issavedet": 1, "detpos": [[31.0, 31.0, 61.0, 1.0]],
+                                           "maxdetphoton": 62 ** 3}
+    d = engine.run(cfg)["detp"].astype(np.float64)
+    r = ref_mcx.run(problems.reflectance_cube(n) | {"issaveref": 2, "issavedet": 1,
+                                                     "detpos": [[31.0, 31.0, 61.0, 1.0]],
+                                                     "maxdetphoton": 62 ** 3}, keep_field=False)["detp"]
+    r = r.astype(np.float64)
+    assert d.shape == r.shape == (2, 62 ** 3)
+    void = np.ones((62, 62, 62), bool)
+    void[1:-1, 1:-1, 1:-1] = False
+    v = void.ravel(order="F")
+    assert not d[:, ~v].any() and not d[1].any()
+    print("slot sums", d[0].sum(), r[0].sum())
+    assert d[0].sum() == pytest.approx(r[0].sum(), rel=0.01)
+    face = lambda x: x[0].reshape(62, 62, 62, order="F")[:, :, 0].sum()      # noqa: E731
+    assert face(d) == pytest.approx(face(r), rel=0.02)
