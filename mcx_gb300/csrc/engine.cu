@@ -11,8 +11,11 @@
 // tstart, tstep, tend, steps, dim, medianum, prop, detnum, detpos, maxdetphoton, maxgate, respin,
 // vol, isreflect, isnormalized, issavedet, issaveseed, issave2pt, isspecular, outputtype,
 // minenergy, unitinmm, flog, maxvoidstep, voidtime, savedetflag, deviceid, parentid, gscatter,
-// bc, replay, replaydet.
-// Config fields written: exportfield (+=), exportdetected and seeddata (realloc), detectedcount,
+// bc, replay, replaydet, mediabyte, debuglevel, maxjumpdebug, issaveref, srcnum, srcid,
+// extrasrclen, srcdata, nphase, invcdf, nangle, angleinvcdf, polmedianum, smatrix, srciquv,
+// istrajstokes, omega.
+// Config fields written: exportfield (+=), exportdetected and seeddata (realloc), exportdebugdata
+// and debugdatalen (trajectories), detectedcount,
 // runtime, energytot, energyabs, energyesc, normalizer, his.{normalizer,detected,respin,colcount,
 // seedbyte,...}, deviceid (compacted by mcx_list_gpu).
 
