@@ -56,8 +56,10 @@ CONTEST_DECKS = ("cube60", "cube60b", "cube60planar")
 # of `bench.py --workload W --photons 20000000 --steps 1 --warmup 1`.  The DRAM bytes are the
 # field's first read and its write-back: the field and labels stay in L2, so they do not grow
 # with the photon count.
-NCU_PER_STEP = {"workload0": 222.8, "workload1": 272.0, "workload2": None}
-NCU_DRAM_PER_LAUNCH = {"workload0": 1.63e6, "workload1": 41.59e6, "workload2": None}
+# workload2: `bench.py --workload workload2 --photons 2000000 --steps 1 --warmup 1 --no-cpu-baseline`,
+# the timed launch (-s 7 -c 1): 5.382e10 warp instructions x 15.63 lanes over 2e6 x 1606.5 steps.
+NCU_PER_STEP = {"workload0": 222.8, "workload1": 272.0, "workload2": 261.8}
+NCU_DRAM_PER_LAUNCH = {"workload0": 1.63e6, "workload1": 41.59e6, "workload2": 25.97e6}
 
 
 def _dist():
@@ -123,6 +125,30 @@ def peaks() -> dict:
         d["_source"] = "measured"
         return d
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0, "_source": "fallback"}
+
+
+def workload_config(name: str, cfg: dict, nphoton: int, world: int) -> dict:
+    """The `config` object of a single-workload line, identical in both arms: what is simulated,
+    not how (launch shapes and build details ride in their own keys)."""
+    gates = max(1, int((cfg["tend"] - cfg["tstart"]) / cfg["tstep"] + 0.5))
+    ndet = int(np.asarray(cfg["detpos"]).reshape(-1, 4).shape[0]) if cfg.get("issavedet") and "detpos" in cfg else 0
+    return {"workload": name, "photons_per_step": int(nphoton), "volume": list(np.asarray(cfg["vol"]).shape),
+            "gates": gates, "detectors": ndet, "parallelism": f"replicas{world}",
+            "l2": "flushed before each timed step"}
+
+
+class L2Flush:
+    """Writes 256 MB (> the 129 MB L2) on the device before each timed step."""
+
+    def __init__(self):
+        import torch
+
+        self.torch = torch
+        self.buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.buf.zero_()
+        self.torch.cuda.synchronize()
 
 
 def make_cfg(name: str, nphoton: int, seed: int):
@@ -479,18 +505,22 @@ def reference_arm(args, world, rank) -> None:
             build_s = time.perf_counter() - t0
             for i in range(args.warmup):
                 ref_mcx.run(make_cfg(name, min(nphoton, 10_000_000), 100 + i), keep_field=False)
+            flush = L2Flush()
             runs = []
             for i in range(args.steps):
+                c = make_cfg(name, nphoton, 200 + i)
+                flush()
                 t0 = time.perf_counter()
-                r = ref_mcx.run(make_cfg(name, nphoton, 200 + i), keep_field=False)
+                r = ref_mcx.run(c, keep_field=False)
                 runs.append((r, time.perf_counter() - t0))
             speed = statistics.mean(r["speed"] for r, _ in runs)
             norm_ms = statistics.mean(r["normalized_ms"] for r, _ in runs)
             wall = statistics.mean(w for _, w in runs)
             line = dict(base, value=speed, ms_per_step=nphoton / speed,
-                        config={"workload": name, "photons_per_step": nphoton, "threads": runs[0][0]["threads"],
-                                "build": "src/mcx_core.cu -DUSE_ATOMIC -DSAVE_DETECTORS -use_fast_math -arch=sm_103a",
-                                "build_s": round(build_s, 1)},
+                        config=workload_config(name, make_cfg(name, nphoton, 200), nphoton, world),
+                        reference_build={"threads": runs[0][0]["threads"],
+                                         "build": "src/mcx_core.cu -DUSE_ATOMIC -DSAVE_DETECTORS -use_fast_math -arch=sm_103a",
+                                         "build_s": round(build_s, 1)},
                         e2e={"value": nphoton / norm_ms, "unit": "photons/ms", "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0, "ms_per_step": norm_ms, "process_wall_s": wall},
                         absorbed=[r["absorbed"] for r, _ in runs],
@@ -665,10 +695,8 @@ def main() -> None:
         "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "photons_per_step": nphoton, "volume": list(cfg["vol"].shape),
-                   "gates": pc.ngates, "parallelism": f"replicas{world}", "l2": "flushed before each timed step",
-                   "grid": st.grid, "block": st.block, "chunk": st.chunk,
-                   "detectors": int(pc.c.detnum)},
+        "config": workload_config(name, cfg, nphoton, world),
+        "launch": {"grid": st.grid, "block": st.block, "chunk": st.chunk},
         "e2e": {"value": e2e, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_tot / args.steps},
         "wall_ms_per_step": wall_ms / args.steps,

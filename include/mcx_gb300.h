@@ -126,6 +126,23 @@ int mcxg_replayinit(Config* cfg, const float* detps, const int dimdetps[2], int 
  * photon alive forever.  No counterpart in MCX. */
 void mcxg_set_step_cap(unsigned int steps);
 
+/* Field accumulation of the following mcx_run_simulation calls: 64 accumulates the fluence in
+ * FP64 on the device (MCX's USE_DOUBLE build, src/mcx_core.cu:55-63, 2243-2263: one FP64 copy
+ * instead of the two-copy FP32 spill; exportfield stays float, as in MCX), anything else restores
+ * FP32.  The default is FP32, or FP64 when the environment variable MCXG_FIELD_FP64=1 is set when
+ * the first simulation starts, so unmodified front-ends can select it without recompiling, as
+ * MCX needs.  No counterpart in MCX, which fixes the choice at compile time. */
+void mcxg_set_field_precision(int bits);
+
+/* The photon split mcx_run_simulation uses over the devices listed in cfg->deviceid (1-based ids,
+ * as mcx_list_gpu leaves them; the same device may appear more than once): offsets[d] and
+ * counts[d] of each launch's n photons for device d, in proportion to cfg->workload, or to the
+ * devices' core counts in gpu[] (1 each when gpu is NULL) when cfg->workload is all zero, which
+ * it then receives, as src/mcx_core.cu:2980-3007 fills it.  Unlike MCX, which truncates every
+ * share, the last device takes the remainder so the shares add up to n.  Returns the number of
+ * devices, or a negative MCX error id (-1: an active device without workload).  Host-only. */
+int mcxg_photon_shares(Config* cfg, const GPUInfo* gpu, uint64_t nphoton, uint64_t* offsets, uint64_t* counts);
+
 /* mcx_run_simulation with the fluence accumulated in FP64 on the device instead of MCX's FP32
  * two-copy scheme: the reference-accuracy twin the FP32 accumulation error is stated against.
  * Same inputs, outputs and errors as mcx_run_simulation (src/mcx_core.h:200).  No counterpart
@@ -154,16 +171,27 @@ int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, do
  * One transport launch over photons [photon_offset, photon_offset + nphoton) of the prepared
  * Config `cfg` (mcxg_validatecfg or MCX's mcx_validatecfg), time-gate group `gate_group`, on
  * `stream` (a cudaStream_t; NULL = legacy default stream) of the current device.  The caller
- * owns every buffer: d_labels (Nvox bytes, bit 7 = detector mask, bits 0-6 = medium label),
- * d_field and d_spill (maxgate x Nvox floats each, zeroed by the caller before the first call;
- * the fluence is their sum, unnormalised), d_detp (maxdetphoton x reclen floats; may be NULL when
- * no detectors are saved).  Nothing is allocated: the photon counter, counters, FP64 energy
- * tallies, error word and detector table live in a static device array of
- * mcxg_noalloc_scratch_bytes() bytes that every GPU using the library keeps until the process
- * exits.  Limits: at most 256 detectors.  The first call on a device looks up that array's device
- * address, so make it before any stream capture.  Calls share the array and clear it on entry:
- * calls that overlap on the GPU race and must be serialised.  When `stats` is non-NULL the call
- * waits for the stream and reports energies, counters and the error word there.  Returns 0 or a
+ * owns every buffer: d_labels (Nvox bytes, bit 7 = detector mask, bits 0-6 = medium label, every
+ * label below cfg->medianum), d_field and d_spill (G x Nvox floats each, zeroed by the caller
+ * before the first call; the fluence is their sum, unnormalised), d_detp (maxdetphoton x reclen
+ * floats; may be NULL when no detectors are saved).  G, the gates of one group, is
+ * min(cfg->maxgate, T) when cfg->maxgate > 0 and T otherwise, with
+ * T = max(1, (int)((tend - tstart) / tstep + 0.5f)) (no memory cap, unlike mcx_run_simulation).
+ * Nothing is allocated: the photon counter, counters, FP64 energy tallies, error word and
+ * detector table live in a static device array of mcxg_noalloc_scratch_bytes() bytes that every
+ * GPU using the library keeps until the process exits.  Limits: at most 256 detectors.  The
+ * first call on a device looks up that array's device address, so make it before any stream
+ * capture.  Calls share the array and clear it on entry: calls that overlap on the GPU race and
+ * must be serialised.  The call waits for `stream` twice: after checking the labels on the device
+ * and after the launch, to read the error word back.  It returns -4 for a label at or above
+ * cfg->medianum (before any photon runs) and -6 for a run stopped by the per-photon step cap
+ * (mcxg_set_step_cap) or the voxel-index guard.  `stats` (may be NULL) receives energies,
+ * counters, the error word and the detected-photon count, which the caller needs to know how
+ * many records of d_detp are valid (records past maxdetphoton are dropped, as MCX drops them).
+ * Rejected with -6: per-voxel media formats, replay and seed saving, polarised media,
+ * trajectories, extra sources, pattern sources, diffuse reflectance, phase-function and
+ * launch-angle tables, output types other than flux / fluence / energy, and MCX seeding
+ * (mcxg_set_seeding(1) or MCXG_SEEDING=mcx), which need further device buffers.  Returns 0 or a
  * negative MCX error id (message via mcxg_last_error). */
 int mcxg_run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, float* d_spill, float* d_detp,
                      uint64_t photon_offset, uint64_t nphoton, int gate_group, void* stream, mcxg_stats* stats);

@@ -53,6 +53,10 @@ lib.mcxg_photon_stream.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_float),
 lib.mcxg_photon_stream.restype = C.c_int
 lib.mcxg_replayinit.argtypes = [_CFG, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_int]
 lib.mcxg_replayinit.restype = C.c_int
+lib.mcxg_set_field_precision.argtypes = [C.c_int]
+lib.mcxg_set_field_precision.restype = None
+lib.mcxg_photon_shares.argtypes = [_CFG, C.POINTER(abi.GPUInfo), C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+lib.mcxg_photon_shares.restype = C.c_int
 lib.mcxg_set_step_cap.argtypes = [C.c_uint]
 lib.mcxg_set_step_cap.restype = None
 lib.mcxg_run_batch.argtypes = [C.POINTER(C.POINTER(abi.Config)), C.c_int, C.c_int, C.POINTER(abi.Stats),
@@ -111,4 +115,5 @@ EXPORTED = [
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
     "mcxg_set_seeding", "mcxg_probe_atomic_rate",
     "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap", "mcxg_dn_last_error",
+    "mcxg_set_field_precision", "mcxg_photon_shares",
 ] + list(_DN)

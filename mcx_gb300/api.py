@@ -211,6 +211,9 @@ class PreparedConfig:
             c.savedetflag = int(f)
         if "bc" in cfg:
             c.bc = str(cfg["bc"]).encode()[:12]
+        if "workload" in cfg:            # per-device photon shares (pmcx's cfg.workload)
+            for i, x in enumerate(np.asarray(cfg["workload"], np.float32).reshape(-1)[: abi.MAX_DEVICE]):
+                c.workload[i] = float(x)
         for key, n in (("srcpos", 4), ("srcdir", 4), ("srcparam1", 4), ("srcparam2", 4), ("srciquv", 4)):
             if key in cfg:
                 _set_vec(getattr(c, key), np.asarray(cfg[key], np.float64).reshape(-1)[:4]
@@ -356,13 +359,16 @@ def gpuinfo() -> list[dict[str, Any]]:
     return out
 
 
-def run(cfg: dict[str, Any], verbose: bool = False, fp64_field: bool = False) -> dict[str, Any]:
+def run(cfg: dict[str, Any], verbose: bool = False, fp64_field: bool = False,
+        devices: list[int] | None = None) -> dict[str, Any]:
     """Run one simulation on the GPU; same inputs and outputs as ``pmcx.run``.
 
     ``fp64_field`` accumulates the fluence in FP64 on the device (the reference-accuracy twin of
-    the FP32 production path, used to state its accumulation error)."""
+    the FP32 production path, used to state its accumulation error).  ``devices`` lists the
+    0-based CUDA devices to split the photons over (MCX's multi-GPU run; a device may be listed
+    more than once), in place of ``gpuid``; ``cfg["workload"]`` weights their shares."""
     pc = prepare(cfg, verbose=verbose)
-    return run_prepared(pc, fp64_field=fp64_field)
+    return run_prepared(pc, fp64_field=fp64_field, devices=devices)
 
 
 def _active_devices(c) -> None:
@@ -489,13 +495,18 @@ def _result(pc: PreparedConfig, flux, maxgate, detp, st) -> dict[str, Any]:
     return out
 
 
-def run_prepared(pc: PreparedConfig, fp64_field: bool = False) -> dict[str, Any]:
+def run_prepared(pc: PreparedConfig, fp64_field: bool = False, devices: list[int] | None = None) -> dict[str, Any]:
     c = pc.c
     nact, info = _active_devices(c)
     if nact == 0:
         if info:
             libc.free(info)
         raise MCXError(-1, "no active GPU device found")
+    if devices:
+        if len(devices) > abi.MAX_DEVICE - 1:
+            raise MCXError(-1, "too many devices")
+        ids = bytes(int(d) + 1 for d in devices)
+        C.memmove(C.addressof(c) + abi.Config.deviceid.offset, ids + b"\x00", len(ids) + 1)
     flux, maxgate = _attach_field(pc)
     try:
         (lib.mcxg_run_simulation_fp64 if fp64_field else lib.mcx_run_simulation)(C.byref(c), info)

@@ -30,6 +30,7 @@
 #include <mutex>
 #include <stdlib.h>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mcx_abi.h"
@@ -63,6 +64,10 @@ std::vector<std::pair<std::string, int>> g_tune_cache;
 // per-thread streams), 0 = per-photon streams, 1 = MCX's per-thread streams.
 int g_seeding = -1;
 
+// Field accumulation of mcx_run_simulation: 0 = not chosen yet (environment MCXG_FIELD_FP64=1
+// selects FP64), 32 = FP32 with MCX's two-copy spill, 64 = FP64 (MCX's USE_DOUBLE build).
+int g_field_bits = 0;
+
 // Per-photon step cap of new sessions (a photon longer than this is stopped and reported).
 constexpr unsigned kDefaultStepCap = 20000000u;
 unsigned g_step_cap = kDefaultStepCap;
@@ -78,6 +83,22 @@ int seeding_mode() {
 }  // namespace
 
 [[noreturn]] void raise(int id, const std::string& msg, const char* file, int line) { throw Error{id, msg, file, line}; }
+
+int current_seeding_mode() { return seeding_mode(); }
+
+bool field_fp64() {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    if (g_field_bits == 0) {
+        const char* e = std::getenv("MCXG_FIELD_FP64");
+        g_field_bits = (e && std::strcmp(e, "1") == 0) ? 64 : 32;
+    }
+    return g_field_bits == 64;
+}
+
+unsigned current_step_cap() {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    return g_step_cap;
+}
 
 #define CK(call)                                                                         \
     do {                                                                                 \
@@ -382,7 +403,7 @@ struct Session {
         if (stream) cudaStreamDestroy(stream);
     }
 
-    void create(const Config* cfg, int dev, bool fp64_field) {
+    void create(const Config* cfg, int dev, bool fp64_field, int gate_cap = 0) {
         device = dev;
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -415,6 +436,7 @@ struct Session {
         const size_t per_gate = (nvox * (use64 ? sizeof(double) : 2 * sizeof(float)) + nvox * sizeof(float)) * chans;
         const size_t budget = freeb > (size_t)(1u << 30) ? freeb - (size_t)(1u << 30) : freeb / 2;
         if ((size_t)maxgate * per_gate > budget) maxgate = std::max<int>(1, (int)(budget / per_gate));
+        if (gate_cap > 0) maxgate = std::min(maxgate, gate_cap);
         // a replay of every detector at once keeps one block of gates per detector
         // (src/mcx_core.cu:2907-2913)
         blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
@@ -812,6 +834,7 @@ struct Session {
 
     // Merge shadow copies, optionally scale, and copy the field out.
     void read_field(float* host, float scale, int positive_only) {
+        CK(cudaSetDevice(device));
         CK(launch_merge_field(outbuf.as<float>(), field.as<float>(), shadow.as<float>(), field64.as<double>(), fieldlen, scale,
                               positive_only, stream));
         CK(cudaMemcpyAsync(host, outbuf.p, fieldlen * sizeof(float), cudaMemcpyDeviceToHost, stream));
@@ -828,6 +851,7 @@ struct Session {
     }
 
     void read_stats(mcxg_stats* st) {
+        CK(cudaSetDevice(device));
         double e[kNumEnergy];
         unsigned long long c[kNumCounters];
         unsigned ef = 0;
@@ -865,6 +889,11 @@ extern "C" int mcxg_get_stats(mcxg_stats* out) {
 extern "C" void mcxg_set_seeding(int mode) {
     std::lock_guard<std::mutex> g(g_override_mu);
     g_seeding = (mode == 1) ? 1 : 0;
+}
+
+extern "C" void mcxg_set_field_precision(int bits) {
+    std::lock_guard<std::mutex> g(g_override_mu);
+    g_field_bits = (bits == 64) ? 64 : 32;
 }
 
 extern "C" void mcxg_set_step_cap(unsigned int steps) {
@@ -1027,10 +1056,12 @@ void begin_outputs(Config* cfg, const Session& S) {
 }
 
 // Detected photons of the last launch appended to exportdetected (src/mcx_core.cu:3645-3666).
-void append_detected(Config* cfg, Session& S) {
+void append_detected(Config* cfg, Session& S, std::mutex* mu = nullptr) {
     if (!S.savedet) return;
     const unsigned reclen = S.kp.reclen;
     const unsigned det = S.detected();
+    std::unique_lock<std::mutex> lk;
+    if (mu) lk = std::unique_lock<std::mutex>(*mu);
     cfg->his.detected += det;
     const unsigned keep = std::min(det, cfg->maxdetphoton);
     if (det > cfg->maxdetphoton && cfg->flog)
@@ -1051,14 +1082,18 @@ void append_detected(Config* cfg, Session& S) {
 }
 
 // Trajectory records of the last launch appended to exportdebugdata (src/mcx_core.cu:3594-3614).
-void append_trajectory(Config* cfg, Session& S) {
+void append_trajectory(Config* cfg, Session& S, std::mutex* mu = nullptr) {
     if (!S.kp.traj) return;
     unsigned rec = 0;
     CK(cudaMemcpyAsync(&rec, S.trajcount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
     CK(cudaStreamSynchronize(S.stream));
+    std::unique_lock<std::mutex> lk;
+    if (mu) lk = std::unique_lock<std::mutex>(*mu);
     if (rec > S.kp.traj_max && cfg->flog)
         fprintf(cfg->flog, "WARNING: the saved trajectory positions are more than what your have specified (%u > %u), please use the --maxjumpdebug option to specify a greater number\n",
                 rec, S.kp.traj_max);
+    else if (rec && cfg->flog)
+        fprintf(cfg->flog, "saved trajectory positions: %u, total: %u\t", rec, cfg->debugdatalen + rec);
     rec = std::min(rec, S.kp.traj_max);
     if (rec) {
         cfg->exportdebugdata = (float*)realloc(cfg->exportdebugdata,
@@ -1073,22 +1108,29 @@ void append_trajectory(Config* cfg, Session& S) {
 
 // End of one gate window: statistics, energies, normalised field added to exportfield
 // (src/mcx_core.cu:3716-3770, 3823-3925).
-void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg_stats& total) {
-    mcxg_stats st{};
-    S.read_stats(&st);
-    if (st.error_flags & kErrStepCap)
-        MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
-    if (st.error_flags & kErrIndex)
-        MCXG_RAISE(-6, "internal error: a photon's voxel index left the volume; the photon was stopped");
-    total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
-    total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
-    total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;
-    total.n_launch += st.n_launch; total.n_photon += st.n_photon; total.n_detected += st.n_detected;
-    total.n_tile_deposit += st.n_tile_deposit;
-    total.grid = st.grid; total.block = st.block; total.chunk = st.chunk; total.launches += st.launches;
-    total.error_flags |= st.error_flags;
-    cfg->energytot += st.e_launch;
-    cfg->energyesc += st.e_escape + st.e_detect;
+// With several devices (src/mcx_core.cu:3730-3759) their energies are summed first, so one
+// normaliser scales every device's field, and the scaled fields are summed into exportfield.
+void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<float>& host_field, mcxg_stats& total) {
+    double e_launch = 0.0;
+    for (Session* D : SS) {
+        mcxg_stats st{};
+        D->read_stats(&st);
+        if (st.error_flags & kErrStepCap)
+            MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
+        if (st.error_flags & kErrIndex)
+            MCXG_RAISE(-6, "internal error: a photon's voxel index left the volume; the photon was stopped");
+        total.e_launch += st.e_launch; total.e_escape += st.e_escape; total.e_detect += st.e_detect;
+        total.e_absdep += st.e_absdep; total.e_absother += st.e_absother;
+        total.n_steps += st.n_steps; total.n_scatter += st.n_scatter; total.n_deposit += st.n_deposit;
+        total.n_launch += st.n_launch; total.n_photon += st.n_photon; total.n_detected += st.n_detected;
+        total.n_tile_deposit += st.n_tile_deposit;
+        total.grid = st.grid; total.block = st.block; total.chunk = st.chunk; total.launches += st.launches;
+        total.error_flags |= st.error_flags;
+        cfg->energytot += st.e_launch;
+        cfg->energyesc += st.e_escape + st.e_detect;
+        e_launch += st.e_launch;
+    }
+    Session& S = *SS[0];
 
     if (cfg->issave2pt) {
         // normalisation (src/mcx_core.cu:3823-3925): flux scale = unitinmm/(Etot*Vvox*tstep)
@@ -1097,7 +1139,7 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
         std::vector<float> chan_scale;          // photon sharing: one scale per pattern
         const int ot = cfg->outputtype;
         const bool path_units = (ot == otJacobian || ot == otRF || ot == otWLTOF);
-        if (cfg->isnormalized && st.e_launch > 0.0) {
+        if (cfg->isnormalized && e_launch > 0.0) {
             const double Vvox = (double)cfg->steps.x * cfg->steps.y * cfg->steps.z;
             if (ot == otFlux || ot == otFluence) {
                 double sc = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
@@ -1148,7 +1190,8 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
             cfg->his.normalizer = scale;
         }
         host_field.resize(S.fieldlen);
-        S.read_field(host_field.data(), (block_scale.empty() && chan_scale.empty()) ? scale : 1.f, cfg->isnormalized == 2);
+        for (Session* D : SS) {
+        D->read_field(host_field.data(), (block_scale.empty() && chan_scale.empty()) ? scale : 1.f, cfg->isnormalized == 2);
         float* out = cfg->exportfield;
         if (!chan_scale.empty()) {
             for (size_t i = 0; i < S.fieldlen; i++) {
@@ -1164,20 +1207,24 @@ void finish_window(Config* cfg, Session& S, std::vector<float>& host_field, mcxg
                 out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * block_scale[(i / per) % S.blocks];
             }
         }
+        }
     }
 }
 
 // End of a run: runtime, absorbed energy, the log lines and the standalone file output
 // (src/mcx_core.cu:3932-4030).
-void end_outputs(Config* cfg, Session& S, double kernel_ms, int reps) {
+void end_outputs(Config* cfg, Session& S, double kernel_ms, int reps, int threads = 0) {
+    if (threads <= 0) threads = S.grid * S.block;
     cfg->runtime = (unsigned)std::ceil(kernel_ms);
     cfg->energyabs = cfg->energytot - cfg->energyesc;
-    if (cfg->flog && cfg->printnum >= 0) {
+    // the run summary is printed whatever printnum says: MCX's CLI sets printnum to -1 unless
+    // -l is given, and still prints the summary to stdout (src/mcx_core.cu:3996-4030)
+    if (cfg->flog) {
         const double np = (double)cfg->nphoton * (cfg->respin > 1 ? cfg->respin : 1);
         if (S.savedet) fprintf(cfg->flog, "detected %u photons, total: %lu\n", cfg->his.detected, (unsigned long)cfg->detectedcount);
         fprintf(cfg->flog, "kernel complete:  \t%.3f ms\n", kernel_ms);
         fprintf(cfg->flog, "simulated %.0f photons (%.0f) with %d threads (repeat x%d)\nMCX simulation speed: %.2f photon/ms\n",
-                np, np, S.grid * S.block, reps, np / std::max(1e-3, kernel_ms));
+                np, np, threads, reps, np / std::max(1e-3, kernel_ms));
         fprintf(cfg->flog, "total simulated energy: %.2f\tabsorbed: %5.5f%%\n(loss due to initial specular reflection is excluded in the total)\n",
                 cfg->energytot, cfg->energytot > 0 ? (cfg->energytot - cfg->energyesc) / cfg->energytot * 100.0 : 0.0);
         fflush(cfg->flog);
@@ -1192,25 +1239,177 @@ void end_outputs(Config* cfg, Session& S, double kernel_ms, int reps) {
             cfg->his.detected = (unsigned)cfg->detectedcount;
             mcx_savedetphoton(cfg->exportdetected, cfg->seeddata, (int)cfg->detectedcount, 0, cfg);
         }
+        // trajectories go through the same writer with their own record length (3980-3987)
+        if ((cfg->debuglevel & (kDebugMove | kDebugMoveOnly)) && cfg->exportdebugdata && mcx_savedetphoton) {
+            cfg->his.colcount = (unsigned)S.kp.traj_reclen;
+            cfg->his.savedphoton = cfg->debugdatalen;
+            cfg->his.totalphoton = (unsigned)cfg->nphoton;
+            cfg->his.detected = 0;
+            mcx_savedetphoton(cfg->exportdebugdata, nullptr, (int)cfg->debugdatalen, 0, cfg);
+        }
     }
 }
 
+// MCX's -D R (src/mcx_core.cu:3055-3112): instead of a simulation, one GPU thread fills the
+// field with the generator's uniforms from four seed words drawn with the C library's rand()
+// as MCX draws them; the field is exported and saved like a fluence.
+void rng_debug_output(Config* cfg, int gpuid) {
+    CK(cudaSetDevice(gpuid));
+    const size_t nvox = (size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z;
+    int totalgates = (int)((cfg->tend - cfg->tstart) / cfg->tstep + 0.5f);
+    if (totalgates < 1) totalgates = 1;
+    const int maxgate = (cfg->maxgate > 0) ? std::min<int>((int)cfg->maxgate, totalgates) : totalgates;
+    const size_t fieldlen = nvox * (size_t)maxgate;
+    if (fieldlen > (size_t)INT32_MAX) MCXG_RAISE(-6, "the -D R field is too large");
+    uint32_t words[4];
+    for (auto& wd : words) {
+        const uint32_t a = (uint32_t)rand(), b = (uint32_t)rand(), c = (uint32_t)rand();
+        wd = (a << 16) | (b << 1) | (c >> 14);
+    }
+    if (cfg->flog) {
+        fprintf(cfg->flog, "generating %lu random numbers ... \t", (unsigned long)fieldlen);
+        fflush(cfg->flog);
+    }
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DevBuf seeds, out;
+    try {
+        seeds.alloc(sizeof(words), st);
+        out.alloc(fieldlen * sizeof(float), st);
+        CK(cudaMemcpyAsync(seeds.p, words, sizeof(words), cudaMemcpyHostToDevice, st));
+        CK(launch_rng_test(seeds.as<uint32_t>(), out.as<float>(), (int)fieldlen, st));
+        std::vector<float> host(fieldlen);
+        CK(cudaMemcpyAsync(host.data(), out.p, fieldlen * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        seeds.release();
+        out.release();
+        CK(cudaStreamSynchronize(st));
+        cudaStreamDestroy(st);
+        st = nullptr;
+        if (cfg->flog) fprintf(cfg->flog, "kernel complete\n");
+        if (cfg->exportfield == nullptr && cfg->issave2pt) cfg->exportfield = (float*)calloc(fieldlen, sizeof(float));
+        if (cfg->exportfield) std::memcpy(cfg->exportfield, host.data(), fieldlen * sizeof(float));
+        if (cfg->issave2pt && cfg->parentid == mpStandalone && mcx_savedata) mcx_savedata(host.data(), fieldlen, cfg);
+    } catch (...) {
+        seeds.release();
+        out.release();
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+        throw;
+    }
+}
+
+// Photon shares of the devices listed in cfg->deviceid (src/mcx_core.cu:2980-3007): in
+// proportion to cfg->workload, or to the devices' core counts when no workload is given (written
+// back to cfg->workload, as MCX's master thread does).  The devices split each launch's photon
+// range [0, n) into consecutive pieces; unlike MCX, whose per-device counts are truncated, the
+// last device takes the remainder, so the shares always add up to n.
+std::vector<double> device_weights(Config* cfg, const GPUInfo* gpu, int ndev) {
+    double full = 0.0;
+    for (int i = 0; i < ndev; i++) full += cfg->workload[i];
+    if (full < kEPS)
+        for (int i = 0; i < ndev; i++)
+            cfg->workload[i] = gpu ? (float)gpu[cfg->deviceid[i] - 1].core : 1.f;
+    std::vector<double> w(ndev);
+    for (int i = 0; i < ndev; i++) {
+        if (!(cfg->workload[i] > 0.f)) MCXG_RAISE(-1, "workload was unspecified for an active device");
+        w[i] = cfg->workload[i];
+    }
+    return w;
+}
+
+void split_photons(const std::vector<double>& w, uint64_t n, std::vector<uint64_t>& offset, std::vector<uint64_t>& count) {
+    const size_t nd = w.size();
+    double full = 0.0;
+    for (double x : w) full += x;
+    offset.assign(nd, 0);
+    count.assign(nd, 0);
+    uint64_t done = 0;
+    for (size_t d = 0; d < nd; d++) {
+        const uint64_t c = (d + 1 == nd) ? n - done : std::min<uint64_t>(n - done, (uint64_t)((double)n * w[d] / full));
+        offset[d] = done;
+        count[d] = c;
+        done += c;
+    }
+}
+
+int active_devices(const Config* cfg) {
+    int n = 0;
+    while (n < MCXG_MAX_DEVICE && cfg->deviceid[n]) n++;
+    return n;
+}
+
+// Runs f(d) for every device index d, d = 0 on the calling thread and the others on their own
+// threads; the first exception (by device order) is rethrown after all have finished.
+template <class F>
+void on_devices(int ndev, F&& f) {
+    if (ndev == 1) {
+        f(0);
+        return;
+    }
+    std::vector<std::exception_ptr> err(ndev);
+    std::vector<std::thread> th;
+    for (int d = 1; d < ndev; d++)
+        th.emplace_back([&, d]() {
+            try {
+                f(d);
+            } catch (...) {
+                err[d] = std::current_exception();
+            }
+        });
+    try {
+        f(0);
+    } catch (...) {
+        err[0] = std::current_exception();
+    }
+    for (auto& t : th) t.join();
+    for (auto& e : err)
+        if (e) std::rethrow_exception(e);
+}
+
+// mcx_run_simulation (src/mcx_core.cu:2740-4110).  MCX's front-ends call it once per listed
+// device from `#pragma omp parallel`; here the master thread (OpenMP thread 0, or the only caller)
+// drives every device of cfg->deviceid from host threads of its own and the other OpenMP
+// threads return at once, so the call needs no barrier with the caller's threads.  Each device
+// runs its share of every launch on its own session; fields, energies, detected photons and
+// trajectories are merged as MCX merges them (3645-3666, 3716-3770), and the one normalisation
+// uses the energy of all devices.  The same device may be listed more than once (replicas
+// sharing its SMs).
 void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
     const auto t_start = std::chrono::steady_clock::now();
     const int threadid = omp_get_thread_num ? omp_get_thread_num() : 0;
-    if (threadid >= MCXG_MAX_DEVICE || cfg->deviceid[threadid] == '\0') return;
-    if (threadid > 0) {
-        // one device per call: replicas on further devices are left to the caller
-        if (cfg->flog) fprintf(cfg->flog, "WARNING: the GB300 engine runs on one device per call; thread %d idle\n", threadid);
+    if (threadid > 0) return;
+    const int ndev = active_devices(cfg);
+    if (ndev == 0) return;
+    std::vector<int> ids(ndev);
+    for (int d = 0; d < ndev; d++) {
+        ids[d] = cfg->deviceid[d] - 1;
+        if (ids[d] < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
+    }
+    const int gpuid = ids[0];
+    if (cfg->debuglevel & kDebugRNG) {
+        rng_debug_output(cfg, gpuid);
         return;
     }
-    const int gpuid = cfg->deviceid[threadid] - 1;
-    if (gpuid < 0) MCXG_RAISE(-1, "GPU ID must be non-zero");
     check_config(cfg);
+    const std::vector<double> weights = device_weights(cfg, gpu, ndev);
 
     std::memset(&t_stats, 0, sizeof(t_stats));
-    Session S;
-    S.create(cfg, gpuid, fp64_field);
+    std::vector<std::unique_ptr<Session>> SS(ndev);
+    for (auto& p : SS) p = std::make_unique<Session>();
+    on_devices(ndev, [&](int d) { SS[d]->create(cfg, ids[d], fp64_field); });
+    // every device holds the same gate group: the smallest any of them fits
+    int maxgate = SS[0]->kp.maxgate;
+    for (auto& p : SS) maxgate = std::min(maxgate, p->kp.maxgate);
+    on_devices(ndev, [&](int d) {
+        if (SS[d]->kp.maxgate != maxgate) {
+            SS[d] = std::make_unique<Session>();
+            SS[d]->create(cfg, ids[d], fp64_field, maxgate);
+        }
+    });
+    Session& S = *SS[0];
     {
         // large runs tune the deposit tile with short pilot launches (cached per configuration)
         int tile_override;
@@ -1221,38 +1420,56 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
         const char* e = std::getenv("MCXG_TUNE");
         const bool tune = !(e && std::strcmp(e, "0") == 0);
         if (tune && tile_override < 0 && cfg->nphoton * (uint64_t)std::abs(cfg->respin) >= 20000000ull)
-            S.autotune(cfg->nphoton);
+            on_devices(ndev, [&](int d) { SS[d]->autotune(cfg->nphoton); });
     }
-    const int maxgate = S.kp.maxgate;
     begin_outputs(cfg, S);
     const int reps = std::abs(cfg->respin);
     const uint64_t nper = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps;
     const uint64_t seed = (uint64_t)(uint32_t)cfg->seed;
+    std::vector<uint64_t> offset, count;
+    split_photons(weights, nper, offset, count);
     if (cfg->flog && cfg->printnum >= 0)
-        fprintf(cfg->flog, "GPU=%d (%s) np=%.0f grid=%d block=%d chunk=%d maxgate=%d repetition=%d\n", gpuid + 1,
-                gpu ? gpu[gpuid].name : "", (double)cfg->nphoton, S.grid, S.block, S.kp.chunk, maxgate, reps);
+        for (int d = 0; d < ndev; d++)
+            fprintf(cfg->flog, "GPU=%d (%s) np=%.0f grid=%d block=%d chunk=%d maxgate=%d repetition=%d\n", ids[d] + 1,
+                    gpu ? gpu[ids[d]].name : "", (double)count[d] * (cfg->respin > 0 ? 1 : reps), SS[d]->grid,
+                    SS[d]->block, SS[d]->kp.chunk, maxgate, reps);
 
     std::vector<float> host_field;
     mcxg_stats total{};
+    std::vector<Session*> all;
+    for (auto& p : SS) all.push_back(p.get());
+    std::mutex mu;
     uint64_t run_index = 0;
     for (int gate0 = 0; gate0 < S.totalgates; gate0 += maxgate) {
         const float twin0 = cfg->tstart + cfg->tstep * gate0;
-        S.set_window(twin0, twin0 + cfg->tstep * maxgate);
-        S.reset();
-        for (int it = 0; it < reps; it++) {
-            if (S.savedet) CK(cudaMemsetAsync(S.detcount.p, 0, sizeof(unsigned), S.stream));
-            if (S.kp.traj) CK(cudaMemsetAsync(S.trajcount.p, 0, sizeof(unsigned), S.stream));
-            S.run(run_index * nper, nper, seed);
-            run_index++;
-            append_detected(cfg, S);
-            append_trajectory(cfg, S);
-        }
-        finish_window(cfg, S, host_field, total);
+        on_devices(ndev, [&](int d) {
+            Session& D = *SS[d];
+            CK(cudaSetDevice(D.device));
+            D.set_window(twin0, twin0 + cfg->tstep * maxgate);
+            D.reset();
+            // MCX seeds the generator of device thread d with seed + d (src/mcx_core.cu:3248)
+            const uint64_t seed_d = (D.kp.seed_mode == 1) ? (uint64_t)(uint32_t)(cfg->seed + d) : seed;
+            for (int it = 0; it < reps; it++) {
+                if (D.savedet) CK(cudaMemsetAsync(D.detcount.p, 0, sizeof(unsigned), D.stream));
+                if (D.kp.traj) CK(cudaMemsetAsync(D.trajcount.p, 0, sizeof(unsigned), D.stream));
+                if (count[d]) D.run((run_index + it) * nper + offset[d], count[d], seed_d);
+                append_detected(cfg, D, ndev > 1 ? &mu : nullptr);
+                append_trajectory(cfg, D, ndev > 1 ? &mu : nullptr);
+            }
+        });
+        run_index += reps;
+        finish_window(cfg, all, host_field, total);
     }
-    total.kernel_ms = S.kernel_ms;
+    double kernel_ms = 0.0;
+    int threads = 0;
+    for (auto& p : SS) {
+        kernel_ms = std::max(kernel_ms, p->kernel_ms);
+        threads += p->grid * p->block;
+    }
+    total.kernel_ms = kernel_ms;
     total.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     t_stats = total;
-    end_outputs(cfg, S, S.kernel_ms, reps);
+    end_outputs(cfg, S, kernel_ms, reps, threads);
 }
 
 // Many independent simulations on one device (the batched workload): every Config gets its
@@ -1367,7 +1584,7 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
                 if (w >= reps[i] * groups[i]) continue;
                 append_detected(cfgs[i], *S[i]);
                 append_trajectory(cfgs[i], *S[i]);
-                if (w % reps[i] == reps[i] - 1) finish_window(cfgs[i], *S[i], host_field, totals[i]);
+                if (w % reps[i] == reps[i] - 1) finish_window(cfgs[i], {S[i].get()}, host_field, totals[i]);
             }
         }
         if (graph_ms) *graph_ms = total_ms;
@@ -1400,9 +1617,28 @@ extern "C" int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats
 extern "C" void mcx_run_simulation(Config* cfg, GPUInfo* gpu) {
     mcxg_clear_error();
     try {
-        run_simulation(cfg, gpu, false);
+        run_simulation(cfg, gpu, field_fp64());
     } catch (const Error& e) {
         report(e);
+    }
+}
+
+// The photon split of mcx_run_simulation over the devices listed in cfg->deviceid.
+extern "C" int mcxg_photon_shares(Config* cfg, const GPUInfo* gpu, uint64_t nphoton, uint64_t* offsets, uint64_t* counts) {
+    mcxg_clear_error();
+    try {
+        const int ndev = active_devices(cfg);
+        if (ndev == 0) return 0;
+        std::vector<uint64_t> off, cnt;
+        split_photons(device_weights(cfg, gpu, ndev), nphoton, off, cnt);
+        for (int d = 0; d < ndev; d++) {
+            offsets[d] = off[d];
+            counts[d] = cnt[d];
+        }
+        return ndev;
+    } catch (const Error& e) {
+        mcxg_set_error(e.id ? e.id : -1, e.msg.c_str());
+        return e.id ? e.id : -1;
     }
 }
 

@@ -114,11 +114,20 @@ void fill_kparams(const Config* cfg, KParams& k, bool& reflect, bool& savedet) {
     k.ndet = (int)cfg->detnum;
 
     fill_source(k, cfg, nullptr);
-    k.step_cap = 20000000u;
+    k.step_cap = current_step_cap();
     k.chunk = 64;
 
     // shared-memory deposit tile over the entry point, as the session places it by default
     place_tile(k, 16);
+}
+
+// Sets kErrBadLabel in *err when a voxel's label (bits 0-6) is not below medianum: the kernel
+// would read such a label's properties past the end of the medium table.
+__global__ void check_labels_kernel(const uint8_t* __restrict__ labels, size_t n, unsigned medianum, unsigned* err) {
+    bool bad = false;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        bad |= (unsigned)(labels[i] & kLabelMask) >= medianum;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(err, (unsigned)kErrBadLabel);
 }
 
 #define NCK(call)                                                                \
@@ -136,6 +145,9 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
     if (cfg->detnum > (unsigned)kMaxDetectors)
         MCXG_RAISE(-6, "the allocation-free entry point holds at most 256 detectors in its static scratch");
     if (cfg->dim.x >= 32768 || cfg->dim.y >= 32768 || cfg->dim.z >= 32768) MCXG_RAISE(-6, "volume dimensions must be below 32768");
+    if (current_seeding_mode() == 1)
+        MCXG_RAISE(-6, "the allocation-free entry point runs per-photon RNG streams only: MCX seeding (mcxg_set_seeding(1) or "
+                       "MCXG_SEEDING=mcx) needs a device buffer of per-thread seed words");
     int device = 0;
     NCK(cudaGetDevice(&device));
     unsigned char* s = scratch_for(device);
@@ -167,22 +179,40 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
     if (cfg->detnum)
         NCK(cudaMemcpyAsync(s + kOffDetPos, cfg->detpos, sizeof(float4) * cfg->detnum, cudaMemcpyHostToDevice, stream));
 
-    const int block = 256;
-    const size_t smem = transport_smem_bytes(k, block, savedet);
-    const int bps = transport_blocks_per_sm(reflect, savedet, transport_mode(k), block, smem);
-    if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
     int sms = 0;
     NCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    // every label must index the medium table: checked on the device before any photon runs
+    unsigned words[2] = {0u, 0u};
+    check_labels_kernel<<<4 * sms, 256, 0, stream>>>(d_labels, (size_t)k.nvox, (unsigned)k.medianum,
+                                                     reinterpret_cast<unsigned*>(s + kOffErr));
+    NCK(cudaGetLastError());
+    NCK(cudaMemcpyAsync(words, s + kOffErr, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    NCK(cudaStreamSynchronize(stream));
+    if (words[0] & kErrBadLabel) MCXG_RAISE(-4, "input media optical properties are less than the labels in the volume");
+
+    // launch shape as the session picks it: without room for the deposit tile, run without it
+    const int block = 256;
+    size_t smem = transport_smem_bytes(k, block, savedet);
+    int bps = transport_blocks_per_sm(reflect, savedet, transport_mode(k), block, smem);
+    if (bps <= 0 && k.tile_on) {
+        k.tile_on = 0;
+        smem = transport_smem_bytes(k, block, savedet);
+        bps = transport_blocks_per_sm(reflect, savedet, transport_mode(k), block, smem);
+    }
+    if (bps <= 0) MCXG_RAISE(-6, "the transport kernel does not fit on this device");
     NCK(launch_transport(k, reflect, savedet, bps * sms, block, smem, stream));
 
+    // the error word and the detected count are always read back: a run stopped by the step cap
+    // or the index guard fails even when the caller asks for no statistics
+    double e[kNumEnergy];
+    unsigned long long c[kNumCounters];
     if (stats) {
-        double e[kNumEnergy];
-        unsigned long long c[kNumCounters];
-        unsigned words[2];
         NCK(cudaMemcpyAsync(e, s + kOffEnergy, sizeof(e), cudaMemcpyDeviceToHost, stream));
         NCK(cudaMemcpyAsync(c, s + kOffCounters, sizeof(c), cudaMemcpyDeviceToHost, stream));
-        NCK(cudaMemcpyAsync(words, s + kOffErr, sizeof(words), cudaMemcpyDeviceToHost, stream));
-        NCK(cudaStreamSynchronize(stream));
+    }
+    NCK(cudaMemcpyAsync(words, s + kOffErr, sizeof(words), cudaMemcpyDeviceToHost, stream));
+    NCK(cudaStreamSynchronize(stream));
+    if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->e_launch = e[kELaunch]; stats->e_escape = e[kEEscape]; stats->e_detect = e[kEDetect];
         stats->e_absdep = e[kEAbsDep]; stats->e_absother = e[kEAbsOther];
@@ -192,6 +222,8 @@ void run_noalloc(const Config* cfg, const uint8_t* d_labels, float* d_field, flo
         stats->grid = bps * sms; stats->block = block; stats->chunk = k.chunk; stats->launches = 1;
         stats->error_flags = words[0];
     }
+    if (words[0] & kErrStepCap) MCXG_RAISE(-6, "a photon exceeded the per-photon step cap; the simulation was stopped");
+    if (words[0] & kErrIndex) MCXG_RAISE(-6, "internal error: a photon's voxel index left the volume; the photon was stopped");
 }
 
 }  // namespace

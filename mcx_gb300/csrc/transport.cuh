@@ -217,6 +217,12 @@ size_t source_pattern_len(const struct MCXConfig* cfg);
 // Rejects source settings the engine does not run (MCX error -6).
 void check_source(const struct MCXConfig* cfg);
 
+// Process-wide settings of new simulations (engine.cu): the RNG seeding scheme (0 = per-photon
+// streams, 1 = MCX's per-thread streams; mcxg_set_seeding or MCXG_SEEDING=mcx) and the per-photon
+// step cap (mcxg_set_step_cap).
+int current_seeding_mode();
+unsigned current_step_cap();
+
 // Void skipping of a pencil source launched outside the volume or in a 0 voxel, traced once on
 // the host (engine.cu).  Returns the entry voxel or -1.
 int host_skipvoid(const struct MCXConfig* cfg, float4& p, float3& v, float& t, int fd[3]);

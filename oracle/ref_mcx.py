@@ -42,9 +42,17 @@ CPP_FILES = ["mcx_neurojson.cpp", "mcx_mie.cpp"]
 ZMAT_FILES = ["zmat/zmatlib.c", "zmat/miniz/miniz.c", "zmat/lz4/lz4.c", "zmat/lz4/lz4hc.c"]
 
 
-def stage(reference: str | Path = "/root/reference") -> Path:
+def reference_root(reference: str | Path | None = None) -> Path:
+    """The reference checkout: the argument, else the MCX_REFERENCE_ROOT environment variable."""
+    root = reference or os.environ.get("MCX_REFERENCE_ROOT")
+    if not root:
+        raise RuntimeError("name the MCX checkout: stage(<path>), `ref_mcx.py stage <path>` or MCX_REFERENCE_ROOT=<path>")
+    return Path(root)
+
+
+def stage(reference: str | Path | None = None) -> Path:
     """Copy the reference's src/ tree into baseline/_ref/src (run where the checkout exists)."""
-    src = Path(reference) / "src"
+    src = reference_root(reference) / "src"
     if SRC.exists():
         shutil.rmtree(SRC)
     SRC.parent.mkdir(parents=True, exist_ok=True)
@@ -70,10 +78,9 @@ def _run(cmd: list[str], cwd: Path) -> None:
         raise RuntimeError("reference build step failed:\n" + " ".join(cmd) + "\n" + p.stdout[-3000:] + p.stderr[-3000:])
 
 
-def build(force: bool = False) -> Path:
-    """Compile the reference `mcx` binary for sm_103a from baseline/_ref/src."""
-    if BIN.exists() and not force:
-        return BIN
+def _object_jobs(with_core: bool) -> tuple[list[list[str]], list[Path]]:
+    """Compile commands and objects of the reference's `mcx` binary: its CUDA translation unit
+    (src/mcx_core.cu) when `with_core`, and its host files (CLI, input parsing, output writers)."""
     if not available():
         raise RuntimeError("the reference sources are not staged in baseline/_ref/src")
     cuda = _cuda_home()
@@ -86,11 +93,12 @@ def build(force: bool = False) -> Path:
     inc = ["-Izmat", "-Izmat/easylzma", "-Izmat/miniz", "-Iubj", f"-I{cuda}/include"]
     jobs = []
     objs = []
-    o = obj / "mcx_core.o"
-    objs.append(o)
-    jobs.append([str(cuda / "bin" / "nvcc"), "-c", "-DUSE_ATOMIC", "-use_fast_math", "-DSAVE_DETECTORS", "-arch=sm_103a",
-                 "-Xcompiler", "-fopenmp", "-DMCX_TARGET_NAME=\"Kilo-Kelvin\"", "-lineinfo", *inc, "-o", str(o),
-                 "mcx_core.cu"])
+    if with_core:
+        o = obj / "mcx_core.o"
+        objs.append(o)
+        jobs.append([str(cuda / "bin" / "nvcc"), "-c", "-DUSE_ATOMIC", "-use_fast_math", "-DSAVE_DETECTORS",
+                     "-arch=sm_103a", "-Xcompiler", "-fopenmp", "-DMCX_TARGET_NAME=\"Kilo-Kelvin\"", "-lineinfo", *inc,
+                     "-o", str(o), "mcx_core.cu"])
     for f in C_FILES:
         o = obj / (f.replace("/", "_") + ".o")
         objs.append(o)
@@ -106,13 +114,50 @@ def build(force: bool = False) -> Path:
         jobs.append(["gcc", "-O3", "-fPIC", "-DNO_ZLIB", "-DNO_ZSTD", "-DNO_BLOSC2", *inc, "-Izmat/easylzma/pavlov",
                      "-c", "-o", str(o), f])
     # objects already built from the same sources are kept (the CUDA file dominates the build)
-    jobs = [j for j in jobs if not Path(j[j.index("-o") + 1]).exists()]
+    return [j for j in jobs if not Path(j[j.index("-o") + 1]).exists()], objs
+
+
+def _compile(jobs: list[list[str]]) -> None:
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(lambda c: _run(c, SRC), jobs))
+
+
+def build(force: bool = False) -> Path:
+    """Compile the reference `mcx` binary for sm_103a from baseline/_ref/src."""
+    if BIN.exists() and not force:
+        return BIN
+    jobs, objs = _object_jobs(with_core=True)
+    _compile(jobs)
     BIN.parent.mkdir(parents=True, exist_ok=True)
-    _run(["g++", "-o", str(BIN), *map(str, objs), "-fopenmp", f"-L{cuda}/lib64", "-lcudart_static", "-ldl", "-lrt",
-          "-lpthread", "-lm"], SRC)
+    _run(["g++", "-o", str(BIN), *map(str, objs), "-fopenmp", f"-L{_cuda_home()}/lib64", "-lcudart_static", "-ldl",
+          "-lrt", "-lpthread", "-lm"], SRC)
     return BIN
+
+
+FRONTEND_BIN = REF / "bin" / "mcx_on_gb300"
+
+
+def build_frontend(engine_lib: str | Path, force: bool = False) -> Path:
+    """MCX's own command-line front-end (src/mcx.c with the unchanged input parsing, output
+    writers and error handler of src/mcx_utils.c and their helpers) linked against the GB300
+    engine's shared library in place of the reference's src/mcx_core.cu: the drop-in boundary
+    (mcx_run_simulation / mcx_list_gpu, src/mcx_core.h:200-201) exercised by the real caller.
+    The executable exports its symbols so the engine's weak mcx_error / mcx_savedata /
+    mcx_savedetphoton references bind to the front-end's own."""
+    engine_lib = Path(engine_lib).resolve()
+    if FRONTEND_BIN.exists() and not force and FRONTEND_BIN.stat().st_mtime >= engine_lib.stat().st_mtime:
+        return FRONTEND_BIN
+    jobs, objs = _object_jobs(with_core=False)
+    _compile(jobs)
+    FRONTEND_BIN.parent.mkdir(parents=True, exist_ok=True)
+    # only the front-end's handlers are exported to the engine; the CUDA runtime the front-end's
+    # timer (src/mcx_tictoc.c) links stays private to the executable
+    dyn = REF / "obj" / "frontend_exports.txt"
+    dyn.write_text("{ mcx_error; mcx_savedata; mcx_savedetphoton; };\n")
+    _run(["g++", "-o", str(FRONTEND_BIN), *map(str, objs), "-fopenmp", f"-Wl,--dynamic-list={dyn}", str(engine_lib),
+          f"-Wl,-rpath,{engine_lib.parent}", f"-L{_cuda_home()}/lib64", "-lcudart_static", "-ldl", "-lrt", "-lpthread",
+          "-lm"], SRC)
+    return FRONTEND_BIN
 
 
 MIE_LIB = REF / "lib" / "libmcxmie.so"
@@ -284,6 +329,6 @@ if __name__ == "__main__":
     import sys
 
     if len(sys.argv) > 1 and sys.argv[1] == "stage":
-        print(stage(sys.argv[2] if len(sys.argv) > 2 else "/root/reference"))
+        print(stage(sys.argv[2] if len(sys.argv) > 2 else None))
     else:
         print(build(force="--force" in sys.argv))

@@ -93,4 +93,9 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    import os
+
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MCX_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <MCX checkout> (or set MCX_REFERENCE_ROOT)")
+    main(Path(root))

@@ -11,7 +11,17 @@ import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REFERENCE_SRC = Path("/root/reference/src")
+
+def _reference_src() -> Path:
+    """MCX's src/ tree: $MCX_REFERENCE_ROOT/src when set, else the copy oracle/ref_mcx.py stages
+    into baseline/_ref/src."""
+    import os
+
+    root = os.environ.get("MCX_REFERENCE_ROOT")
+    return Path(root) / "src" if root else ROOT / "baseline" / "_ref" / "src"
+
+
+REFERENCE_SRC = _reference_src()
 
 def _probe_offsets(include_dir: Path, header: str, tmp_path: Path) -> dict[str, int]:
     """Compile a C probe printing offsetof() of every Config field and the struct sizes."""
@@ -234,3 +244,37 @@ def test_debug_flags_and_trajectory_only(engine):
     pc = engine.prepare(problems.cube60(100) | {"debuglevel": "T", "issavedet": 1,
                                                   "detpos": np.array([[29, 34, 0, 2]], np.float32)})
     assert pc.c.issave2pt == b"\x00" and pc.c.issavedet == b"\x00"
+
+
+def test_photon_shares_over_devices(built):
+    """The multi-device photon split (src/mcx_core.cu:2980-3007): shares in proportion to the
+    workload, or to the core counts when none is given; the last device takes the remainder."""
+    from mcx_gb300 import abi, prepare, problems
+    from mcx_gb300._lib import lib
+
+    pc = prepare(problems.cube60(1000))
+    c = pc.c
+
+    def shares(ids, n, work=None, cores=None):
+        C.memmove(C.addressof(c) + abi.Config.deviceid.offset, bytes(ids) + b"\0", len(ids) + 1)
+        for i in range(len(ids)):
+            c.workload[i] = 0.0 if work is None else work[i]
+        info = None
+        if cores is not None:
+            info = (abi.GPUInfo * max(ids))()
+            for i, k in enumerate(cores):
+                info[i].core = k
+        off = (C.c_uint64 * len(ids))()
+        cnt = (C.c_uint64 * len(ids))()
+        rc = lib.mcxg_photon_shares(C.byref(c), info, n, off, cnt)
+        return rc, list(off), list(cnt)
+
+    assert shares([1], 1000) == (1, [0], [1000])
+    assert shares([1, 2], 1001) == (2, [0, 500], [500, 501])
+    assert shares([1, 2], 1000, work=[3.0, 1.0]) == (2, [0, 750], [750, 250])
+    rc, off, cnt = shares([1, 2, 3], 10 ** 9 + 7, cores=[19456, 19456, 9728])
+    assert rc == 3 and sum(cnt) == 10 ** 9 + 7 and off == [0, cnt[0], cnt[0] + cnt[1]]
+    assert cnt[0] == cnt[1] == (10 ** 9 + 7) * 2 // 5 and list(c.workload[:3]) == [19456.0, 19456.0, 9728.0]
+    assert shares([1, 1], 7) == (2, [0, 3], [3, 4])          # one device listed twice
+    rc, _, _ = shares([1, 2], 100, work=[1.0, 0.0])
+    assert rc == -1 and b"workload" in lib.mcxg_last_error()

@@ -77,3 +77,38 @@ def test_noalloc_matches_session_twice(engine):
         assert (np.abs(got[hot] - ref_field[hot]) / ref_field[hot]).max() < 2e-3, call
         rec = detp.cpu().numpy()[: ref_ndet * reclen].reshape((reclen, ref_ndet), order="F")
         assert np.array_equal(rec[:, np.lexsort(rec[::-1])], ref_rec[:, np.lexsort(ref_rec[::-1])]), call
+
+
+def test_noalloc_reports_errors_without_stats(engine):
+    """Errors come back through the return value even when the caller passes no statistics: a
+    run stopped by the per-photon step cap, a label past the medium table, MCX seeding."""
+    torch = pytest.importorskip("torch")
+    from mcx_gb300._lib import lib
+
+    pc = engine.prepare(problems.workload0(20_000, seed=SEED))
+    nx, ny, nz = pc.dims
+    nvox = nx * ny * nz
+    dev = torch.device("cuda", 0)
+    field = torch.zeros(nvox * pc.ngates, dtype=torch.float32, device=dev)
+    spill = torch.zeros_like(field)
+
+    def call(labels):
+        return lib.mcxg_run_noalloc(C.byref(pc.c), labels.data_ptr(), field.data_ptr(), spill.data_ptr(), None,
+                                    0, 20_000, 0, None, None)
+
+    good = torch.from_numpy(byte_labels(pc.vol)).to(dev)
+    assert call(good) == 0, lib.mcxg_last_error()
+    lib.mcxg_set_step_cap(100)
+    try:
+        assert call(good) == -6 and b"step cap" in lib.mcxg_last_error()
+    finally:
+        lib.mcxg_set_step_cap(0)
+    bad = good.clone()
+    bad[nvox // 2] = int(pc.c.medianum)           # one label past the table
+    assert call(bad) == -4
+    lib.mcxg_set_seeding(1)
+    try:
+        assert call(good) == -6 and b"seeding" in lib.mcxg_last_error()
+    finally:
+        lib.mcxg_set_seeding(0)
+    assert call(good) == 0, lib.mcxg_last_error()
