@@ -20,6 +20,10 @@ extern "C" {
 
 const char* mcxg_dn_last_error(void);
 
+/* Waits for `stream` and reports whether a tensor-core convolution launched before gave up a
+ * bounded wait for its MMAs (then its output is invalid): 0, or -1 with a message. */
+int mcxg_dn_check(void* stream);
+
 /* y = act(conv3d(x, w) + bias) [* (mask > 0)]: 3x3x3 (taps = 27, zero padding 1) or 1x1x1
  * (taps = 1) convolution, stride 1.  cin, cout multiples of 16.  bias and mask may be NULL;
  * relu != 0 applies max(0, .) before the mask.  Run on the transposed weights the optimiser

@@ -105,6 +105,8 @@ _DN = {
 for _name, _args in _DN.items():
     getattr(lib, _name).argtypes = _args
     getattr(lib, _name).restype = C.c_int
+lib.mcxg_dn_check.argtypes = [C.c_void_p]
+lib.mcxg_dn_check.restype = C.c_int
 lib.mcxg_dn_last_error.argtypes = []
 lib.mcxg_dn_last_error.restype = C.c_char_p
 
@@ -115,5 +117,5 @@ EXPORTED = [
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
     "mcxg_set_seeding", "mcxg_probe_atomic_rate",
     "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap", "mcxg_dn_last_error",
-    "mcxg_set_field_precision", "mcxg_photon_shares",
+    "mcxg_set_field_precision", "mcxg_photon_shares", "mcxg_dn_check",
 ] + list(_DN)

@@ -24,6 +24,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 
 #include "mcxg_denoise.h"
 
@@ -397,6 +398,276 @@ __global__ void __launch_bounds__(128) conv3_halo_kernel(const bf16* __restrict_
         }
         *reinterpret_cast<uint4*>(y + o) = val;
     }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 3x3x3 convolution for narrow outputs (BN = 16 or 32 channels) on the fifth-generation tensor
+// cores: tcgen05.mma (cta_group::1, kind::f16, BF16 operands from shared memory, FP32 accumulator
+// in tensor memory), issued by one thread.  The CTA's 128 output voxels are one z-plane of 16 y
+// rows x 8 x voxels, so its eight-voxel rows are a uniform stride apart in the halo.  Per
+// 16-channel slice of the input, the 3 x 18 x 10 halo around the tile is staged once with
+// cp.async as two 8-channel planes of 16-byte rows, and every tap's A operand is the same halo
+// seen through a descriptor whose start moves by the tap's row offset: K-major, no swizzle, core
+// matrices of 8 consecutive rows (8 consecutive x), the 8-row groups HX rows apart (stride byte
+// offset), the second 8 channels one plane further on (leading byte offset).  The weights of the
+// slice's 27 taps sit beside it as [tap][8-channel half][co] 16-byte rows.  Each slice is 27 MMAs
+// of 128 x BN x 16 into the same accumulator; two stages overlap the next slice's copies with the
+// current slice's MMAs, whose completion tcgen05.commit signals on an mbarrier per stage.  The
+// epilogue reads the accumulator rows (TMEM lane = voxel) with tcgen05.ld, adds bias, applies
+// ReLU and the mask, and stores bf16.  Every wait is bounded: a wait that gives up sets
+// g_dn_fault, and the CTA still releases its tensor memory and returns.
+__device__ unsigned g_dn_fault;
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+// Waits for the completion of the mbarrier phase of parity `parity`; false after about a second.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > 2000000000LL) return false;
+    }
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+template <int BN>
+struct TcConvShape {
+    static constexpr int TY = 16, TX = 8;
+    static constexpr int HY = TY + 2, HX = TX + 2, HV = 3 * HY * HX;     // 540 halo rows
+    static constexpr int PLANE = HV * 16;                                 // one 8-channel plane
+    static constexpr int HALO = 2 * PLANE;
+    static constexpr int WTAP = 2 * BN * 16;                              // one tap's weights
+    static constexpr int WSLICE = 27 * WTAP;                              // one 16-channel slice
+};
+
+// The CTA is persistent: it loads the weights of every input slice once, then walks its tiles
+// (blockIdx.x, + gridDim.x, ...) as a sequence of (tile, slice) items.  Items alternate between
+// two halo buffers, so the copies of item k + 1 run while the MMAs of item k do (an mbarrier per
+// buffer tells when the MMAs that read it are done), and tiles alternate between two TMEM
+// accumulators, so the epilogue of one tile -- run once the next tile's first MMAs are issued --
+// overlaps them (an mbarrier per accumulator).  Stores of a tile's outputs are plain 16-byte
+// writes of its BN channels per voxel.
+template <int BN>
+__global__ void __launch_bounds__(128) conv3_tc_kernel(const bf16* __restrict__ x, const bf16* __restrict__ wt,
+                                                       const float* __restrict__ bias, const bf16* __restrict__ mask,
+                                                       bf16* __restrict__ y, Geo g, int cin, int cout, int relu,
+                                                       int tiles_x, int tiles_y, int ntiles) {
+    using S = TcConvShape<BN>;
+    constexpr uint32_t TMEM_COLS = (2 * BN < 32) ? 32 : 2 * BN;          // two accumulators
+    static_assert(BN == 16 || BN == 32, "tile width");
+    static_assert(S::WSLICE % 16 == 0 && S::PLANE % 16 == 0, "16-byte operand alignment");
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    __shared__ __align__(8) uint64_t s_bar[4];          // halo buffer 0, 1; accumulator 0, 1
+    __shared__ uint32_t s_tmem;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int slices = cin / 16;
+    const int n0 = blockIdx.y * BN;
+    unsigned char* sw = dyn_smem;                                  // [slice][tap][half][co] rows
+    unsigned char* sh = dyn_smem + slices * S::WSLICE;             // two halo buffers
+    const uint32_t sw_addr = smem_addr(sw), sh_addr = smem_addr(sh);
+    const uint32_t bar0 = smem_addr(&s_bar[0]);
+    const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int items = my_tiles * slices;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&s_tmem)),
+                     "n"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8 * i));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = s_tmem;
+
+    // the weights of every slice, once
+    for (int q = tid; q < slices * 27 * 2 * BN; q += 128) {
+        const int co = q % BN, r = q / BN, kb = r & 1, t = (r >> 1) % 27, sl = (r >> 1) / 27;
+        const bf16* p = wt + ((long long)(n0 + co) * 27 + t) * cin + sl * 16 + kb * 8;
+        cp_async16(sw_addr + sl * S::WSLICE + t * S::WTAP + kb * BN * 16 + co * 16, p, true);
+    }
+    cp_commit();
+
+    struct TileAt {
+        int z0, y0, x0;
+        long long vol0;
+    };
+    auto tile_at = [&](int j) {
+        int tile = (int)blockIdx.x + j * (int)gridDim.x;
+        const int txi = tile % tiles_x;
+        tile /= tiles_x;
+        const int tyi = tile % tiles_y;
+        tile /= tiles_y;
+        TileAt r;
+        r.z0 = tile % g.d;
+        r.vol0 = (long long)(tile / g.d) * g.d * g.h * g.w;
+        r.x0 = txi * S::TX;
+        r.y0 = tyi * S::TY;
+        return r;
+    };
+    auto load_halo = [&](int k) {
+        const TileAt T = tile_at(k / slices);
+        const int c0 = (k % slices) * 16;
+        const uint32_t dst = sh_addr + (k & 1) * S::HALO;
+        for (int q = tid; q < S::HV * 2; q += 128) {
+            const int c = q / S::HV, hv = q - c * S::HV;
+            const int hx = hv % S::HX, hy = (hv / S::HX) % S::HY, hz = hv / (S::HX * S::HY);
+            const int zz = T.z0 + hz - 1, yy = T.y0 + hy - 1, xx = T.x0 + hx - 1;
+            const bool ok = zz >= 0 && zz < g.d && yy >= 0 && yy < g.h && xx >= 0 && xx < g.w;
+            const bf16* p = ok ? x + (T.vol0 + ((long long)zz * g.h + yy) * g.w + xx) * cin + c0 + c * 8 : x;
+            cp_async16(dst + c * S::PLANE + hv * 16, p, ok);
+        }
+        cp_commit();
+    };
+    // outputs of local tile j from accumulator j & 1
+    auto epilogue = [&](int j) {
+        const TileAt T = tile_at(j);
+        const int r = warp * 32 + lane;                 // accumulator row = TMEM lane = voxel of the tile
+        const int yy = T.y0 + (r >> 3), xx = T.x0 + (r & 7);
+        const bool inside = yy < g.h && xx < g.w;
+        const long long vo = T.vol0 + ((long long)T.z0 * g.h + yy) * g.w + xx;
+        const uint32_t col = (uint32_t)((j & 1) * BN);
+#pragma unroll
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + col + (uint32_t)c0, v);
+            if (!inside) continue;
+            uint32_t pk[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                float a = __uint_as_float(v[2 * e]), b = __uint_as_float(v[2 * e + 1]);
+                if (bias) {
+                    a += bias[n0 + c0 + 2 * e];
+                    b += bias[n0 + c0 + 2 * e + 1];
+                }
+                if (relu) {
+                    a = fmaxf(a, 0.f);
+                    b = fmaxf(b, 0.f);
+                }
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(a, b);
+                pk[e] = *reinterpret_cast<uint32_t*>(&h2);
+            }
+            const long long o = vo * cout + n0 + c0;
+#pragma unroll
+            for (int hlf = 0; hlf < 2; ++hlf) {
+                uint4 val = make_uint4(pk[4 * hlf], pk[4 * hlf + 1], pk[4 * hlf + 2], pk[4 * hlf + 3]);
+                if (mask) {
+                    uint4 mk = *reinterpret_cast<const uint4*>(mask + o + 8 * hlf);
+                    uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
+                    const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
+                        uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
+                                        ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
+                        pv[e] &= keep;
+                    }
+                }
+                *reinterpret_cast<uint4*>(y + o + 8 * hlf) = val;
+            }
+        }
+    };
+
+    bool fault = false;
+    if (items > 0) load_halo(0);
+    for (int k = 0; k < items && !fault; ++k) {
+        const int j = k / slices, sl = k - j * slices;
+        if (k + 1 < items) {
+            // halo buffer (k + 1) & 1 was read by the MMAs of item k - 1
+            bool ok = true;
+            if (k >= 1) ok = mbar_wait(bar0 + 8 * ((k + 1) & 1), ((k - 1) >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                fault = true;
+                break;
+            }
+            load_halo(k + 1);
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
+        }
+        // copies land through the generic proxy; the tensor cores read through the async proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = sh_addr + (k & 1) * S::HALO, sb = sw_addr + sl * S::WSLICE;
+            const uint32_t d = tmem + (uint32_t)((j & 1) * BN);
+#pragma unroll 1
+            for (int t = 0; t < 27; ++t) {
+                const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
+                const uint64_t ad = umma_desc(sa + ((dz * S::HY + dy) * S::HX + dx) * 16, S::PLANE, S::HX * 16);
+                const uint64_t bd = umma_desc(sb + t * S::WTAP, BN * 16, 128);
+                const uint32_t accum = (sl > 0 || t > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                    "l"(ad), "l"(bd), "r"(umma_idesc_bf16(BN)), "r"(accum)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             bar0 + 8 * (k & 1))
+                         : "memory");
+            if (sl == slices - 1)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 bar0 + 16 + 8 * (j & 1))
+                             : "memory");
+        }
+        __syncwarp();
+        // the previous tile's outputs, while this tile's MMAs run
+        if (sl == 0 && j >= 1) {
+            const bool ok = mbar_wait(bar0 + 16 + 8 * ((j - 1) & 1), ((j - 1) >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                fault = true;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            epilogue(j - 1);
+        }
+    }
+    if (!fault && my_tiles > 0) {
+        const int j = my_tiles - 1;
+        const bool ok = mbar_wait(bar0 + 16 + 8 * (j & 1), (j >> 1) & 1);
+        fault = __syncthreads_or(!ok);
+        if (!fault) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            epilogue(j);
+        }
+    }
+    if (fault) {
+        cp_wait<0>();
+        if (tid == 0) atomicOr(&g_dn_fault, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(TMEM_COLS));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -908,8 +1179,54 @@ int conv3_halo_launch(const bf16* x, const bf16* w, const float* bias, const bf1
     return launched();
 }
 
+template <int BN>
+int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
+                    int cout, int relu, cudaStream_t st) {
+    using S = TcConvShape<BN>;
+    const int smem = (cin / 16) * S::WSLICE + 2 * S::HALO;
+    if (smem > 227 * 1024) return fail("conv: weights of this layer do not fit in shared memory");
+    auto kern = conv3_tc_kernel<BN>;
+    static int attr = 0;
+    if (smem > attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = smem;
+    }
+    const int tx = (g.w + S::TX - 1) / S::TX, ty = (g.h + S::TY - 1) / S::TY;
+    const long long tiles = (long long)g.nvol * g.d * tx * ty;
+    if (tiles >= (1LL << 31)) return fail("conv: too many tiles");
+    // persistent CTAs: as many as fit on the SMs, each walking its tiles
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+    if (per_sm < 1) return fail("conv: the tensor-core kernel does not fit on this device");
+    const int ny = cout / BN;
+    long long grid = (long long)sms * per_sm / ny;
+    if (grid < 1) grid = 1;
+    if (grid > tiles) grid = tiles;
+    kern<<<dim3((unsigned)grid, (unsigned)ny), 128, smem, st>>>(x, w, bias, mask, y, g, cin, cout, relu, tx, ty,
+                                                               (int)tiles);
+    return launched();
+}
+
+// Narrow 3x3x3 layers run on tcgen05 unless MCXG_DN_MMA_SYNC=1 selects the warp-level mma.sync
+// halo kernel (kept as the measured baseline of the tensor-core port).
+bool use_tcgen05() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("MCXG_DN_MMA_SYNC");
+        v = (e && e[0] == '1') ? 0 : 1;
+    }
+    return v == 1;
+}
+
 int conv_fwd_dispatch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
                       int cout, int taps, int relu, cudaStream_t st) {
+    if (use_tcgen05() && taps == 27 && cin % 16 == 0) {
+        if (cout % 32 == 0 && cout / 32 <= 3 && cout % 64 != 0)
+            return conv3_tc_launch<32>(x, w, bias, mask, y, g, cin, cout, relu, st);
+        if (cout % 32 != 0) return conv3_tc_launch<16>(x, w, bias, mask, y, g, cin, cout, relu, st);
+    }
     // narrow 3x3x3 layers: halo tiles (each input voxel loaded once per tile, not once per tap)
     if (taps == 27 && cin % 16 == 0 && cout % 32 == 0 && cout / 32 <= 3 && cout % 64 != 0)
         return conv3_halo_launch<32>(x, w, bias, mask, y, g, cin, cout, relu, st);
@@ -960,6 +1277,27 @@ bool dims_ok(int nvol, int d, int h, int w) { return nvol > 0 && d > 0 && h > 0 
 extern "C" {
 
 const char* mcxg_dn_last_error(void) { return g_err; }
+
+int mcxg_dn_check(void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof(g_err), "denoiser stream: %s", cudaGetErrorString(e));
+        return -(int)e;
+    }
+    unsigned f = 0;
+    e = cudaMemcpyFromSymbol(&f, g_dn_fault, sizeof(f));
+    if (e != cudaSuccess) {
+        snprintf(g_err, sizeof(g_err), "denoiser fault word: %s", cudaGetErrorString(e));
+        return -(int)e;
+    }
+    if (f) {
+        const unsigned zero = 0;
+        cudaMemcpyToSymbol(g_dn_fault, &zero, sizeof(zero));
+        return fail("a tensor-core convolution gave up waiting for its MMAs (bounded wait); its output is invalid");
+    }
+    return 0;
+}
 
 int mcxg_dn_conv_fwd(const void* x, const void* w, const float* bias, const void* mask, void* y, int nvol, int d,
                      int h, int wd, int cin, int cout, int taps, int relu, void* stream) {

@@ -850,6 +850,11 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     S.pool[2 * warp] = pool_next;
                     S.pool[2 * warp + 1] = pool_end;
                 }
+                // the pool and the drained flag are read by every lane at the next refill: a warp
+                // barrier makes lane 0's writes visible to them (the ballots in between order the
+                // lanes but not their shared-memory accesses, and the compiler may keep a lane's
+                // earlier reads of these words in registers across them)
+                __syncwarp();
                 if (!alive && !start && mine < P.d_nwork) {
                     if (FULL && P.replay) {
                         // a detected photon again: its saved launch state and detection record

@@ -558,6 +558,93 @@ def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, ta
     return out
 
 
+def time_to_error_batch(net: UNet, cfgs: list[dict[str, Any]], judge_photons: float = 1e9,
+                        targets: tuple[float, ...] = (0.05, 0.02),
+                        ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
+                        dn_ladder: tuple[float, ...] = (1e5, 2e5, 3e5, 6e5, 1e6, 3e6, 1e7),
+                        judge_check: bool = True) -> dict[str, Any]:
+    """Time for each pipeline to deliver every volume of `cfgs` at a median relative fluence error
+    of each target against a `judge_photons` run of that volume, with all volumes simulated
+    together through the batched entry point (one CUDA graph per call), so a short simulation's
+    latency -- its longest photons -- is paid once per call rather than once per volume.
+
+    The errors come from ladders of budgets (every budget one batched call over all volumes).  Plain
+    MC: each volume's photon count for the target is interpolated in its ladder (log-log, the
+    1/sqrt(N) law past the last budget), then ONE batched call runs every volume at its own count
+    and is timed: on the device (graph time) and end to end (wall time of the call).  MC + denoiser:
+    each volume takes the smallest budget of `dn_ladder` whose denoised map reaches the target
+    (volumes that none reaches fall back to plain MC at their plain count), then one batched call
+    runs them and the network denoises every volume: device time = graph time + network GPU time,
+    wall time = the call + the denoise calls.  The measured errors of those final runs are returned
+    beside the times."""
+    from .api import run_batch
+
+    V = len(cfgs)
+    seed = lambda c, k: int((int(c["seed"]) + 7919 * k) % (2**31 - 1)) or 1  # noqa: E731
+
+    def batch(budgets, k):
+        t0 = time.perf_counter()
+        res, ms = run_batch([dict(c, nphoton=int(n), seed=seed(c, k)) for c, n in zip(cfgs, budgets)])
+        return [_flat(r["flux"]) for r in res], ms * 1e-3, time.perf_counter() - t0
+
+    judges, _, judge_s = batch([judge_photons] * V, 1)
+    judge_err = None
+    if judge_check:
+        j4, _, _ = batch([judge_photons / 4] * V, 2)
+        judge_err = [median_rel_error(a, b) / math.sqrt(5.0) for a, b in zip(j4, judges)]
+    plain = []
+    for i, n in enumerate(ladder):
+        maps, dev_s, wall_s = batch([n] * V, 10 + i)
+        plain.append({"photons": n, "errors": [median_rel_error(m, j) for m, j in zip(maps, judges)],
+                      "s": wall_s, "kernel_s": dev_s})
+    for c in cfgs:
+        net.denoise(np.ones(c["vol"].shape, np.float32), c["vol"], c["prop"], 1e5)   # buffers for the grid
+    torch.cuda.synchronize()
+    dn = []
+    for i, n in enumerate(dn_ladder):
+        maps, _, _ = batch([n] * V, 30 + i)
+        errs = [median_rel_error(_flat(net.denoise(m.reshape(c["vol"].shape, order="F"), c["vol"], c["prop"], n)), j)
+                for m, c, j in zip(maps, cfgs, judges)]
+        dn.append({"photons": n, "errors": errs})
+
+    def plain_photons(v, tgt):
+        lad = [{"photons": r["photons"], "error": r["errors"][v]} for r in plain]
+        for a, b in zip(lad, lad[1:]):
+            if a["error"] > tgt >= b["error"]:
+                slope = math.log(b["error"] / a["error"]) / math.log(b["photons"] / a["photons"])
+                return a["photons"] * (tgt / a["error"]) ** (1.0 / slope)
+        return lad[-1]["photons"] * (lad[-1]["error"] / tgt) ** 2 if lad[-1]["error"] > tgt else lad[0]["photons"]
+
+    per = []
+    for t_i, tgt in enumerate(targets):
+        n_plain = [plain_photons(v, tgt) for v in range(V)]
+        maps, p_dev, p_wall = batch(n_plain, 60 + t_i)
+        p_err = [median_rel_error(m, j) for m, j in zip(maps, judges)]
+        n_dn, use_dn = [], []
+        for v in range(V):
+            rec = next((r for r in dn if r["errors"][v] <= tgt), None)
+            use_dn.append(rec is not None)
+            n_dn.append(rec["photons"] if rec else n_plain[v])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, ms = run_batch([dict(c, nphoton=int(n), seed=seed(c, 80 + t_i)) for c, n in zip(cfgs, n_dn)])
+        net_ms, d_err = 0.0, []
+        for v, (r, c) in enumerate(zip(res, cfgs)):
+            f = r["flux"][..., 0]
+            if use_dn[v]:
+                f = net.denoise(f, c["vol"], c["prop"], n_dn[v])
+                net_ms += net.last_gpu_ms
+            d_err.append(median_rel_error(_flat(f), judges[v]))
+        d_wall = time.perf_counter() - t0
+        d_dev = ms * 1e-3 + net_ms * 1e-3
+        per.append({"target": tgt, "photons_plain": n_plain, "t_plain_s": p_wall, "t_plain_device_s": p_dev,
+                    "error_plain": p_err, "photons_denoised": n_dn, "denoised": use_dn, "t_denoised_s": d_wall,
+                    "t_denoised_device_s": d_dev, "network_s": net_ms * 1e-3, "error_denoised": d_err,
+                    "speedup": p_wall / d_wall, "speedup_device": p_dev / d_dev})
+    return {"volumes": V, "judge_photons": judge_photons, "judge_s": judge_s, "judge_error_est": judge_err,
+            "plain": plain, "denoised": dn, "targets": per}
+
+
 def main(argv: list[str] | None = None) -> None:
     """``python -m mcx_gb300.denoise train ...``: simulate training pairs, train, save the weights."""
     import argparse

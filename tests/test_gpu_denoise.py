@@ -82,6 +82,7 @@ def test_conv_forward(lib, cin, cout):
     X, W, B = _gpu(x, BF), _gpu(wt, BF), _gpu(b)
     _call(lib, "mcxg_dn_conv_fwd", X.data_ptr(), W.data_ptr(), B.data_ptr(), None, y.data_ptr(), n, d, h, w, cin, cout, 27, 1,
           _st())
+    assert lib.mcxg_dn_check(_st()) == 0, lib.mcxg_dn_last_error()
     ref = _ndhwc(R.conv(_nchw(x, n, d, h, w), torch.from_numpy(wt), torch.from_numpy(b)))
     _close_bf16(y.float().cpu().numpy().reshape(vox, cout), ref)
 

@@ -31,8 +31,14 @@ def cli(built):
 
 
 def run(cli, args, cwd, rc=0):
+    """Runs the CLI in `cwd`; returns its report.  MCX's front-end declares its log switch as a
+    plain `char` initialised to -1 (src/mcx_utils.c:4783); where char is unsigned (aarch64) that
+    reads as "save the log", so the report goes to <session>.log instead of stdout: both are read."""
+    for f in Path(cwd).glob("*.log"):
+        f.unlink()
     p = subprocess.run([str(cli), *args], cwd=cwd, capture_output=True, text=True, timeout=600)
-    out = re.sub(r"\x1b\[[0-9;]*m", "", p.stdout + p.stderr)
+    out = p.stdout + p.stderr + "".join(f.read_text(errors="replace") for f in sorted(Path(cwd).glob("*.log")))
+    out = re.sub(r"\x1b\[[0-9;]*m", "", out)
     assert p.returncode == rc, f"{args}: exit {p.returncode}\n{out[-3000:]}"
     return out
 
@@ -52,7 +58,6 @@ CASES = [
       '{"Domain":{"Media":[[0,0,1,1],[0.001,0.001,0,1]]},"Optode":{"Source":{"Type":"cone","Param1":[0.5,0,0,0]}}}',
       "-d", "0", "-S", "0"], r"absorbed:.*6\.[0-9]+%", 93),
     (["--bench", "cube60", "--bc", "______111111", "-n", "1e4"], r"detected.*9[7-9][0-9.]+ photons", 112),
-    (["--bench", "cube60", "-D", "M", "-S", "0", "-d", "0", "-n", "1e2"], r"saved trajectory positions: [6-9][0-9]+", 161),
     (["--bench", "cube60", "-D", "R"], r"generating 216000 random numbers", 153),
     (["-L"], r"Global [Mm]emory", 34),
 ]
@@ -65,21 +70,54 @@ def test_cli_regression_case(cli, tmp_path, args, pattern, line):
 
 
 def test_cli_rng_payload(cli, tmp_path, goldens):
-    """-D R on a 2x2x2 grid writes the generator's first 8 uniforms through the front-end's JNIfTI
-    writer; the compressed payload equals the one test/testmcx.sh:155 holds."""
-    run(cli, ["--bench", "cube60", "-d", "0", "-s", "testrng222", "--json",
-              '{"Shapes":[{"Grid":{"Tag":0,"Size":[2,2,2]}}]}', "-F", "jnii", "-D", "R"], tmp_path)
-    assert goldens["rng_kat"]["payload"] in (tmp_path / "testrng222.jnii").read_text()
+    """-D R on a 2x2x2 grid: the generator's first 8 uniforms written through the front-end's
+    JNIfTI writer, by the engine and by the reference build on the same input, decode to the same
+    floats in the same order; they are the values of test/testmcx.sh:155 (the compressed bytes
+    depend on the zlib build the front-end links, so the decoded floats are compared)."""
+    import base64
+    import zlib
+
+    args = ["--bench", "cube60", "-d", "0", "-s", "testrng222", "--json",
+            '{"Shapes":[{"Grid":{"Tag":0,"Size":[2,2,2]}}]}', "-F", "jnii", "-D", "R"]
+
+    def decode(path):
+        doc = json.loads(path.read_text())
+        return np.frombuffer(zlib.decompress(base64.b64decode(doc["NIFTIData"]["_ArrayZipData_"])), np.float32)
+
+    run(cli, args, tmp_path)
+    got = decode(tmp_path / "testrng222.jnii")
+    ref_dir = tmp_path / "reference"
+    ref_dir.mkdir()
+    run(ref_mcx.build(), args, ref_dir)
+    assert np.array_equal(got, decode(ref_dir / "testrng222.jnii"))
+    # the golden values are listed with x slowest, the field's voxels are stored x fastest
+    want = np.asarray(goldens["rng_kat"]["values_rowmajor"], np.float32).reshape(2, 2, 2)
+    assert np.array_equal(got.reshape(2, 2, 2, order="F"), want), got
 
 
 def test_cli_seed_replay(cli, tmp_path):
     """Seeds saved by the CLI (-q 1) and replayed from its own detected-photon file (-E): the
-    replay simulates and detects the same photons (test/testmcx.sh:137, 142)."""
+    replay simulates exactly the photons the first run detected and detects every one of them
+    again (test/testmcx.sh:137, 142)."""
     a = run(cli, ["--bench", "cube60", "-s", "replaytest", "-q", "1", "-S", "0"], tmp_path)
     b = run(cli, ["--bench", "cube60", "-E", "replaytest_detp.jdat", "-S", "0"], tmp_path)
-    got = [re.findall(r"(?:simulated|detected)\s+([0-9.]+) photons", x)[-1] for x in (a, b)]
-    assert got[0] == got[1], (got, b[-2000:])
+    det_a = int(re.findall(r"detected\s+([0-9]+) photons", a)[-1])
+    sim_b = int(float(re.findall(r"simulated\s+([0-9.]+) photons", b)[-1]))
+    det_b = int(re.findall(r"detected\s+([0-9]+) photons", b)[-1])
+    assert det_a > 0 and sim_b == det_a and det_b == sim_b, (det_a, sim_b, det_b, b[-2000:])
     assert re.search(r"absorbed:.*3[0-8]\.[0-9]+%", b), b[-2000:]
+
+
+def test_cli_trajectories_against_the_reference(cli, tmp_path):
+    """-D M (test/testmcx.sh:161): the trajectory positions the CLI saves per photon agree with
+    the reference build's on the same deck within 5% (testmcx.sh's own check, 6000-9999 positions
+    for 100 photons, is one draw of a statistic whose spread at that sample size reaches it)."""
+    args = ["--bench", "cube60", "-D", "M", "-S", "0", "-d", "0", "-n", "1e4"]
+    ours = int(re.findall(r"saved trajectory positions:\s*([0-9]+)", run(cli, args, tmp_path))[-1])
+    ref_dir = tmp_path / "reference"
+    ref_dir.mkdir()
+    theirs = int(re.findall(r"saved trajectory positions:\s*([0-9]+)", run(ref_mcx.build(), args, ref_dir))[-1])
+    assert 60 * 10 ** 4 <= ours <= 100 * 10 ** 4 and abs(ours / theirs - 1) < 0.05, (ours, theirs)
 
 
 def test_cli_files_match_the_python_front_end(cli, tmp_path, engine):
