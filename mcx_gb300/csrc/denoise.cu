@@ -19,7 +19,9 @@
 // gradient is multiplied by (layer input > 0) in its epilogue, so every gradient handed to a
 // weight-gradient launch is already the pre-activation gradient.
 #include <cuda_bf16.h>
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include <cmath>
@@ -403,19 +405,18 @@ __global__ void __launch_bounds__(128) conv3_halo_kernel(const bf16* __restrict_
 // ---------------------------------------------------------------------------------------------
 // 3x3x3 convolution for narrow outputs (BN = 16 or 32 channels) on the fifth-generation tensor
 // cores: tcgen05.mma (cta_group::1, kind::f16, BF16 operands from shared memory, FP32 accumulator
-// in tensor memory), issued by one thread.  The CTA's 128 output voxels are one z-plane of 16 y
-// rows x 8 x voxels, so its eight-voxel rows are a uniform stride apart in the halo.  Per
-// 16-channel slice of the input, the 3 x 18 x 10 halo around the tile is staged once with
-// cp.async as two 8-channel planes of 16-byte rows, and every tap's A operand is the same halo
+// in tensor memory), issued by one thread, with the input halos brought in by TMA.  The CTA's 128
+// output voxels are one z-plane of 16 y rows x 8 x voxels, so its eight-voxel rows are a uniform
+// stride apart in the halo.  Per 16-channel slice of the input, the 3 x 18 x 10 halo around the
+// tile lands as two 8-channel planes of 16-byte rows, and every tap's A operand is the same halo
 // seen through a descriptor whose start moves by the tap's row offset: K-major, no swizzle, core
 // matrices of 8 consecutive rows (8 consecutive x), the 8-row groups HX rows apart (stride byte
-// offset), the second 8 channels one plane further on (leading byte offset).  The weights of the
-// slice's 27 taps sit beside it as [tap][8-channel half][co] 16-byte rows.  Each slice is 27 MMAs
-// of 128 x BN x 16 into the same accumulator; two stages overlap the next slice's copies with the
-// current slice's MMAs, whose completion tcgen05.commit signals on an mbarrier per stage.  The
-// epilogue reads the accumulator rows (TMEM lane = voxel) with tcgen05.ld, adds bias, applies
-// ReLU and the mask, and stores bf16.  Every wait is bounded: a wait that gives up sets
-// g_dn_fault, and the CTA still releases its tensor memory and returns.
+// offset), the second 8 channels one plane further on (leading byte offset).  The weights of a
+// slice's 27 taps sit in shared memory as [tap][8-channel half][co] 16-byte rows.  Each slice is
+// 27 MMAs of 128 x BN x 16 into one accumulator.  The epilogue reads the accumulator rows (TMEM
+// lane = voxel) with tcgen05.ld, adds bias, applies ReLU and the mask, and stores bf16.  Every
+// wait is bounded: a wait that gives up sets g_dn_fault, and the CTA still releases its tensor
+// memory and returns.
 __device__ unsigned g_dn_fault;
 
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -456,39 +457,54 @@ template <int BN>
 struct TcConvShape {
     static constexpr int TY = 16, TX = 8;
     static constexpr int HY = TY + 2, HX = TX + 2, HV = 3 * HY * HX;     // 540 halo rows
-    static constexpr int PLANE = HV * 16;                                 // one 8-channel plane
-    static constexpr int HALO = 2 * PLANE;
+    static constexpr int PLANE = 8704;                                    // 540 x 16 B, padded to 128 B
+    static constexpr int HALO = 2 * PLANE;                                // one stage: 16 channels
+    static constexpr int HALO_BYTES = 2 * HV * 16;                        // bytes the two copies bring
     static constexpr int WTAP = 2 * BN * 16;                              // one tap's weights
     static constexpr int WSLICE = 27 * WTAP;                              // one 16-channel slice
+    static constexpr int MAX_STAGES = 4;
 };
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Warp roles: warps 0-3 drain the accumulators (warp w reads TMEM lanes 32w..32w+31, the voxels of
+// its quarter of the tile), warp 4 issues the TMA copies of the halos, warp 5 issues the MMAs.
 // The CTA is persistent: it loads the weights of every input slice once, then walks its tiles
-// (blockIdx.x, + gridDim.x, ...) as a sequence of (tile, slice) items.  Items alternate between
-// two halo buffers, so the copies of item k + 1 run while the MMAs of item k do (an mbarrier per
-// buffer tells when the MMAs that read it are done), and tiles alternate between two TMEM
-// accumulators, so the epilogue of one tile -- run once the next tile's first MMAs are issued --
-// overlaps them (an mbarrier per accumulator).  Stores of a tile's outputs are plain 16-byte
-// writes of its BN channels per voxel.
+// (blockIdx.x, + gridDim.x, ...) as a sequence of (tile, slice) items.  Each item is one halo: two
+// TMA tile copies (channels c..c+7 and c+8..c+15) of a 3 x 18 x 10 voxel box of the channels-last
+// activations, described by a 5-D tensor map (channel, x, y, z, volume) whose out-of-volume rows
+// arrive as zeros; the box lands as 540 rows of 16 bytes, x fastest, which is the A operand's
+// canonical no-swizzle K-major layout.  Halos cycle through `stages` buffers (full barriers: the
+// copies landed; empty barriers: the MMAs that read the buffer finished), and tiles through two
+// TMEM accumulators (accfull: a tile's MMAs finished; accempty: its epilogue has read it), so
+// copies, MMAs and epilogues of neighbouring items overlap.
 template <int BN>
-__global__ void __launch_bounds__(128) conv3_tc_kernel(const bf16* __restrict__ x, const bf16* __restrict__ wt,
-                                                       const float* __restrict__ bias, const bf16* __restrict__ mask,
-                                                       bf16* __restrict__ y, Geo g, int cin, int cout, int relu,
-                                                       int tiles_x, int tiles_y, int ntiles) {
+__global__ void __launch_bounds__(192) conv3_tc_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                       const bf16* __restrict__ wt, const float* __restrict__ bias,
+                                                       const bf16* __restrict__ mask, bf16* __restrict__ y, Geo g,
+                                                       int cin, int cout, int relu, int tiles_x, int tiles_y,
+                                                       int ntiles, int stages) {
     using S = TcConvShape<BN>;
     constexpr uint32_t TMEM_COLS = (2 * BN < 32) ? 32 : 2 * BN;          // two accumulators
     static_assert(BN == 16 || BN == 32, "tile width");
-    static_assert(S::WSLICE % 16 == 0 && S::PLANE % 16 == 0, "16-byte operand alignment");
-    extern __shared__ __align__(128) unsigned char dyn_smem[];
-    __shared__ __align__(8) uint64_t s_bar[4];          // halo buffer 0, 1; accumulator 0, 1
+    static_assert(S::WSLICE % 128 == 0 && S::PLANE % 128 == 0 && S::PLANE >= S::HV * 16, "TMA / UMMA alignment");
+    extern __shared__ __align__(1024) unsigned char dyn_smem[];
+    __shared__ __align__(8) uint64_t s_bar[2 * S::MAX_STAGES + 4];
     __shared__ uint32_t s_tmem;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int slices = cin / 16;
     const int n0 = blockIdx.y * BN;
-    unsigned char* sw = dyn_smem;                                  // [slice][tap][half][co] rows
-    unsigned char* sh = dyn_smem + slices * S::WSLICE;             // two halo buffers
-    const uint32_t sw_addr = smem_addr(sw), sh_addr = smem_addr(sh);
-    const uint32_t bar0 = smem_addr(&s_bar[0]);
+    // weights first, then the halo stages (the weight block is a multiple of 128 bytes)
+    const uint32_t sw_addr = smem_addr(dyn_smem);
+    const uint32_t sh_addr = sw_addr + slices * S::WSLICE;
+    const uint32_t full0 = smem_addr(&s_bar[0]), empty0 = full0 + 8 * S::MAX_STAGES;
+    const uint32_t accfull0 = empty0 + 8 * S::MAX_STAGES, accempty0 = accfull0 + 16;
     const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int items = my_tiles * slices;
 
@@ -498,172 +514,168 @@ __global__ void __launch_bounds__(128) conv3_tc_kernel(const bf16* __restrict__ 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
-        for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8 * i));
+        for (int i = 0; i < 2 * S::MAX_STAGES + 2; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full0 + 8 * i));
+        for (int i = 0; i < 2; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(accempty0 + 8 * i));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = s_tmem;
-
-    // the weights of every slice, once
-    for (int q = tid; q < slices * 27 * 2 * BN; q += 128) {
+    // the weights of every slice, once: [slice][tap][8-channel half][co] rows of 16 bytes
+    for (int q = tid; q < slices * 27 * 2 * BN; q += 192) {
         const int co = q % BN, r = q / BN, kb = r & 1, t = (r >> 1) % 27, sl = (r >> 1) / 27;
         const bf16* p = wt + ((long long)(n0 + co) * 27 + t) * cin + sl * 16 + kb * 8;
         cp_async16(sw_addr + sl * S::WSLICE + t * S::WTAP + kb * BN * 16 + co * 16, p, true);
     }
     cp_commit();
+    cp_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = s_tmem;
 
     struct TileAt {
-        int z0, y0, x0;
-        long long vol0;
+        int x0, y0, z0, n;
     };
     auto tile_at = [&](int j) {
         int tile = (int)blockIdx.x + j * (int)gridDim.x;
-        const int txi = tile % tiles_x;
-        tile /= tiles_x;
-        const int tyi = tile % tiles_y;
-        tile /= tiles_y;
         TileAt r;
+        r.x0 = (tile % tiles_x) * S::TX;
+        tile /= tiles_x;
+        r.y0 = (tile % tiles_y) * S::TY;
+        tile /= tiles_y;
         r.z0 = tile % g.d;
-        r.vol0 = (long long)(tile / g.d) * g.d * g.h * g.w;
-        r.x0 = txi * S::TX;
-        r.y0 = tyi * S::TY;
+        r.n = tile / g.d;
         return r;
-    };
-    auto load_halo = [&](int k) {
-        const TileAt T = tile_at(k / slices);
-        const int c0 = (k % slices) * 16;
-        const uint32_t dst = sh_addr + (k & 1) * S::HALO;
-        for (int q = tid; q < S::HV * 2; q += 128) {
-            const int c = q / S::HV, hv = q - c * S::HV;
-            const int hx = hv % S::HX, hy = (hv / S::HX) % S::HY, hz = hv / (S::HX * S::HY);
-            const int zz = T.z0 + hz - 1, yy = T.y0 + hy - 1, xx = T.x0 + hx - 1;
-            const bool ok = zz >= 0 && zz < g.d && yy >= 0 && yy < g.h && xx >= 0 && xx < g.w;
-            const bf16* p = ok ? x + (T.vol0 + ((long long)zz * g.h + yy) * g.w + xx) * cin + c0 + c * 8 : x;
-            cp_async16(dst + c * S::PLANE + hv * 16, p, ok);
-        }
-        cp_commit();
-    };
-    // outputs of local tile j from accumulator j & 1
-    auto epilogue = [&](int j) {
-        const TileAt T = tile_at(j);
-        const int r = warp * 32 + lane;                 // accumulator row = TMEM lane = voxel of the tile
-        const int yy = T.y0 + (r >> 3), xx = T.x0 + (r & 7);
-        const bool inside = yy < g.h && xx < g.w;
-        const long long vo = T.vol0 + ((long long)T.z0 * g.h + yy) * g.w + xx;
-        const uint32_t col = (uint32_t)((j & 1) * BN);
-#pragma unroll
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            uint32_t v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + col + (uint32_t)c0, v);
-            if (!inside) continue;
-            uint32_t pk[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                float a = __uint_as_float(v[2 * e]), b = __uint_as_float(v[2 * e + 1]);
-                if (bias) {
-                    a += bias[n0 + c0 + 2 * e];
-                    b += bias[n0 + c0 + 2 * e + 1];
-                }
-                if (relu) {
-                    a = fmaxf(a, 0.f);
-                    b = fmaxf(b, 0.f);
-                }
-                __nv_bfloat162 h2 = __floats2bfloat162_rn(a, b);
-                pk[e] = *reinterpret_cast<uint32_t*>(&h2);
-            }
-            const long long o = vo * cout + n0 + c0;
-#pragma unroll
-            for (int hlf = 0; hlf < 2; ++hlf) {
-                uint4 val = make_uint4(pk[4 * hlf], pk[4 * hlf + 1], pk[4 * hlf + 2], pk[4 * hlf + 3]);
-                if (mask) {
-                    uint4 mk = *reinterpret_cast<const uint4*>(mask + o + 8 * hlf);
-                    uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
-                    const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
-                        uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
-                                        ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
-                        pv[e] &= keep;
-                    }
-                }
-                *reinterpret_cast<uint4*>(y + o + 8 * hlf) = val;
-            }
-        }
     };
 
     bool fault = false;
-    if (items > 0) load_halo(0);
-    for (int k = 0; k < items && !fault; ++k) {
-        const int j = k / slices, sl = k - j * slices;
-        if (k + 1 < items) {
-            // halo buffer (k + 1) & 1 was read by the MMAs of item k - 1
-            bool ok = true;
-            if (k >= 1) ok = mbar_wait(bar0 + 8 * ((k + 1) & 1), ((k - 1) >> 1) & 1);
-            if (__syncthreads_or(!ok)) {
-                fault = true;
-                break;
+    if (warp == 4) {
+        // ---- producer: TMA halo copies ----------------------------------------------------------
+        if (lane == 0) {
+            const uint64_t map = reinterpret_cast<uint64_t>(&tmap);
+            for (int k = 0; k < items; ++k) {
+                const int b = k % stages;
+                if (k >= stages && !mbar_wait(empty0 + 8 * b, ((k / stages) - 1) & 1)) {
+                    fault = true;
+                    break;
+                }
+                const TileAt T = tile_at(k / slices);
+                const int c0 = (k % slices) * 16;
+                const uint32_t bar = full0 + 8 * b, dst = sh_addr + b * S::HALO;
+                mbar_expect_tx(bar, S::HALO_BYTES);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    asm volatile(
+                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+                        "%5, %6}], [%7];\n" ::"r"(dst + h * S::PLANE),
+                        "l"(map), "r"(c0 + 8 * h), "r"(T.x0 - 1), "r"(T.y0 - 1), "r"(T.z0 - 1), "r"(T.n), "r"(bar)
+                        : "memory");
             }
-            load_halo(k + 1);
-            cp_wait<1>();
-        } else {
-            cp_wait<0>();
-        }
-        // copies land through the generic proxy; the tensor cores read through the async proxy
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t sa = sh_addr + (k & 1) * S::HALO, sb = sw_addr + sl * S::WSLICE;
-            const uint32_t d = tmem + (uint32_t)((j & 1) * BN);
-#pragma unroll 1
-            for (int t = 0; t < 27; ++t) {
-                const int dz = t / 9, dy = (t / 3) % 3, dx = t % 3;
-                const uint64_t ad = umma_desc(sa + ((dz * S::HY + dy) * S::HX + dx) * 16, S::PLANE, S::HX * 16);
-                const uint64_t bd = umma_desc(sb + t * S::WTAP, BN * 16, 128);
-                const uint32_t accum = (sl > 0 || t > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                    "l"(ad), "l"(bd), "r"(umma_idesc_bf16(BN)), "r"(accum)
-                    : "memory");
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             bar0 + 8 * (k & 1))
-                         : "memory");
-            if (sl == slices - 1)
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                                 bar0 + 16 + 8 * (j & 1))
-                             : "memory");
         }
         __syncwarp();
-        // the previous tile's outputs, while this tile's MMAs run
-        if (sl == 0 && j >= 1) {
-            const bool ok = mbar_wait(bar0 + 16 + 8 * ((j - 1) & 1), ((j - 1) >> 1) & 1);
-            if (__syncthreads_or(!ok)) {
+    } else if (warp == 5) {
+        // ---- MMA issue: one thread --------------------------------------------------------------
+        if (lane == 0) {
+            for (int k = 0; k < items; ++k) {
+                const int j = k / slices, sl = k - j * slices, b = k % stages;
+                if (!mbar_wait(full0 + 8 * b, (k / stages) & 1)) {
+                    fault = true;
+                    break;
+                }
+                if (sl == 0 && j >= 2 && !mbar_wait(accempty0 + 8 * (j & 1), ((j - 2) >> 1) & 1)) {
+                    fault = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)((j & 1) * BN);
+                // descriptors of tap 0; a tap moves the start address (bits 0-13, in 16-byte units)
+                // by a constant, so the 27 MMAs issue back to back
+                const uint64_t ad0 = umma_desc(sh_addr + b * S::HALO, S::PLANE, S::HX * 16);
+                const uint64_t bd0 = umma_desc(sw_addr + sl * S::WSLICE, BN * 16, 128);
+#pragma unroll
+                for (int t = 0; t < 27; ++t) {
+                    const uint64_t ad = ad0 + (uint64_t)((((t / 9) * S::HY + (t / 3) % 3) * S::HX + t % 3) * 16 >> 4);
+                    const uint64_t bd = bd0 + (uint64_t)(t * S::WTAP >> 4);
+                    const uint32_t accum = (sl > 0 || t > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                        "l"(ad), "l"(bd), "n"(umma_idesc_bf16(BN)), "r"(accum)
+                        : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 empty0 + 8 * b)
+                             : "memory");
+                if (sl == slices - 1)
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     accfull0 + 8 * (j & 1))
+                                 : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warps 0-3 -------------------------------------------------------------------
+        for (int j = 0; j < my_tiles; ++j) {
+            const bool ok = mbar_wait(accfull0 + 8 * (j & 1), (j >> 1) & 1);
+            if (!__all_sync(0xffffffffu, ok)) {
                 fault = true;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            epilogue(j - 1);
+            const TileAt T = tile_at(j);
+            const int r = warp * 32 + lane;             // accumulator row = TMEM lane = voxel of the tile
+            const int yy = T.y0 + (r >> 3), xx = T.x0 + (r & 7);
+            const bool inside = yy < g.h && xx < g.w;
+            const long long vo = (((long long)T.n * g.d + T.z0) * g.h + yy) * g.w + xx;
+            uint32_t v[BN];
+#pragma unroll
+            for (int c0 = 0; c0 < BN; c0 += 16)
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * BN + c0),
+                          *reinterpret_cast<uint32_t(*)[16]>(v + c0));
+            // the accumulator is free again once every lane of the four warps has read it
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(accempty0 + 8 * (j & 1));
+            if (!inside) continue;
+#pragma unroll
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t pk[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    float a = __uint_as_float(v[c0 + 2 * e]), bb = __uint_as_float(v[c0 + 2 * e + 1]);
+                    if (bias) {
+                        a += bias[n0 + c0 + 2 * e];
+                        bb += bias[n0 + c0 + 2 * e + 1];
+                    }
+                    if (relu) {
+                        a = fmaxf(a, 0.f);
+                        bb = fmaxf(bb, 0.f);
+                    }
+                    __nv_bfloat162 h2 = __floats2bfloat162_rn(a, bb);
+                    pk[e] = *reinterpret_cast<uint32_t*>(&h2);
+                }
+                const long long o = vo * cout + n0 + c0;
+#pragma unroll
+                for (int hlf = 0; hlf < 2; ++hlf) {
+                    uint4 val = make_uint4(pk[4 * hlf], pk[4 * hlf + 1], pk[4 * hlf + 2], pk[4 * hlf + 3]);
+                    if (mask) {
+                        uint4 mk = *reinterpret_cast<const uint4*>(mask + o + 8 * hlf);
+                        uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
+                        const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
+                            uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
+                                            ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
+                            pv[e] &= keep;
+                        }
+                    }
+                    *reinterpret_cast<uint4*>(y + o + 8 * hlf) = val;
+                }
+            }
         }
     }
-    if (!fault && my_tiles > 0) {
-        const int j = my_tiles - 1;
-        const bool ok = mbar_wait(bar0 + 16 + 8 * (j & 1), (j >> 1) & 1);
-        fault = __syncthreads_or(!ok);
-        if (!fault) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            epilogue(j);
-        }
-    }
-    if (fault) {
-        cp_wait<0>();
-        if (tid == 0) atomicOr(&g_dn_fault, 1u);
-    }
+    if (fault && lane == 0) atomicOr(&g_dn_fault, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -1179,12 +1191,45 @@ int conv3_halo_launch(const bf16* x, const bf16* w, const float* bias, const bf1
     return launched();
 }
 
+// cuTensorMapEncodeTiled, found through the runtime (the engine links no driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
 template <int BN>
 int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16* mask, bf16* y, Geo g, int cin,
                     int cout, int relu, cudaStream_t st) {
     using S = TcConvShape<BN>;
-    const int smem = (cin / 16) * S::WSLICE + 2 * S::HALO;
-    if (smem > 227 * 1024) return fail("conv: weights of this layer do not fit in shared memory");
+    if (!aligned16(x)) return fail("conv: the input must be 16-byte aligned");
+    auto encode = tensor_map_encoder();
+    if (!encode) return fail("conv: cuTensorMapEncodeTiled is not available");
+    // activations [nvol][d][h][w][cin] as a 5-D tensor (channel fastest) with a 8 x 10 x 18 x 3 x 1 box
+    CUtensorMap tmap;
+    const cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)g.w, (cuuint64_t)g.h, (cuuint64_t)g.d, (cuuint64_t)g.nvol};
+    const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, (cuuint64_t)g.w * cin * 2, (cuuint64_t)g.h * g.w * cin * 2,
+                                   (cuuint64_t)g.d * g.h * g.w * cin * 2};
+    const cuuint32_t box[5] = {8, (cuuint32_t)S::HX, (cuuint32_t)S::HY, 3, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    if (encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(x), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return fail("conv: cuTensorMapEncodeTiled rejected the activation layout");
+    const int wbytes = (cin / 16) * S::WSLICE;
+    const int limit = 227 * 1024;
+    int stages = (limit - wbytes) / S::HALO;
+    if (stages > S::MAX_STAGES) stages = S::MAX_STAGES;
+    if (stages < 2) return fail("conv: weights of this layer do not fit in shared memory");
+    const int smem = wbytes + stages * S::HALO;
     auto kern = conv3_tc_kernel<BN>;
     static int attr = 0;
     if (smem > attr) {
@@ -1194,18 +1239,19 @@ int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16*
     const int tx = (g.w + S::TX - 1) / S::TX, ty = (g.h + S::TY - 1) / S::TY;
     const long long tiles = (long long)g.nvol * g.d * tx * ty;
     if (tiles >= (1LL << 31)) return fail("conv: too many tiles");
-    // persistent CTAs: as many as fit on the SMs, each walking its tiles
-    int dev = 0, sms = 0, per_sm = 0;
+    // persistent CTAs: as many as shared memory lets stay resident on every SM
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
-    if (per_sm < 1) return fail("conv: the tensor-core kernel does not fit on this device");
+    int per_sm = (228 * 1024) / (smem + 2048);
+    if (per_sm > 8) per_sm = 8;
+    if (per_sm < 1) per_sm = 1;
     const int ny = cout / BN;
     long long grid = (long long)sms * per_sm / ny;
     if (grid < 1) grid = 1;
     if (grid > tiles) grid = tiles;
-    kern<<<dim3((unsigned)grid, (unsigned)ny), 128, smem, st>>>(x, w, bias, mask, y, g, cin, cout, relu, tx, ty,
-                                                               (int)tiles);
+    kern<<<dim3((unsigned)grid, (unsigned)ny), 192, smem, st>>>(tmap, w, bias, mask, y, g, cin, cout, relu, tx, ty,
+                                                               (int)tiles, stages);
     return launched();
 }
 

@@ -1189,7 +1189,11 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
             // taken at exit (2191-2292)
             bool rec = false;
             if (P.save2pt && t >= tw0 && t < tw1) {
-                int tshift = (P.maxgate > 1) ? min(P.maxgate - 1, (int)floorf(fmaf(t, bin_a, -bin_b))) : 0;
+                // the window test above runs on t in grid units, the bin on t x bin_a - bin_b: at a
+                // window that does not start at 0 the two roundings can disagree by one ulp, so a
+                // deposit that passed the test may compute bin -1; it belongs to the first gate (MCX's
+                // (t - twin0) x Rtstep is exactly >= 0 there), and must never index below the field
+                int tshift = (P.maxgate > 1) ? min(P.maxgate - 1, max(0, (int)floorf(fmaf(t, bin_a, -bin_b)))) : 0;
                 float weight;
                 if (P.outputtype == kOutEnergy) {
                     weight = w0 - w;

@@ -651,8 +651,11 @@ def main(argv: list[str] | None = None) -> None:
     import json
 
     ap = argparse.ArgumentParser(prog="python -m mcx_gb300.denoise")
-    ap.add_argument("command", choices=["train", "forward"],
-                    help="train: simulate pairs, train, save; forward: time the network on one volume")
+    ap.add_argument("command", choices=["train", "forward", "conv"],
+                    help="train: simulate pairs, train, save; forward: time the network on one volume; "
+                         "conv: run one 3x3x3 convolution --repeat times (a fixed workload for profilers)")
+    ap.add_argument("--cin", type=int, default=16, help="conv: input channels")
+    ap.add_argument("--cout", type=int, default=16, help="conv: output channels")
     ap.add_argument("--repeat", type=int, default=10, help="forward: timed passes")
     ap.add_argument("--count", type=int, default=64, help="training volumes")
     ap.add_argument("--edge", type=int, default=128, help="edge of the simulated training volumes")
@@ -665,6 +668,21 @@ def main(argv: list[str] | None = None) -> None:
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     a = ap.parse_args(argv)
+    if a.command == "conv":
+        # one convolution on random bf16 activations [1][edge]^3[cin] and weights [cout][27][cin],
+        # through the same C entry point the network uses
+        n = a.edge
+        g = torch.Generator(device="cuda").manual_seed(a.seed)
+        x = torch.randn(n ** 3 * a.cin, generator=g, device="cuda").to(torch.bfloat16)
+        w = (torch.randn(a.cout * TAPS * a.cin, generator=g, device="cuda") * 0.05).to(torch.bfloat16)
+        y = torch.empty(n ** 3 * a.cout, device="cuda", dtype=torch.bfloat16)
+        st = torch.cuda.current_stream().cuda_stream
+        for _ in range(a.repeat):
+            _ok(lib.mcxg_dn_conv_fwd(x.data_ptr(), w.data_ptr(), None, None, y.data_ptr(), 1, n, n, n, a.cin, a.cout,
+                                     TAPS, 1, st), "conv")
+        _ok(lib.mcxg_dn_check(st), "conv")
+        print(json.dumps({"cin": a.cin, "cout": a.cout, "edge": n, "launches": a.repeat}))
+        return
     if a.command == "forward":
         net = UNet(load_params() if DEFAULT_WEIGHTS.exists() else None, seed=a.seed)
         n = a.edge
