@@ -405,10 +405,10 @@ __global__ void __launch_bounds__(128) conv3_halo_kernel(const bf16* __restrict_
 // ---------------------------------------------------------------------------------------------
 // 3x3x3 convolution for narrow outputs (BN = 16 or 32 channels) on the fifth-generation tensor
 // cores: tcgen05.mma (cta_group::1, kind::f16, BF16 operands from shared memory, FP32 accumulator
-// in tensor memory), issued by one thread, with the input halos brought in by TMA.  The CTA's 128
-// output voxels are one z-plane of 16 y rows x 8 x voxels, so its eight-voxel rows are a uniform
-// stride apart in the halo.  Per 16-channel slice of the input, the 3 x 18 x 10 halo around the
-// tile lands as two 8-channel planes of 16-byte rows, and every tap's A operand is the same halo
+// in tensor memory), issued by one thread, with the input halos brought in by TMA.  A tile is two
+// z-planes of 16 y rows x 8 x voxels; each plane is one M = 128 MMA, whose eight-voxel rows are
+// a uniform stride apart in the halo.  Per 16-channel slice of the input, the 4 x 18 x 10 halo
+// around the tile lands as two 8-channel planes of 16-byte rows, and every tap's A operand is the same halo
 // seen through a descriptor whose start moves by the tap's row offset: K-major, no swizzle, core
 // matrices of 8 consecutive rows (8 consecutive x), the 8-row groups HX rows apart (stride byte
 // offset), the second 8 channels one plane further on (leading byte offset).  The weights of a
@@ -455,9 +455,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
 
 template <int BN>
 struct TcConvShape {
-    static constexpr int TY = 16, TX = 8;
-    static constexpr int HY = TY + 2, HX = TX + 2, HV = 3 * HY * HX;     // 540 halo rows
-    static constexpr int PLANE = 8704;                                    // 540 x 16 B, padded to 128 B
+    static constexpr int TZ = 2, TY = 16, TX = 8;                         // two z-planes of 128 voxels
+    static constexpr int HZ = TZ + 2, HY = TY + 2, HX = TX + 2, HV = HZ * HY * HX;   // 720 halo rows
+    static constexpr int PLANE = HV * 16;                                 // 11520 B, a multiple of 128
     static constexpr int HALO = 2 * PLANE;                                // one stage: 16 channels
     static constexpr int HALO_BYTES = 2 * HV * 16;                        // bytes the two copies bring
     static constexpr int WTAP = 2 * BN * 16;                              // one tap's weights
@@ -476,9 +476,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 // its quarter of the tile), warp 4 issues the TMA copies of the halos, warp 5 issues the MMAs.
 // The CTA is persistent: it loads the weights of every input slice once, then walks its tiles
 // (blockIdx.x, + gridDim.x, ...) as a sequence of (tile, slice) items.  Each item is one halo: two
-// TMA tile copies (channels c..c+7 and c+8..c+15) of a 3 x 18 x 10 voxel box of the channels-last
+// TMA tile copies (channels c..c+7 and c+8..c+15) of a 4 x 18 x 10 voxel box of the channels-last
 // activations, described by a 5-D tensor map (channel, x, y, z, volume) whose out-of-volume rows
-// arrive as zeros; the box lands as 540 rows of 16 bytes, x fastest, which is the A operand's
+// arrive as zeros; the box lands as 720 rows of 16 bytes, x fastest, which is the A operand's
 // canonical no-swizzle K-major layout.  Halos cycle through `stages` buffers (full barriers: the
 // copies landed; empty barriers: the MMAs that read the buffer finished), and tiles through two
 // TMEM accumulators (accfull: a tile's MMAs finished; accempty: its epilogue has read it), so
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(192) conv3_tc_kernel(const __grid_constant__ C
                                                        int cin, int cout, int relu, int tiles_x, int tiles_y,
                                                        int ntiles, int stages) {
     using S = TcConvShape<BN>;
-    constexpr uint32_t TMEM_COLS = (2 * BN < 32) ? 32 : 2 * BN;          // two accumulators
+    constexpr uint32_t TMEM_COLS = 4 * BN;          // two tiles in flight x two z-planes of BN columns
     static_assert(BN == 16 || BN == 32, "tile width");
     static_assert(S::WSLICE % 128 == 0 && S::PLANE % 128 == 0 && S::PLANE >= S::HV * 16, "TMA / UMMA alignment");
     extern __shared__ __align__(1024) unsigned char dyn_smem[];
@@ -543,8 +543,9 @@ __global__ void __launch_bounds__(192) conv3_tc_kernel(const __grid_constant__ C
         tile /= tiles_x;
         r.y0 = (tile % tiles_y) * S::TY;
         tile /= tiles_y;
-        r.z0 = tile % g.d;
-        r.n = tile / g.d;
+        const int tz = (g.d + S::TZ - 1) / S::TZ;
+        r.z0 = (tile % tz) * S::TZ;
+        r.n = tile / tz;
         return r;
     };
 
@@ -587,21 +588,26 @@ __global__ void __launch_bounds__(192) conv3_tc_kernel(const __grid_constant__ C
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t d = tmem + (uint32_t)((j & 1) * BN);
-                // descriptors of tap 0; a tap moves the start address (bits 0-13, in 16-byte units)
-                // by a constant, so the 27 MMAs issue back to back
+                const uint32_t d = tmem + (uint32_t)((j & 1) * 2 * BN);
+                // descriptors of tap 0; a tap (and the second z-plane, one halo plane further on)
+                // moves the start address (bits 0-13, in 16-byte units) by a constant, so the 54 MMAs
+                // issue back to back; both planes share the tap's weights
                 const uint64_t ad0 = umma_desc(sh_addr + b * S::HALO, S::PLANE, S::HX * 16);
                 const uint64_t bd0 = umma_desc(sw_addr + sl * S::WSLICE, BN * 16, 128);
 #pragma unroll
                 for (int t = 0; t < 27; ++t) {
-                    const uint64_t ad = ad0 + (uint64_t)((((t / 9) * S::HY + (t / 3) % 3) * S::HX + t % 3) * 16 >> 4);
                     const uint64_t bd = bd0 + (uint64_t)(t * S::WTAP >> 4);
                     const uint32_t accum = (sl > 0 || t > 0) ? 1u : 0u;
-                    asm volatile(
-                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                        "l"(ad), "l"(bd), "n"(umma_idesc_bf16(BN)), "r"(accum)
-                        : "memory");
+#pragma unroll
+                    for (int zp = 0; zp < S::TZ; ++zp) {
+                        const uint64_t ad =
+                            ad0 + (uint64_t)((((t / 9 + zp) * S::HY + (t / 3) % 3) * S::HX + t % 3) * 16 >> 4);
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d + zp * BN),
+                            "l"(ad), "l"(bd), "n"(umma_idesc_bf16(BN)), "r"(accum)
+                            : "memory");
+                    }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                                  empty0 + 8 * b)
@@ -623,54 +629,58 @@ __global__ void __launch_bounds__(192) conv3_tc_kernel(const __grid_constant__ C
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const TileAt T = tile_at(j);
-            const int r = warp * 32 + lane;             // accumulator row = TMEM lane = voxel of the tile
+            const int r = warp * 32 + lane;             // accumulator row = TMEM lane = voxel of a plane
             const int yy = T.y0 + (r >> 3), xx = T.x0 + (r & 7);
-            const bool inside = yy < g.h && xx < g.w;
-            const long long vo = (((long long)T.n * g.d + T.z0) * g.h + yy) * g.w + xx;
-            uint32_t v[BN];
+            uint32_t v[S::TZ][BN];
 #pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 16)
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * BN + c0),
-                          *reinterpret_cast<uint32_t(*)[16]>(v + c0));
-            // the accumulator is free again once every lane of the four warps has read it
+            for (int zp = 0; zp < S::TZ; ++zp)
+#pragma unroll
+                for (int c0 = 0; c0 < BN; c0 += 16)
+                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((j & 1) * 2 * BN + zp * BN + c0),
+                              *reinterpret_cast<uint32_t(*)[16]>(&v[zp][c0]));
+            // the accumulators are free again once every lane of the four warps has read them
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(accempty0 + 8 * (j & 1));
-            if (!inside) continue;
 #pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 16) {
-                uint32_t pk[8];
+            for (int zp = 0; zp < S::TZ; ++zp) {
+                if (yy >= g.h || xx >= g.w || T.z0 + zp >= g.d) continue;
+                const long long vo = (((long long)T.n * g.d + T.z0 + zp) * g.h + yy) * g.w + xx;
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    float a = __uint_as_float(v[c0 + 2 * e]), bb = __uint_as_float(v[c0 + 2 * e + 1]);
-                    if (bias) {
-                        a += bias[n0 + c0 + 2 * e];
-                        bb += bias[n0 + c0 + 2 * e + 1];
-                    }
-                    if (relu) {
-                        a = fmaxf(a, 0.f);
-                        bb = fmaxf(bb, 0.f);
-                    }
-                    __nv_bfloat162 h2 = __floats2bfloat162_rn(a, bb);
-                    pk[e] = *reinterpret_cast<uint32_t*>(&h2);
-                }
-                const long long o = vo * cout + n0 + c0;
+                for (int c0 = 0; c0 < BN; c0 += 16) {
+                    uint32_t pk[8];
 #pragma unroll
-                for (int hlf = 0; hlf < 2; ++hlf) {
-                    uint4 val = make_uint4(pk[4 * hlf], pk[4 * hlf + 1], pk[4 * hlf + 2], pk[4 * hlf + 3]);
-                    if (mask) {
-                        uint4 mk = *reinterpret_cast<const uint4*>(mask + o + 8 * hlf);
-                        uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
-                        const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
-                            uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
-                                            ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
-                            pv[e] &= keep;
+                    for (int e = 0; e < 8; ++e) {
+                        float a = __uint_as_float(v[zp][c0 + 2 * e]), bb = __uint_as_float(v[zp][c0 + 2 * e + 1]);
+                        if (bias) {
+                            a += bias[n0 + c0 + 2 * e];
+                            bb += bias[n0 + c0 + 2 * e + 1];
                         }
+                        if (relu) {
+                            a = fmaxf(a, 0.f);
+                            bb = fmaxf(bb, 0.f);
+                        }
+                        __nv_bfloat162 h2 = __floats2bfloat162_rn(a, bb);
+                        pk[e] = *reinterpret_cast<uint32_t*>(&h2);
                     }
-                    *reinterpret_cast<uint4*>(y + o + 8 * hlf) = val;
+                    const long long o = vo * cout + n0 + c0;
+#pragma unroll
+                    for (int hlf = 0; hlf < 2; ++hlf) {
+                        uint4 val = make_uint4(pk[4 * hlf], pk[4 * hlf + 1], pk[4 * hlf + 2], pk[4 * hlf + 3]);
+                        if (mask) {
+                            uint4 mk = *reinterpret_cast<const uint4*>(mask + o + 8 * hlf);
+                            uint32_t* pv = reinterpret_cast<uint32_t*>(&val);
+                            const uint32_t* pm = reinterpret_cast<const uint32_t*>(&mk);
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                uint32_t lo = (pm[e] & 0xFFFFu), hi = pm[e] >> 16;
+                                uint32_t keep = ((lo & 0x8000u) == 0 && lo != 0 ? 0xFFFFu : 0u) |
+                                                ((hi & 0x8000u) == 0 && hi != 0 ? 0xFFFF0000u : 0u);
+                                pv[e] &= keep;
+                            }
+                        }
+                        *reinterpret_cast<uint4*>(y + o + 8 * hlf) = val;
+                    }
                 }
             }
         }
@@ -1213,12 +1223,12 @@ int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16*
     if (!aligned16(x)) return fail("conv: the input must be 16-byte aligned");
     auto encode = tensor_map_encoder();
     if (!encode) return fail("conv: cuTensorMapEncodeTiled is not available");
-    // activations [nvol][d][h][w][cin] as a 5-D tensor (channel fastest) with a 8 x 10 x 18 x 3 x 1 box
+    // activations [nvol][d][h][w][cin] as a 5-D tensor (channel fastest) with a 8 x 10 x 18 x 4 x 1 box
     CUtensorMap tmap;
     const cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)g.w, (cuuint64_t)g.h, (cuuint64_t)g.d, (cuuint64_t)g.nvol};
     const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, (cuuint64_t)g.w * cin * 2, (cuuint64_t)g.h * g.w * cin * 2,
                                    (cuuint64_t)g.d * g.h * g.w * cin * 2};
-    const cuuint32_t box[5] = {8, (cuuint32_t)S::HX, (cuuint32_t)S::HY, 3, 1};
+    const cuuint32_t box[5] = {8, (cuuint32_t)S::HX, (cuuint32_t)S::HY, (cuuint32_t)S::HZ, 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     if (encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(x), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1229,6 +1239,8 @@ int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16*
     int stages = (limit - wbytes) / S::HALO;
     if (stages > S::MAX_STAGES) stages = S::MAX_STAGES;
     if (stages < 2) return fail("conv: weights of this layer do not fit in shared memory");
+    // two CTAs per SM hide each other's waits better than a fourth halo stage does
+    while (stages > 3 && 2 * (wbytes + stages * S::HALO + 2048) > 228 * 1024) --stages;
     const int smem = wbytes + stages * S::HALO;
     auto kern = conv3_tc_kernel<BN>;
     static int attr = 0;
@@ -1237,7 +1249,7 @@ int conv3_tc_launch(const bf16* x, const bf16* w, const float* bias, const bf16*
         attr = smem;
     }
     const int tx = (g.w + S::TX - 1) / S::TX, ty = (g.h + S::TY - 1) / S::TY;
-    const long long tiles = (long long)g.nvol * g.d * tx * ty;
+    const long long tiles = (long long)g.nvol * ((g.d + S::TZ - 1) / S::TZ) * tx * ty;
     if (tiles >= (1LL << 31)) return fail("conv: too many tiles");
     // persistent CTAs: as many as shared memory lets stay resident on every SM
     int dev = 0, sms = 0;
