@@ -218,11 +218,12 @@ def _json_input(cfg: dict[str, Any], session: str, volfile: str) -> dict:
         session_keys["DoSaveRef"] = int(cfg["issaveref"])
     if cfg.get("debuglevel"):
         session_keys["DebugFlag"] = str(cfg["debuglevel"])       # -D letters, e.g. "M" for trajectories
+    svmc = vol.ndim == 4 and vol.dtype == np.uint8 and vol.shape[0] == 8
     out = {
         "Session": session_keys,
-        "Domain": {"Dim": list(vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0,
+        "Domain": {"Dim": list(vol.shape[1:] if svmc else vol.shape), "OriginType": 1 if cfg.get("issrcfrom0", 0) else 0,
                    "LengthUnit": float(cfg.get("unitinmm", 1.0)),
-                   "MediaFormat": "byte", "VolumeFile": volfile,
+                   "MediaFormat": "svmc" if svmc else "byte", "VolumeFile": volfile,
                    "Media": [{"mua": float(r[0]), "mus": float(r[1]), "g": float(r[2]), "n": float(r[3])} for r in prop]},
         "Forward": {"T0": float(cfg["tstart"]), "T1": float(cfg["tend"]), "Dt": float(cfg["tstep"])},
         "Optode": {"Source": {"Type": _src_name(cfg.get("srctype", "pencil")),
@@ -270,7 +271,13 @@ def run(cfg: dict[str, Any], workdir: str | Path | None = None, keep_field: bool
     tmp.mkdir(parents=True, exist_ok=True)
     vol = np.asarray(cfg["vol"]).astype(np.uint8)
     volfile = tmp / "vol.bin"
-    vol.ravel(order="F").tofile(volfile)
+    if vol.ndim == 4 and vol.shape[0] == 8:
+        # split voxels (MediaFormat "svmc", src/mcx_utils.c:3527, 1708-1731): 8 bytes per voxel,
+        # [lower label, upper label, plane point x, y, z, normal x, y, z], voxels x fastest
+        vol.reshape(8, -1, order="F").T.copy().tofile(volfile)
+        vol = vol[0]
+    else:
+        vol.ravel(order="F").tofile(volfile)
     session = "ref"
     (tmp / "in.json").write_text(json.dumps(_json_input(cfg, session, str(volfile))))
     p = subprocess.run([str(exe), "-f", "in.json"], cwd=tmp, capture_output=True, text=True, timeout=timeout)
