@@ -151,3 +151,30 @@ def test_cli_engine_error_goes_through_mcx_error(cli, tmp_path):
     out = run(cli, ["--bench", "cube60", "--json", json.dumps({"Domain": {"Media": [[0, 0, 1, 1]]}}), "-n", "1e3"],
               tmp_path, rc=256 - 4)
     assert re.search(r"MCX ERROR\(-4\):input media optical properties are less than the labels", out), out[-2000:]
+
+
+def test_cli_jdat_matches_the_python_writer(cli, tmp_path, engine):
+    """The detected-photon .jdat the CLI writes through MCX's own writer (mcx_savejdet; -F jnii is
+    the front-end's default) and the one mcx_gb300.mch.save_jdet writes for the Python front-end's
+    run of the same deck and seed: the same header fields, and -- the engine's photons having
+    per-photon random streams -- the same detected records and seeds, as sets."""
+    from mcx_gb300 import mch, problems
+
+    run(cli, ["--bench", "cube60b", "-n", "1e5", "-E", "1234", "-s", "jd", "-q", "1", "-S", "0"], tmp_path)
+    info_c, rec_c, seed_c = mch.load_jdet(tmp_path / "jd_detp.jdat")
+    cfg = problems.cube60b(1e5) | {"seed": 1234, "issaveseed": 1}
+    pc = engine.prepare(cfg)
+    res = engine.run_prepared(pc)
+    info_p, rec_p, seed_p = mch.load_jdet(mch.save_jdet(tmp_path / "py_detp.jdat", pc, res))
+    print({k: (info_c[k], info_p[k]) for k in info_c if k != "Media"})
+    for k in ("Version", "MediaNum", "DetNum", "ColumnNum", "TotalPhoton", "DetectedPhoton", "SavedPhoton",
+              "LengthUnit", "SeedByte", "Repeat", "SrcNum", "SaveDetFlag", "TotalSource"):
+        assert info_c[k] == info_p[k], k
+    assert info_p["Normalizer"] == pytest.approx(info_c["Normalizer"], rel=1e-6)
+    for mc, mp in zip(info_c["Media"], info_p["Media"]):
+        assert all(mp[q] == pytest.approx(mc[q], rel=1e-6, abs=1e-9) for q in ("mua", "mus", "g", "n"))
+
+    def rows(rec, seeds):
+        return sorted(rec[:, i].tobytes() + seeds[:, i].tobytes() for i in range(rec.shape[1]))
+
+    assert rec_c.shape == rec_p.shape and rows(rec_c, seed_c) == rows(rec_p, seed_p)
