@@ -367,8 +367,8 @@ def denoise_main(args, world, rank) -> None:
                 "h2d_bytes_per_step": int(h2d / V), "d2h_bytes_per_step": int(d2h / V)},
         "targets": [{k: rnd(v) for k, v in t.items()} for t in res["targets"]],
         "judge_error_est": rnd(res["judge_error_est"]),
-        "ladder": [(r["photons"], rnd(r["errors"])) for r in res["plain"]],
-        "denoised_ladder": [(r["photons"], rnd(r["errors"])) for r in res["denoised"]],
+        "ladder": [(r["photons"], rnd(r["errors"]), round(r["kernel_s"], 5)) for r in res["plain"]],
+        "denoised_ladder": [(r["photons"], rnd(r["errors"]), round(r["kernel_s"], 5)) for r in res["denoised"]],
         "at_2pct": {"value": t2["t_denoised_device_s"], "plain_mc_s": t2["t_plain_device_s"],
                     "speedup": t2["speedup_device"], "e2e_speedup": t2["speedup"]},
         "roofline": {"bound": "tensor", "kernel": "U-Net forward at 128^3 (14 implicit-GEMM convolutions)",

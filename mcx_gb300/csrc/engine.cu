@@ -1475,10 +1475,12 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
 // Many independent simulations on one device (the batched workload): every Config gets its
 // own session -- volume, media, source and field on the device -- and all transport launches
 // go into one CUDA graph over `nstreams` streams, largest photon budget first.  A launch is a
-// full-device persistent grid drawing on its own photon counter; as the CTAs of one launch run
-// out of photons, the block scheduler fills the freed SMs with CTAs of the launches queued on
-// the other streams, so the tail of one simulation overlaps the next.  Each Config's outputs are
-// those of mcx_run_simulation; `runtime` is the batch's graph time.
+// persistent grid drawing on its own photon counter, sized by its stream's share of the photons;
+// as the CTAs of one launch run out of photons, the block scheduler fills the freed SMs with CTAs
+// of the launches on the other streams, so the tail of one simulation overlaps the others.  Each
+// Config's outputs are those of mcx_run_simulation; `runtime` is the batch's graph time.
+constexpr int kMinBatchCTAs = 16;
+
 void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms) {
     if (count <= 0 || !cfgs) MCXG_RAISE(-4, "an empty batch");
     nstreams = std::max(1, std::min(nstreams, 32));
@@ -1506,6 +1508,8 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
     }
     for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
 
+    std::vector<int> full_grid(count);
+    for (int i = 0; i < count; i++) full_grid[i] = S[i]->grid;
     std::vector<int> order(count);
     for (int i = 0; i < count; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cfgs[a]->nphoton > cfgs[b]->nphoton; });
@@ -1555,15 +1559,36 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
                 if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
             }
             for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
-            CK(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
-            CK(cudaEventRecord(fork, origin));
-            for (int k = 0; k < nstreams; k++) CK(cudaStreamWaitEvent(st[k], fork, 0));
+            // CTAs of each launch: its stream's share of the wave's photons, times two, of a full
+            // grid.  A launch whose photons are fewer than its threads holds every CTA until the
+            // longest photon of that CTA ends, so full grids would run such simulations one after
+            // the other, each at its latency; shared out, the launches of all streams are resident
+            // together and the oversubscribed CTAs take the SMs that early finishers free.
+            std::vector<int> stream_of(count, -1);
+            std::vector<double> load(nstreams, 0.0);
             int slot = 0;
             for (int j = 0; j < count; j++) {
                 const int i = order[j];
                 if (w >= reps[i] * groups[i]) continue;
+                stream_of[i] = slot++ % nstreams;
+                load[stream_of[i]] += (double)nper[i];
+            }
+            double wave_load = 0.0;
+            for (double l : load) wave_load += l;
+            for (int i = 0; i < count; i++) {
+                if (stream_of[i] < 0) continue;
+                const double share = wave_load > 0.0 ? 2.0 * load[stream_of[i]] / wave_load : 1.0;
+                const int full = full_grid[i];
+                S[i]->grid = std::max(std::min(full, kMinBatchCTAs), std::min(full, (int)std::ceil(full * share)));
+            }
+            CK(cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed));
+            CK(cudaEventRecord(fork, origin));
+            for (int k = 0; k < nstreams; k++) CK(cudaStreamWaitEvent(st[k], fork, 0));
+            for (int j = 0; j < count; j++) {
+                const int i = order[j];
+                if (stream_of[i] < 0) continue;
                 const Config* cfg = cfgs[i];
-                S[i]->enqueue(st[slot++ % nstreams], (uint64_t)w * nper[i], nper[i], (uint64_t)(uint32_t)cfg->seed,
+                S[i]->enqueue(st[stream_of[i]], (uint64_t)w * nper[i], nper[i], (uint64_t)(uint32_t)cfg->seed,
                               w % reps[i] == 0);
             }
             for (int k = 0; k < nstreams; k++) {
