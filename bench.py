@@ -302,10 +302,13 @@ def _dn_flops(d: int, h: int, w: int, nvol: int = 1) -> float:
 def denoise_main(args, world, rank) -> None:
     """MC + learned denoiser against plain MC on held-out 128^3 volumes of the batched workload's
     property ranges: per volume, the time to a median relative fluence error of 5% against a
-    `--judge-photons` run (mcx_gb300.denoise.time_to_error).  value = summed device time of
-    MC + denoiser (transport kernel + network); e2e = summed wall time through the public calls
-    (mcx_gb300.run, UNet.denoise) from host buffers; plain-MC times and the speed-up ride along.
-    One step = one volume; warm-up = full denoise pipelines at 1e5 photons on the first volume."""
+    `--judge-photons` run (mcx_gb300.denoise.time_to_error_batch).  value = device time of MC +
+    denoiser over all volumes (the batched transport graph + the network); e2e = wall time of the
+    same pipeline through the public calls (mcx_gb300.denoise.pipeline_maps: run_batch with the
+    fields kept on the device, UNet.denoise_device, one pinned copy back per volume) from host
+    inputs to host maps; plain MC runs through the same pipeline without the network, and its
+    times and the speed-ups ride along.  One step = one volume; warm-up = full denoise pipelines
+    at 1e5 photons on the first volume."""
     import torch
 
     from mcx_gb300 import denoise as dn
@@ -349,8 +352,10 @@ def denoise_main(args, world, rank) -> None:
     tflops = flops / (fwd_ms * 1e-3) / 1e12
     t5, t2 = res["targets"][0], res["targets"][1]
     V = len(cfgs)
-    h2d = sum(c["vol"].size * 4 + np.asarray(c["prop"]).nbytes + 4 * c["vol"].size for c in cfgs)  # MC inputs + map up
-    d2h = sum(8 * c["vol"].size for c in cfgs)                                                        # map down twice
+    # MC inputs (the volume as MCX's 32-bit words, the media table) and the network's labels up;
+    # one fp32 map per volume down
+    h2d = sum(c["vol"].size * 4 + 2 * np.asarray(c["prop"]).nbytes + c["vol"].size for c in cfgs)
+    d2h = sum(4 * c["vol"].size for c in cfgs)
     launches = V + 22 * sum(t5["denoised"])
     rnd = lambda x: [round(v, 5) for v in x] if isinstance(x, list) else x  # noqa: E731
     line = {
@@ -359,7 +364,7 @@ def denoise_main(args, world, rank) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, bf16 network (fp32 accumulate)",
         "data": "synthetic",
         "config": {"workload": "denoise", "volumes": V, "edge": n, "judge_photons": args.judge_photons,
-                   "target_error": 0.05, "weights": weights, "pipeline": "all volumes in one batched call per budget",
+                   "target_error": 0.05, "weights": weights, "pipeline": "all volumes in one batched call per budget, fields kept on the device",
                    "l2": "inputs (128^3 fields and activations) larger than L2"},
         "plain_mc_s": t5["t_plain_device_s"],
         "speedup": t5["speedup_device"],
@@ -590,7 +595,7 @@ def main() -> None:
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scale", type=float, default=0.1, help="photon-budget scale of the batched workload")
-    ap.add_argument("--streams", type=int, default=4, help="streams of the batched workload's graph")
+    ap.add_argument("--streams", type=int, default=16, help="streams of the batched workload's graph")
     ap.add_argument("--ref-sample", type=int, default=16, help="batch instances the reference arm runs")
     ap.add_argument("--no-detectors", action="store_true",
                     help="drop the deck's detectors (measures the cost of detected-photon bookkeeping)")

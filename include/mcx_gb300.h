@@ -162,6 +162,15 @@ void mcxg_run_simulation_fp64(Config* cfg, GPUInfo* gpu);
  * `stats` (count entries) and `graph_ms` may be NULL.  Returns 0 or a negative MCX error id (message via mcxg_last_error). */
 int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms);
 
+/* mcxg_run_batch with the fluence kept on the device: for every i with dev_fields[i] != NULL the
+ * normalised field of cfgs[i] (the size of its exportfield, which is neither allocated nor written)
+ * is stored into that device buffer, for a consumer on the GPU such as a denoiser; the other
+ * outputs are as mcxg_run_batch gives them.  Such a Config must save a field and run in one
+ * repetition of one gate group, with one source pattern and no per-detector replay blocks.  The
+ * buffers are complete when the call returns. */
+int mcxg_run_batch_device(Config** cfgs, int count, int nstreams, float* const* dev_fields, mcxg_stats* stats,
+                          double* graph_ms);
+
 /* ---- Allocation-free transport ----------------------------------------------------------- */
 
 /* No counterpart in MCX: an addition for callers that may not call cudaMalloc while they run,

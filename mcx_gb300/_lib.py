@@ -62,6 +62,9 @@ lib.mcxg_set_step_cap.restype = None
 lib.mcxg_run_batch.argtypes = [C.POINTER(C.POINTER(abi.Config)), C.c_int, C.c_int, C.POINTER(abi.Stats),
                                 C.POINTER(C.c_double)]
 lib.mcxg_run_batch.restype = C.c_int
+lib.mcxg_run_batch_device.argtypes = [C.POINTER(C.POINTER(abi.Config)), C.c_int, C.c_int, C.POINTER(C.c_void_p),
+                                       C.POINTER(abi.Stats), C.POINTER(C.c_double)]
+lib.mcxg_run_batch_device.restype = C.c_int
 lib.mcxg_session_create.argtypes = [_CFG, C.c_int]
 lib.mcxg_session_create.restype = C.c_void_p
 lib.mcxg_session_reset.argtypes = [C.c_void_p]
@@ -116,6 +119,6 @@ EXPORTED = [
     "mcxg_rng_test", "mcxg_photon_stream", "mcxg_session_create", "mcxg_session_reset", "mcxg_session_run",
     "mcxg_session_read", "mcxg_session_destroy", "mcxg_set_launch", "mcxg_run_noalloc", "mcxg_noalloc_scratch_bytes",
     "mcxg_set_seeding", "mcxg_probe_atomic_rate",
-    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_replayinit", "mcxg_set_step_cap", "mcxg_dn_last_error",
+    "mcxg_session_autotune", "mcxg_run_batch", "mcxg_run_batch_device", "mcxg_replayinit", "mcxg_set_step_cap", "mcxg_dn_last_error",
     "mcxg_set_field_precision", "mcxg_photon_shares", "mcxg_dn_check",
 ] + list(_DN)

@@ -526,11 +526,17 @@ def run_prepared(pc: PreparedConfig, fp64_field: bool = False, devices: list[int
     return out
 
 
-def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[str, Any]], float]:
+def run_batch(cfgs: list[dict[str, Any]], streams: int = 4, device_fields: list | None = None
+              ) -> tuple[list[dict[str, Any]], float]:
     """Run many independent simulations in one CUDA graph on one GPU (``mcxg_run_batch``).
 
     Returns the per-simulation results -- the same dicts ``run`` gives -- and the graph time in
-    ms (all waves: repetitions and gate groups run as further graphs)."""
+    ms (all waves: repetitions and gate groups run as further graphs).
+
+    ``device_fields``: one contiguous float32 CUDA tensor per simulation (or None for a host
+    field), of the simulation's field size (nx * ny * nz * gates); the normalised fluence is
+    stored there on the device (``mcxg_run_batch_device``) and the result has no ``flux``.  Each
+    such simulation runs one repetition of one gate group."""
     pcs = [prepare(cfg) for cfg in cfgs]
     for pc in pcs:
         nact, info = _active_devices(pc.c)
@@ -538,12 +544,33 @@ def run_batch(cfgs: list[dict[str, Any]], streams: int = 4) -> tuple[list[dict[s
             libc.free(info)
         if nact == 0:
             raise MCXError(-1, "no active GPU device found")
-    fields = [_attach_field(pc) for pc in pcs]
+    if device_fields is not None and len(device_fields) != len(pcs):
+        raise MCXError(-4, f"{len(device_fields)} device fields for {len(pcs)} simulations")
+    fields, ptrs = [], None
+    if device_fields is not None:
+        ptrs = (C.c_void_p * len(pcs))()
+    for i, pc in enumerate(pcs):
+        dev = None if device_fields is None else device_fields[i]
+        if dev is None:
+            fields.append(_attach_field(pc))
+            continue
+        flux, maxgate = _attach_field(pc)
+        pc.c.exportfield = None
+        if flux is None:
+            raise MCXError(-4, "a device field was given for a simulation that saves no field")
+        if not (getattr(dev, "is_cuda", False) and dev.dtype.is_floating_point and dev.element_size() == 4
+                and dev.is_contiguous() and dev.numel() == flux.size):
+            raise MCXError(-4, f"device field {i} must be a contiguous float32 CUDA tensor of {flux.size} elements")
+        ptrs[i] = dev.data_ptr()
+        fields.append((None, maxgate))
     arr = (C.POINTER(abi.Config) * len(pcs))(*[C.pointer(pc.c) for pc in pcs])
     stats = (abi.Stats * len(pcs))()
     ms = C.c_double(0.0)
     try:
-        _check(lib.mcxg_run_batch(arr, len(pcs), int(streams), stats, C.byref(ms)))
+        if ptrs is None:
+            _check(lib.mcxg_run_batch(arr, len(pcs), int(streams), stats, C.byref(ms)))
+        else:
+            _check(lib.mcxg_run_batch_device(arr, len(pcs), int(streams), ptrs, stats, C.byref(ms)))
     finally:
         for pc in pcs:
             _take_seeds(pc)

@@ -832,6 +832,14 @@ struct Session {
         launches = 1;
     }
 
+    // Merge shadow copies and scale into a device buffer of the caller (fieldlen floats), in
+    // stream order: nothing crosses to the host.
+    void read_field_device(float* dev, float scale, int positive_only) {
+        CK(cudaSetDevice(device));
+        CK(launch_merge_field(dev, field.as<float>(), shadow.as<float>(), field64.as<double>(), fieldlen, scale,
+                              positive_only, stream));
+    }
+
     // Merge shadow copies, optionally scale, and copy the field out.
     void read_field(float* host, float scale, int positive_only) {
         CK(cudaSetDevice(device));
@@ -1033,8 +1041,8 @@ void check_config(const Config* cfg) {
 
 // Output buffers and counters of a run, as mcx_run_simulation leaves them before its first
 // launch (src/mcx_core.cu:2907-2921): exportfield is accumulated into, exportdetected grows.
-void begin_outputs(Config* cfg, const Session& S) {
-    if (cfg->exportfield == nullptr && cfg->issave2pt) cfg->exportfield = (float*)calloc(S.fieldlen, sizeof(float));
+void begin_outputs(Config* cfg, const Session& S, bool host_field = true) {
+    if (host_field && cfg->exportfield == nullptr && cfg->issave2pt) cfg->exportfield = (float*)calloc(S.fieldlen, sizeof(float));
     if (cfg->exportdetected == nullptr)
         cfg->exportdetected = (float*)malloc((size_t)S.kp.reclen * std::max(1u, cfg->maxdetphoton) * sizeof(float));
     if (S.kp.saveseed && cfg->seeddata == nullptr)
@@ -1110,7 +1118,8 @@ void append_trajectory(Config* cfg, Session& S, std::mutex* mu = nullptr) {
 // (src/mcx_core.cu:3716-3770, 3823-3925).
 // With several devices (src/mcx_core.cu:3730-3759) their energies are summed first, so one
 // normaliser scales every device's field, and the scaled fields are summed into exportfield.
-void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<float>& host_field, mcxg_stats& total) {
+void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<float>& host_field, mcxg_stats& total,
+                   float* dev_out = nullptr) {
     double e_launch = 0.0;
     for (Session* D : SS) {
         mcxg_stats st{};
@@ -1188,6 +1197,12 @@ void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<flo
             }
             cfg->normalizer = scale;
             cfg->his.normalizer = scale;
+        }
+        if (dev_out) {
+            if (SS.size() != 1 || !block_scale.empty() || !chan_scale.empty())
+                MCXG_RAISE(-4, "a field on the device is given for one device, one pattern and no detector blocks only");
+            S.read_field_device(dev_out, scale, cfg->isnormalized == 2);
+            return;
         }
         host_field.resize(S.fieldlen);
         for (Session* D : SS) {
@@ -1481,7 +1496,7 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
 // Config's outputs are those of mcx_run_simulation; `runtime` is the batch's graph time.
 constexpr int kMinBatchCTAs = 16;
 
-void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms) {
+void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms, float* const* dev_fields = nullptr) {
     if (count <= 0 || !cfgs) MCXG_RAISE(-4, "an empty batch");
     nstreams = std::max(1, std::min(nstreams, 32));
     const int gpuid = cfgs[0]->deviceid[0] - 1;
@@ -1503,7 +1518,10 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
         groups[i] = (S[i]->totalgates + S[i]->kp.maxgate - 1) / S[i]->kp.maxgate;
         nper[i] = (cfg->respin > 0) ? (uint64_t)cfg->nphoton : (uint64_t)cfg->nphoton / (uint64_t)reps[i];
         waves = std::max(waves, reps[i] * groups[i]);
-        begin_outputs(cfg, *S[i]);
+        const bool on_device = dev_fields && dev_fields[i];
+        if (on_device && (reps[i] * groups[i] != 1 || !cfg->issave2pt))
+            MCXG_RAISE(-4, "a field on the device needs a fluence output in one repetition of one gate group");
+        begin_outputs(cfg, *S[i], !on_device);
         std::memset(&totals[i], 0, sizeof(mcxg_stats));
     }
     for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
@@ -1609,9 +1627,12 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
                 if (w >= reps[i] * groups[i]) continue;
                 append_detected(cfgs[i], *S[i]);
                 append_trajectory(cfgs[i], *S[i]);
-                if (w % reps[i] == reps[i] - 1) finish_window(cfgs[i], {S[i].get()}, host_field, totals[i]);
+                if (w % reps[i] == reps[i] - 1)
+                    finish_window(cfgs[i], {S[i].get()}, host_field, totals[i], dev_fields ? dev_fields[i] : nullptr);
             }
         }
+        if (dev_fields)
+            for (auto& s : S) CK(cudaStreamSynchronize(s->stream));     // the fields are complete on return
         if (graph_ms) *graph_ms = total_ms;
         for (int i = 0; i < count; i++) {
             totals[i].kernel_ms = total_ms;
@@ -1632,6 +1653,19 @@ extern "C" int mcxg_run_batch(Config** cfgs, int count, int nstreams, mcxg_stats
     mcxg_clear_error();
     try {
         run_batch(cfgs, count, nstreams, stats, graph_ms);
+        return 0;
+    } catch (const Error& e) {
+        report(e);
+        return e.id ? e.id : -1;
+    }
+}
+
+extern "C" int mcxg_run_batch_device(Config** cfgs, int count, int nstreams, float* const* dev_fields, mcxg_stats* stats,
+                                     double* graph_ms) {
+    mcxg_clear_error();
+    try {
+        if (!dev_fields) MCXG_RAISE(-4, "no device fields given");
+        run_batch(cfgs, count, nstreams, stats, graph_ms, dev_fields);
         return 0;
     } catch (const Error& e) {
         report(e);

@@ -303,21 +303,35 @@ class UNet:
         if f.ndim == 4:
             f = f[..., 0]
         nx, ny, nz = f.shape
-        fl = torch.from_numpy(np.ascontiguousarray(f.reshape(-1, order="F"))).to(self.dev).view(1, -1)
-        lab = torch.from_numpy(np.ascontiguousarray(np.asarray(vol, np.uint8).reshape(-1, order="F"))).to(self.dev).view(1, -1)
-        pr = torch.from_numpy(np.ascontiguousarray(prop, np.float32)).to(self.dev).view(1, -1, 4)
-        lp = torch.tensor([math.log10(nphoton)], dtype=torch.float32, device=self.dev)
+        fl = torch.from_numpy(np.ascontiguousarray(f.reshape(-1, order="F"))).to(self.dev)
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         ev[0].record()
-        x0, xres = self.pack(fl, lab, pr, lp, nz, ny, nx)
-        out = self._buf("out", nx * ny * nz, torch.float32)
-        self.forward(x0, xres, 1, nz, ny, nx, out=out)
-        # back to linear fluence on the device: one fp32 map crosses the bus
-        flux_out = torch.clamp_(torch.pow(10.0, out).sub_(FLUX_FLOOR), min=0.0)
+        flux_out = self.denoise_device(fl, vol, prop, nphoton)
         ev[1].record()
         lf = flux_out.cpu().numpy()
         self.last_gpu_ms = ev[0].elapsed_time(ev[1])     # pack + network + exponent on the device
         return lf.reshape((nx, ny, nz), order="F")
+
+    def denoise_device(self, flux: torch.Tensor, vol: np.ndarray, prop: np.ndarray, nphoton: float,
+                       out: torch.Tensor | None = None) -> torch.Tensor:
+        """`denoise` on a fluence map already on the device (fp32, x fastest: the layout of
+        ``run_batch(..., device_fields=...)``), stream-ordered and without a host round trip:
+        returns the denoised linear fluence in the same layout (in `out` when given).  Only the
+        labels and the media table cross the bus."""
+        nx, ny, nz = np.asarray(vol).shape[:3]
+        fl = flux.reshape(1, -1)
+        lab = torch.from_numpy(np.ascontiguousarray(np.asarray(vol, np.uint8).reshape(-1, order="F")))
+        lab = lab.to(self.dev, non_blocking=True).view(1, -1)
+        pr = torch.from_numpy(np.ascontiguousarray(prop, np.float32)).to(self.dev).view(1, -1, 4)
+        lp = torch.full((1,), math.log10(nphoton), dtype=torch.float32, device=self.dev)
+        x0, xres = self.pack(fl, lab, pr, lp, nz, ny, nx)
+        logf = self._buf("out", nx * ny * nz, torch.float32)
+        self.forward(x0, xres, 1, nz, ny, nx, out=logf)
+        # back to linear fluence on the device
+        if out is None:
+            out = torch.empty(nx * ny * nz, dtype=torch.float32, device=self.dev)
+        torch.pow(10.0, logf, out=out)
+        return torch.clamp_(out.sub_(FLUX_FLOOR), min=0.0)
 
 
 # -- data -------------------------------------------------------------------------------------
@@ -560,58 +574,78 @@ def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, ta
     return out
 
 
+def pipeline_maps(cfgs: list[dict[str, Any]], budgets: list[float], seeds: list[int], net: UNet | None = None,
+                  denoise: list[bool] | None = None, streams: int = 16) -> tuple[list[np.ndarray], float, float]:
+    """One pass of the pipeline over many volumes, from host inputs to host maps: one batched MC
+    call whose fluence maps stay on the device (``run_batch(..., device_fields=...)``), the network
+    on the volumes flagged in `denoise` (``UNet.denoise_device``, stream-ordered), and one copy of
+    every final map into pinned host memory.  Returns (maps, flat fp32 x fastest; MC graph time
+    in s; network GPU time in s)."""
+    from .api import run_batch
+
+    V = len(cfgs)
+    denoise = denoise or [False] * V
+    fields = [torch.empty(int(np.asarray(c["vol"]).size), dtype=torch.float32, device="cuda") for c in cfgs]
+    _, ms = run_batch([dict(c, nphoton=int(n), seed=k) for c, n, k in zip(cfgs, budgets, seeds)], streams=streams,
+                      device_fields=fields)
+    host = [torch.empty(f.numel(), dtype=torch.float32, pin_memory=True) for f in fields]
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    ev[0].record()
+    for v, c in enumerate(cfgs):
+        f = fields[v]
+        if denoise[v]:
+            f = net.denoise_device(f, c["vol"], c["prop"], budgets[v], out=f)
+        host[v].copy_(f, non_blocking=True)
+    ev[1].record()
+    torch.cuda.synchronize()
+    net_s = ev[0].elapsed_time(ev[1]) * 1e-3 if any(denoise) else 0.0
+    return [h.numpy() for h in host], ms * 1e-3, net_s
+
+
 def time_to_error_batch(net: UNet, cfgs: list[dict[str, Any]], judge_photons: float = 1e9,
                         targets: tuple[float, ...] = (0.05, 0.02),
                         ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
                         dn_ladder: tuple[float, ...] = (1e5, 2e5, 3e5, 6e5, 1e6, 3e6, 1e7),
-                        judge_check: bool = True) -> dict[str, Any]:
+                        judge_check: bool = True, streams: int = 16) -> dict[str, Any]:
     """Time for each pipeline to deliver every volume of `cfgs` at a median relative fluence error
     of each target against a `judge_photons` run of that volume, with all volumes simulated
-    together through the batched entry point (one CUDA graph per call), so a short simulation's
-    latency -- its longest photons -- is paid once per call rather than once per volume.
+    together through the batched entry point (one CUDA graph per call, short simulations side by
+    side), so a short simulation's latency -- its longest photons -- is paid once per call rather
+    than once per volume.  Both pipelines run through `pipeline_maps` (host inputs to host maps).
 
     The errors come from ladders of budgets (every budget one batched call over all volumes).  Plain
     MC: each volume's photon count for the target is interpolated in its ladder (log-log, the
-    1/sqrt(N) law past the last budget), then ONE batched call runs every volume at its own count
-    and is timed: on the device (graph time) and end to end (wall time of the call).  MC + denoiser:
-    each volume takes the smallest budget of `dn_ladder` whose denoised map reaches the target
-    (volumes that none reaches fall back to plain MC at their plain count), then one batched call
-    runs them and the network denoises every volume: device time = graph time + network GPU time,
-    wall time = the call + the denoise calls.  The measured errors of those final runs are returned
-    beside the times."""
-    from .api import run_batch
-
+    1/sqrt(N) law past the last budget), then ONE pipeline pass runs every volume at its own count
+    and is timed: on the device (graph time) and end to end (wall time of the pass).  MC +
+    denoiser: each volume takes the smallest budget of `dn_ladder` whose denoised map reaches the
+    target (volumes that none reaches fall back to plain MC at their plain count), then one pass
+    runs them and denoises: device time = graph time + network GPU time, wall time = the pass.
+    The measured errors of those final runs are returned beside the times; they are computed
+    after the clock stops."""
     V = len(cfgs)
     seed = lambda c, k: int((int(c["seed"]) + 7919 * k) % (2**31 - 1)) or 1  # noqa: E731
 
-    # one stream per volume (up to 32): a short simulation's launch ends on its longest photons
-    # while its other CTAs are already done, and the next volume's CTAs take their SMs
-    streams = max(1, min(32, V))
-
-    def batch(budgets, k):
+    def batch(budgets, k, dn_flags=None):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res, ms = run_batch([dict(c, nphoton=int(n), seed=seed(c, k)) for c, n in zip(cfgs, budgets)], streams=streams)
-        return [_flat(r["flux"]) for r in res], ms * 1e-3, time.perf_counter() - t0
+        maps, mc_s, net_s = pipeline_maps(cfgs, budgets, [seed(c, k) for c in cfgs], net, dn_flags, streams)
+        return maps, mc_s, net_s, time.perf_counter() - t0
 
-    judges, _, judge_s = batch([judge_photons] * V, 1)
+    judges, _, _, judge_s = batch([judge_photons] * V, 1)
     judge_err = None
     if judge_check:
-        j4, _, _ = batch([judge_photons / 4] * V, 2)
+        j4 = batch([judge_photons / 4] * V, 2)[0]
         judge_err = [median_rel_error(a, b) / math.sqrt(5.0) for a, b in zip(j4, judges)]
     plain = []
     for i, n in enumerate(ladder):
-        maps, dev_s, wall_s = batch([n] * V, 10 + i)
+        maps, mc_s, _, wall_s = batch([n] * V, 10 + i)
         plain.append({"photons": n, "errors": [median_rel_error(m, j) for m, j in zip(maps, judges)],
-                      "s": wall_s, "kernel_s": dev_s})
-    for c in cfgs:
-        net.denoise(np.ones(c["vol"].shape, np.float32), c["vol"], c["prop"], 1e5)   # buffers for the grid
-    torch.cuda.synchronize()
+                      "s": wall_s, "kernel_s": mc_s})
     dn = []
     for i, n in enumerate(dn_ladder):
-        maps, dev_s, _ = batch([n] * V, 30 + i)
-        errs = [median_rel_error(_flat(net.denoise(m.reshape(c["vol"].shape, order="F"), c["vol"], c["prop"], n)), j)
-                for m, c, j in zip(maps, cfgs, judges)]
-        dn.append({"photons": n, "errors": errs, "kernel_s": dev_s})
+        maps, mc_s, net_s, wall_s = batch([n] * V, 30 + i, [True] * V)
+        dn.append({"photons": n, "errors": [median_rel_error(m, j) for m, j in zip(maps, judges)],
+                   "kernel_s": mc_s, "network_s": net_s, "s": wall_s})
 
     def plain_photons(v, tgt):
         lad = [{"photons": r["photons"], "error": r["errors"][v]} for r in plain]
@@ -624,31 +658,19 @@ def time_to_error_batch(net: UNet, cfgs: list[dict[str, Any]], judge_photons: fl
     per = []
     for t_i, tgt in enumerate(targets):
         n_plain = [plain_photons(v, tgt) for v in range(V)]
-        maps, p_dev, p_wall = batch(n_plain, 60 + t_i)
+        maps, p_dev, _, p_wall = batch(n_plain, 60 + t_i)
         p_err = [median_rel_error(m, j) for m, j in zip(maps, judges)]
         n_dn, use_dn = [], []
         for v in range(V):
             rec = next((r for r in dn if r["errors"][v] <= tgt), None)
             use_dn.append(rec is not None)
             n_dn.append(rec["photons"] if rec else n_plain[v])
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res, ms = run_batch([dict(c, nphoton=int(n), seed=seed(c, 80 + t_i)) for c, n in zip(cfgs, n_dn)],
-                            streams=streams)
-        net_ms, d_maps = 0.0, []
-        for v, (r, c) in enumerate(zip(res, cfgs)):
-            f = r["flux"][..., 0]
-            if use_dn[v]:
-                f = net.denoise(f, c["vol"], c["prop"], n_dn[v])
-                net_ms += net.last_gpu_ms
-            d_maps.append(f)
-        d_wall = time.perf_counter() - t0
-        # the errors against the judge are the check, not part of the pipeline's time
-        d_err = [median_rel_error(_flat(f), j) for f, j in zip(d_maps, judges)]
-        d_dev = ms * 1e-3 + net_ms * 1e-3
+        maps, mc_s, net_s, d_wall = batch(n_dn, 80 + t_i, use_dn)
+        d_err = [median_rel_error(m, j) for m, j in zip(maps, judges)]
+        d_dev = mc_s + net_s
         per.append({"target": tgt, "photons_plain": n_plain, "t_plain_s": p_wall, "t_plain_device_s": p_dev,
                     "error_plain": p_err, "photons_denoised": n_dn, "denoised": use_dn, "t_denoised_s": d_wall,
-                    "t_denoised_device_s": d_dev, "network_s": net_ms * 1e-3, "error_denoised": d_err,
+                    "t_denoised_device_s": d_dev, "network_s": net_s, "error_denoised": d_err,
                     "speedup": p_wall / d_wall, "speedup_device": p_dev / d_dev})
     return {"volumes": V, "judge_photons": judge_photons, "judge_s": judge_s, "judge_error_est": judge_err,
             "plain": plain, "denoised": dn, "targets": per}

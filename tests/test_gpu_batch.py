@@ -84,3 +84,35 @@ def test_batch_repetitions_and_gate_groups(engine):
         fa, fb = ra["flux"], rb["flux"]
         assert fa.shape == fb.shape
         assert np.abs(fa - fb).max() <= 1e-4 * np.abs(fa).max() + 1e-12
+
+
+def test_batch_fields_on_the_device(engine):
+    """mcxg_run_batch_device: the normalised fields land in the caller's CUDA buffers, equal to
+    the host fields of the same batch within FP32 summation order, with the same counters; host
+    and device fields can be mixed; the contract's refusals raise MCX errors."""
+    import torch
+
+    from mcx_gb300.api import MCXError
+
+    insts = problems.denoise_instances(3, 32, seed=5)
+    for c in insts:
+        c["nphoton"] = 200_000
+    host, _ = engine.run_batch(insts, streams=3)
+    bufs = [torch.full((c["vol"].size,), -1.0, device="cuda") for c in insts]
+    dev, ms = engine.run_batch(insts, streams=3, device_fields=[bufs[0], None, bufs[2]])
+    assert ms > 0 and "flux" not in dev[0] and "flux" in dev[1] and "flux" not in dev[2]
+    for i, (h, d) in enumerate(zip(host, dev)):
+        for key in ("n_steps", "n_scatter", "n_photon"):
+            assert h["stat"][key] == d["stat"][key], key
+        for key in ("energytot", "normalizer"):
+            assert d["stat"][key] == pytest.approx(h["stat"][key], rel=1e-6), key
+        fa = h["flux"][..., 0].ravel(order="F").astype(np.float64)
+        fb = (bufs[i].cpu().numpy() if i != 1 else d["flux"][..., 0].ravel(order="F")).astype(np.float64)
+        assert (fb >= 0).all()
+        assert abs(fa.sum() - fb.sum()) <= 1e-5 * fa.sum()
+        hot = fa > np.quantile(fa, 0.99)
+        assert np.max(np.abs(fa[hot] - fb[hot]) / fa[hot]) < 5e-4
+    with pytest.raises(MCXError):           # wrong size
+        engine.run_batch(insts[:1], device_fields=[torch.empty(10, device="cuda")])
+    with pytest.raises(MCXError):           # two repetitions
+        engine.run_batch([dict(insts[0], respin=2)], device_fields=[bufs[0]])

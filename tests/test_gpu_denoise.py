@@ -362,3 +362,25 @@ def test_checkpoint_beats_raw_low_photon_maps(dn):
     print("raw", raw, "box", box, "denoised", den)
     assert np.median(den) <= 0.7 * np.median(raw), (raw, den)
     assert np.median(den) < np.median(box), (box, den)
+
+
+def test_denoise_on_the_device_equals_the_host_call():
+    """UNet.denoise_device on a map already on the GPU gives the host call's map bit for bit (the
+    same kernels in the same order), and several volumes can be queued before one synchronise."""
+    import torch
+
+    from mcx_gb300 import denoise as dn
+    from mcx_gb300 import problems
+
+    net = dn.UNet(seed=3)
+    cfgs = problems.denoise_instances(2, 32, seed=9)
+    rng = np.random.default_rng(1)
+    maps = [rng.random(c["vol"].shape).astype(np.float32) for c in cfgs]
+    want = [net.denoise(m, c["vol"], c["prop"], 1e5) for m, c in zip(maps, cfgs)]
+    dev = [torch.from_numpy(m.ravel(order="F").copy()).cuda() for m in maps]
+    outs = [torch.empty_like(d) for d in dev]
+    for d, o, c in zip(dev, outs, cfgs):
+        net.denoise_device(d, c["vol"], c["prop"], 1e5, out=o)
+    torch.cuda.synchronize()
+    for o, w, c in zip(outs, want, cfgs):
+        assert np.array_equal(o.cpu().numpy(), w.ravel(order="F"))
