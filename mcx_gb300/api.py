@@ -266,9 +266,17 @@ class PreparedConfig:
         if "vol" not in cfg or "prop" not in cfg:
             raise MCXError(-4, "the 'vol' and 'prop' fields are required")
         vol = np.asarray(cfg["vol"])
-        words, mediabyte = pack_media(vol, float(cfg.get("unitinmm", 1.0)))
-        vol32 = words.ravel(order="F").copy()
-        c.dim.x, c.dim.y, c.dim.z = (int(s) for s in words.shape[:3])
+        if vol.ndim == 3 and vol.dtype.kind in "iub" and vol.flags.c_contiguous and not int(cfg.get("isrowmajor", 0)):
+            # C-ordered labels: widened in their own order, and the engine's preparation transposes
+            # them to MCX's x-fastest order (MCX's isrowmajor input, src/mcx_utils.c:1620-1631)
+            vol32 = vol.astype(np.uint32).reshape(-1)
+            mediabyte = {1: 1, 2: 2, 4: 4, 8: 4}[vol.dtype.itemsize]
+            c.dim.x, c.dim.y, c.dim.z = (int(s) for s in vol.shape)
+            c.isrowmajor = b"\x01"
+        else:
+            words, mediabyte = pack_media(vol, float(cfg.get("unitinmm", 1.0)))
+            vol32 = words.ravel(order="F").copy()
+            c.dim.x, c.dim.y, c.dim.z = (int(s) for s in words.shape[:3])
         c.mediabyte = mediabyte
         self.vol = vol32
         c.vol = vol32.ctypes.data

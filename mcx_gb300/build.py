@@ -24,7 +24,7 @@ ORACLE_LIB = ORACLE_DIR / "_build" / "libmcx_oracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "--use_fast_math"] + ARCH
-CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-Wall", "-Wno-unused-function"]
+CXX_FLAGS = ["-O2", "-fPIC", "-pthread", "-std=c++17", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["transport.cu", "engine.cu", "noalloc.cu", "denoise.cu"]
 CPP_SOURCES = ["preprocess.cpp"]
@@ -81,7 +81,7 @@ def build_engine(force: bool = False, verbose: bool = False) -> Path:
             pass
     if force or jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC", "-lpthread"])
         os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}")

@@ -276,7 +276,6 @@ void check_source(const Config* cfg) {
         if (!cfg->srcdata) MCXG_RAISE(-4, "extrasrclen is set but the extra sources (srcdata) are missing");
         if (cfg->srcnum > 1) MCXG_RAISE(-4, "simulating multiple sources currently can not be used with photon-sharing");
         if (cfg->srcid > (int)cfg->extrasrclen + 1) MCXG_RAISE(-4, "srcid exceeds total defined source count");
-        if (cfg->seed == kSEED_FROM_FILE) MCXG_RAISE(-6, "replay with extra sources is not supported by the GB300 engine");
         for (unsigned i = 0; i < cfg->extrasrclen; i++)
             if (std::isinf(cfg->srcdata[i].srcdir.w) && cfg->srcdata[i].srcdir.w > 0.f)
                 MCXG_RAISE(-4, "a focal length of +inf is not a valid source setting (srcdir.w)");
@@ -376,7 +375,8 @@ struct Session {
     DevBuf phase_tab, angle_tab;   // user phase function and launch-angle inverse CDFs
     DevBuf extra_src;              // extra sources, 5 float4 each
     DevBuf replay_seed, replay_w, replay_tof, replay_detid, seeddata, voxwords, voxwords2, traj, trajcount, smat;
-    unsigned blocks = 1;       // field blocks of maxgate gates (detectors of an all-detector replay)
+    unsigned blocks = 1;       // field blocks of maxgate gates: sources kept apart x detectors of an all-detector replay
+    unsigned det_blocks = 1;   // the detector blocks within one source's block
     unsigned halves = 1;       // 2: RF replay, real then imaginary part
     unsigned chans = 1;        // photon sharing: one channel per pattern, adjacent per voxel and gate
     double kernel_ms = 0.0;
@@ -439,9 +439,9 @@ struct Session {
         if (gate_cap > 0) maxgate = std::min(maxgate, gate_cap);
         // a replay of every detector at once keeps one block of gates per detector
         // (src/mcx_core.cu:2907-2913)
-        blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
-        // every source kept apart (srcid -1): one block of gates per source (src/mcx_core.cu:3039)
-        if (cfg->extrasrclen && cfg->srcid < 0) blocks = cfg->extrasrclen + 1;
+        det_blocks = (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) ? std::max(1u, cfg->detnum) : 1;
+        // every source kept apart (srcid -1): one such block per source (src/mcx_core.cu:3039-3046)
+        blocks = det_blocks * ((cfg->extrasrclen && cfg->srcid < 0) ? cfg->extrasrclen + 1 : 1);
         // RF replay outputs carry a real and an imaginary field (src/mcx_core.cu:2908-2913)
         halves = (cfg->outputtype == otRF || cfg->outputtype == otRFmus) ? 2 : 1;
         if ((size_t)maxgate * blocks * halves * per_gate > budget)
@@ -1154,14 +1154,13 @@ void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<flo
                 double sc = cfg->unitinmm / (cfg->energytot * Vvox * cfg->tstep);
                 if (ot == otFluence) sc *= cfg->tstep;
                 scale = (float)sc;
-                // every source simulated apart: each got 1/(n+1) of the photons (3908-3910)
-                if (cfg->extrasrclen && cfg->srcid < 0) scale *= (float)(cfg->extrasrclen + 1);
             } else if (ot == otEnergy || ot == otL) {
                 scale = (float)(1.0 / cfg->energytot);
-                if (cfg->extrasrclen && cfg->srcid < 0) scale *= (float)(cfg->extrasrclen + 1);
             } else if (cfg->seed == kSEED_FROM_FILE && cfg->replaydet == -1) {
-                // each detector's block over its replayed weight; paths carry unitinmm
-                for (unsigned d = 1; d <= S.blocks; d++) {
+                // each detector's block over its replayed weight; paths carry unitinmm.  MCX scales
+                // the detector blocks of the first source only (src/mcx_core.cu:3845-3873): with
+                // every source kept apart, the other sources' blocks stay as accumulated
+                for (unsigned d = 1; d <= S.det_blocks; d++) {
                     float sd = path_units ? cfg->unitinmm : 1.f;
                     if (cfg->isnormalized != 2) {
                         double sum = 0.0;
@@ -1177,6 +1176,9 @@ void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<flo
                 for (size_t i = 0; i < (size_t)cfg->nphoton; i++) sum += cfg->replay.weight[i];
                 scale = (sum > 0.0) ? (float)(cfg->unitinmm / sum) : 0.f;
             }
+            // every source simulated apart: each got 1/(n+1) of the photons (3908-3910); in an
+            // all-detector replay this reaches the reported normaliser only, as in MCX
+            if (cfg->extrasrclen && cfg->srcid < 0) scale *= (float)(cfg->extrasrclen + 1);
             if (S.chans > 1) {
                 // photon sharing: each pattern's channel over its total intensity
                 // (src/mcx_core.cu:3778-3795, 3895-3906), Kahan-summed in float as MCX sums it
@@ -1219,7 +1221,8 @@ void finish_window(Config* cfg, const std::vector<Session*>& SS, std::vector<flo
             const size_t per = S.fieldlen / (S.blocks * S.halves);     // one detector's gates
             for (size_t i = 0; i < S.fieldlen; i++) {
                 const float v = host_field[i];
-                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * block_scale[(i / per) % S.blocks];
+                const size_t b = (i / per) % S.blocks;
+                out[i] += (cfg->isnormalized == 2 && v < 0.f) ? v : v * (b < S.det_blocks ? block_scale[b] : 1.f);
             }
         }
         }

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <ctime>
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "../../include/mcx_abi.h"
@@ -280,6 +281,35 @@ void prep_polarized(Config* cfg) {
     }
 }
 
+// dst[z][y][x] = src[x][y][z] for a d.x x d.y x d.z volume: for each y a (d.x x d.z) matrix
+// transpose, done in 32 x 32 tiles so that both sides stay in cache lines, the y slabs shared out
+// over a few threads for large volumes.
+void row_to_column_major(const uint32_t* src, uint32_t* dst, uint3 d) {
+    constexpr uint32_t T = 32;
+    auto slab = [&](uint32_t y0, uint32_t y1) {
+        for (uint32_t y = y0; y < y1; y++)
+            for (uint32_t x0 = 0; x0 < d.x; x0 += T)
+                for (uint32_t z0 = 0; z0 < d.z; z0 += T) {
+                    const uint32_t x1 = std::min(d.x, x0 + T), z1 = std::min(d.z, z0 + T);
+                    for (uint32_t x = x0; x < x1; x++) {
+                        const uint32_t* s = src + ((size_t)x * d.y + y) * d.z;
+                        for (uint32_t z = z0; z < z1; z++) dst[((size_t)z * d.y + y) * d.x + x] = s[z];
+                    }
+                }
+    };
+    const size_t n = (size_t)d.x * d.y * d.z;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = (n < (1u << 20)) ? 1u : std::min<unsigned>({hw, 8u, d.y});
+    if (nt <= 1) {
+        slab(0, d.y);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++)
+        th.emplace_back(slab, (uint32_t)((uint64_t)d.y * t / nt), (uint32_t)((uint64_t)d.y * (t + 1) / nt));
+    for (auto& t : th) t.join();
+}
+
 void validate(Config* cfg) {
     // replay of saved photons (src/mcx_utils.c:1651-1664)
     if (cfg->seed == kSEED_FROM_FILE && (cfg->respin > 1 || cfg->respin < 0)) {
@@ -357,13 +387,9 @@ void validate(Config* cfg) {
         }
     }
     if (cfg->isrowmajor) {
-        // C-order input: transpose to MCX's x-fastest order
-        const uint3 d = cfg->dim;
-        std::vector<uint32_t> tmp((size_t)d.x * d.y * d.z);
-        for (uint32_t x = 0; x < d.x; x++)
-            for (uint32_t y = 0; y < d.y; y++)
-                for (uint32_t z = 0; z < d.z; z++)
-                    tmp[(size_t)z * d.y * d.x + (size_t)y * d.x + x] = cfg->vol[((size_t)x * d.y + y) * d.z + z];
+        // C-order input: transpose to MCX's x-fastest order (src/mcx_utils.c:1620-1631)
+        std::vector<uint32_t> tmp((size_t)cfg->dim.x * cfg->dim.y * cfg->dim.z);
+        row_to_column_major(cfg->vol, tmp.data(), cfg->dim);
         std::memcpy(cfg->vol, tmp.data(), tmp.size() * sizeof(uint32_t));
         cfg->isrowmajor = 0;
     }

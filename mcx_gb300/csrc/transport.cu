@@ -914,6 +914,9 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 S.ssrc[tid] = k;
                 if (k > 1) alt = P.extrasrc + 5 * (k - 2);
             }
+            // a replay of one chosen source skips the draw by which the recorded run picked its
+            // source among all of them (src/mcx_core.cu:1229-1231)
+            if (FULL && start && P.replay && P.srcid >= 1) (void)rng_next(r0, r1);
             bool entered = false;
             if (start && P.srctype == kSrcPencil && !(FULL && (P.nangle > 0 || P.nextra))) {
                 // launch (pencil branch of src/mcx_core.cu:1236-1243, 1646-1717; the void
@@ -1052,7 +1055,11 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     const int rb = S.rbin[tid];
                     if (rb >= 0) {
                         float q = S.rw[tid];
-                        const size_t at = (size_t)idx + (size_t)rb * P.nvox;
+                        // every source apart: the source's block of (detector) blocks, as at deposits
+                        const int sb = (P.nextra && P.srcid < 0)
+                                           ? (S.ssrc[tid] - 1) * ((P.replaydet == -1) ? P.detnum : 1) * P.maxgate
+                                           : 0;
+                        const size_t at = (size_t)idx + (size_t)(rb + sb) * P.nvox;
                         if (P.outputtype == kOutDCS) q *= 1.f - ct;
                         else if (P.outputtype == kOutWPTOF) q *= S.rtof[tid];
                         if (P.outputtype == kOutRFmus) {
@@ -1211,9 +1218,13 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     // cos(omega t) here, x sin(omega t) in the imaginary half
                     const int rb = S.rbin[tid];
                     weight = (rb < 0) ? 0.f : -S.rw[tid] * pathlen * S.rcos[tid];
-                    if (rb >= 0)
-                        field_add_small(P, (size_t)idxold + (size_t)rb * P.nvox + P.rf_offset,
+                    if (rb >= 0) {
+                        const int sb = (P.nextra && P.srcid < 0)
+                                           ? (S.ssrc[tid] - 1) * ((P.replaydet == -1) ? P.detnum : 1) * P.maxgate
+                                           : 0;
+                        field_add_small(P, (size_t)idxold + (size_t)(rb + sb) * P.nvox + P.rf_offset,
                                         -S.rw[tid] * pathlen * S.rcos[B + tid]);
+                    }
                     tshift = rb;
                 } else {
                     weight = 0.f;                           // scattering-event outputs (below)
@@ -1222,7 +1233,10 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                     rec = true;
                     c_dep++;
                     // all sources kept apart (srcid -1): one block of gates per source (2225-2227)
-                    const int sblk = (FULL && P.nextra && P.srcid < 0) ? (S.ssrc[tid] - 1) * P.maxgate : 0;
+                    // (in an all-detector replay a source's block holds one block per detector)
+                    const int sblk = (FULL && P.nextra && P.srcid < 0)
+                                         ? (S.ssrc[tid] - 1) * ((P.replay && P.replaydet == -1) ? P.detnum : 1) * P.maxgate
+                                         : 0;
                     const size_t addr = (size_t)idxold + (size_t)(tshift + sblk) * P.nvox;
                     // the index range of the tile box (empty without a tile) screens most deposits out
                     // with one compare before the box test

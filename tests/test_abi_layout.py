@@ -278,3 +278,19 @@ def test_photon_shares_over_devices(built):
     assert shares([1, 1], 7) == (2, [0, 3], [3, 4])          # one device listed twice
     rc, _, _ = shares([1, 2], 100, work=[1.0, 0.0])
     assert rc == -1 and b"workload" in lib.mcxg_last_error()
+
+
+@pytest.mark.parametrize("shape,dtype", [((7, 5, 3), np.uint8), ((130, 90, 100), np.uint8), ((4, 6, 8), np.int16)])
+def test_row_major_labels_transposed_by_preparation(engine, shape, dtype):
+    """A C-ordered label array goes to the engine as it lies, with MCX's isrowmajor flag: the
+    preparation (threaded, tiled above 2^20 voxels) leaves the same x-fastest words as the
+    Fortran-ordered copy of the same array, which takes the column-major path."""
+    rng = np.random.default_rng(sum(shape))
+    vol = rng.integers(0, 3, shape).astype(dtype)
+    base = {"nphoton": 10, "prop": [[0, 0, 1, 1], [0.01, 1, 0.9, 1.37], [0.02, 2, 0.8, 1.4]], "tstart": 0.0,
+            "tend": 1e-9, "tstep": 1e-9, "srcpos": [1.0, 1.0, 0.0], "srcdir": [0.0, 0.0, 1.0]}
+    a = engine.prepare(dict(base, vol=vol))
+    b = engine.prepare(dict(base, vol=np.asfortranarray(vol)))
+    assert a.c.isrowmajor == b"\x00" and tuple(a.dims) == shape
+    assert np.array_equal(a.vol, b.vol)
+    assert np.array_equal(a.vol[: vol.size], vol.ravel(order="F").astype(np.uint32))

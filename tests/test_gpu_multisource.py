@@ -53,3 +53,75 @@ def test_sources(engine):
     assert set(np.unique(src)) == {1, 2} and det.min() >= 1 and det.max() <= 4
     second = engine.run(_deck(n, srcpos=POS, srcdir=DIR, srcid=2))["flux"][..., 0]
     _check(second, singles[1], "srcid 2")
+
+
+# -- replay of a several-source run (src/mcx_core.cu:1203-1231) -----------------------------------
+def _ms_replay_deck(base, keep=None, **kw):
+    cfg = _deck(1, srcpos=POS, srcdir=DIR, savedetflag="dsp")
+    keep = np.ones(base["detp"].shape[1], bool) if keep is None else keep
+    cfg.update(seed=base["seeds"][:, keep], detphotons=base["detp"][:, keep], outputtype="j", isnormalized=0)
+    cfg.update(kw)
+    return cfg
+
+
+@pytest.fixture(scope="module")
+def msbase(engine):
+    r = engine.run(_deck(1_000_000, srcpos=POS, srcdir=DIR, srcid=0, issaveseed=1, savedetflag="dsp", seed=4242))
+    src = r["detp"][0].astype(np.int64) >> 16
+    assert set(np.unique(src)) == {1, 2}
+    return r
+
+
+def _records(detp, mask_source=False):
+    d = detp.copy()
+    if mask_source:
+        d[0] = (d[0].astype(np.int64) & 0xFFFF).astype(np.float32)
+    return set(map(tuple, d.T.tolist()))
+
+
+def test_replay_draws_the_recorded_source(engine, msbase):
+    """srcid 0: a replayed photon draws its source from its restored generator state, as the
+    recorded run did, so it follows the recorded path and is detected again with its record."""
+    r = engine.run(_ms_replay_deck(msbase, srcid=0))
+    n = r["stat"]["nphoton"]
+    assert n > 0.99 * msbase["detp"].shape[1] and r["stat"]["detected"] == n
+    assert _records(r["detp"]) <= _records(msbase["detp"])
+
+
+def test_replay_of_one_source_skips_the_source_draw(engine, msbase):
+    """srcid 2: the photons the recorded run launched from source 2, replayed from source 2 alone,
+    skip the draw that picked their source (src/mcx_core.cu:1229-1231) and are detected again."""
+    mine = (msbase["detp"][0].astype(np.int64) >> 16) == 2
+    r = engine.run(_ms_replay_deck(msbase, keep=mine, srcid=2))
+    n = r["stat"]["nphoton"]
+    assert n > 0.99 * mine.sum() and r["stat"]["detected"] == n
+    assert _records(r["detp"]) <= _records(msbase["detp"][:, mine], mask_source=True)
+
+
+def test_replay_every_source_and_detector_apart(engine, msbase):
+    """srcid -1 with replaydet -1: one block per (source, detector), sources outermost; each block
+    holds the Jacobian of that source's photons detected by that detector.  Normalised, MCX scales
+    the first source's detector blocks by their replayed weight and leaves the others as summed
+    (src/mcx_core.cu:3845-3873)."""
+    r = engine.run(_ms_replay_deck(msbase, srcid=-1, replaydet=-1))
+    assert r["flux"].shape[-1] == 8
+    # every replayed photon detected again: its record carries its source and detector
+    prop = np.asarray(_deck(1)["prop"], np.float32)
+    M = prop.shape[0] - 1
+    det = r["detp"]
+    assert r["stat"]["detected"] == r["stat"]["nphoton"]
+    ids = det[0].astype(np.int64)
+    ppath = det[1 + M:1 + 2 * M].astype(np.float64)
+    w = np.exp(-(prop[1:, 0:1].astype(np.float64) * ppath).sum(axis=0))
+    raw = {}
+    for s in (1, 2):
+        for d in range(1, 5):
+            sel = ((ids >> 16) == s) & ((ids & 0xFFFF) == d)
+            blk = r["flux"][..., (s - 1) * 4 + d - 1].astype(np.float64)
+            raw[s, d] = blk
+            np.testing.assert_allclose(blk.sum(), (ppath[:, sel] * w[sel]).sum(), rtol=2e-5, atol=1e-9)
+    n = engine.run(_ms_replay_deck(msbase, srcid=-1, replaydet=-1, isnormalized=1))["flux"]
+    for d in range(1, 5):
+        wsum = w[(ids & 0xFFFF) == d].sum()          # the replayed weight of detector d
+        np.testing.assert_allclose(n[..., d - 1].astype(np.float64).sum(), raw[1, d].sum() / wsum, rtol=2e-5)
+        np.testing.assert_allclose(n[..., 4 + d - 1].astype(np.float64).sum(), raw[2, d].sum(), rtol=2e-5)
