@@ -12,6 +12,7 @@ exactly as pmcx drives MCX's own core.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Any
 
 import numpy as np
@@ -545,7 +546,15 @@ def run_batch(cfgs: list[dict[str, Any]], streams: int = 4, device_fields: list 
     field), of the simulation's field size (nx * ny * nz * gates); the normalised fluence is
     stored there on the device (``mcxg_run_batch_device``) and the result has no ``flux``.  Each
     such simulation runs one repetition of one gate group."""
-    pcs = [prepare(cfg) for cfg in cfgs]
+    if len(cfgs) > 1:
+        # the preparations are independent and spend their time in numpy copies and the engine's
+        # host preparation, both of which run without the interpreter lock
+        from concurrent.futures import ThreadPoolExecutor
+
+        with ThreadPoolExecutor(max_workers=min(8, len(cfgs), os.cpu_count() or 1)) as ex:
+            pcs = list(ex.map(prepare, cfgs))
+    else:
+        pcs = [prepare(cfg) for cfg in cfgs]
     for pc in pcs:
         nact, info = _active_devices(pc.c)
         if info:

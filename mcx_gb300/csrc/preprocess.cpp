@@ -443,8 +443,9 @@ void validate(Config* cfg) {
     // mediabyte 96, 98 and 99 MCX keeps the flags and indexes the slots by the voxel word, past the
     // end of the record, so the engine clears them for every non-label format
     if (cfg->mediabyte > 4 && cfg->savedetflag) cfg->savedetflag &= ~(0x2u | 0x4u | 0x8u | 0x80u);
-    // diffuse reflectance (src/mcx_utils.c:3757-3759, 1808-1818): needs the field; mode 2 (the exit
-    // path per voxel in the detected buffer) is not built
+    // diffuse reflectance (src/mcx_utils.c:3757-3759, 1808-1818): needs the field; mode 2 keeps one
+    // detected record per void voxel with the exit weight and the weighted partial paths summed
+    // there (saveexitppath, src/mcx_core.cu:272-285)
     if (!cfg->issave2pt) cfg->issaveref = 0;
     if (cfg->issaveref > 1) {          // exit weight and paths per void voxel in the detected buffer
         if (!cfg->issavedet) MCXG_RAISE(-4, "you must have at least two outputs if issaveref is greater than 1");
