@@ -1499,6 +1499,14 @@ void run_simulation(Config* cfg, GPUInfo* gpu, bool fp64_field) {
 // Config's outputs are those of mcx_run_simulation; `runtime` is the batch's graph time.
 constexpr int kMinBatchCTAs = 16;
 
+// Oversubscription of the batched grids (CTAs requested over a full grid, summed over the streams
+// of a wave): 2 unless MCXG_BATCH_OVERSUB (1-16) says otherwise.
+double batch_oversubscription() {
+    const char* e = std::getenv("MCXG_BATCH_OVERSUB");
+    const double v = e ? std::atof(e) : 2.0;
+    return (v >= 1.0 && v <= 16.0) ? v : 2.0;
+}
+
 void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double* graph_ms, float* const* dev_fields = nullptr) {
     if (count <= 0 || !cfgs) MCXG_RAISE(-4, "an empty batch");
     nstreams = std::max(1, std::min(nstreams, 32));
@@ -1580,8 +1588,8 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
                 if (S[i]->kp.seed_mode == 1) S[i]->mcx_seed_words((uint64_t)(uint32_t)cfg->seed);
             }
             for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
-            // CTAs of each launch: its stream's share of the wave's photons, times two, of a full
-            // grid.  A launch whose photons are fewer than its threads holds every CTA until the
+            // CTAs of each launch: its stream's share of the wave's photons, times the
+            // oversubscription (two by default), of a full grid.  A launch whose photons are fewer than its threads holds every CTA until the
             // longest photon of that CTA ends, so full grids would run such simulations one after
             // the other, each at its latency; shared out, the launches of all streams are resident
             // together and the oversubscribed CTAs take the SMs that early finishers free.
@@ -1596,9 +1604,10 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
             }
             double wave_load = 0.0;
             for (double l : load) wave_load += l;
+            const double over = batch_oversubscription();
             for (int i = 0; i < count; i++) {
                 if (stream_of[i] < 0) continue;
-                const double share = wave_load > 0.0 ? 2.0 * load[stream_of[i]] / wave_load : 1.0;
+                const double share = wave_load > 0.0 ? over * load[stream_of[i]] / wave_load : 1.0;
                 const int full = full_grid[i];
                 S[i]->grid = std::max(std::min(full, kMinBatchCTAs), std::min(full, (int)std::ceil(full * share)));
             }

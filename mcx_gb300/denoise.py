@@ -365,7 +365,7 @@ def simulate(cfgs: list[dict[str, Any]], chunk: int = 96) -> list[np.ndarray]:
 
     out = []
     for i in range(0, len(cfgs), chunk):
-        res, _ = run_batch(cfgs[i:i + chunk])
+        res, _ = run_batch(cfgs[i:i + chunk], streams=16)
         out += [_flat(r["flux"]) for r in res]
     return out
 
