@@ -162,7 +162,9 @@ def test_cli_jdat_matches_the_python_writer(cli, tmp_path, engine):
 
     run(cli, ["--bench", "cube60b", "-n", "1e5", "-E", "1234", "-s", "jd", "-q", "1", "-S", "0"], tmp_path)
     info_c, rec_c, seed_c = mch.load_jdet(tmp_path / "jd_detp.jdat")
-    cfg = problems.cube60b(1e5) | {"seed": 1234, "issaveseed": 1}
+    # -S 0 on the CLI: no field, so no normalisation and the header's normaliser stays 1, as MCX
+    # leaves it (src/mcx_core.cu:3823)
+    cfg = problems.cube60b(1e5) | {"seed": 1234, "issaveseed": 1, "issave2pt": 0}
     pc = engine.prepare(cfg)
     res = engine.run_prepared(pc)
     info_p, rec_p, seed_p = mch.load_jdet(mch.save_jdet(tmp_path / "py_detp.jdat", pc, res))
