@@ -1589,10 +1589,11 @@ void run_batch(Config** cfgs, int count, int nstreams, mcxg_stats* stats, double
             }
             for (auto& s : S) CK(cudaStreamSynchronize(s->stream));
             // CTAs of each launch: its stream's share of the wave's photons, times the
-            // oversubscription (two by default), of a full grid.  A launch whose photons are fewer than its threads holds every CTA until the
-            // longest photon of that CTA ends, so full grids would run such simulations one after
-            // the other, each at its latency; shared out, the launches of all streams are resident
-            // together and the oversubscribed CTAs take the SMs that early finishers free.
+            // oversubscription (two by default), of a full grid.  A launch whose photons are fewer
+            // than its threads holds every CTA until the longest photon of that CTA ends, so full
+            // grids would run such simulations one after the other, each at its latency; shared
+            // out, the launches of all streams are resident together and the oversubscribed CTAs
+            // take the SMs that early finishers free.
             std::vector<int> stream_of(count, -1);
             std::vector<double> load(nstreams, 0.0);
             int slot = 0;
