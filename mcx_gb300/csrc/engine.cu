@@ -1249,7 +1249,8 @@ void end_outputs(Config* cfg, Session& S, double kernel_ms, int reps, int thread
     }
     // file output in the standalone CLI (src/mcx_core.cu:3932-3978) when its writers are linked
     if (cfg->parentid == mpStandalone) {
-        if (cfg->issave2pt && mcx_savedata) mcx_savedata(cfg->exportfield, S.fieldlen, cfg);
+        // (no host field when mcxg_run_batch_device kept it on the device)
+        if (cfg->issave2pt && cfg->exportfield && mcx_savedata) mcx_savedata(cfg->exportfield, S.fieldlen, cfg);
         if (cfg->issavedet && cfg->exportdetected && mcx_savedetphoton) {
             cfg->his.unitinmm = cfg->unitinmm;
             cfg->his.savedphoton = (unsigned)cfg->detectedcount;
