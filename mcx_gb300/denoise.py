@@ -341,6 +341,41 @@ class UNet:
         torch.pow(10.0, logf, out=out)
         return torch.clamp_(out.sub_(FLUX_FLOOR), min=0.0)
 
+    def denoise_many_device(self, flux: torch.Tensor, vols: list[np.ndarray], props: list[np.ndarray],
+                            nphotons: list[float], out: torch.Tensor | None = None) -> torch.Tensor:
+        """`denoise_device` on several volumes of one shape in one pass of the network: `flux`
+        [n, voxels] fp32 on the device (x fastest per row), returns [n, voxels] (in `out` when
+        given).  Each volume's result is the one `denoise_device` gives it: every kernel works per
+        output voxel, so batching changes only how many CTAs a layer has -- the 16^3 and 32^3
+        levels of one 128^3 volume fill a fraction of the SMs, n of them fill the GPU."""
+        n = len(vols)
+        shape = np.asarray(vols[0]).shape[:3]
+        if any(np.asarray(v).shape[:3] != shape for v in vols) or flux.shape[0] != n:
+            raise ValueError("denoise_many_device needs n volumes of one shape and an [n, voxels] flux")
+        nx, ny, nz = shape
+        vox = nx * ny * nz
+        vs = [np.asarray(v) for v in vols]
+        if all(v.flags.c_contiguous for v in vs):
+            lab = torch.from_numpy(np.stack([v.astype(np.uint8, copy=False) for v in vs])).to(self.dev)
+            lab = lab.permute(0, 3, 2, 1).contiguous().view(n, vox)
+        else:
+            lab = torch.cat([self.labels_device(v) for v in vs])
+        nprop = max(np.asarray(p).reshape(-1, 4).shape[0] for p in props)
+        pr = np.zeros((n, nprop, 4), np.float32)
+        for i, p in enumerate(props):
+            p = np.asarray(p, np.float32).reshape(-1, 4)
+            pr[i, :p.shape[0]] = p
+            pr[i, p.shape[0]:] = p[-1]             # rows no label of this volume reads
+        pr = torch.from_numpy(pr).to(self.dev)
+        lp = torch.tensor([math.log10(x) for x in nphotons], dtype=torch.float32, device=self.dev)
+        x0, xres = self.pack(flux.reshape(n, vox), lab, pr, lp, nz, ny, nx)
+        logf = self._buf("out", n * vox, torch.float32)
+        self.forward(x0, xres, n, nz, ny, nx, out=logf)
+        if out is None:
+            out = torch.empty(n, vox, dtype=torch.float32, device=self.dev)
+        torch.pow(10.0, logf.view(n, vox), out=out)
+        return torch.clamp_(out.sub_(FLUX_FLOOR), min=0.0)
+
 
 # -- data -------------------------------------------------------------------------------------
 def median_rel_error(est: np.ndarray, ref: np.ndarray, frac: float = VALID_FRAC) -> float:
@@ -586,29 +621,49 @@ def pipeline_maps(cfgs: list[dict[str, Any]], budgets: list[float], seeds: list[
                   denoise: list[bool] | None = None, streams: int = 16) -> tuple[list[np.ndarray], float, float]:
     """One pass of the pipeline over many volumes, from host inputs to host maps: one batched MC
     call whose fluence maps stay on the device (``run_batch(..., device_fields=...)``), the network
-    on the volumes flagged in `denoise` (``UNet.denoise_device``, stream-ordered), and one copy of
-    every final map into pinned host memory.  Returns (maps, flat fp32 x fastest; MC graph time
+    on the volumes flagged in `denoise` (one batched pass, ``UNet.denoise_many_device``, when the
+    volumes share a shape), and one copy of every final map into pinned host memory.  Returns (maps, flat fp32 x fastest; MC graph time
     in s; network GPU time in s)."""
     from .api import run_batch
 
     V = len(cfgs)
     denoise = denoise or [False] * V
-    fields = [torch.empty(int(np.asarray(c["vol"]).size), dtype=torch.float32, device="cuda") for c in cfgs]
+    sizes = [int(np.asarray(c["vol"]).size) for c in cfgs]
+    same = len(set(sizes)) == 1
+    if same:
+        # one [V, voxels] block: its rows are the fields, the network takes them as one batch
+        block = torch.empty(V, sizes[0], dtype=torch.float32, device="cuda")
+        fields = list(block)
+    else:
+        fields = [torch.empty(n, dtype=torch.float32, device="cuda") for n in sizes]
     _, ms = run_batch([dict(c, nphoton=int(n), seed=k) for c, n, k in zip(cfgs, budgets, seeds)], streams=streams,
                       device_fields=fields)
     host = [torch.empty(f.numel(), dtype=torch.float32, pin_memory=True) for f in fields]
-    # the network's GPU time: events around each volume's pack + network + exponent only
+    # the network's GPU time: events around the pack + network + exponent only
     evs = []
-    for v, c in enumerate(cfgs):
-        f = fields[v]
-        if denoise[v]:
+    sel = [v for v in range(V) if denoise[v]]
+    if sel and same:
+        idx = torch.tensor(sel, device="cuda")
+        sub = block if len(sel) == V else block.index_select(0, idx)
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev[0].record()
+        res = net.denoise_many_device(sub, [cfgs[v]["vol"] for v in sel], [cfgs[v]["prop"] for v in sel],
+                                      [budgets[v] for v in sel], out=sub if len(sel) == V else None)
+        ev[1].record()
+        evs.append(ev)
+        if len(sel) != V:
+            block.index_copy_(0, idx, res)
+    elif sel:
+        for v in sel:
+            c = cfgs[v]
             lab = net.labels_device(c["vol"])
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record()
-            f = net.denoise_device(f, c["vol"], c["prop"], budgets[v], out=f, labels=lab)
+            net.denoise_device(fields[v], c["vol"], c["prop"], budgets[v], out=fields[v], labels=lab)
             ev[1].record()
             evs.append(ev)
-        host[v].copy_(f, non_blocking=True)
+    for f, h in zip(fields, host):
+        h.copy_(f, non_blocking=True)
     torch.cuda.synchronize()
     net_s = sum(a.elapsed_time(b) for a, b in evs) * 1e-3
     return [h.numpy() for h in host], ms * 1e-3, net_s

@@ -384,3 +384,25 @@ def test_denoise_on_the_device_equals_the_host_call():
     torch.cuda.synchronize()
     for o, w, c in zip(outs, want, cfgs):
         assert np.array_equal(o.cpu().numpy(), w.ravel(order="F"))
+
+
+def test_denoise_many_volumes_in_one_pass_equals_one_at_a_time():
+    """UNet.denoise_many_device (the volumes of one shape as one batch through every kernel) gives
+    each volume exactly what denoise_device gives it alone; media tables of different lengths are
+    padded with rows no label reads."""
+    import torch
+
+    from mcx_gb300 import denoise as dn
+    from mcx_gb300 import problems
+
+    net = dn.UNet(seed=4)
+    cfgs = problems.denoise_instances(3, 32, seed=21)
+    rng = np.random.default_rng(2)
+    block = torch.from_numpy(rng.random((3, 32 ** 3)).astype(np.float32)).cuda()
+    budgets = [1e5, 3e5, 1e6]
+    alone = [net.denoise_device(block[i].clone(), c["vol"], c["prop"], n).cpu().numpy()
+             for i, (c, n) in enumerate(zip(cfgs, budgets))]
+    many = net.denoise_many_device(block.clone(), [c["vol"] for c in cfgs], [c["prop"] for c in cfgs], budgets)
+    torch.cuda.synchronize()
+    for i in range(3):
+        assert np.array_equal(many[i].cpu().numpy(), alone[i]), i
