@@ -155,8 +155,9 @@ void mcxg_run_simulation_fp64(Config* cfg, GPUInfo* gpu);
  * Runs `count` prepared Configs (each after mcxg_validatecfg or mcx_validatecfg) on the device of
  * cfgs[0]->deviceid[0], as one CUDA graph of their transport launches over `nstreams` streams
  * (1..32), largest photon budget first, each launch's grid sized by its stream's share of the
- * photons (times MCXG_BATCH_OVERSUB, default 2) so that the launches of all streams run side by
- * side and the block scheduler fills the SMs a finishing launch frees.  Every Config receives exactly the outputs
+ * photons (times an oversubscription of 1 or 2, or MCXG_BATCH_OVERSUB when set) so that the
+ * launches of all streams run side by side and the block scheduler fills the SMs a finishing
+ * launch frees.  Every Config receives exactly the outputs
  * mcx_run_simulation gives it (exportfield accumulated, exportdetected, energies, normaliser,
  * detected count); its `runtime` is the whole batch's graph time.  Repetitions (respin) and gate
  * groups run in waves, one graph per wave holding every Config's next (group, repetition).
