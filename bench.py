@@ -356,7 +356,9 @@ def denoise_main(args, world, rank) -> None:
     # one fp32 map per volume down
     h2d = sum(c["vol"].size * 4 + 2 * np.asarray(c["prop"]).nbytes + c["vol"].size for c in cfgs)
     d2h = sum(4 * c["vol"].size for c in cfgs)
-    launches = V + 22 * sum(t5["denoised"])
+    # the timed 5% pass: per volume the label packing, transport and merge kernels; one batched
+    # network pass (pack, 14 convolutions, pools, upsampling, head) over the denoised volumes
+    launches = 3 * V + (22 if any(t5["denoised"]) else 0)
     rnd = lambda x: [round(v, 5) for v in x] if isinstance(x, list) else x  # noqa: E731
     line = {
         "metric": DN_METRIC, "value": t5["t_denoised_device_s"], "unit": "s", "n_gpus": 1, "steps": args.steps,
