@@ -305,7 +305,7 @@ def denoise_main(args, world, rank) -> None:
     `--judge-photons` run (mcx_gb300.denoise.time_to_error_batch).  value = device time of MC +
     denoiser over all volumes (the batched transport graph + the network); e2e = wall time of the
     same pipeline through the public calls (mcx_gb300.denoise.pipeline_maps: run_batch with the
-    fields kept on the device, UNet.denoise_device, one pinned copy back per volume) from host
+    fields kept on the device, UNet.denoise_many_device, one pinned copy back per volume) from host
     inputs to host maps; plain MC runs through the same pipeline without the network, and its
     times and the speed-ups ride along.  One step = one volume; warm-up = full denoise pipelines
     at 1e5 photons on the first volume."""

@@ -15,9 +15,11 @@ the fused head + masked-L1 loss, and AdamW on fp32 master weights.  PyTorch only
 memory and the stream.  Training pairs come from the engine itself (``make_pairs``): the same
 volume simulated at 1e5 / 1e6 photons (inputs) and at a high photon count (target).
 
-The MC stays the judge: ``time_to_error`` reports how long plain MC needs to reach a given median
-relative fluence error against a high-photon run, and how long MC + denoiser needs, with plain MC
-as the fallback wherever the denoised map does not reach it.
+The MC stays the judge: ``time_to_error_batch`` reports how long plain MC needs to reach a given
+median relative fluence error against a high-photon run, and how long MC + denoiser needs, with
+plain MC as the fallback wherever the denoised map does not reach it; both run through
+``pipeline_maps`` (the batched MC with its fields kept on the device, the network on the device,
+one copy of every final map to the host).
 """
 
 from __future__ import annotations
@@ -528,95 +530,6 @@ def evaluate_loss(net: UNet, data: dict[str, Any], batch: int = 4) -> list[float
 
 
 # -- the metric -------------------------------------------------------------------------------
-def _time_at(plain: list[dict], target: float) -> tuple[float, float, float]:
-    """(photons, wall s, device s) plain MC needs for a median error of `target`: photons by
-    log-log interpolation between the bracketing budgets of the ladder (the 1/sqrt(N) law past
-    the last one), times interpolated linearly in photons between the same budgets -- so plain MC
-    pays the per-call costs and long-photon latency its measured runs paid -- and extrapolated at
-    the last segment's rate."""
-    n_star, seg = None, None
-    for a, b in zip(plain, plain[1:]):
-        if a["error"] > target >= b["error"]:
-            slope = math.log(b["error"] / a["error"]) / math.log(b["photons"] / a["photons"])
-            n_star, seg = a["photons"] * (target / a["error"]) ** (1.0 / slope), (a, b)
-            break
-    if n_star is None:
-        last = plain[-1]
-        if last["error"] > target:
-            n_star, seg = last["photons"] * (last["error"] / target) ** 2, (plain[-2], plain[-1])
-        else:
-            n_star, seg = plain[0]["photons"], (plain[0], plain[1])
-
-    def at(key):
-        a, b = seg
-        return max(plain[0][key], a[key] + (n_star - a["photons"]) * (b[key] - a[key]) / (b["photons"] - a["photons"]))
-
-    return n_star, at("s"), at("kernel_s")
-
-
-def time_to_error(net: UNet, cfg: dict[str, Any], judge_photons: float = 1e9, targets: tuple[float, ...] = (0.05, 0.02),
-                  ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7, 3e7, 1e8),
-                  dn_ladder: tuple[float, ...] = (1e5, 3e5, 1e6, 3e6, 1e7), judge_check: bool = True) -> dict[str, Any]:
-    """Time to reach a median relative fluence error of each of `targets` against a
-    `judge_photons` run, for plain MC and for MC + denoiser, on one volume.
-
-    Plain MC runs each budget of `ladder` end to end through the engine's API and is priced by
-    ``_time_at``, on the device (transport kernel time) and end to end (wall time of the calls).
-    MC + denoiser takes the smallest budget of `dn_ladder` whose denoised map reaches the target:
-    on the device its transport time plus the network's, end to end the wall time of the
-    simulation call plus upload, network and download.  Where no budget reaches a target, plain
-    MC is the fallback and its times are the pipeline's.  With `judge_check`, a second,
-    independent run of a quarter of the judge's photons estimates the judge's own median error
-    (their difference has sqrt(5) times the judge's standard error).  The first target's figures
-    are also returned at the top level."""
-    from .api import run
-
-    t0 = time.perf_counter()
-    judge = _flat(run(dict(cfg, nphoton=judge_photons, seed=int(cfg["seed"]) + 1))["flux"])
-    judge_s = time.perf_counter() - t0
-    judge_err = None
-    if judge_check:
-        j4 = _flat(run(dict(cfg, nphoton=judge_photons / 4, seed=int(cfg["seed"]) + 99))["flux"])
-        judge_err = median_rel_error(j4, judge) / math.sqrt(5.0)
-    plain = []
-    for n in ladder:
-        t0 = time.perf_counter()
-        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 2 + int(math.log10(n) * 10)))
-        dt = time.perf_counter() - t0
-        plain.append({"photons": n, "error": median_rel_error(_flat(r["flux"]), judge), "s": dt,
-                      "kernel_s": r["stat"]["kernel_ms"] * 1e-3})
-    vol, prop = cfg["vol"], cfg["prop"]
-    net.denoise(np.ones(vol.shape, np.float32), vol, prop, 1e5)       # buffers for this grid
-    torch.cuda.synchronize()
-    dn = []
-    for n in dn_ladder:
-        t0 = time.perf_counter()
-        r = run(dict(cfg, nphoton=n, seed=int(cfg["seed"]) + 100 + int(math.log10(n) * 10)))
-        d = net.denoise(r["flux"], vol, prop, n)
-        dt = time.perf_counter() - t0
-        dn.append({"photons": n, "error": median_rel_error(_flat(d), judge),
-                   "error_plain": median_rel_error(_flat(r["flux"]), judge), "s": dt,
-                   "kernel_s": r["stat"]["kernel_ms"] * 1e-3, "network_s": net.last_gpu_ms * 1e-3})
-    per = []
-    for tgt in targets:
-        n_plain, t_wall, t_dev = _time_at(plain, tgt)
-        chosen = next((rec for rec in dn if rec["error"] <= tgt), None)
-        rec = {"target": tgt, "photons_plain": n_plain, "t_plain_s": t_wall, "t_plain_device_s": t_dev,
-               "fallback": chosen is None}
-        if chosen is None:
-            rec.update(photons_denoised=n_plain, t_denoised_s=t_wall, t_denoised_device_s=t_dev)
-        else:
-            rec.update(photons_denoised=chosen["photons"], t_denoised_s=chosen["s"],
-                       t_denoised_device_s=chosen["kernel_s"] + chosen["network_s"])
-        rec["speedup"] = rec["t_plain_s"] / rec["t_denoised_s"]
-        rec["speedup_device"] = rec["t_plain_device_s"] / rec["t_denoised_device_s"]
-        per.append(rec)
-    out = {"plain": plain, "denoised": dn, "targets": per, "judge_photons": judge_photons, "judge_s": judge_s,
-           "judge_error_est": judge_err}
-    out.update({k: v for k, v in per[0].items() if k != "target"})
-    return out
-
-
 def pipeline_maps(cfgs: list[dict[str, Any]], budgets: list[float], seeds: list[int], net: UNet | None = None,
                   denoise: list[bool] | None = None, streams: int = 16) -> tuple[list[np.ndarray], float, float]:
     """One pass of the pipeline over many volumes, from host inputs to host maps: one batched MC
