@@ -294,3 +294,20 @@ def test_row_major_labels_transposed_by_preparation(engine, shape, dtype):
     assert a.c.isrowmajor == b"\x00" and tuple(a.dims) == shape
     assert np.array_equal(a.vol, b.vol)
     assert np.array_equal(a.vol[: vol.size], vol.ravel(order="F").astype(np.uint32))
+
+
+def test_batch_entry_points_refuse_bad_calls_before_any_device_work(engine):
+    """mcxg_run_batch / mcxg_run_batch_device check their arguments on the host first: an empty
+    batch and a missing device-field array come back as MCX error -4 with a message."""
+    import ctypes as C
+
+    from mcx_gb300 import abi
+    from mcx_gb300._lib import lib
+
+    arr = (C.POINTER(abi.Config) * 1)()
+    stats = (abi.Stats * 1)()
+    ms = C.c_double(0.0)
+    assert lib.mcxg_run_batch(arr, 0, 4, stats, C.byref(ms)) == -4
+    assert b"empty batch" in lib.mcxg_last_error()
+    assert lib.mcxg_run_batch_device(arr, 1, 4, None, stats, C.byref(ms)) == -4
+    assert b"no device fields" in lib.mcxg_last_error()
