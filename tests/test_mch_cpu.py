@@ -176,3 +176,20 @@ def test_jdat_trajectory(engine, tmp_path):
     assert doc["Info"]["ColumnNum"] == 6 and doc["Info"]["DetectedPhoton"] == 5 and doc["Info"]["SavedPhoton"] == 5
     info, d, s = mch.load_jdet(f)
     assert np.array_equal(d, traj) and s is None
+
+
+def test_jdata_decode_orders_and_types():
+    """JData arrays as MCX's writers emit them: row-major by default, "_ArrayOrder_": "c" for
+    column-major volumes (src/mcx_utils.c:4573-4575, 4594-4596), uint8 to double payloads."""
+    import base64
+    import zlib
+
+    from mcx_gb300 import mch
+
+    a = np.arange(24, dtype=np.float64).reshape(2, 3, 4)
+    col = {"_ArrayType_": "double", "_ArraySize_": [2, 3, 4], "_ArrayOrder_": "c", "_ArrayZipType_": "zlib",
+           "_ArrayZipSize_": 24, "_ArrayZipData_": base64.b64encode(zlib.compress(a.tobytes(order="F"))).decode()}
+    assert np.array_equal(mch.jdata_decode(col), a)
+    for jt, dt in (("uint8", np.uint8), ("int16", np.int16), ("uint32", np.uint32), ("single", np.float32)):
+        v = (np.arange(6) * 3).astype(dt).reshape(2, 3)
+        assert np.array_equal(mch.jdata_decode(mch.jdata_encode(v, jt)), v)
