@@ -1122,15 +1122,19 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
         float len = stay ? __fdividef(pscat, musp) : dist;
         bool hit = false;                                   // split voxel: the flight stops on its plane
         if constexpr (SVMC) {
-            // ray_plane_intersect (src/mcx_core.cu:747-772)
+            // ray_plane_intersect (src/mcx_core.cu:747-772) in MCX's arithmetic, so that the same
+            // photons take the same decisions: the flight length as the loop recomputes it from
+            // the scattering length (2109), the signed distances of both ends, len x d0 / (d0 - d1)
             const float vn = vx * sv.nx + vy * sv.ny + vz * sv.nz;
             if (sv.split && sv_test && vn > 0.f) {
+                const float lm = (pr.y == 0.f) ? len : slen / musp;
+                const float qx = fmaf(lm, vx, px), qy = fmaf(lm, vy, py), qz = fmaf(lm, vz, pz);
                 const float d0 = (px - sv.rx) * sv.nx + (py - sv.ry) * sv.ny + (pz - sv.rz) * sv.nz;
-                const float d1 = d0 + len * vn;
-                if (d0 * d1 <= 0.f) {
-                    const float l0 = len * __fdividef(d0, d0 - d1);
-                    if (l0 > 0.f) len = l0;
-                    slen = len * musp;
+                const float d1 = (qx - sv.rx) * sv.nx + (qy - sv.ry) * sv.ny + (qz - sv.rz) * sv.nz;
+                if (!(d0 * d1 > 0.f)) {
+                    const float l0 = lm * d0 / (d0 - d1);
+                    len = (l0 > 0.f) ? l0 : lm;
+                    slen = len * pr.y * ((nscat >= gscat) ? (1.f - pr.z) : 1.f);
                     hit = true;
                 }
             }
@@ -1330,25 +1334,26 @@ __global__ void __launch_bounds__(256, MINB) transport_kernel(const __grid_const
                 if (nlo != nup) {
                     sv.nx = -sv.nx; sv.ny = -sv.ny; sv.nz = -sv.nz;
                     const float n2 = S.prop[sv.tissue()].w;           // the tissue entered
+                    // (in reflectray's arithmetic: the second term uses the square of the root)
                     const float ic = fabsf(vx * sv.nx + vy * sv.ny + vz * sv.nz);
                     const float a2 = n1 * n1, b2 = n2 * n2;
-                    const float c2 = 1.f - __fdividef(a2, b2) * (1.f - ic * ic);
+                    const float c2 = 1.f - a2 / b2 * (1.f - ic * ic);
                     bool refl = true;
                     float ct = 0.f;
                     if (c2 > 0.f) {
-                        ct = sqrtf(c2);
                         float re = a2 * ic * ic + b2 * c2;
+                        ct = sqrtf(c2);
                         const float im = 2.f * n1 * n2 * ic * ct;
-                        float R = __fdividef(re - im, re + im);
-                        re = b2 * ic * ic + a2 * c2;
-                        R = (R + __fdividef(re - im, re + im)) * 0.5f;
+                        float R = (re - im) / (re + im);
+                        re = b2 * ic * ic + a2 * ct * ct;
+                        R = (R + (re - im) / (re + im)) * 0.5f;
                         refl = rng_next(r0, r1) <= R;
                     }
                     if (refl) {                     // back into the tissue it came from
                         vx -= 2.f * ic * sv.nx; vy -= 2.f * ic * sv.ny; vz -= 2.f * ic * sv.nz;
                         sv.isup = !sv.isup;
                     } else {                        // refracted into the other tissue
-                        const float q = __fdividef(n1, n2);
+                        const float q = n1 / n2;
                         vx = ct * sv.nx + q * (vx - ic * sv.nx);
                         vy = ct * sv.ny + q * (vy - ic * sv.ny);
                         vz = ct * sv.nz + q * (vz - ic * sv.nz);
