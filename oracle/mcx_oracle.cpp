@@ -140,6 +140,41 @@ struct Ctx {
                 r1.g, n};
     }
 
+    // MEDIA_2LABEL_SPLIT (src/mcx_core.cu:688-730): the voxel's first word holds [lower][upper]
+    // [point x][point y], its second (after all first words) [point z][normal x][normal y]
+    // [normal z], bytes over 0..1 of the voxel and -1..1 of the normal (mcx_preprocess's layout,
+    // src/mcx_utils.c:1708-1731).  Sets the photon's split-voxel state for its voxel and position
+    // and returns the properties of the tissue it is in; outside the volume row 0, state kept.
+    template <class PH>
+    Prop svmc_prop(PH& ph) const {
+        if (ph.idx1d == 0xFFFFFFFFu || ph.idx1d == 0x7FFFFFFFu) return prop[0];
+        const uint32_t w1 = P->vol[ph.idx1d] & 0x7FFFFFFFu, w0 = P->vol[(size_t)dimxyz + ph.idx1d];
+        ph.sv_lo = (int)(w1 >> 24);
+        ph.sv_up = (int)((w1 >> 16) & 0xFFu);
+        if (ph.sv_up) {
+            ph.rp[0] = ((w1 >> 8) & 0xFFu) * (1.f / 255.f) + ph.fd[0];
+            ph.rp[1] = (w1 & 0xFFu) * (1.f / 255.f) + ph.fd[1];
+            ph.rp[2] = (w0 >> 24) * (1.f / 255.f) + ph.fd[2];
+            float n[3] = {((w0 >> 16) & 0xFFu) * (2.f / 255.f) - 1, ((w0 >> 8) & 0xFFu) * (2.f / 255.f) - 1,
+                          (w0 & 0xFFu) * (2.f / 255.f) - 1};
+            const float inv = 1.f / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int i = 0; i < 3; i++) ph.nv[i] = n[i] * inv;
+            const float side = (ph.rp[0] - ph.p[0]) * ph.nv[0] + (ph.rp[1] - ph.p[1]) * ph.nv[1] +
+                               (ph.rp[2] - ph.p[2]) * ph.nv[2];
+            ph.sv_split = true;
+            if (side < 0.f) {            // the upper tissue; the normal always points to the other side
+                ph.sv_isup = true;
+                for (int i = 0; i < 3; i++) ph.nv[i] = -ph.nv[i];
+                return prop[ph.sv_up];
+            }
+            ph.sv_isup = false;
+            return prop[ph.sv_lo];
+        }
+        ph.sv_split = false;
+        ph.sv_isup = false;
+        return prop[ph.sv_lo];
+    }
+
     // MEDIA_2LABEL_MIX (src/mcx_core.cu:649-666): a word [15-bit fraction][label 1][label 0] is
     // label 1 with probability fraction / 32767, else label 0, drawn when the photon enters the
     // voxel; the detector bit is kept.  Other formats pass through.
@@ -250,6 +285,12 @@ struct Photon {
     int isdet;
     Prop prop;
     float ppath[3 * 128];          // nscat(M) | ppath(M) | mom(M), per medium label 1..M
+    // split voxel of the current position (MEDIA_2LABEL_SPLIT, src/mcx_core.cu:688-730): the two
+    // labels, the plane's point and its normal turned toward the other tissue, the side the photon
+    // is on, and whether the next flight tests the plane
+    int sv_lo, sv_up;
+    bool sv_split, sv_isup, testint;
+    float rp[3], nv[3];
 };
 
 // src/mcx_core.cu:866-956 (label media, no SVMC).  Returns the entry voxel or -1.
@@ -584,6 +625,10 @@ struct Runner {
         } while ((ph.mediaid & kMED_MASK) == 0 || std::fabs(ph.w) <= P->minenergy);
         ph.mediaid = C.pick(ph.mediaid, rng);
         ph.prop = C.prop_of(ph.mediaid & kMED_MASK, ph.idx1d);
+        if (P->mediaformat == 97) {      // the launch voxel's tissue (src/mcx_core.cu:1246-1251, 1679)
+            ph.prop = C.svmc_prop(ph);
+            ph.testint = true;
+        }
         T.e_launch += ph.w;
         T.launches++;
         ph.w0 = ph.w;
@@ -595,6 +640,47 @@ struct Runner {
         ph.mediaid &= kMED_MASK;
         if (P->savedet) std::memset(ph.ppath, 0, sizeof(float) * C.partialdata);
         return true;
+    }
+
+    // Reflection or refraction at a split voxel's plane (reflectray, src/mcx_core.cu:784-830); the
+    // normal points along the flight into the tissue entered.  True when the photon is refracted
+    // into the background tissue (label 0), where it ends.
+    bool reflectray(Photon& ph, float n1, Rng& rng) {
+        const float Icos = std::fabs(ph.v[0] * ph.nv[0] + ph.v[1] * ph.nv[1] + ph.v[2] * ph.nv[2]);
+        const float n2 = C.prop[ph.sv_isup ? ph.sv_up : ph.sv_lo].n;
+        const float tmp0 = n1 * n1, tmp1 = n2 * n2;
+        float tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+        if (tmp2 > 0.f) {
+            float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+            tmp2 = std::sqrt(tmp2);
+            const float Im = 2.f * n1 * n2 * Icos * tmp2;
+            float Rtotal = (Re - Im) / (Re + Im);
+            Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+            Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+            if (rng.next() <= Rtotal) {
+                for (int i = 0; i < 3; i++) ph.v[i] += -2.f * Icos * ph.nv[i];
+                ph.sv_isup = !ph.sv_isup;
+            } else {
+                const float q = n1 / n2;
+                for (int i = 0; i < 3; i++) {
+                    ph.v[i] += -Icos * ph.nv[i];
+                    ph.v[i] = tmp2 * ph.nv[i] + q * ph.v[i];
+                    ph.nv[i] = -ph.nv[i];
+                }
+                // MCX tests the flag itself on the upper side (a split voxel's upper label is never 0)
+                if ((ph.sv_isup ? 1 : ph.sv_lo) == 0) return true;
+                ph.prop = C.prop[ph.sv_isup ? ph.sv_up : ph.sv_lo];
+            }
+        } else {
+            for (int i = 0; i < 3; i++) ph.v[i] += -2.f * Icos * ph.nv[i];
+            ph.sv_isup = !ph.sv_isup;
+        }
+        const float inv = 1.f / std::sqrt(ph.v[0] * ph.v[0] + ph.v[1] * ph.v[1] + ph.v[2] * ph.v[2]);
+        for (int i = 0; i < 3; i++) {
+            ph.v[i] *= inv;
+            ph.rv[i] = 1.f / ph.v[i];
+        }
+        return false;
     }
 
     // One photon with its own per-photon stream.
@@ -618,6 +704,7 @@ struct Runner {
         const uint32_t M = C.medianum - 1;
         const float n0 = C.prop[0].n;
         const double maxsteps = 1e9;
+        const bool svmc = P->mediaformat == 97;
 
         for (double guard = 0; guard < maxsteps; guard += 1) {
             T.steps++;
@@ -652,7 +739,7 @@ struct Runner {
             }
 
             float n1 = ph.prop.n;
-            ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
+            if (!svmc) ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
 
             float len = hitgrid(ph.p, ph.v, ph.rv, ph.fd);
             float musp = ph.prop.mus * ((ph.nscat + 1.f > (float)P->gscatter) ? (1.f - ph.prop.g) : 1.f);
@@ -660,8 +747,27 @@ struct Runner {
             slen = std::fmin(slen, ph.pscat);
             len = (ph.prop.mus == 0.f) ? len : (slen / musp);
 
+            // the flight stops on a split voxel's plane (ray_plane_intersect, src/mcx_core.cu:747-772)
+            bool hit = false;
+            if (svmc && ph.sv_split && ph.testint) {
+                const float vn = ph.v[0] * ph.nv[0] + ph.v[1] * ph.nv[1] + ph.v[2] * ph.nv[2];
+                if (vn > 0.f) {
+                    float d0 = 0.f, d1 = 0.f;
+                    for (int i = 0; i < 3; i++) {
+                        d0 += (ph.p[i] - ph.rp[i]) * ph.nv[i];
+                        d1 += (ph.p[i] + len * ph.v[i] - ph.rp[i]) * ph.nv[i];
+                    }
+                    if (!(d0 * d1 > 0.f)) {
+                        const float len0 = len * d0 / (d0 - d1);
+                        len = (len0 > 0.f) ? len0 : len;
+                        slen = len * ph.prop.mus * ((ph.nscat + 1.f > (float)P->gscatter) ? (1.f - ph.prop.g) : 1.f);
+                        hit = true;
+                    }
+                }
+            }
+
             ph.p[0] += len * ph.v[0]; ph.p[1] += len * ph.v[1]; ph.p[2] += len * ph.v[2];
-            const bool stay = (slen == ph.pscat);
+            const bool stay = (slen == ph.pscat) || hit;
             if (ph.fd[3] == 0) ph.fd[0] += stay ? 0 : (ph.v[0] > 0.f ? 1 : -1);
             if (ph.fd[3] == 1) ph.fd[1] += stay ? 0 : (ph.v[1] > 0.f ? 1 : -1);
             if (ph.fd[3] == 2) ph.fd[2] += stay ? 0 : (ph.v[2] > 0.f ? 1 : -1);
@@ -687,7 +793,7 @@ struct Runner {
             }
             ph.isdet = (int)isdet;
 
-            if (ph.idx1d != idx1dold && mediaidold) {
+            if ((ph.idx1d != idx1dold || hit) && mediaidold) {
                 bool rec = false;
                 if (P->save2pt && ph.t >= C.twin0 && ph.t < C.twin1) {
                     int tshift = (int)std::floor((ph.t - C.twin0) * C.Rtstep);
@@ -713,9 +819,24 @@ struct Runner {
             const uint32_t med = ph.mediaid;
             const int bcf = (int)(isdet & 0xF);
 
-            // termination: exit to a 0 voxel without reflection, or beyond the time window
+            // split voxels: a new voxel's tissue at the new position; across the plane, the other
+            // tissue (src/mcx_core.cu:2295-2303)
+            if (svmc) {
+                if (ph.idx1d != idx1dold) {
+                    ph.prop = C.svmc_prop(ph);
+                    ph.testint = true;
+                } else if (hit) {
+                    for (int i = 0; i < 3; i++) ph.nv[i] = -ph.nv[i];
+                    ph.sv_isup = !ph.sv_isup;
+                    ph.testint = false;
+                }
+            }
+
+            // termination: exit to a 0 voxel without reflection, into a split voxel's background
+            // tissue without reflection, or beyond the time window
             if ((med == 0 && ((!C.isreflect || (C.isreflect && n1 == n0)) ||
                               ((bcf == BC_UNKNOWN && !P->isreflect) || bcf == BC_ABSORB || bcf == BC_CYCLIC)) && bcf != BC_MIRROR) ||
+                (svmc && (ph.idx1d != idx1dold || hit) && !ph.sv_isup && !ph.sv_lo && (!C.isreflect || n1 == n0)) ||
                 ph.t > C.twin1) {
                 if (isdet == BC_CYCLIC) {
                     float* pp = ph.p;
@@ -752,8 +873,22 @@ struct Runner {
                 }
             }
 
-            if (C.isreflect) {
-                ph.prop = C.prop_of(med, ph.idx1d);
+            if (svmc && !C.isreflect) {
+                ph.prop = C.prop[ph.sv_isup ? ph.sv_up : ph.sv_lo];   // src/mcx_core.cu:2504-2507
+            } else if (svmc && hit) {
+                // Fresnel at the plane (src/mcx_core.cu:2386-2404): the normal turned back along the flight
+                if (C.prop[ph.sv_lo].n != C.prop[ph.sv_up].n) {
+                    for (int i = 0; i < 3; i++) ph.nv[i] = -ph.nv[i];
+                    if (reflectray(ph, n1, rng)) {      // out into the background tissue
+                        terminate(ph, mediaidold & kDET_MASK, T);
+                        T.photons++;
+                        return;
+                    }
+                } else {
+                    ph.prop = C.prop[ph.sv_isup ? ph.sv_up : ph.sv_lo];
+                }
+            } else if (C.isreflect) {
+                if (!svmc) ph.prop = C.prop_of(med, ph.idx1d);
                 if (((med && P->isreflect) ||
                      (med == 0 && ((bcf == BC_UNKNOWN && P->isreflect) || bcf == BC_REFLECT || bcf == BC_MIRROR))) &&
                     (bcf == BC_MIRROR || n1 != ph.prop.n)) {
@@ -772,7 +907,7 @@ struct Runner {
                     }
                     if (Rtotal < 1.f && !(med == 0 && bcf == BC_MIRROR) && rng.next() > Rtotal) {
                         transmit(ph.v, n1, ph.prop.n, a);
-                        if (med == 0) {
+                        if (med == 0 || (svmc && (ph.sv_isup ? ph.sv_up : ph.sv_lo) == 0)) {
                             uint32_t detflag = (((ph.idx1d == kOUT_MAX && P->bc[9 + a]) || (ph.idx1d == kOUT_MIN && P->bc[6 + a]))
                                                 ? kOUT_MIN : (mediaidold & kDET_MASK));
                             ph.mediaid = 0;
@@ -788,9 +923,21 @@ struct Runner {
                         ph.fd[a] = (short)std::floor(ph.p[a]);
                         ph.idx1d = idx1dold;
                         ph.mediaid = C.pick(P->vol[ph.idx1d], rng) & kMED_MASK;
-                        ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
+                        if (!svmc) {
+                            ph.prop = C.prop_of(ph.mediaid, ph.idx1d);
+                        } else {
+                            // back in the voxel it left: its tissue at the reflected position; reflected
+                            // into a split voxel's background tissue, the photon ends
+                            // (src/mcx_core.cu:2474-2490)
+                            ph.prop = C.svmc_prop(ph);
+                            if ((ph.sv_isup ? ph.sv_up : ph.sv_lo) == 0) {
+                                terminate(ph, mediaidold & kDET_MASK, T);
+                                T.photons++;
+                                return;
+                            }
+                        }
                     }
-                } else {
+                } else if (!svmc) {
                     ph.prop = C.prop_of(mediaidold & kMED_MASK, idx1dold);
                 }
             }
