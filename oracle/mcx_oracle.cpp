@@ -16,6 +16,8 @@
 //   launchnewphoton (pencil branch) ... src/mcx_core.cu:1089-1243, 1646-1717
 //   savedetphoton / finddetector ...... src/mcx_core.cu:258-270, 365-417
 //   mcx_main_loop<1,r,1,0,0> .......... src/mcx_core.cu:1767-2528
+//   split voxels (MEDIA_2LABEL_SPLIT) . src/mcx_core.cu:688-830 (updateproperty, ray_plane_intersect,
+//                                        reflectray), 2112-2133, 2295-2310, 2386-2404, 2474-2507
 // The control flow follows the reference step for step, in plain FP32 with libm's
 // logf/expf/sincosf/acosf/sinf standing in for the CUDA fast-math intrinsics the reference
 // is compiled with.  Differences that are deliberate:
