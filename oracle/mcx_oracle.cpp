@@ -18,6 +18,8 @@
 //   mcx_main_loop<1,r,1,0,0> .......... src/mcx_core.cu:1767-2528
 //   split voxels (MEDIA_2LABEL_SPLIT) . src/mcx_core.cu:688-830 (updateproperty, ray_plane_intersect,
 //                                        reflectray), 2112-2133, 2295-2310, 2386-2404, 2474-2507
+//   extra sources ..................... src/mcx_core.cu:1217-1227 (source draw), 2225-2227 (blocks),
+//                                        383 (source in the detector id); src/mcx_utils.c:1688-1692
 // The control flow follows the reference step for step, in plain FP32 with libm's
 // logf/expf/sincosf/acosf/sinf standing in for the CUDA fast-math intrinsics the reference
 // is compiled with.  Differences that are deliberate:
@@ -293,6 +295,7 @@ struct Photon {
     int sv_lo, sv_up;
     bool sv_split, sv_isup, testint;
     float rp[3], nv[3];
+    int src;                       // 1-based source of the photon (extra sources)
 };
 
 // src/mcx_core.cu:866-956 (label media, no SVMC).  Returns the entry voxel or -1.
@@ -365,7 +368,7 @@ void savedetphoton(const Ctx& C, OracleResult* R, std::atomic<uint64_t>& slot, c
     if (base >= C.P->maxdetphoton || !R->detp) return;
     float* rec = R->detp + base * C.reclen;
     uint32_t k = 0, flag = C.P->savedetflag;
-    if (flag & 0x1) rec[k++] = (float)detid;
+    if (flag & 0x1) rec[k++] = (float)((C.P->nextra && C.P->srcid <= 0) ? (detid | (ph.src << 16)) : detid);
     for (uint32_t i = 0; i < C.partialdata; i++) rec[k++] = ph.ppath[i];
     if (flag & 0x10) { rec[k++] = ph.p[0]; rec[k++] = ph.p[1]; rec[k++] = ph.p[2]; }
     if (flag & 0x20) { rec[k++] = ph.v[0]; rec[k++] = ph.v[1]; rec[k++] = ph.v[2]; }
@@ -376,6 +379,7 @@ struct Runner {
     Ctx C;
     OracleResult* R;
     std::atomic<uint64_t>* detslot;
+    const OracleProblem* srcs = nullptr;   // source k's problem at srcs[k - 1]: the primary, then the extras
 
     void deposit(uint32_t idx, int tshift, double val) {
         double* f = R->field + (size_t)idx + (size_t)tshift * C.dimxyz;
@@ -407,8 +411,7 @@ struct Runner {
     // reference's order (launchnewphoton, src/mcx_core.cu:1261-1640; no launch-angle table).
     // Sets the launch voxel for shapes that move the photon.  False when the weight is at or
     // below minenergy (the reference then draws again without counting an attempt).
-    bool sample_source(Photon& ph, Rng& rng) {
-        const OracleProblem* P = C.P;
+    bool sample_source(Photon& ph, Rng& rng, const OracleProblem* P) {
         const float* a = P->srcparam1;
         const float* b = P->srcparam2;
         const float W = P->srcpos[3];
@@ -597,7 +600,14 @@ struct Runner {
     }
 
     bool launch(Photon& ph, Tally& T, Rng& rng) {
-        const OracleProblem* P = C.P;
+        // the photon's source, drawn before its launch when every source runs
+        // (src/mcx_core.cu:1217-1227)
+        ph.src = 1;
+        if (C.P->nextra && C.P->srcid != 1) {
+            if (C.P->srcid > 1) ph.src = C.P->srcid;
+            else ph.src = (int)(rng.next() * 0.9998f * (float)(C.P->nextra + 1)) + 1;
+        }
+        const OracleProblem* P = srcs ? srcs + (ph.src - 1) : C.P;
         float attempts = 1.f;
         do {
             ph.p[0] = P->srcpos[0]; ph.p[1] = P->srcpos[1]; ph.p[2] = P->srcpos[2]; ph.w = P->srcpos[3];
@@ -605,7 +615,7 @@ struct Runner {
             ph.pscat = 0.f; ph.t = 0.f; ph.pathlen = C.minaccumtime;
             ph.idx1d = P->src_idx;
             ph.mediaid = P->src_med;
-            if (P->srctype != 0 && !sample_source(ph, rng)) {
+            if (P->srctype != 0 && !sample_source(ph, rng, P)) {
                 // weight at or below minenergy: draw again (bounded here, unlike the reference)
                 attempts += 1.f;
                 if (attempts > (float)P->maxvoidstep) return false;
@@ -800,6 +810,7 @@ struct Runner {
                 if (P->save2pt && ph.t >= C.twin0 && ph.t < C.twin1) {
                     int tshift = (int)std::floor((ph.t - C.twin0) * C.Rtstep);
                     if (tshift > (int)C.maxgate - 1) tshift = (int)C.maxgate - 1;
+                    if (P->nextra && P->srcid < 0) tshift += (ph.src - 1) * (int)C.maxgate;   // 2225-2227
                     float weight = 0.f;
                     if (P->outputtype == 2) weight = ph.w0 - ph.w;                     // energy
                     else if (P->outputtype == 0 || P->outputtype == 1)                 // flux / fluence
@@ -998,11 +1009,36 @@ int oracle_run(const OracleProblem* P, OracleResult* R) {
     for (uint32_t i = 0; i < P->medianum; i++) props[i] = {P->prop[4 * i], P->prop[4 * i + 1], P->prop[4 * i + 2], P->prop[4 * i + 3]};
     C.prop = props.data();
 
+    // the extra sources as problems of their own: position, direction, parameters and, for
+    // point sources, the launch voxel and its label (src/mcx_utils.c:1679-1692, 1748-1756)
+    std::vector<OracleProblem> srcs(1 + (P->extrasrc ? P->nextra : 0), *P);
+    for (uint32_t k = 1; k < srcs.size(); k++) {
+        OracleProblem& S = srcs[k];
+        const float* x = P->extrasrc + 16 * (k - 1);
+        std::memcpy(S.srcpos, x, 4 * sizeof(float));
+        std::memcpy(S.srcdir, x + 4, 4 * sizeof(float));
+        std::memcpy(S.srcparam1, x + 8, 4 * sizeof(float));
+        std::memcpy(S.srcparam2, x + 12, 4 * sizeof(float));
+        if (S.srcpos[3] == 0.f) S.srcpos[3] = 1.f;
+        const float nd = std::sqrt(S.srcdir[0] * S.srcdir[0] + S.srcdir[1] * S.srcdir[1] + S.srcdir[2] * S.srcdir[2]);
+        if (nd > 0.f)
+            for (int i = 0; i < 3; i++) S.srcdir[i] /= nd;
+        S.src_idx = 0;
+        S.src_med = 0;
+        if (S.srcpos[0] >= 0.f && S.srcpos[1] >= 0.f && S.srcpos[2] >= 0.f && S.srcpos[0] < C.maxx &&
+            S.srcpos[1] < C.maxy && S.srcpos[2] < C.maxz) {
+            S.src_idx = (uint32_t)((int)std::floor(S.srcpos[2]) * C.dimxy + (int)std::floor(S.srcpos[1]) * C.nx +
+                                   (int)std::floor(S.srcpos[0]));
+            S.src_med = P->vol[S.src_idx] & kMED_MASK;
+        }
+    }
+
     std::atomic<uint64_t> slot(0);
     Runner run;
     run.C = C;
     run.R = R;
     run.detslot = &slot;
+    run.srcs = srcs.data();
 
     int nthreads = P->nthreads > 0 ? P->nthreads : 1;
     std::vector<Tally> tallies(nthreads);

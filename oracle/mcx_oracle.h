@@ -43,9 +43,16 @@ typedef struct OracleProblem {
     int srctype;
     float srcparam1[4], srcparam2[4];
     const float* srcpattern;
-    /* MCX mediabyte: 1/2/4 label volumes; 100-104 per-voxel formats whose 32-bit words encode the
-     * properties (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730) */
+    /* MCX mediabyte: 1/2/4 label volumes; 96 and 98-104 per-voxel formats whose 32-bit words
+     * encode the properties (src/mcx_const.h:72-80, decoded as src/mcx_core.cu:582-730); 97 split
+     * voxels, two words per voxel (the first words of all voxels, then the second words) */
     int mediaformat;
+    /* extra sources (src/mcx_core.cu:1217-1227): nextra x 16 floats, MCX's ExtraSrc layout
+     * {pos (w = weight), dir (w = focal length), param1, param2}; srcid 0 / -1 draws each photon's
+     * source (-1: one block of gates per source), srcid k >= 1 runs source k */
+    const float* extrasrc;
+    uint32_t nextra;
+    int srcid;
 } OracleProblem;
 
 /* Outputs: raw (unnormalised) field in FP64, optional per-voxel deposit counts, detected

@@ -33,6 +33,7 @@ class OracleProblem(C.Structure):
         ("photon_offset", C.c_uint64), ("seed", C.c_uint64), ("nthreads", C.c_int), ("seed_mode", C.c_int),
         ("mcx_threads", C.c_uint32), ("srctype", C.c_int), ("srcparam1", C.c_float * 4),
         ("srcparam2", C.c_float * 4), ("srcpattern", C.c_void_p), ("mediaformat", C.c_int),
+        ("extrasrc", C.c_void_p), ("nextra", C.c_uint32), ("srcid", C.c_int),
     ]
 
 
@@ -134,9 +135,13 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
     P.srcparam2[:] = [c.srcparam2.x, c.srcparam2.y, c.srcparam2.z, c.srcparam2.w]
     P.srcpattern = c.srcpattern
     P.mediaformat = int(c.mediabyte)
+    P.nextra = int(c.extrasrclen)
+    P.extrasrc = c.srcdata if P.nextra else None
+    P.srcid = int(c.srcid)
+    blocks = P.nextra + 1 if (P.nextra and P.srcid < 0) else 1     # one block of gates per source
 
-    field = np.zeros(nvox * maxgate, dtype=np.float64)
-    hit = np.zeros(nvox * maxgate, dtype=np.uint64) if hits else None
+    field = np.zeros(nvox * maxgate * blocks, dtype=np.float64)
+    hit = np.zeros(nvox * maxgate * blocks, dtype=np.uint64) if hits else None
     reclen = int(pc.reclen)
     detp = np.zeros(max(1, int(c.maxdetphoton)) * max(1, reclen), dtype=np.float32) if savedet else None
     R = OracleResult()
@@ -158,9 +163,11 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
                 scale *= float(c.tstep)
         else:
             scale = 1.0 / etot
+        if blocks > 1:
+            scale *= blocks          # every source ran a share of the photons (src/mcx_core.cu:3908-3910)
     out: dict[str, Any] = {
-        "raw": field.reshape((nx, ny, nz, maxgate), order="F"),
-        "flux": (field * scale).reshape((nx, ny, nz, maxgate), order="F"),
+        "raw": field.reshape((nx, ny, nz, maxgate * blocks), order="F"),
+        "flux": (field * scale).reshape((nx, ny, nz, maxgate * blocks), order="F"),
         "normalizer": scale,
         "stat": {
             "energytot": etot, "energyesc": R.e_escape + R.e_detect, "energyabs": etot - (R.e_escape + R.e_detect),
@@ -171,7 +178,7 @@ def run(pc, nphoton: int | None = None, seed: int | None = None, photon_offset: 
         },
     }
     if hit is not None:
-        out["hits"] = hit.reshape((nx, ny, nz, maxgate), order="F")
+        out["hits"] = hit.reshape((nx, ny, nz, maxgate * blocks), order="F")
     if detp is not None:
         nsaved = int(R.n_saved)
         out["detp"] = detp[: nsaved * reclen].reshape((reclen, nsaved), order="F")
